@@ -1,0 +1,457 @@
+"""Benchmark of the FastPM particle-mesh step on GB300.
+
+Workload: 512^3 particles on a 512^3 mesh (FP32 positions and
+velocities), box 512 Mpc/h, Planck15 cosmology, initial conditions from a
+seeded Gaussian random field (NumPy PCG64 white noise coloured by the
+Eisenstein-Hu linear power spectrum), 2LPT to a = 0.1, then K FastPM steps
+(K = --steps, 40 by default) linear in a up to a = 1.  One step is one
+force evaluation (paint, R2C, fused k-space kernel, batched C2R) plus the
+fused gather + kick + drift over all particles.
+
+Metric: particle-steps per second (Np * K / time of the K timed steps).
+The JSON line also carries: the forward+adjoint rate (hand-written
+adjoint, positions stored every step), the one-kernel-per-op GPU form,
+the end-to-end rate through the C ABI with host buffers, per-phase times,
+the roofline of the dominant kernel, the CPU baseline (the NumPy oracle on
+the host cores) and the SM clocks sampled during the timed region.
+
+``--impl reference`` times the reference's algorithm on the CPU instead
+(the NumPy restatement in ``oracle/``; JAX is not available), printing
+the same metric.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 512
+BOX_PER_CELL = 1.0  # box 512 Mpc/h on 512^3
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--mesh", type=int, default=N_DEFAULT)
+    ap.add_argument("--paint-mode", default="atomic")
+    ap.add_argument("--skip", default="", help="comma list of legs to skip: "
+                    "adjoint,plain,e2e,cpu,clocks")
+    ap.add_argument("--phases-only", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+def max_over_ranks(value, world):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        rows = [r.split(",") for r in out.strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for r in rows for n, v in zip(names, r[5:9]) if "Active" in v and
+                          "Not" not in v})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def initial_state(n, cosmo, device, seed=0):
+    """2LPT particles at a = 0.1 from a seeded Gaussian random field."""
+    import torch
+    from jaxpm_gb300 import distributed, pm
+    box = [n * BOX_PER_CELL] * 3
+    ic = pm.linear_field((n,) * 3, box, pm.pk_table(cosmo), seed=seed, device=device)
+    lat = distributed.uniform_particles((n,) * 3, device=device).reshape(-1, 3)
+    with torch.no_grad():
+        dx, p, _ = pm.lpt(cosmo, ic, lat, a=0.1, order=2)
+        x = (lat + dx).contiguous()
+        v = p.contiguous()
+    del ic, lat, dx
+    return x, v
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu
+    summary (``profiles/traffic.md``: lines ``kernel: bytes_per_particle``),
+    scaled to this run's particle count by the caller."""
+    path = os.path.join(ROOT, "profiles", "traffic.md")
+    out = {}
+    try:
+        for line in open(path):
+            if line.startswith("traffic_per_particle "):
+                _, k, v = line.split()
+                out[k] = float(v)
+    except OSError:
+        pass
+    return out
+
+
+def run_gb300(args):
+    import torch
+    from jaxpm_gb300 import _lib, cosmology, painting, simulate
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    lib = _lib.load()
+    skip = set(filter(None, args.skip.split(",")))
+    n = args.mesh
+    Np = n**3
+    K, W = args.steps, args.warmup
+    cosmo = cosmology.Planck15()
+    mode = painting._mode(args.paint_mode)
+
+    x0, v0 = initial_state(n, cosmo, dev)
+    sim = simulate.FastPM((n,) * 3, cosmo, 0.1, 1.0, K, paint_mode=mode, device=dev)
+    x, v = x0.clone(), v0.clone()
+    stream = torch.cuda.current_stream(dev)
+    s = _lib.stream(dev)
+    nx = ny = nz = n
+    ncell = n**3
+    nh = n * n * (n // 2 + 1)
+    ws = sim.ws
+    # buffers of the phase-by-phase step (the same calls the composite
+    # pmgb_fpm_step_f32 makes, issued separately so each phase is timed)
+    buf = {"mesh": torch.empty(ncell, dtype=torch.float32, device=dev),
+           "dk": torch.empty(nh, dtype=torch.complex64, device=dev),
+           "fk": torch.empty(3 * nh, dtype=torch.complex64, device=dev),
+           "f3": torch.empty(3 * ncell, dtype=torch.float32, device=dev),
+           "det": torch.empty(ncell * 8 if mode == _lib.PAINT_DETERMINISTIC else 1,
+                              dtype=torch.uint8, device=dev)}
+    P = lambda name: _lib.ptr(buf[name])  # noqa: E731
+    det_bytes = ncell * 8 if mode == _lib.PAINT_DETERMINISTIC else 0
+
+    phase_names = ["paint", "r2c", "kspace", "c2r", "read_kick_drift"]
+    events = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(K)]
+
+    def step_phased(i, ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        _lib.call("pmgb_cic_paint_f32", P("mesh"), nx, ny, nz, _lib.ptr(x), Np, None, 1.0, mode,
+                  0, P("det"), det_bytes, s)
+        if ev is not None:
+            ev[1].record(stream)
+        _lib.call("pmgb_fft_r2c_f32", P("mesh"), P("dk"), nx, ny, nz, 1, s)
+        if ev is not None:
+            ev[2].record(stream)
+        _lib.call("pmgb_kspace_forces_f32", P("dk"), P("fk"), nh, nx, ny, nz, 0.0, 1, 0,
+                  1.0 / ncell, s)
+        if ev is not None:
+            ev[3].record(stream)
+        _lib.call("pmgb_fft_c2r_f32", P("fk"), P("f3"), nx, ny, nz, 3, 0, s)
+        if ev is not None:
+            ev[4].record(stream)
+        _lib.call("pmgb_read3_kick_drift_f32", P("f3"), ncell, nx, ny, nz, _lib.ptr(x),
+                  _lib.ptr(v), Np, float(sim.kick[i]), float(sim.drift[i]), None, s)
+        if ev is not None:
+            ev[5].record(stream)
+
+    # warm-up on the initial state, then reset
+    for i in range(W):
+        step_phased(i % K)
+    x.copy_(x0)
+    v.copy_(v0)
+    torch.cuda.synchronize(dev)
+
+    clocks = ClockSampler(local) if "clocks" not in skip else None
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for i in range(K):
+        step_phased(i, events[i])
+    t1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    clk = clocks.stop() if clocks else None
+    ms = t0.elapsed_time(t1)
+    ms_max = max_over_ranks(ms, world)
+    value = world * Np * K / (ms_max / 1e3)
+    phase_ms = {name: float(np.mean([events[i][j].elapsed_time(events[i][j + 1])
+                                     for i in range(K)])) for j, name in enumerate(phase_names)}
+    x_final = x
+
+    # sanity: mass of the final density equals the particle count
+    rho = painting.cic_paint(torch.zeros((n,) * 3, device=dev), x_final, mode="deterministic")
+    mass_err = abs(rho.double().sum().item() - Np) / Np
+    del rho
+
+    result = {"metric": "particle-steps/s (FastPM PM step, 512^3 particles on 512^3 mesh)",
+              "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": K,
+              "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True,
+              "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+              "data": "synthetic: seeded Gaussian random field (NumPy PCG64 noise, "
+                      "Eisenstein-Hu P(k)), 2LPT to a=0.1",
+              "config": {"workload": f"FastPM {n}^3 particles on {n}^3 mesh, box {n} Mpc/h, "
+                                     f"2LPT a=0.1, {K} steps to a=1",
+                         "particles": Np, "mesh": [n, n, n], "box_mpc_h": n * BOX_PER_CELL,
+                         "paint_mode": args.paint_mode, "parallelism":
+                             "replicas" if world > 1 else "single",
+                         "l2": "inputs larger than L2 (positions+velocities 3.2 GB, "
+                               "meshes 0.54 GB each)"},
+              "phases_ms": phase_ms, "mass_rel_err": mass_err,
+              "gpu_launches": 3 * K + (K if mode == _lib.PAINT_DETERMINISTIC else 0)}
+
+    # roofline of the dominant own kernel
+    peak, peak_kind = peaks()
+    alg = {"paint": 16.0, "read_kick_drift": 60.0, "kspace": 16.0}
+    own = {k: phase_ms[k] for k in alg}
+    dom = max(own, key=own.get)
+    achieved = alg[dom] * Np / (phase_ms[dom] / 1e3) / 1e9
+    tr = profile_traffic().get(dom)
+    result["roofline"] = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak,
+                          "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                          "algorithmic_bytes_per_particle": alg[dom],
+                          "traffic": (tr * Np if tr is not None else None)}
+    result["kernels_frac_of_peak"] = {k: alg[k] * Np / (phase_ms[k] / 1e3) / 1e9 / peak
+                                      for k in alg}
+    if args.phases_only:
+        print(json.dumps(result))
+        return
+
+    # forward + adjoint (hand-written adjoint, positions stored every step)
+    if "adjoint" not in skip:
+        store = torch.empty((K, Np, 3), dtype=torch.float32, device=dev)
+        gx = torch.ones_like(x0) * 1e-3
+        gv = torch.zeros_like(v0)
+        sim.vjp(x0, v0, gx, gv, store=store)  # warm-up (plans, buffers)
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        sim.vjp(x0, v0, gx, gv, store=store)
+        a1.record(stream)
+        torch.cuda.synchronize(dev)
+        ams = max_over_ranks(a0.elapsed_time(a1), world)
+        result["fwd_adjoint"] = {"value": world * Np * K / (ams / 1e3),
+                                 "unit": "particle-steps/s", "ms_per_step": ams / K,
+                                 "cost_vs_forward": ams / ms_max}
+        del store
+
+    # one-kernel-per-op GPU form
+    if "plain" not in skip:
+        plain = simulate.FastPM((n,) * 3, cosmo, 0.1, 1.0, K, plain=True, device=dev)
+        xp, vp = x0.clone(), v0.clone()
+        plain.step(xp, vp, 0)
+        xp.copy_(x0)
+        vp.copy_(v0)
+        torch.cuda.synchronize(dev)
+        b0 = torch.cuda.Event(enable_timing=True)
+        b1 = torch.cuda.Event(enable_timing=True)
+        b0.record(stream)
+        plain.run(xp, vp)
+        b1.record(stream)
+        torch.cuda.synchronize(dev)
+        pms = max_over_ranks(b0.elapsed_time(b1), world)
+        result["plain_gpu"] = {"value": world * Np * K / (pms / 1e3), "unit": "particle-steps/s",
+                               "ms_per_step": pms / K, "fused_speedup": pms / ms_max}
+        del plain, xp, vp
+
+    # end to end through the C ABI with host buffers: every step copies
+    # positions and velocities from pinned host memory, runs the composite
+    # pmgb_fpm_step_f32 call and copies them back
+    if "e2e" not in skip:
+        hx = x0.cpu().pin_memory()
+        hv = v0.cpu().pin_memory()
+        dx_, dv_ = torch.empty_like(x0), torch.empty_like(v0)
+        steps_e2e = K
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(steps_e2e):
+            dx_.copy_(hx, non_blocking=True)
+            dv_.copy_(hv, non_blocking=True)
+            _lib.call("pmgb_fpm_step_f32", _lib.ptr(dx_), _lib.ptr(dv_), Np, nx, ny, nz,
+                      float(sim.kick[i]), float(sim.drift[i]), 0.0, mode, _lib.ptr(ws),
+                      sim.ws_bytes, s)
+            hx.copy_(dx_, non_blocking=True)
+            hv.copy_(dv_, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ems = max_over_ranks(e0.elapsed_time(e1), world)
+        nbytes = 2 * Np * 12
+        result["e2e"] = {"value": world * Np * steps_e2e / (ems / 1e3), "unit": "particle-steps/s",
+                         "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
+                         "ms_per_step": ems / steps_e2e,
+                         "api": "pmgb_fpm_step_f32 (C ABI) with pinned host buffers"}
+
+    if clk is not None:
+        result["clocks"] = clk
+
+    if rank == 0 and "cpu" not in skip:
+        result["cpu_baseline"] = cpu_baseline_sample(cosmo)
+    if rank == 0:
+        print(json.dumps(result))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# CPU: the oracle (NumPy restatement of the reference's algorithm)
+# ---------------------------------------------------------------------------
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def oracle_state(n, seed=0):
+    from oracle import cic, cosmology as oc, nbody as onb
+    cosmo = oc.Cosmology()
+    k = np.logspace(-4, 1, 128)
+    pk = oc.linear_matter_power(cosmo, k)
+    noise = np.random.Generator(np.random.PCG64(seed)).standard_normal((n,) * 3,
+                                                                        dtype=np.float32)
+    ic = onb.linear_field(noise, [n * BOX_PER_CELL] * 3, k, pk)
+    lat = cic.lattice((n,) * 3).reshape(-1, 3).astype(np.float32)
+    dx, p, _ = onb.lpt(cosmo, ic, lat, a=0.1, order=2)
+    return cosmo, lat + dx, p
+
+
+def cpu_baseline_sample(cosmo_unused=None, n=256):
+    """One oracle FastPM step (paint, C2C FFTs, k-space, three reads, kick,
+    drift) on a 256^3 sub-problem, timed on the host cores."""
+    from oracle import nbody as onb
+    cosmo, x, v = oracle_state(n)
+    kc, dc = onb.fpm_coefficients(cosmo, 0.1, 1.0, 40)
+    t = time.perf_counter()
+    onb.fpm_step(x, v, (n,) * 3, kc[0], dc[0])
+    dt = time.perf_counter() - t
+    return {"value": n**3 / dt, "unit": "particle-steps/s", "cores": host_threads(),
+            "kind": "port",
+            "sample": f"one FastPM step of the NumPy oracle on {n}^3 particles/{n}^3 mesh "
+                      f"({dt:.1f} s; FFTs on all host threads via scipy.fft, scatter/gather "
+                      "single-threaded NumPy)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    n_sample = 128
+    K, W = args.steps, args.warmup
+    from oracle import nbody as onb
+    cosmo, x0, v0 = oracle_state(n_sample)
+    kc, dc = onb.fpm_coefficients(cosmo, 0.1, 1.0, K)
+    x, v = x0, v0
+    for i in range(W):
+        x, v = onb.fpm_step(x, v, (n_sample,) * 3, kc[i % K], dc[i % K])
+    x, v = x0, v0
+    t = time.perf_counter()
+    for i in range(K):
+        x, v = onb.fpm_step(x, v, (n_sample,) * 3, kc[i], dc[i])
+    dt = time.perf_counter() - t
+    value = n_sample**3 * K / dt
+    n = args.mesh
+    out = {"metric": "particle-steps/s (FastPM PM step, 512^3 particles on 512^3 mesh)",
+           "value": value, "unit": "particle-steps/s", "n_gpus": 0, "steps": K, "warmup": W,
+           "ms_per_step": dt / K * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "impl": "reference",
+           "data": "synthetic: seeded Gaussian random field, 2LPT to a=0.1",
+           "config": {"workload": f"FastPM {n}^3 particles on {n}^3 mesh, box {n} Mpc/h, "
+                                  f"2LPT a=0.1, {K} steps to a=1"},
+           "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": host_threads(),
+                            "kind": "port",
+                            "sample": f"each timed step is one FastPM step of the NumPy oracle "
+                                      f"(the reference's algorithm restated; JAX is not "
+                                      f"installed) on a {n_sample}^3 sub-problem"},
+           "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,288 @@
+/*
+ * pmgb.h -- C ABI of the GB300 particle-mesh engine (libpmgb.so).
+ *
+ * The engine replaces the single-device hot path of JaxPM: CIC painting and
+ * reading (jaxpm/painting.py), the Fourier-space force solver
+ * (jaxpm/pm.py:12-58, jaxpm/kernels.py:41-115), the FFT wrappers
+ * (jaxpm/distributed.py:37-42) and the FastPM leapfrog kick/drift
+ * (jaxpm/ode.py:13-82).  Every reference citation below is relative to the
+ * JaxPM project root.
+ *
+ * Conventions
+ *  - All pointers are device pointers owned by the caller unless stated.
+ *    Meshes are float32, C order [nx][ny][nz].  Particle arrays are float32
+ *    [np][3] (the reference layout of positions, velocities and forces).
+ *    Half spectra are interleaved complex64 [nx][ny][nz/2+1].
+ *  - Calls are stream ordered: they enqueue work on `stream` and return
+ *    without synchronising.  `stream` is a cudaStream_t (0 = legacy default).
+ *  - Every call returns PMGB_OK or an error code; pmgb_last_error() gives a
+ *    message for the last failing call made by the calling thread.
+ *  - Scratch memory is passed in as (workspace, workspace_bytes); the
+ *    matching *_workspace_size() query returns the bytes needed.  cuFFT
+ *    plans are created on first use per (device, shape, batch) and cached
+ *    for the life of the process behind a mutex.
+ *  - Kernels never trap and never spin: every index is wrapped into the
+ *    mesh, so any finite position is safe.
+ */
+#ifndef PMGB_H_
+#define PMGB_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *pmgb_stream_t; /* identical to cudaStream_t */
+
+enum pmgb_status {
+  PMGB_OK = 0,
+  PMGB_ERR_INVALID_ARGUMENT = 1, /* bad shape, null pointer, bad mode    */
+  PMGB_ERR_WORKSPACE = 2,        /* workspace missing or too small       */
+  PMGB_ERR_CUDA = 3,             /* CUDA runtime error (message has it)  */
+  PMGB_ERR_CUFFT = 4,            /* cuFFT error                          */
+  PMGB_ERR_UNSUPPORTED = 5       /* valid request this build cannot serve */
+};
+
+/* Paint algorithms for the absolute-position painters. */
+enum pmgb_paint_mode {
+  PMGB_PAINT_ATOMIC = 0,  /* one thread per particle, 8 global fp32 atomics  */
+  PMGB_PAINT_BINNED = 1,  /* particle chunks binned into a shared-memory box,
+                             coalesced flush; global atomics when a chunk's box
+                             does not fit                                   */
+  PMGB_PAINT_DETERMINISTIC = 2 /* fixed-point 64-bit integer accumulation:
+                             bit-identical results run to run             */
+};
+
+/* ---- library ----------------------------------------------------------- */
+
+/* Version of this ABI (major*10000 + minor*100 + patch). */
+int pmgb_version(void);
+
+/* Message for the last failing call on this thread ("" if none). */
+const char *pmgb_last_error(void);
+
+/* ---- CIC mass assignment: absolute positions --------------------------- */
+
+/* Scratch bytes needed by pmgb_cic_paint_f32 for this mode and size. */
+size_t pmgb_cic_paint_workspace_size(int nx, int ny, int nz, int64_t np,
+                                     int mode);
+
+/* mesh[c] (+)= sum_p weight_p * W(pos_p, c), W the CIC kernel, indices
+ * wrapped periodically.  weight_p = weight_scale * (weights ? weights[p] : 1).
+ * accumulate = 0 overwrites mesh (it is zeroed first), 1 adds to it.
+ * Replaces _cic_paint_impl / cic_paint, jaxpm/painting.py:15-45 and :48-75
+ * (any particle count; the reference wrapper requires np == nx*ny*nz). */
+int pmgb_cic_paint_f32(float *mesh, int nx, int ny, int nz, const float *pos,
+                       int64_t np, const float *weights, float weight_scale,
+                       int mode, int accumulate, void *workspace,
+                       size_t workspace_bytes, pmgb_stream_t stream);
+
+/* out[p] = sum_c W(pos_p, c) * mesh[c].
+ * Replaces _cic_read_impl / cic_read, jaxpm/painting.py:78-128. */
+int pmgb_cic_read_f32(const float *mesh, int nx, int ny, int nz,
+                      const float *pos, int64_t np, float *out,
+                      pmgb_stream_t stream);
+
+/* Three meshes at once: mesh3 + i*comp_stride is component i;
+ * out3[p][i] = read(component i).  Replaces the three cic_read calls of
+ * jaxpm/pm.py:54-56 (indices and weights computed once). */
+int pmgb_cic_read3_f32(const float *mesh3, int64_t comp_stride, int nx,
+                       int ny, int nz, const float *pos, int64_t np,
+                       float *out3, pmgb_stream_t stream);
+
+/* Neighbour cells and weights of every particle, in the reference's order
+ * (jaxpm/painting.py:21-37): idx [np][8][3] int32 (wrapped), w [np][8]. */
+int pmgb_cic_weights_f32(const float *pos, int64_t np, int nx, int ny, int nz,
+                         int32_t *idx, float *w, pmgb_stream_t stream);
+
+/* Adjoint of pmgb_cic_paint_f32: given the cotangent mesh g_mesh,
+ * g_pos[p][d] = weight_p * sum_c dW/dx_d * g_mesh[c]   (if g_pos != NULL)
+ * g_w[p]      = sum_c W * g_mesh[c]                      (if g_w != NULL). */
+int pmgb_cic_paint_vjp_f32(const float *g_mesh, int nx, int ny, int nz,
+                           const float *pos, int64_t np, const float *weights,
+                           float weight_scale, float *g_pos, float *g_w,
+                           pmgb_stream_t stream);
+
+/* Adjoint of pmgb_cic_read_f32: g_mesh += paint of g_out (if g_mesh != NULL),
+ * g_pos[p][d] = g_out[p] * sum_c dW/dx_d * mesh[c] (if g_pos != NULL). */
+int pmgb_cic_read_vjp_f32(const float *mesh, int nx, int ny, int nz,
+                          const float *pos, int64_t np, const float *g_out,
+                          float *g_mesh, float *g_pos, pmgb_stream_t stream);
+
+/* ---- CIC mass assignment: relative (lattice + displacement) ------------ */
+
+/* mesh (+)= paint of particles at lattice point i plus disp[i]; disp is
+ * [nx*ny*nz][3].  Replaces cic_paint_dx, jaxpm/painting.py:161-215, with the
+ * enmesh arithmetic of jaxpm/painting_utils.py:28-96. */
+int pmgb_cic_paint_dx_f32(float *mesh, int nx, int ny, int nz,
+                          const float *disp, const float *weights,
+                          float weight_scale, int accumulate,
+                          pmgb_stream_t stream);
+
+/* out[i] = read at lattice point i plus disp[i].
+ * Replaces cic_read_dx, jaxpm/painting.py:218-260. */
+int pmgb_cic_read_dx_f32(const float *mesh, int nx, int ny, int nz,
+                         const float *disp, float *out, pmgb_stream_t stream);
+
+/* Neighbours and weights of the relative mode, in its neighbour order
+ * (jaxpm/painting_utils.py:43-45,84-96): idx [n][8][3], w [n][8]. */
+int pmgb_enmesh_f32(const float *disp, int nx, int ny, int nz, int32_t *idx,
+                    float *w, pmgb_stream_t stream);
+
+/* ---- FFT (jaxpm/distributed.py:37-42) ---------------------------------- */
+
+/* Forward real-to-complex 3-D FFT, unnormalised, of `batch` meshes
+ * (in + b*nx*ny*nz -> out + b*nx*ny*(nz/2+1)).  Replaces fft3d of a real
+ * field (the reference transforms C2C; the half spectrum is identical). */
+int pmgb_fft_r2c_f32(const float *in, void *out, int nx, int ny, int nz,
+                     int batch, pmgb_stream_t stream);
+
+/* Inverse complex-to-real 3-D FFT of `batch` half spectra, scaled by
+ * 1/(nx*ny*nz) when normalize != 0.  The input is overwritten.  Replaces
+ * ifft3d(x) = pifft3d(x).real. */
+int pmgb_fft_c2r_f32(void *in, float *out, int nx, int ny, int nz, int batch,
+                     int normalize, pmgb_stream_t stream);
+
+/* ---- Fourier-space force kernel (jaxpm/pm.py:49-56) --------------------- */
+
+/* One pass from delta_k to the three force spectra:
+ * force_k[i] = -grad_i(k) * invlaplace(k) * longrange(k) * delta_k * scale,
+ * grad order 1 = i(8 sin w - sin 2w)/6 or order 0 = i k with the Nyquist
+ * entry zeroed (jaxpm/kernels.py:41-66); invlaplace = -1/k^2, k=0 -> 0,
+ * fd_laplace selects the sinc-corrected form (kernels.py:69-92); longrange =
+ * exp(-k^2 r_split^2) or 1 (kernels.py:95-115).  force_k + i*comp_stride is
+ * component i.  Pass scale = 1/(nx*ny*nz) to fold the inverse-FFT
+ * normalisation in. */
+int pmgb_kspace_forces_f32(const void *delta_k, void *force_k,
+                           int64_t comp_stride, int nx, int ny, int nz,
+                           float r_split, int grad_order, int fd_laplace,
+                           float scale, pmgb_stream_t stream);
+
+/* Adjoint of pmgb_kspace_forces_f32 on half spectra:
+ * g_delta_k = sum_i conj(K_i(k)) * g_force_k[i] * scale. */
+int pmgb_kspace_forces_vjp_f32(const void *g_force_k, int64_t comp_stride,
+                               void *g_delta_k, int nx, int ny, int nz,
+                               float r_split, int grad_order, int fd_laplace,
+                               float scale, pmgb_stream_t stream);
+
+/* One-multiply-per-kernel forms of the same operator (comparison baseline):
+ * spec *= invlaplace(k)*scale; spec *= longrange(k); out = -grad_d(k)*in. */
+int pmgb_kspace_invlaplace_f32(void *spec, int nx, int ny, int nz,
+                               int fd_laplace, float scale,
+                               pmgb_stream_t stream);
+int pmgb_kspace_longrange_f32(void *spec, int nx, int ny, int nz,
+                              float r_split, pmgb_stream_t stream);
+int pmgb_kspace_gradient_f32(const void *in, void *out, int nx, int ny, int nz,
+                             int direction, int grad_order,
+                             pmgb_stream_t stream);
+
+/* ---- FastPM step (jaxpm/ode.py:13-82) ----------------------------------- */
+
+/* Fused gather + leapfrog update: F = read3(force meshes at pos),
+ * vel += kick * F, pos += drift * vel (both in place).  If forces_out is
+ * not NULL, F is also stored [np][3].  kick/drift are the host-computed
+ * FastPM coefficients (growth-factor kick and drift of ode.py:20-80 times
+ * the step, with 1.5*Omega_m folded into kick). */
+int pmgb_read3_kick_drift_f32(const float *force3, int64_t comp_stride, int nx,
+                              int ny, int nz, float *pos, float *vel,
+                              int64_t np, float kick, float drift,
+                              float *forces_out, pmgb_stream_t stream);
+
+/* Separate kick (vel += kick*forces) and drift (pos += drift*vel) kernels
+ * of the one-kernel-per-op form. */
+int pmgb_kick_f32(float *vel, const float *forces, int64_t np, float kick,
+                  pmgb_stream_t stream);
+int pmgb_drift_f32(float *pos, const float *vel, int64_t np, float drift,
+                   pmgb_stream_t stream);
+
+/* ---- composite calls ---------------------------------------------------- */
+
+/* Scratch bytes for pmgb_pm_forces_f32 / pmgb_fpm_step_f32 /
+ * pmgb_pm_forces_vjp_f32 on this mesh and particle count. */
+size_t pmgb_pm_workspace_size(int nx, int ny, int nz, int64_t np,
+                              int paint_mode);
+
+/* forces[p] = pm_forces(pos)[p] (jaxpm/pm.py:12-58 with
+ * paint_absolute_pos=True): paint, R2C, fused k-space kernel, batched C2R,
+ * read3. */
+int pmgb_pm_forces_f32(const float *pos, int64_t np, int nx, int ny, int nz,
+                       float r_split, int paint_mode, float *forces,
+                       void *workspace, size_t workspace_bytes,
+                       pmgb_stream_t stream);
+
+/* One fused FastPM step on (pos, vel) in place: forces at pos, kick, drift
+ * (jaxpm/ode.py:35-58 kick then :20-33 drift, forces of pm.py:12-58).
+ * If force3_out is not NULL the three force meshes [3][nx][ny][nz] of this
+ * step are copied there (for adjoints). */
+int pmgb_fpm_step_f32(float *pos, float *vel, int64_t np, int nx, int ny,
+                      int nz, float kick, float drift, float r_split,
+                      int paint_mode, void *workspace, size_t workspace_bytes,
+                      pmgb_stream_t stream);
+
+/* The same step as one kernel per operation: global-atomic paint, R2C,
+ * invlaplace, longrange, three gradient multiplies, three C2R, three
+ * separate reads, kick, drift.  The comparison baseline. */
+int pmgb_fpm_step_plain_f32(float *pos, float *vel, int64_t np, int nx,
+                            int ny, int nz, float kick, float drift,
+                            float r_split, void *workspace,
+                            size_t workspace_bytes, pmgb_stream_t stream);
+
+/* Vector-Jacobian product of pm_forces w.r.t. positions:
+ * g_pos = (d forces / d pos)^T g_forces (overwritten).  Recomputes the
+ * forward meshes, paints the cotangents, applies the adjoint k-space
+ * operator and gathers both position terms in one pass. */
+int pmgb_pm_forces_vjp_f32(const float *pos, int64_t np, int nx, int ny,
+                           int nz, float r_split, int paint_mode,
+                           const float *g_forces, float *g_pos,
+                           void *workspace, size_t workspace_bytes,
+                           pmgb_stream_t stream);
+
+/* ---- initial conditions (jaxpm/pm.py:61-144) ----------------------------- */
+
+/* linear_field colouring (jaxpm/pm.py:134-143) on a half spectrum:
+ * spec *= sqrt(interp(|k|, table_k, table_p) * nx*ny*nz / V) * scale with
+ * |k| = sqrt(sum_i (w_i / box_i * n_i)^2), w_i = 2*pi*fftfreq(n_i), and
+ * interp the clamped linear interpolation of jnp.interp.  table_k/table_p
+ * are device float32 arrays of n_table entries, table_k increasing. */
+int pmgb_linear_field_colour_f32(void *spec, int nx, int ny, int nz,
+                                 float box_x, float box_y, float box_z,
+                                 const float *table_k, const float *table_p,
+                                 int n_table, float scale,
+                                 pmgb_stream_t stream);
+
+/* Scratch bytes for pmgb_lpt2_source_f32. */
+size_t pmgb_lpt2_source_workspace_size(int nx, int ny, int nz);
+
+/* Second-order LPT source (jaxpm/pm.py:88-109): from the half spectrum
+ * delta_k, delta2 = sum_{i<j} (phi_ii phi_jj - phi_ij^2) with
+ * phi_ij = ifft3d(grad_i grad_j * invlaplace * delta_k). */
+int pmgb_lpt2_source_f32(const void *delta_k, float *delta2, int nx, int ny,
+                         int nz, void *workspace, size_t workspace_bytes,
+                         pmgb_stream_t stream);
+
+/* out = ca*a + cb*b over n floats (b may be NULL: out = ca*a): the LPT
+ * combinations dx, p, f of jaxpm/pm.py:85-87 and :118-124. */
+int pmgb_lpt_combine_f32(const float *a, const float *b, int64_t n, float ca,
+                         float cb, float *out, pmgb_stream_t stream);
+
+/* ---- power spectrum (jaxpm/utils.py:14-128) ------------------------------ */
+
+/* Binned auto power of a half spectrum (the unnormalised R2C of a mesh):
+ * for bin b (np.digitize of |k| against kedges[0..n_edges-1], b in
+ * 0..n_edges), psum[b] = sum |X|^2/(nx*ny*nz), pcount[b] = number of modes,
+ * ksum[b] = sum |k|, all over the full spectrum (modes with
+ * 0 < kz < nz/2 count twice).  |k| uses box lengths (h/Mpc).  Output arrays
+ * are device float64 [n_edges+1]; n_edges <= 2000. */
+int pmgb_power_spectrum_f32(const void *spec, int nx, int ny, int nz,
+                            double box_x, double box_y, double box_z,
+                            const double *kedges, int n_edges, double *psum,
+                            double *pcount, double *ksum,
+                            pmgb_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PMGB_H_ */

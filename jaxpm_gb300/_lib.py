@@ -1,0 +1,152 @@
+"""ctypes binding of ``libpmgb.so`` (the C ABI declared in ``include/pmgb.h``).
+
+The library is loaded from ``jaxpm_gb300/_lib/libpmgb.so`` (built in-tree
+by ``jaxpm_gb300.build``).  There is no fallback: if the library is missing
+or fails to load, every GPU entry point raises ``PmgbUnavailable``.
+Device buffers are torch CUDA tensors; calls are issued on the current
+torch CUDA stream.
+"""
+import ctypes
+import os
+
+import torch
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libpmgb.so")
+
+PMGB_OK = 0
+PAINT_ATOMIC = 0
+PAINT_BINNED = 1
+PAINT_DETERMINISTIC = 2
+
+_STATUS = {
+    1: "invalid argument",
+    2: "workspace",
+    3: "CUDA error",
+    4: "cuFFT error",
+    5: "unsupported",
+}
+
+c_int, c_int64, c_float, c_size_t = ctypes.c_int, ctypes.c_int64, ctypes.c_float, ctypes.c_size_t
+P = ctypes.c_void_p
+
+# name: (restype, argtypes)
+SIGNATURES = {
+    "pmgb_version": (c_int, []),
+    "pmgb_last_error": (ctypes.c_char_p, []),
+    "pmgb_cic_paint_workspace_size": (c_size_t, [c_int, c_int, c_int, c_int64, c_int]),
+    "pmgb_cic_paint_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P, c_float, c_int, c_int,
+                                   P, c_size_t, P]),
+    "pmgb_cic_read_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P, P]),
+    "pmgb_cic_read3_f32": (c_int, [P, c_int64, c_int, c_int, c_int, P, c_int64, P, P]),
+    "pmgb_cic_weights_f32": (c_int, [P, c_int64, c_int, c_int, c_int, P, P, P]),
+    "pmgb_cic_paint_vjp_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P, c_float, P, P, P]),
+    "pmgb_cic_read_vjp_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P, P, P, P]),
+    "pmgb_cic_paint_dx_f32": (c_int, [P, c_int, c_int, c_int, P, P, c_float, c_int, P]),
+    "pmgb_cic_read_dx_f32": (c_int, [P, c_int, c_int, c_int, P, P, P]),
+    "pmgb_enmesh_f32": (c_int, [P, c_int, c_int, c_int, P, P, P]),
+    "pmgb_fft_r2c_f32": (c_int, [P, P, c_int, c_int, c_int, c_int, P]),
+    "pmgb_fft_c2r_f32": (c_int, [P, P, c_int, c_int, c_int, c_int, c_int, P]),
+    "pmgb_kspace_forces_f32": (c_int, [P, P, c_int64, c_int, c_int, c_int, c_float, c_int, c_int,
+                                       c_float, P]),
+    "pmgb_kspace_forces_vjp_f32": (c_int, [P, c_int64, P, c_int, c_int, c_int, c_float, c_int,
+                                           c_int, c_float, P]),
+    "pmgb_kspace_invlaplace_f32": (c_int, [P, c_int, c_int, c_int, c_int, c_float, P]),
+    "pmgb_kspace_longrange_f32": (c_int, [P, c_int, c_int, c_int, c_float, P]),
+    "pmgb_kspace_gradient_f32": (c_int, [P, P, c_int, c_int, c_int, c_int, c_int, P]),
+    "pmgb_read3_kick_drift_f32": (c_int, [P, c_int64, c_int, c_int, c_int, P, P, c_int64,
+                                          c_float, c_float, P, P]),
+    "pmgb_kick_f32": (c_int, [P, P, c_int64, c_float, P]),
+    "pmgb_drift_f32": (c_int, [P, P, c_int64, c_float, P]),
+    "pmgb_pm_workspace_size": (c_size_t, [c_int, c_int, c_int, c_int64, c_int]),
+    "pmgb_pm_forces_f32": (c_int, [P, c_int64, c_int, c_int, c_int, c_float, c_int, P, P,
+                                   c_size_t, P]),
+    "pmgb_fpm_step_f32": (c_int, [P, P, c_int64, c_int, c_int, c_int, c_float, c_float, c_float,
+                                  c_int, P, c_size_t, P]),
+    "pmgb_fpm_step_plain_f32": (c_int, [P, P, c_int64, c_int, c_int, c_int, c_float, c_float,
+                                        c_float, P, c_size_t, P]),
+    "pmgb_pm_forces_vjp_f32": (c_int, [P, c_int64, c_int, c_int, c_int, c_float, c_int, P, P, P,
+                                       c_size_t, P]),
+    "pmgb_linear_field_colour_f32": (c_int, [P, c_int, c_int, c_int, c_float, c_float, c_float,
+                                             P, P, c_int, c_float, P]),
+    "pmgb_lpt2_source_workspace_size": (c_size_t, [c_int, c_int, c_int]),
+    "pmgb_lpt2_source_f32": (c_int, [P, P, c_int, c_int, c_int, P, c_size_t, P]),
+    "pmgb_lpt_combine_f32": (c_int, [P, P, c_int64, c_float, c_float, P, P]),
+    "pmgb_power_spectrum_f32": (c_int, [P, c_int, c_int, c_int, ctypes.c_double, ctypes.c_double,
+                                        ctypes.c_double, P, c_int, P, P, P, P]),
+}
+
+
+class PmgbError(RuntimeError):
+    """A libpmgb call returned an error status."""
+
+
+class PmgbUnavailable(RuntimeError):
+    """libpmgb.so is not built or cannot be loaded."""
+
+
+_lib = None
+
+
+def load():
+    """Loads (once) and returns the ctypes handle of libpmgb.so."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise PmgbUnavailable(
+            f"{LIB_PATH} is missing: build it with `python -m jaxpm_gb300.build`")
+    try:
+        lib = ctypes.CDLL(LIB_PATH)
+    except OSError as e:
+        raise PmgbUnavailable(f"cannot load {LIB_PATH}: {e}") from e
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def call(name, *args):
+    """Calls ``name`` and raises ``PmgbError`` on a non-zero status."""
+    lib = load()
+    status = getattr(lib, name)(*args)
+    if status != PMGB_OK:
+        msg = lib.pmgb_last_error().decode(errors="replace")
+        kind = _STATUS.get(status, f"status {status}")
+        err = PmgbError(f"{name}: {kind}: {msg}")
+        err.status = status
+        raise err
+    return status
+
+
+def ptr(t):
+    """Device pointer of a tensor (None/NULL for None)."""
+    if t is None:
+        return None
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def stream(device=None):
+    """The current torch CUDA stream as a cudaStream_t value."""
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def require_cuda(*tensors):
+    """Checks that every tensor is a contiguous float32/complex64 CUDA tensor
+    on one device; the GPU path has no CPU fallback."""
+    dev = None
+    for t in tensors:
+        if t is None:
+            continue
+        if not t.is_cuda:
+            raise ValueError("jaxpm_gb300 runs on CUDA tensors only; got a tensor on "
+                             f"{t.device}")
+        if not t.is_contiguous():
+            raise ValueError("jaxpm_gb300 expects contiguous tensors")
+        if dev is None:
+            dev = t.device
+        elif t.device != dev:
+            raise ValueError(f"tensors on different devices: {dev} and {t.device}")
+    return dev

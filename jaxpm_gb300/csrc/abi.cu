@@ -1,0 +1,416 @@
+// Exported C ABI of libpmgb (declared in include/pmgb.h): argument checks,
+// per-thread error messages, then a call into the kernels' host code.
+#include <map>
+#include <mutex>
+#include <string>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace pmgb {
+
+namespace {
+thread_local std::string t_err;
+std::mutex g_sm_mu;
+std::map<int, int> g_sm;
+}  // namespace
+
+int fail(int code, const std::string &msg) {
+  t_err = msg;
+  return code;
+}
+
+void clear_error() { t_err.clear(); }
+
+int sm_count() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+  std::lock_guard<std::mutex> lk(g_sm_mu);
+  auto it = g_sm.find(dev);
+  if (it != g_sm.end()) return it->second;
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+    n = 148;
+  g_sm[dev] = n;
+  return n;
+}
+
+int check_mesh(int nx, int ny, int nz) {
+  const int lim = 1 << 24;
+  if (nx <= 0 || ny <= 0 || nz <= 0 || nx >= lim || ny >= lim || nz >= lim)
+    return fail(PMGB_ERR_INVALID_ARGUMENT,
+                "mesh shape must be positive and below 2^24 per axis, got (" +
+                    std::to_string(nx) + ", " + std::to_string(ny) + ", " +
+                    std::to_string(nz) + ")");
+  if ((double)nx * ny * nz >= 1099511627776.0)
+    return fail(PMGB_ERR_INVALID_ARGUMENT, "mesh has 2^40 cells or more");
+  return PMGB_OK;
+}
+
+}  // namespace pmgb
+
+using namespace pmgb;
+
+#define BEGIN() clear_error()
+#define NEED(ptr) PMGB_REQUIRE((ptr) != nullptr, std::string(#ptr) + " is NULL")
+#define NONNEG(np) PMGB_REQUIRE((np) >= 0, std::string(#np) + " is negative")
+
+static int check_mode(int mode) {
+  PMGB_REQUIRE(mode == PMGB_PAINT_ATOMIC || mode == PMGB_PAINT_BINNED ||
+                   mode == PMGB_PAINT_DETERMINISTIC,
+               "unknown paint mode " + std::to_string(mode));
+  return PMGB_OK;
+}
+
+extern "C" {
+
+int pmgb_version(void) { return 100; }
+
+const char *pmgb_last_error(void) { return t_err.c_str(); }
+
+size_t pmgb_cic_paint_workspace_size(int nx, int ny, int nz, int64_t np, int mode) {
+  return paint_workspace_size(nx, ny, nz, np, mode);
+}
+
+int pmgb_cic_paint_f32(float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
+                       const float *weights, float weight_scale, int mode, int accumulate,
+                       void *workspace, size_t workspace_bytes, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  PMGB_TRY(check_mode(mode));
+  NONNEG(np);
+  NEED(mesh);
+  if (np > 0) NEED(pos);
+  return paint(mesh, nx, ny, nz, pos, np, weights, weight_scale, mode, accumulate, workspace,
+               workspace_bytes, stream);
+}
+
+int pmgb_cic_read_f32(const float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
+                      float *out, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NONNEG(np);
+  if (np == 0) return PMGB_OK;
+  NEED(mesh);
+  NEED(pos);
+  NEED(out);
+  return read(mesh, nx, ny, nz, pos, np, out, stream);
+}
+
+int pmgb_cic_read3_f32(const float *mesh3, int64_t comp_stride, int nx, int ny, int nz,
+                       const float *pos, int64_t np, float *out3, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NONNEG(np);
+  PMGB_REQUIRE(comp_stride >= (int64_t)nx * ny * nz, "comp_stride smaller than the mesh");
+  if (np == 0) return PMGB_OK;
+  NEED(mesh3);
+  NEED(pos);
+  NEED(out3);
+  return read3(mesh3, comp_stride, nx, ny, nz, pos, np, out3, stream);
+}
+
+int pmgb_cic_weights_f32(const float *pos, int64_t np, int nx, int ny, int nz, int32_t *idx,
+                         float *w, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NONNEG(np);
+  if (np == 0) return PMGB_OK;
+  NEED(pos);
+  NEED(idx);
+  NEED(w);
+  return cic_weights(pos, np, nx, ny, nz, idx, w, stream);
+}
+
+int pmgb_cic_paint_vjp_f32(const float *g_mesh, int nx, int ny, int nz, const float *pos,
+                           int64_t np, const float *weights, float weight_scale, float *g_pos,
+                           float *g_w, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NONNEG(np);
+  if (np == 0) return PMGB_OK;
+  NEED(g_mesh);
+  NEED(pos);
+  return paint_vjp(g_mesh, nx, ny, nz, pos, np, weights, weight_scale, g_pos, g_w, stream);
+}
+
+int pmgb_cic_read_vjp_f32(const float *mesh, int nx, int ny, int nz, const float *pos,
+                          int64_t np, const float *g_out, float *g_mesh, float *g_pos,
+                          pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NONNEG(np);
+  if (np == 0) return PMGB_OK;
+  NEED(pos);
+  NEED(g_out);
+  if (g_pos) NEED(mesh);
+  return read_vjp(mesh, nx, ny, nz, pos, np, g_out, g_mesh, g_pos, stream);
+}
+
+int pmgb_cic_paint_dx_f32(float *mesh, int nx, int ny, int nz, const float *disp,
+                          const float *weights, float weight_scale, int accumulate,
+                          pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NEED(mesh);
+  NEED(disp);
+  return paint_dx(mesh, nx, ny, nz, disp, weights, weight_scale, accumulate, stream);
+}
+
+int pmgb_cic_read_dx_f32(const float *mesh, int nx, int ny, int nz, const float *disp,
+                         float *out, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NEED(mesh);
+  NEED(disp);
+  NEED(out);
+  return read_dx(mesh, nx, ny, nz, disp, out, stream);
+}
+
+int pmgb_enmesh_f32(const float *disp, int nx, int ny, int nz, int32_t *idx, float *w,
+                    pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NEED(disp);
+  NEED(idx);
+  NEED(w);
+  return enmesh(disp, nx, ny, nz, idx, w, stream);
+}
+
+int pmgb_fft_r2c_f32(const float *in, void *out, int nx, int ny, int nz, int batch,
+                     pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  PMGB_REQUIRE(batch >= 1, "batch must be >= 1");
+  NEED(in);
+  NEED(out);
+  return fft_r2c(in, out, nx, ny, nz, batch, stream);
+}
+
+int pmgb_fft_c2r_f32(void *in, float *out, int nx, int ny, int nz, int batch, int normalize,
+                     pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  PMGB_REQUIRE(batch >= 1, "batch must be >= 1");
+  NEED(in);
+  NEED(out);
+  PMGB_TRY(fft_c2r(in, out, nx, ny, nz, batch, stream));
+  if (normalize) {
+    const int64_t n = (int64_t)nx * ny * nz;
+    PMGB_TRY(scale_inplace(out, n * batch, 1.0f / (float)n, stream));
+  }
+  return PMGB_OK;
+}
+
+static int check_kspace(int nx, int ny, int nz, int grad_order, int fd) {
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  PMGB_REQUIRE(grad_order == 0 || grad_order == 1, "grad_order must be 0 or 1");
+  PMGB_REQUIRE(fd == 0 || fd == 1, "fd_laplace must be 0 or 1");
+  return PMGB_OK;
+}
+
+int pmgb_kspace_forces_f32(const void *delta_k, void *force_k, int64_t comp_stride, int nx,
+                           int ny, int nz, float r_split, int grad_order, int fd_laplace,
+                           float scale, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_kspace(nx, ny, nz, grad_order, fd_laplace));
+  NEED(delta_k);
+  NEED(force_k);
+  PMGB_REQUIRE(comp_stride >= (int64_t)nx * ny * (nz / 2 + 1),
+               "comp_stride smaller than the half spectrum");
+  return kspace_forces(delta_k, force_k, comp_stride, nx, ny, nz, r_split, grad_order,
+                       fd_laplace, scale, stream);
+}
+
+int pmgb_kspace_forces_vjp_f32(const void *g_force_k, int64_t comp_stride, void *g_delta_k,
+                               int nx, int ny, int nz, float r_split, int grad_order,
+                               int fd_laplace, float scale, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_kspace(nx, ny, nz, grad_order, fd_laplace));
+  NEED(g_force_k);
+  NEED(g_delta_k);
+  PMGB_REQUIRE(comp_stride >= (int64_t)nx * ny * (nz / 2 + 1),
+               "comp_stride smaller than the half spectrum");
+  return kspace_forces_vjp(g_force_k, comp_stride, g_delta_k, nx, ny, nz, r_split, grad_order,
+                           fd_laplace, scale, stream);
+}
+
+int pmgb_kspace_invlaplace_f32(void *spec, int nx, int ny, int nz, int fd_laplace, float scale,
+                               pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_kspace(nx, ny, nz, 1, fd_laplace));
+  NEED(spec);
+  return kspace_invlaplace(spec, nx, ny, nz, fd_laplace, scale, stream);
+}
+
+int pmgb_kspace_longrange_f32(void *spec, int nx, int ny, int nz, float r_split,
+                              pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NEED(spec);
+  return kspace_longrange(spec, nx, ny, nz, r_split, stream);
+}
+
+int pmgb_kspace_gradient_f32(const void *in, void *out, int nx, int ny, int nz, int direction,
+                             int grad_order, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_kspace(nx, ny, nz, grad_order, 0));
+  PMGB_REQUIRE(direction >= 0 && direction < 3, "direction must be 0, 1 or 2");
+  NEED(in);
+  NEED(out);
+  return kspace_gradient(in, out, nx, ny, nz, direction, grad_order, stream);
+}
+
+int pmgb_read3_kick_drift_f32(const float *force3, int64_t comp_stride, int nx, int ny, int nz,
+                              float *pos, float *vel, int64_t np, float kick, float drift,
+                              float *forces_out, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NONNEG(np);
+  PMGB_REQUIRE(comp_stride >= (int64_t)nx * ny * nz, "comp_stride smaller than the mesh");
+  if (np == 0) return PMGB_OK;
+  NEED(force3);
+  NEED(pos);
+  NEED(vel);
+  return read3_kick_drift(force3, comp_stride, nx, ny, nz, pos, vel, np, kick, drift,
+                          forces_out, stream);
+}
+
+int pmgb_kick_f32(float *vel, const float *forces, int64_t np, float k, pmgb_stream_t stream) {
+  BEGIN();
+  NONNEG(np);
+  if (np == 0) return PMGB_OK;
+  NEED(vel);
+  NEED(forces);
+  return kick(vel, forces, np, k, stream);
+}
+
+int pmgb_drift_f32(float *pos, const float *vel, int64_t np, float d, pmgb_stream_t stream) {
+  BEGIN();
+  NONNEG(np);
+  if (np == 0) return PMGB_OK;
+  NEED(pos);
+  NEED(vel);
+  return drift(pos, vel, np, d, stream);
+}
+
+size_t pmgb_pm_workspace_size(int nx, int ny, int nz, int64_t np, int paint_mode) {
+  if (nx <= 0 || ny <= 0 || nz <= 0 || np < 0) return 0;
+  return pm_workspace_size(nx, ny, nz, np, paint_mode);
+}
+
+int pmgb_pm_forces_f32(const float *pos, int64_t np, int nx, int ny, int nz, float r_split,
+                       int paint_mode, float *forces, void *workspace, size_t workspace_bytes,
+                       pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  PMGB_TRY(check_mode(paint_mode));
+  NONNEG(np);
+  if (np > 0) {
+    NEED(pos);
+    NEED(forces);
+  }
+  return pm_forces(pos, np, nx, ny, nz, r_split, paint_mode, forces, workspace, workspace_bytes,
+                   stream);
+}
+
+int pmgb_fpm_step_f32(float *pos, float *vel, int64_t np, int nx, int ny, int nz, float kick,
+                      float drift, float r_split, int paint_mode, void *workspace,
+                      size_t workspace_bytes, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  PMGB_TRY(check_mode(paint_mode));
+  NONNEG(np);
+  if (np > 0) {
+    NEED(pos);
+    NEED(vel);
+  }
+  return fpm_step(pos, vel, np, nx, ny, nz, kick, drift, r_split, paint_mode, workspace,
+                  workspace_bytes, stream);
+}
+
+int pmgb_fpm_step_plain_f32(float *pos, float *vel, int64_t np, int nx, int ny, int nz,
+                            float kick, float drift, float r_split, void *workspace,
+                            size_t workspace_bytes, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NONNEG(np);
+  if (np > 0) {
+    NEED(pos);
+    NEED(vel);
+  }
+  return fpm_step_plain(pos, vel, np, nx, ny, nz, kick, drift, r_split, workspace,
+                        workspace_bytes, stream);
+}
+
+int pmgb_pm_forces_vjp_f32(const float *pos, int64_t np, int nx, int ny, int nz, float r_split,
+                           int paint_mode, const float *g_forces, float *g_pos,
+                           void *workspace, size_t workspace_bytes, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  PMGB_TRY(check_mode(paint_mode));
+  NONNEG(np);
+  if (np > 0) {
+    NEED(pos);
+    NEED(g_forces);
+    NEED(g_pos);
+  }
+  return pm_forces_vjp(pos, np, nx, ny, nz, r_split, paint_mode, g_forces, g_pos, workspace,
+                       workspace_bytes, stream);
+}
+
+int pmgb_linear_field_colour_f32(void *spec, int nx, int ny, int nz, float box_x, float box_y,
+                                 float box_z, const float *table_k, const float *table_p,
+                                 int n_table, float scale, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  PMGB_REQUIRE(box_x > 0 && box_y > 0 && box_z > 0, "box lengths must be positive");
+  PMGB_REQUIRE(n_table >= 2, "the power table needs at least two entries");
+  NEED(spec);
+  NEED(table_k);
+  NEED(table_p);
+  return linear_field_colour(spec, nx, ny, nz, box_x, box_y, box_z, table_k, table_p, n_table,
+                             scale, stream);
+}
+
+size_t pmgb_lpt2_source_workspace_size(int nx, int ny, int nz) {
+  if (nx <= 0 || ny <= 0 || nz <= 0) return 0;
+  return lpt2_source_workspace_size(nx, ny, nz);
+}
+
+int pmgb_lpt2_source_f32(const void *delta_k, float *delta2, int nx, int ny, int nz,
+                         void *workspace, size_t workspace_bytes, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NEED(delta_k);
+  NEED(delta2);
+  return lpt2_source(delta_k, delta2, nx, ny, nz, workspace, workspace_bytes, stream);
+}
+
+int pmgb_lpt_combine_f32(const float *a, const float *b, int64_t n, float ca, float cb,
+                         float *out, pmgb_stream_t stream) {
+  BEGIN();
+  NONNEG(n);
+  if (n == 0) return PMGB_OK;
+  NEED(a);
+  NEED(out);
+  return lpt_combine(a, b, n, ca, cb, out, stream);
+}
+
+int pmgb_power_spectrum_f32(const void *spec, int nx, int ny, int nz, double box_x, double box_y,
+                            double box_z, const double *kedges, int n_edges, double *psum,
+                            double *pcount, double *ksum, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  PMGB_REQUIRE(n_edges >= 1 && n_edges <= 2000, "n_edges must be in 1..2000");
+  PMGB_REQUIRE(box_x > 0 && box_y > 0 && box_z > 0, "box lengths must be positive");
+  NEED(spec);
+  NEED(kedges);
+  NEED(psum);
+  NEED(pcount);
+  NEED(ksum);
+  return power_spectrum(spec, nx, ny, nz, box_x, box_y, box_z, kedges, n_edges, psum, pcount,
+                        ksum, stream);
+}
+
+}  // extern "C"

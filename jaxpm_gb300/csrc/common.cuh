@@ -1,0 +1,135 @@
+// Shared helpers of libpmgb: status handling, launch geometry and the CIC
+// arithmetic that every painter and reader uses.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <climits>
+#include <string>
+
+#include "../../include/pmgb.h"
+
+namespace pmgb {
+
+// Records `msg` as the calling thread's last error and returns `code`.
+int fail(int code, const std::string &msg);
+// Clears the calling thread's last error.
+void clear_error();
+
+// Number of SMs of the current device (cached per device).
+int sm_count();
+
+#define PMGB_CUDA(call)                                                     \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess)                                                  \
+      return ::pmgb::fail(PMGB_ERR_CUDA, std::string(#call) + ": " +       \
+                                             cudaGetErrorString(e_));       \
+  } while (0)
+
+#define PMGB_LAUNCHED(name)                                                 \
+  do {                                                                      \
+    cudaError_t e_ = cudaGetLastError();                                    \
+    if (e_ != cudaSuccess)                                                  \
+      return ::pmgb::fail(PMGB_ERR_CUDA, std::string(name) + " launch: " + \
+                                             cudaGetErrorString(e_));       \
+  } while (0)
+
+#define PMGB_REQUIRE(cond, msg)                                             \
+  do {                                                                      \
+    if (!(cond)) return ::pmgb::fail(PMGB_ERR_INVALID_ARGUMENT, msg);       \
+  } while (0)
+
+#define PMGB_TRY(call)                                                      \
+  do {                                                                      \
+    int s_ = (call);                                                        \
+    if (s_ != PMGB_OK) return s_;                                           \
+  } while (0)
+
+// Validates a mesh shape: positive, and small enough that cell indices and
+// the float32 cell coordinates stay exact (< 2^24 per axis, < 2^40 cells).
+int check_mesh(int nx, int ny, int nz);
+
+// Grid size for a grid-stride loop over n items with `threads` per block:
+// enough blocks to fill every SM `per_sm` times, never more than needed.
+inline unsigned grid_for(int64_t n, int threads, int per_sm = 8) {
+  int64_t need = (n + threads - 1) / threads;
+  int64_t cap = (int64_t)sm_count() * per_sm;
+  if (need < 1) need = 1;
+  return (unsigned)(need < cap ? need : cap);
+}
+
+// ---------------------------------------------------------------------------
+// CIC arithmetic, absolute mode (reference: jaxpm/painting.py:21-37).
+// Every operation is rounded separately (no FMA contraction) so that the
+// float32 weights equal the reference's bit for bit:
+//   c0 = floor(x), c1 = floor(x) + 1 (in float),
+//   k0 = 1 - |x - c0|, k1 = 1 - |x - c1|,
+//   cell = int32(c) floor-mod n.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ int wrap_index(int i, int n) {
+  int r = i % n;
+  return r < 0 ? r + n : r;
+}
+
+struct Axis {
+  int i0, i1;    // wrapped cells of the lower and upper neighbour
+  float k0, k1;  // their CIC factors
+};
+
+__device__ __forceinline__ Axis cic_axis(float x, int n) {
+  Axis a;
+  float f = floorf(x);
+  float c1 = __fadd_rn(f, 1.0f);
+  a.k0 = __fsub_rn(1.0f, fabsf(__fsub_rn(x, f)));
+  a.k1 = __fsub_rn(1.0f, fabsf(__fsub_rn(x, c1)));
+  a.i0 = wrap_index((int)f, n);
+  a.i1 = wrap_index((int)c1, n);
+  return a;
+}
+
+// Derivative of each factor w.r.t. x: d(1 - |x - c|)/dx = -1 for x >= c,
+// +1 otherwise (JAX's select(u >= 0, g, -g) rule for abs; floor has zero
+// derivative).
+struct AxisGrad {
+  float d0, d1;
+};
+
+__device__ __forceinline__ AxisGrad cic_axis_grad(float x) {
+  AxisGrad g;
+  float f = floorf(x);
+  float c1 = __fadd_rn(f, 1.0f);
+  g.d0 = (__fsub_rn(x, f) >= 0.0f) ? -1.0f : 1.0f;
+  g.d1 = (__fsub_rn(x, c1) >= 0.0f) ? -1.0f : 1.0f;
+  return g;
+}
+
+// Neighbour n of the reference's connection list (painting.py:24-25):
+// (0,0,0),(1,0,0),(0,1,0),(0,0,1),(1,1,0),(1,0,1),(0,1,1),(1,1,1).
+__host__ __device__ constexpr int conn_x(int n) {
+  return (n == 1 || n == 4 || n == 5 || n == 7) ? 1 : 0;
+}
+__host__ __device__ constexpr int conn_y(int n) {
+  return (n == 2 || n == 4 || n == 6 || n == 7) ? 1 : 0;
+}
+__host__ __device__ constexpr int conn_z(int n) {
+  return (n == 3 || n == 5 || n == 6 || n == 7) ? 1 : 0;
+}
+
+__device__ __forceinline__ int64_t cell_index(int ix, int iy, int iz, int ny,
+                                              int nz) {
+  return ((int64_t)ix * ny + iy) * nz + iz;
+}
+
+// Loads particle p's three coordinates from an [np][3] array.
+__device__ __forceinline__ void load3(const float *__restrict__ a, int64_t p,
+                                      float &x, float &y, float &z) {
+  const float *q = a + 3 * p;
+  x = __ldg(q);
+  y = __ldg(q + 1);
+  z = __ldg(q + 2);
+}
+
+}  // namespace pmgb

@@ -1,0 +1,91 @@
+// Internal host-side entry points shared between the translation units of
+// libpmgb.  The exported C ABI (abi.cu) validates arguments and forwards here.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace pmgb {
+
+// cic.cu
+size_t paint_workspace_size(int nx, int ny, int nz, int64_t np, int mode);
+int paint(float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
+          const float *weights, float wscale, int mode, int accumulate,
+          void *ws, size_t ws_bytes, cudaStream_t s);
+int read(const float *mesh, int nx, int ny, int nz, const float *pos,
+         int64_t np, float *out, cudaStream_t s);
+int read3(const float *mesh3, int64_t cs, int nx, int ny, int nz,
+          const float *pos, int64_t np, float *out, cudaStream_t s);
+int cic_weights(const float *pos, int64_t np, int nx, int ny, int nz,
+                int32_t *idx, float *w, cudaStream_t s);
+int paint_vjp(const float *g_mesh, int nx, int ny, int nz, const float *pos,
+              int64_t np, const float *weights, float wscale, float *g_pos,
+              float *g_w, cudaStream_t s);
+int read_vjp(const float *mesh, int nx, int ny, int nz, const float *pos,
+             int64_t np, const float *g_out, float *g_mesh, float *g_pos,
+             cudaStream_t s);
+int paint_dx(float *mesh, int nx, int ny, int nz, const float *disp,
+             const float *weights, float wscale, int accumulate,
+             cudaStream_t s);
+int read_dx(const float *mesh, int nx, int ny, int nz, const float *disp,
+            float *out, cudaStream_t s);
+int enmesh(const float *disp, int nx, int ny, int nz, int32_t *idx, float *w,
+           cudaStream_t s);
+
+// fft.cu
+int fft_r2c(const float *in, void *out, int nx, int ny, int nz, int batch,
+            cudaStream_t s);
+int fft_c2r(void *in, float *out, int nx, int ny, int nz, int batch,
+            cudaStream_t s);
+int scale_inplace(float *x, int64_t n, float scale, cudaStream_t s);
+
+// kspace.cu
+int kspace_forces(const void *dk, void *fk, int64_t cs, int nx, int ny, int nz,
+                  float r_split, int grad_order, int fd, float scale,
+                  cudaStream_t s);
+int kspace_forces_vjp(const void *gfk, int64_t cs, void *gdk, int nx, int ny,
+                      int nz, float r_split, int grad_order, int fd,
+                      float scale, cudaStream_t s);
+int kspace_invlaplace(void *spec, int nx, int ny, int nz, int fd, float scale,
+                      cudaStream_t s);
+int kspace_longrange(void *spec, int nx, int ny, int nz, float r_split,
+                     cudaStream_t s);
+int kspace_gradient(const void *in, void *out, int nx, int ny, int nz, int dir,
+                    int grad_order, cudaStream_t s);
+
+// step.cu
+size_t pm_workspace_size(int nx, int ny, int nz, int64_t np, int mode);
+int pm_forces(const float *pos, int64_t np, int nx, int ny, int nz,
+              float r_split, int mode, float *forces, void *ws, size_t bytes,
+              cudaStream_t s);
+int read3_kick_drift(const float *f3, int64_t cs, int nx, int ny, int nz,
+                     float *pos, float *vel, int64_t np, float kick,
+                     float drift, float *fout, cudaStream_t s);
+int fpm_step(float *pos, float *vel, int64_t np, int nx, int ny, int nz,
+             float kick, float drift, float r_split, int mode, void *ws,
+             size_t bytes, cudaStream_t s);
+int fpm_step_plain(float *pos, float *vel, int64_t np, int nx, int ny, int nz,
+                   float kick, float drift, float r_split, void *ws,
+                   size_t bytes, cudaStream_t s);
+int kick(float *vel, const float *forces, int64_t np, float k, cudaStream_t s);
+int drift(float *pos, const float *vel, int64_t np, float d, cudaStream_t s);
+int pm_forces_vjp(const float *pos, int64_t np, int nx, int ny, int nz,
+                  float r_split, int mode, const float *g, float *gpos,
+                  void *ws, size_t bytes, cudaStream_t s);
+
+// lpt.cu
+int linear_field_colour(void *spec, int nx, int ny, int nz, float bx, float by,
+                        float bz, const float *tk, const float *tp, int nt,
+                        float scale, cudaStream_t s);
+size_t lpt2_source_workspace_size(int nx, int ny, int nz);
+int lpt2_source(const void *dk, float *delta2, int nx, int ny, int nz,
+                void *ws, size_t bytes, cudaStream_t s);
+int lpt_combine(const float *a, const float *b, int64_t n, float ca, float cb,
+                float *out, cudaStream_t s);
+
+// pk.cu
+int power_spectrum(const void *spec, int nx, int ny, int nz, double bx,
+                   double by, double bz, const double *edges, int n_edges,
+                   double *psum, double *pcount, double *ksum, cudaStream_t s);
+
+}  // namespace pmgb

@@ -1,0 +1,182 @@
+"""The FastPM time loop on one GPU: fused steps, the one-kernel-per-op
+comparison form, and a differentiable step with a hand-written adjoint.
+
+A step is one force evaluation plus a kick and a drift (``jaxpm/ode.py:13-82``
+driven on the grid ``a_i = a0 + i*dt``).  The fused step is one library
+call, ``pmgb_fpm_step_f32``: paint -> R2C -> fused k-space -> batched C2R ->
+gather + kick + drift in one kernel.  Positions and velocities are
+``[Np, 3]`` float32 CUDA tensors updated in place.
+"""
+import numpy as np
+import torch
+from torch.utils.checkpoint import checkpoint
+
+from . import _lib
+from .ode import fpm_coefficients
+from .painting import _mode
+
+
+def _ws(nbytes, device):
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device)
+
+
+class FastPM:
+    """Runs FastPM steps from ``a0`` to ``a1`` on a fixed mesh.
+
+    ``paint_mode`` selects the painter of the fused step; ``plain=True``
+    runs the one-kernel-per-op form instead (global-atomic paint, separate
+    k-space multiplies, three gathers, separate kick and drift).
+    The workspace is allocated once, for ``n_particles`` particles."""
+
+    def __init__(self, mesh_shape, cosmo, a0, a1, n_steps, n_particles=None, paint_mode="atomic",
+                 r_split=0.0, plain=False, device="cuda"):
+        self.mesh_shape = tuple(int(s) for s in mesh_shape)
+        self.cosmo = cosmo
+        self.n_steps = int(n_steps)
+        self.kick, self.drift = fpm_coefficients(cosmo, a0, a1, n_steps)
+        self.mode = _mode(paint_mode)
+        self.r_split = float(r_split)
+        self.plain = plain
+        self.n_particles = (int(np.prod(self.mesh_shape)) if n_particles is None
+                            else int(n_particles))
+        nx, ny, nz = self.mesh_shape
+        self.ws_bytes = _lib.load().pmgb_pm_workspace_size(
+            nx, ny, nz, self.n_particles, _lib.PAINT_ATOMIC if plain else self.mode)
+        self.ws = _ws(self.ws_bytes, device)
+
+    def step(self, pos, vel, i, stream=None):
+        """Advances ``(pos, vel)`` in place by step ``i``."""
+        n = pos.numel() // 3
+        if n > self.n_particles:
+            raise ValueError("more particles than the workspace was sized for")
+        nx, ny, nz = self.mesh_shape
+        s = _lib.stream() if stream is None else stream
+        if self.plain:
+            _lib.call("pmgb_fpm_step_plain_f32", _lib.ptr(pos), _lib.ptr(vel), n, nx, ny, nz,
+                      float(self.kick[i]), float(self.drift[i]), self.r_split,
+                      _lib.ptr(self.ws), self.ws_bytes, s)
+        else:
+            _lib.call("pmgb_fpm_step_f32", _lib.ptr(pos), _lib.ptr(vel), n, nx, ny, nz,
+                      float(self.kick[i]), float(self.drift[i]), self.r_split, self.mode,
+                      _lib.ptr(self.ws), self.ws_bytes, s)
+
+    def run(self, pos, vel, steps=None):
+        """Runs ``steps`` (default: all) steps in place and returns
+        ``(pos, vel)``."""
+        _lib.require_cuda(pos, vel)
+        for i in range(self.n_steps if steps is None else steps):
+            self.step(pos, vel, i)
+        return pos, vel
+
+    def step_vjp(self, x, gx, gv, i, stream=None):
+        """Adjoint of step ``i`` taken from positions ``x`` (before the step):
+        given the cotangents ``(gx, gv)`` of the step's outputs, overwrites
+        them with the cotangents of its inputs.  ``u = gv + drift gx``;
+        ``gx += (dF/dx)^T (kick u)``; ``gv = u``."""
+        nx, ny, nz = self.mesh_shape
+        n = x.numel() // 3
+        s = _lib.stream() if stream is None else stream
+        if not hasattr(self, "_adj"):
+            self._adj = (torch.empty_like(x), torch.empty_like(x))
+        ku, gpos = self._adj
+        # gv <- gv + drift*gx (= u); ku <- kick*u
+        _lib.call("pmgb_lpt_combine_f32", _lib.ptr(gv), _lib.ptr(gx), 3 * n, 1.0,
+                  float(self.drift[i]), _lib.ptr(gv), s)
+        _lib.call("pmgb_lpt_combine_f32", _lib.ptr(gv), None, 3 * n, float(self.kick[i]), 0.0,
+                  _lib.ptr(ku), s)
+        mode = _lib.PAINT_ATOMIC if self.plain else self.mode
+        _lib.call("pmgb_pm_forces_vjp_f32", _lib.ptr(x), n, nx, ny, nz, self.r_split, mode,
+                  _lib.ptr(ku), _lib.ptr(gpos), _lib.ptr(self.ws), self.ws_bytes, s)
+        _lib.call("pmgb_lpt_combine_f32", _lib.ptr(gx), _lib.ptr(gpos), 3 * n, 1.0, 1.0,
+                  _lib.ptr(gx), s)
+
+    def vjp(self, pos, vel, g_pos, g_vel, store=None):
+        """Forward run from ``(pos, vel)`` followed by the reverse sweep:
+        returns the final state and the cotangents of the initial state for
+        output cotangents ``(g_pos, g_vel)``.  The positions before every
+        step are kept (``store`` preallocated ``[n_steps, Np, 3]`` buffer,
+        or allocated here); the reverse sweep only needs positions."""
+        n = self.n_steps
+        x, v = pos.clone(), vel.clone()
+        if store is None:
+            store = torch.empty((n, *x.shape), dtype=x.dtype, device=x.device)
+        for i in range(n):
+            store[i].copy_(x)
+            self.step(x, v, i)
+        gx, gv = g_pos.clone(), g_vel.clone()
+        for i in reversed(range(n)):
+            self.step_vjp(store[i], gx, gv, i)
+        return (x, v), (gx, gv)
+
+
+def _combine(x, y, cx, cy):
+    out = torch.empty_like(x)
+    _lib.call("pmgb_lpt_combine_f32", _lib.ptr(x), _lib.ptr(y), x.numel(), float(cx), float(cy),
+              _lib.ptr(out), _lib.stream())
+    return out
+
+
+class _Step(torch.autograd.Function):
+    """One FastPM step ``(x, v) -> (x', v')`` with
+    ``v' = v + kick F(x)``, ``x' = x + drift v'``.
+
+    Backward, given ``(gx', gv')``: ``u = gv' + drift gx'``,
+    ``gx = gx' + (dF/dx)^T (kick u)`` (one ``pmgb_pm_forces_vjp_f32``),
+    ``gv = u``."""
+
+    @staticmethod
+    def forward(ctx, x, v, mesh_shape, kick, drift, mode, r_split):
+        nx, ny, nz = mesh_shape
+        n = x.numel() // 3
+        xo, vo = x.clone(), v.clone()
+        wsb = _lib.load().pmgb_pm_workspace_size(nx, ny, nz, n, mode)
+        ws = _ws(wsb, x.device)
+        _lib.call("pmgb_fpm_step_f32", _lib.ptr(xo), _lib.ptr(vo), n, nx, ny, nz, float(kick),
+                  float(drift), float(r_split), mode, _lib.ptr(ws), wsb, _lib.stream())
+        ctx.save_for_backward(x)
+        ctx.args = (mesh_shape, float(kick), float(drift), mode, float(r_split))
+        return xo, vo
+
+    @staticmethod
+    def backward(ctx, gx, gv):
+        (x,) = ctx.saved_tensors
+        (nx, ny, nz), kick, drift, mode, r_split = ctx.args
+        gx = torch.zeros_like(x) if gx is None else gx.contiguous()
+        gv = torch.zeros_like(x) if gv is None else gv.contiguous()
+        u = _combine(gv, gx, 1.0, drift)
+        ku = _combine(u, None, kick, 0.0)
+        n = x.numel() // 3
+        wsb = _lib.load().pmgb_pm_workspace_size(nx, ny, nz, n, mode)
+        ws = _ws(wsb, x.device)
+        gpos = torch.empty_like(x)
+        _lib.call("pmgb_pm_forces_vjp_f32", _lib.ptr(x), n, nx, ny, nz, r_split, mode,
+                  _lib.ptr(ku), _lib.ptr(gpos), _lib.ptr(ws), wsb, _lib.stream())
+        return _combine(gx, gpos, 1.0, 1.0), u, None, None, None, None, None
+
+
+def fpm_step(x, v, mesh_shape, kick, drift, paint_mode="atomic", r_split=0.0):
+    """Differentiable fused FastPM step (new tensors; inputs unchanged)."""
+    x, v = x.contiguous(), v.contiguous()
+    _lib.require_cuda(x, v)
+    return _Step.apply(x, v, tuple(mesh_shape), kick, drift, _mode(paint_mode), r_split)
+
+
+def nbody(pos, vel, cosmo, mesh_shape, a0, a1, n_steps, paint_mode="atomic", r_split=0.0,
+          checkpoint_every=0):
+    """Differentiable FastPM integration from ``a0`` to ``a1`` in
+    ``n_steps`` steps; returns the final ``(pos, vel)``.  With
+    ``checkpoint_every = k > 0`` only every k-th state is kept for the
+    backward pass and the steps in between are recomputed."""
+    kick, drift = fpm_coefficients(cosmo, a0, a1, n_steps)
+
+    def segment(x, v, lo, hi):
+        for i in range(lo, hi):
+            x, v = fpm_step(x, v, mesh_shape, kick[i], drift[i], paint_mode, r_split)
+        return x, v
+
+    if checkpoint_every and checkpoint_every > 0:
+        for lo in range(0, n_steps, checkpoint_every):
+            hi = min(n_steps, lo + checkpoint_every)
+            pos, vel = checkpoint(segment, pos, vel, lo, hi, use_reentrant=False)
+        return pos, vel
+    return segment(pos, vel, 0, n_steps)

@@ -1,0 +1,74 @@
+"""The C ABI library: it builds, loads, exports every declared symbol and
+rejects bad arguments on the host (no GPU work is issued here)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "pmgb.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(pmgb_\w+)\s*\(", text)))
+
+
+def test_header_declares_the_hot_path():
+    names = declared_symbols()
+    for must in ["pmgb_cic_paint_f32", "pmgb_cic_read_f32", "pmgb_cic_read3_f32",
+                 "pmgb_kspace_forces_f32", "pmgb_fft_r2c_f32", "pmgb_fft_c2r_f32",
+                 "pmgb_pm_forces_f32", "pmgb_fpm_step_f32", "pmgb_pm_forces_vjp_f32",
+                 "pmgb_cic_paint_dx_f32", "pmgb_cic_read_dx_f32"]:
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_every_declared_symbol():
+    from jaxpm_gb300 import _lib
+    assert sorted(_lib.SIGNATURES) == declared_symbols()
+
+
+def test_version_and_empty_error(lib):
+    assert lib.pmgb_version() >= 100
+    assert lib.pmgb_last_error() == b""
+
+
+def test_bad_shape_is_rejected_before_any_gpu_work(lib):
+    from jaxpm_gb300 import _lib
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_cic_paint_f32", None, 0, 4, 4, None, 0, None, 1.0, 0, 0, None, 0, None)
+    assert e.value.status == 1 and "mesh shape" in str(e.value)
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_cic_paint_f32", ctypes.c_void_p(16), 4, 4, 4, None, 10, None, 1.0, 0, 0,
+                  None, 0, None)
+    assert "pos is NULL" in str(e.value)
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_cic_paint_f32", ctypes.c_void_p(16), 4, 4, 4, None, 0, None, 1.0, 7, 0,
+                  None, 0, None)
+    assert "paint mode" in str(e.value)
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_kspace_forces_f32", ctypes.c_void_p(16), ctypes.c_void_p(16), 10, 4, 4, 4,
+                  0.0, 2, 0, 1.0, None)
+    assert "grad_order" in str(e.value)
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_power_spectrum_f32", ctypes.c_void_p(16), 4, 4, 4, 1.0, 1.0, 1.0,
+                  ctypes.c_void_p(16), 5000, ctypes.c_void_p(16), ctypes.c_void_p(16),
+                  ctypes.c_void_p(16), None)
+    assert "n_edges" in str(e.value)
+
+
+def test_workspace_queries(lib):
+    assert lib.pmgb_pm_workspace_size(64, 64, 64, 64**3, 0) >= 64**3 * 4 * 7
+    assert lib.pmgb_pm_workspace_size(64, 64, 64, 64**3, 2) > lib.pmgb_pm_workspace_size(
+        64, 64, 64, 64**3, 0)
+    assert lib.pmgb_cic_paint_workspace_size(8, 8, 8, 10, 2) == 8 * 512
+    assert lib.pmgb_cic_paint_workspace_size(8, 8, 8, 10, 0) == 0
+    assert lib.pmgb_pm_workspace_size(0, 8, 8, 1, 0) == 0
