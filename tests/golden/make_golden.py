@@ -58,7 +58,9 @@ def main():
         out[f"{tag}_disp"] = disp
         out[f"{tag}_rel_idx"] = ridx
         out[f"{tag}_rel_w"] = rw
-        out[f"{tag}_rel_paint64"] = cic.cic_paint_dx(disp.astype(np.float64), dtype=np.float64)
+        # float32 enmesh arithmetic (the reference's dtype: its wrap rounds
+        # -1e-9 up to L and drops that neighbour), float64 accumulation
+        out[f"{tag}_rel_paint32"] = cic.cic_paint_dx(disp, dtype=np.float32)
     np.savez_compressed(os.path.join(OUT, "cic.npz"), **out)
 
     # pm_forces on a 16^3 mesh, float64 oracle (C2C as the reference)
