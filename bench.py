@@ -42,7 +42,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mesh", type=int, default=N_DEFAULT)
-    ap.add_argument("--paint-mode", default="atomic")
+    ap.add_argument("--engine", default="sorted", choices=["sorted", "lattice"])
+    ap.add_argument("--paint-mode", default="atomic", help="painter of the lattice engine")
     ap.add_argument("--skip", default="", help="comma list of legs to skip: "
                     "adjoint,plain,e2e,cpu,clocks")
     ap.add_argument("--phases-only", action="store_true")
@@ -175,19 +176,17 @@ def run_gb300(args):
     Np = n**3
     K, W = args.steps, args.warmup
     cosmo = cosmology.Planck15()
-    mode = painting._mode(args.paint_mode)
+    engine = args.engine
+    mode = _lib.PAINT_BINNED if engine == "sorted" else painting._mode(args.paint_mode)
 
     x0, v0 = initial_state(n, cosmo, dev)
-    sim = simulate.FastPM((n,) * 3, cosmo, 0.1, 1.0, K, paint_mode=mode, device=dev)
-    x, v = x0.clone(), v0.clone()
     stream = torch.cuda.current_stream(dev)
     s = _lib.stream(dev)
     nx = ny = nz = n
     ncell = n**3
     nh = n * n * (n // 2 + 1)
-    ws = sim.ws
-    # buffers of the phase-by-phase step (the same calls the composite
-    # pmgb_fpm_step_f32 makes, issued separately so each phase is timed)
+    # buffers of the phase-by-phase step: the same C-ABI calls the composite
+    # step makes, issued separately so that each phase is timed on the stream
     buf = {"mesh": torch.empty(ncell, dtype=torch.float32, device=dev),
            "dk": torch.empty(nh, dtype=torch.complex64, device=dev),
            "fk": torch.empty(3 * nh, dtype=torch.complex64, device=dev),
@@ -197,37 +196,69 @@ def run_gb300(args):
     P = lambda name: _lib.ptr(buf[name])  # noqa: E731
     det_bytes = ncell * 8 if mode == _lib.PAINT_DETERMINISTIC else 0
 
-    phase_names = ["paint", "r2c", "kspace", "c2r", "read_kick_drift"]
-    events = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(K)]
+    if engine == "sorted":
+        eng = simulate.SortedFastPM((n,) * 3, cosmo, 0.1, 1.0, K, device=dev)
+        kick, drift = eng.kick, eng.drift
+        phase_names = ["paint", "r2c", "kspace", "c2r", "read_kick_drift", "sort"]
+    else:
+        eng = simulate.FastPM((n,) * 3, cosmo, 0.1, 1.0, K, paint_mode=mode, device=dev)
+        kick, drift = eng.kick, eng.drift
+        x, v = x0.clone(), v0.clone()
+        phase_names = ["paint", "r2c", "kspace", "c2r", "read_kick_drift"]
+    events = [[torch.cuda.Event(enable_timing=True) for _ in range(len(phase_names) + 1)]
+              for _ in range(K)]
+
+    def reset():
+        if engine == "sorted":
+            eng.load(x0, v0)
+        else:
+            x.copy_(x0)
+            v.copy_(v0)
+
+    def current_positions():
+        return eng.positions if engine == "sorted" else x
 
     def step_phased(i, ev=None):
-        if ev is not None:
-            ev[0].record(stream)
-        _lib.call("pmgb_cic_paint_f32", P("mesh"), nx, ny, nz, _lib.ptr(x), Np, None, 1.0, mode,
+        rec = (lambda j: ev[j].record(stream)) if ev is not None else (lambda j: None)
+        if engine == "sorted":
+            a, b = eng.cur, 1 - eng.cur
+            px, pv = eng.pos[a], eng.vel[a]
+        else:
+            px, pv = x, v
+        rec(0)
+        _lib.call("pmgb_cic_paint_f32", P("mesh"), nx, ny, nz, _lib.ptr(px), Np, None, 1.0, mode,
                   0, P("det"), det_bytes, s)
-        if ev is not None:
-            ev[1].record(stream)
+        rec(1)
         _lib.call("pmgb_fft_r2c_f32", P("mesh"), P("dk"), nx, ny, nz, 1, s)
-        if ev is not None:
-            ev[2].record(stream)
+        rec(2)
         _lib.call("pmgb_kspace_forces_f32", P("dk"), P("fk"), nh, nx, ny, nz, 0.0, 1, 0,
                   1.0 / ncell, s)
-        if ev is not None:
-            ev[3].record(stream)
+        rec(3)
         _lib.call("pmgb_fft_c2r_f32", P("fk"), P("f3"), nx, ny, nz, 3, 0, s)
-        if ev is not None:
-            ev[4].record(stream)
-        _lib.call("pmgb_read3_kick_drift_f32", P("f3"), ncell, nx, ny, nz, _lib.ptr(x),
-                  _lib.ptr(v), Np, float(sim.kick[i]), float(sim.drift[i]), None, s)
-        if ev is not None:
-            ev[5].record(stream)
+        rec(4)
+        if engine == "sorted":
+            _lib.call("pmgb_read3_kick_drift_binned_f32", P("f3"), ncell, nx, ny, nz,
+                      _lib.ptr(px), _lib.ptr(pv), Np, float(kick[i]), float(drift[i]),
+                      _lib.ptr(eng.sort_ws), eng.sort_bytes, _lib.ptr(eng.stats_buf), s)
+            rec(5)
+            _lib.call("pmgb_tile_scatter_f32", _lib.ptr(px), _lib.ptr(pv), _lib.ptr(eng.ids[a]),
+                      Np, nx, ny, nz, _lib.ptr(eng.pos[b]), _lib.ptr(eng.vel[b]),
+                      _lib.ptr(eng.ids[b]), _lib.ptr(eng.sort_ws), eng.sort_bytes, s)
+            rec(6)
+            eng.cur = b
+        else:
+            _lib.call("pmgb_read3_kick_drift_f32", P("f3"), ncell, nx, ny, nz, _lib.ptr(px),
+                      _lib.ptr(pv), Np, float(kick[i]), float(drift[i]), None, s)
+            rec(5)
 
     # warm-up on the initial state, then reset
+    reset()
     for i in range(W):
         step_phased(i % K)
-    x.copy_(x0)
-    v.copy_(v0)
+    reset()
     torch.cuda.synchronize(dev)
+    if engine == "sorted":
+        eng.stats_buf.zero_()
 
     clocks = ClockSampler(local) if "clocks" not in skip else None
     if clocks:
@@ -249,12 +280,15 @@ def run_gb300(args):
     value = world * Np * K / (ms_max / 1e3)
     phase_ms = {name: float(np.mean([events[i][j].elapsed_time(events[i][j + 1])
                                      for i in range(K)])) for j, name in enumerate(phase_names)}
-    x_final = x
 
     # sanity: mass of the final density equals the particle count
-    rho = painting.cic_paint(torch.zeros((n,) * 3, device=dev), x_final, mode="deterministic")
+    rho = painting.paint(torch.zeros((n,) * 3, device=dev), current_positions(),
+                         mode="deterministic")
     mass_err = abs(rho.double().sum().item() - Np) / Np
     del rho
+    launches_per_step = {"sorted": 7, "lattice": 3}[engine]
+    if mode == _lib.PAINT_DETERMINISTIC:
+        launches_per_step += 1
 
     result = {"metric": "particle-steps/s (FastPM PM step, 512^3 particles on 512^3 mesh)",
               "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": K,
@@ -265,12 +299,15 @@ def run_gb300(args):
               "config": {"workload": f"FastPM {n}^3 particles on {n}^3 mesh, box {n} Mpc/h, "
                                      f"2LPT a=0.1, {K} steps to a=1",
                          "particles": Np, "mesh": [n, n, n], "box_mpc_h": n * BOX_PER_CELL,
-                         "paint_mode": args.paint_mode, "parallelism":
-                             "replicas" if world > 1 else "single",
+                         "engine": engine, "paint_mode": {0: "atomic", 1: "binned",
+                                                          2: "deterministic"}[mode],
+                         "parallelism": "replicas" if world > 1 else "single",
                          "l2": "inputs larger than L2 (positions+velocities 3.2 GB, "
                                "meshes 0.54 GB each)"},
               "phases_ms": phase_ms, "mass_rel_err": mass_err,
-              "gpu_launches": 3 * K + (K if mode == _lib.PAINT_DETERMINISTIC else 0)}
+              "gpu_launches": launches_per_step * K}
+    if engine == "sorted":
+        result["box_fallback_chunks"] = eng.stats
 
     # roofline of the dominant own kernel
     peak, peak_kind = peaks()
@@ -289,18 +326,23 @@ def run_gb300(args):
         print(json.dumps(result))
         return
 
-    # forward + adjoint (hand-written adjoint, positions stored every step)
+    # forward + adjoint (hand-written adjoint; positions, and for the sorted
+    # loop particle ids, stored before every step)
     if "adjoint" not in skip:
-        store = torch.empty((K, Np, 3), dtype=torch.float32, device=dev)
         gx = torch.ones_like(x0) * 1e-3
         gv = torch.zeros_like(v0)
-        sim.vjp(x0, v0, gx, gv, store=store)  # warm-up (plans, buffers)
+        if engine == "sorted":
+            store = (torch.empty((K, Np, 3), dtype=torch.float32, device=dev),
+                     torch.empty((K, Np), dtype=torch.int32, device=dev))
+        else:
+            store = torch.empty((K, Np, 3), dtype=torch.float32, device=dev)
+        eng.vjp(x0, v0, gx, gv, store=store)  # warm-up (plans, buffers)
         torch.cuda.synchronize(dev)
         barrier(world)
         a0 = torch.cuda.Event(enable_timing=True)
         a1 = torch.cuda.Event(enable_timing=True)
         a0.record(stream)
-        sim.vjp(x0, v0, gx, gv, store=store)
+        eng.vjp(x0, v0, gx, gv, store=store)
         a1.record(stream)
         torch.cuda.synchronize(dev)
         ams = max_over_ranks(a0.elapsed_time(a1), world)
@@ -329,34 +371,46 @@ def run_gb300(args):
         del plain, xp, vp
 
     # end to end through the C ABI with host buffers: every step copies
-    # positions and velocities from pinned host memory, runs the composite
-    # pmgb_fpm_step_f32 call and copies them back
+    # positions and velocities (caller's order) from pinned host memory,
+    # sorts them by tile, runs pmgb_fpm_step_sorted_f32, returns them to the
+    # caller's order and copies them back
     if "e2e" not in skip:
         hx = x0.cpu().pin_memory()
         hv = v0.cpu().pin_memory()
         dx_, dv_ = torch.empty_like(x0), torch.empty_like(v0)
-        steps_e2e = K
+        E = eng if engine == "sorted" else simulate.SortedFastPM((n,) * 3, cosmo, 0.1, 1.0, K,
+                                                                device=dev)
         torch.cuda.synchronize(dev)
         barrier(world)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for i in range(steps_e2e):
+        for i in range(K):
             dx_.copy_(hx, non_blocking=True)
             dv_.copy_(hv, non_blocking=True)
-            _lib.call("pmgb_fpm_step_f32", _lib.ptr(dx_), _lib.ptr(dv_), Np, nx, ny, nz,
-                      float(sim.kick[i]), float(sim.drift[i]), 0.0, mode, _lib.ptr(ws),
-                      sim.ws_bytes, s)
+            _lib.call("pmgb_tile_sort_f32", _lib.ptr(dx_), _lib.ptr(dv_), None, Np, nx, ny, nz,
+                      _lib.ptr(E.pos[0]), _lib.ptr(E.vel[0]), _lib.ptr(E.ids[0]),
+                      _lib.ptr(E.sort_ws), E.sort_bytes, s)
+            _lib.call("pmgb_fpm_step_sorted_f32", _lib.ptr(E.pos[0]), _lib.ptr(E.vel[0]),
+                      _lib.ptr(E.ids[0]), _lib.ptr(E.pos[1]), _lib.ptr(E.vel[1]),
+                      _lib.ptr(E.ids[1]), Np, nx, ny, nz, float(E.kick[i]), float(E.drift[i]),
+                      0.0, _lib.ptr(E.ws), E.ws_bytes, _lib.ptr(E.sort_ws), E.sort_bytes, None,
+                      s)
+            _lib.call("pmgb_unpermute3_f32", _lib.ptr(E.pos[1]), _lib.ptr(E.ids[1]), Np,
+                      _lib.ptr(dx_), s)
+            _lib.call("pmgb_unpermute3_f32", _lib.ptr(E.vel[1]), _lib.ptr(E.ids[1]), Np,
+                      _lib.ptr(dv_), s)
             hx.copy_(dx_, non_blocking=True)
             hv.copy_(dv_, non_blocking=True)
         e1.record(stream)
         torch.cuda.synchronize(dev)
         ems = max_over_ranks(e0.elapsed_time(e1), world)
         nbytes = 2 * Np * 12
-        result["e2e"] = {"value": world * Np * steps_e2e / (ems / 1e3), "unit": "particle-steps/s",
+        result["e2e"] = {"value": world * Np * K / (ems / 1e3), "unit": "particle-steps/s",
                          "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                         "ms_per_step": ems / steps_e2e,
-                         "api": "pmgb_fpm_step_f32 (C ABI) with pinned host buffers"}
+                         "ms_per_step": ems / K,
+                         "api": "pmgb_tile_sort_f32 + pmgb_fpm_step_sorted_f32 + "
+                                "pmgb_unpermute3_f32 (C ABI), pinned host buffers"}
 
     if clk is not None:
         result["clocks"] = clk

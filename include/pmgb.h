@@ -239,6 +239,73 @@ int pmgb_pm_forces_vjp_f32(const float *pos, int64_t np, int nx, int ny,
                            void *workspace, size_t workspace_bytes,
                            pmgb_stream_t stream);
 
+/* ---- tile-sorted particle state (the fused FastPM loop) ----------------- */
+/* The fast loop keeps (pos, vel) physically ordered by the 8^3-cell mesh
+ * tile that holds each particle (tiles in Morton order), with id[p] the
+ * particle's index in the caller's order.  Forces, kicks and drifts are
+ * per particle, so the order changes no result; pmgb_unpermute3_f32 returns
+ * arrays to the caller's order. */
+
+/* Scratch bytes of pmgb_tile_sort_f32 / pmgb_fpm_step_sorted_f32 (tile
+ * counts, offsets and one rank per particle). */
+size_t pmgb_tile_sort_workspace_size(int nx, int ny, int nz, int64_t np);
+
+/* Counting sort by tile: (pos, vel, id) -> (pos_out, vel_out, id_out).
+ * vel/vel_out may be NULL; id NULL means the identity (id_out[q] = index of
+ * the particle now at q). */
+int pmgb_tile_sort_f32(const float *pos, const float *vel, const uint32_t *id,
+                       int64_t np, int nx, int ny, int nz, float *pos_out,
+                       float *vel_out, uint32_t *id_out, void *workspace,
+                       size_t workspace_bytes, pmgb_stream_t stream);
+
+/* out[id[p]] = in[p] for [np][3] arrays (back to the caller's order). */
+int pmgb_unpermute3_f32(const float *in, const uint32_t *id, int64_t np,
+                        float *out, pmgb_stream_t stream);
+
+/* out[p] = in[id[p]] for [np][3] arrays (caller's order -> tile order). */
+int pmgb_permute3_f32(const float *in, const uint32_t *id, int64_t np,
+                      float *out, pmgb_stream_t stream);
+
+/* Box-staged gather + kick + drift (the sorted loop's read): each CTA
+ * stages the cell box of its chunk of particles of the three force meshes
+ * in shared memory and interpolates from there (global reads when the box
+ * does not fit).  Same results as pmgb_read3_kick_drift_f32.  With a sort
+ * workspace it also counts the new positions per tile and records each
+ * particle's rank in its tile, for pmgb_tile_scatter_f32. */
+int pmgb_read3_kick_drift_binned_f32(const float *force3, int64_t comp_stride,
+                                     int nx, int ny, int nz, float *pos,
+                                     float *vel, int64_t np, float kick,
+                                     float drift, void *sort_workspace,
+                                     size_t sort_workspace_bytes,
+                                     uint32_t *stats, pmgb_stream_t stream);
+
+/* Exclusive scan of the tile counts left in sort_workspace by
+ * pmgb_read3_kick_drift_binned_f32, then the scatter of (pos, vel, id) to
+ * (pos_out, vel_out, id_out) in tile order. */
+int pmgb_tile_scatter_f32(const float *pos, const float *vel,
+                          const uint32_t *id, int64_t np, int nx, int ny,
+                          int nz, float *pos_out, float *vel_out,
+                          uint32_t *id_out, void *sort_workspace,
+                          size_t sort_workspace_bytes, pmgb_stream_t stream);
+
+/* One FastPM step on tile-sorted particles (jaxpm/ode.py:35-58 kick and
+ * :20-33 drift, forces of jaxpm/pm.py:12-58): shared-memory box paint,
+ * R2C, fused k-space kernel, batched C2R, box-staged gather + kick + drift
+ * that also counts the new positions per tile, scan, scatter.  Reads
+ * (pos, vel, id) and writes the advanced state, sorted by the new
+ * positions, to (pos_out, vel_out, id_out).  `workspace` is sized by
+ * pmgb_pm_workspace_size(..., PMGB_PAINT_BINNED), `sort_workspace` by
+ * pmgb_tile_sort_workspace_size.  stats (nullable, 2 counters the caller
+ * zeroes) accumulates the paint and gather chunks whose cell box did not
+ * fit in shared memory and took the global-memory path. */
+int pmgb_fpm_step_sorted_f32(float *pos, float *vel, uint32_t *id,
+                             float *pos_out, float *vel_out, uint32_t *id_out,
+                             int64_t np, int nx, int ny, int nz, float kick,
+                             float drift, float r_split, void *workspace,
+                             size_t workspace_bytes, void *sort_workspace,
+                             size_t sort_workspace_bytes, uint32_t *stats,
+                             pmgb_stream_t stream);
+
 /* ---- initial conditions (jaxpm/pm.py:61-144) ----------------------------- */
 
 /* linear_field colouring (jaxpm/pm.py:134-143) on a half spectrum:

@@ -72,6 +72,17 @@ SIGNATURES = {
     "pmgb_lpt2_source_workspace_size": (c_size_t, [c_int, c_int, c_int]),
     "pmgb_lpt2_source_f32": (c_int, [P, P, c_int, c_int, c_int, P, c_size_t, P]),
     "pmgb_lpt_combine_f32": (c_int, [P, P, c_int64, c_float, c_float, P, P]),
+    "pmgb_tile_sort_workspace_size": (c_size_t, [c_int, c_int, c_int, c_int64]),
+    "pmgb_tile_sort_f32": (c_int, [P, P, P, c_int64, c_int, c_int, c_int, P, P, P, P, c_size_t,
+                                   P]),
+    "pmgb_unpermute3_f32": (c_int, [P, P, c_int64, P, P]),
+    "pmgb_permute3_f32": (c_int, [P, P, c_int64, P, P]),
+    "pmgb_read3_kick_drift_binned_f32": (c_int, [P, c_int64, c_int, c_int, c_int, P, P, c_int64,
+                                                 c_float, c_float, P, c_size_t, P, P]),
+    "pmgb_tile_scatter_f32": (c_int, [P, P, P, c_int64, c_int, c_int, c_int, P, P, P, P,
+                                      c_size_t, P]),
+    "pmgb_fpm_step_sorted_f32": (c_int, [P, P, P, P, P, P, c_int64, c_int, c_int, c_int, c_float,
+                                         c_float, c_float, P, c_size_t, P, c_size_t, P, P]),
     "pmgb_power_spectrum_f32": (c_int, [P, c_int, c_int, c_int, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, P, c_int, P, P, P, P]),
 }

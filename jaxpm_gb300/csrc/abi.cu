@@ -359,6 +359,116 @@ int pmgb_pm_forces_vjp_f32(const float *pos, int64_t np, int nx, int ny, int nz,
                        workspace_bytes, stream);
 }
 
+size_t pmgb_tile_sort_workspace_size(int nx, int ny, int nz, int64_t np) {
+  if (nx <= 0 || ny <= 0 || nz <= 0 || np < 0) return 0;
+  return sort_workspace_size(nx, ny, nz, np);
+}
+
+static int check_sortable(int nx, int ny, int nz, int64_t np) {
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NONNEG(np);
+  PMGB_REQUIRE(np < (int64_t)UINT32_MAX, "the sorted path indexes particles with 32 bits");
+  PMGB_REQUIRE(tile_key_count(nx, ny, nz) <= ((int64_t)1 << 24),
+               "the sorted path supports at most 256 tiles (2048 cells) per axis");
+  return PMGB_OK;
+}
+
+int pmgb_tile_sort_f32(const float *pos, const float *vel, const uint32_t *id, int64_t np, int nx,
+                       int ny, int nz, float *pos_out, float *vel_out, uint32_t *id_out,
+                       void *workspace, size_t workspace_bytes, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  if (np == 0) return PMGB_OK;
+  NEED(pos);
+  NEED(pos_out);
+  NEED(id_out);
+  PMGB_REQUIRE((vel == nullptr) == (vel_out == nullptr), "vel and vel_out must both be given");
+  PMGB_REQUIRE(pos != pos_out && (!vel || vel != vel_out) && (!id || id != id_out),
+               "the sort cannot run in place");
+  return tile_sort(pos, vel, id, np, nx, ny, nz, pos_out, vel_out, id_out, workspace,
+                   workspace_bytes, stream);
+}
+
+int pmgb_unpermute3_f32(const float *in, const uint32_t *id, int64_t np, float *out,
+                        pmgb_stream_t stream) {
+  BEGIN();
+  NONNEG(np);
+  if (np == 0) return PMGB_OK;
+  NEED(in);
+  NEED(id);
+  NEED(out);
+  PMGB_REQUIRE(in != out, "unpermute cannot run in place");
+  return unpermute3(in, id, np, out, stream);
+}
+
+int pmgb_permute3_f32(const float *in, const uint32_t *id, int64_t np, float *out,
+                      pmgb_stream_t stream) {
+  BEGIN();
+  NONNEG(np);
+  if (np == 0) return PMGB_OK;
+  NEED(in);
+  NEED(id);
+  NEED(out);
+  PMGB_REQUIRE(in != out, "permute cannot run in place");
+  return permute3(in, id, np, out, stream);
+}
+
+int pmgb_read3_kick_drift_binned_f32(const float *force3, int64_t comp_stride, int nx, int ny,
+                                     int nz, float *pos, float *vel, int64_t np, float kick,
+                                     float drift, void *sort_workspace,
+                                     size_t sort_workspace_bytes, uint32_t *stats,
+                                     pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  PMGB_REQUIRE(comp_stride >= (int64_t)nx * ny * nz, "comp_stride smaller than the mesh");
+  if (np == 0) return PMGB_OK;
+  NEED(force3);
+  NEED(pos);
+  NEED(vel);
+  return rkd_binned(force3, comp_stride, nx, ny, nz, pos, vel, np, kick, drift, sort_workspace,
+                    sort_workspace_bytes, stats, stream);
+}
+
+int pmgb_tile_scatter_f32(const float *pos, const float *vel, const uint32_t *id, int64_t np,
+                          int nx, int ny, int nz, float *pos_out, float *vel_out,
+                          uint32_t *id_out, void *sort_workspace, size_t sort_workspace_bytes,
+                          pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  if (np > 0) {
+    NEED(pos);
+    NEED(pos_out);
+    NEED(id_out);
+    PMGB_REQUIRE((vel == nullptr) == (vel_out == nullptr), "vel and vel_out must both be given");
+    PMGB_REQUIRE(pos != pos_out && (!vel || vel != vel_out) && (!id || id != id_out),
+                 "the scatter cannot run in place");
+  }
+  return tile_scatter(pos, vel, id, np, nx, ny, nz, pos_out, vel_out, id_out, sort_workspace,
+                      sort_workspace_bytes, stream);
+}
+
+int pmgb_fpm_step_sorted_f32(float *pos, float *vel, uint32_t *id, float *pos_out, float *vel_out,
+                             uint32_t *id_out, int64_t np, int nx, int ny, int nz, float kick,
+                             float drift, float r_split, void *workspace, size_t workspace_bytes,
+                             void *sort_workspace, size_t sort_workspace_bytes, uint32_t *stats,
+                             pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  if (np > 0) {
+    NEED(pos);
+    NEED(vel);
+    NEED(id);
+    NEED(pos_out);
+    NEED(vel_out);
+    NEED(id_out);
+    PMGB_REQUIRE(pos != pos_out && vel != vel_out && id != id_out,
+                 "the sorted step writes to separate output buffers");
+  }
+  return fpm_step_sorted(pos, vel, id, pos_out, vel_out, id_out, np, nx, ny, nz, kick, drift,
+                         r_split, workspace, workspace_bytes, sort_workspace,
+                         sort_workspace_bytes, stats, stream);
+}
+
 int pmgb_linear_field_colour_f32(void *spec, int nx, int ny, int nz, float box_x, float box_y,
                                  float box_z, const float *table_k, const float *table_p,
                                  int n_table, float scale, pmgb_stream_t stream) {

@@ -40,134 +40,6 @@ paint_atomic_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
 }
 
 // ---------------------------------------------------------------------------
-// Binned painter.  A CTA takes a chunk of consecutive particles, finds the
-// box of cells they touch (unwrapped floor coordinates, so a chunk that
-// straddles the periodic boundary stays compact), accumulates into that box
-// in shared memory, then flushes the non-zero cells with coalesced global
-// atomics (cells consecutive along z go to consecutive addresses).  Particle
-// arrays kept in Lagrangian order (lattice bricks) give compact boxes; a
-// chunk whose box does not fit falls back to direct global atomics.
-// ---------------------------------------------------------------------------
-constexpr int BIN_THREADS = 256;
-constexpr int BIN_PER_THREAD = 8;
-constexpr int BIN_CHUNK = BIN_THREADS * BIN_PER_THREAD;
-constexpr int BIN_CAP = 16384;  // cells of the shared box (64 KB)
-
-__device__ __forceinline__ int warp_min(int v) {
-  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-__device__ __forceinline__ int warp_max(int v) {
-  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-
-__global__ void __launch_bounds__(BIN_THREADS)
-paint_binned_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
-                    const float *__restrict__ pos, int64_t np,
-                    const float *__restrict__ weights, float wscale) {
-  extern __shared__ float box[];
-  __shared__ int red[6][BIN_THREADS / 32];
-  __shared__ int bounds[6];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-
-  for (int64_t chunk = blockIdx.x; chunk * BIN_CHUNK < np; chunk += gridDim.x) {
-    const int64_t base = chunk * BIN_CHUNK;
-    float px[BIN_PER_THREAD], py[BIN_PER_THREAD], pz[BIN_PER_THREAD];
-    int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
-#pragma unroll
-    for (int j = 0; j < BIN_PER_THREAD; ++j) {
-      int64_t p = base + tid + j * BIN_THREADS;
-      if (p < np) {
-        load3(pos, p, px[j], py[j], pz[j]);
-        float f[3] = {floorf(px[j]), floorf(py[j]), floorf(pz[j])};
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          if (fabsf(f[d]) < 1e9f) {
-            lo[d] = min(lo[d], (int)f[d]);
-            hi[d] = max(hi[d], (int)f[d]);
-          } else {  // huge or non-finite: force the global-atomic fallback
-            lo[d] = INT_MIN / 2;
-            hi[d] = INT_MAX / 2;
-          }
-        }
-      }
-    }
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      int a = warp_min(lo[d]), b = warp_max(hi[d]);
-      if (lane == 0) { red[d][warp] = a; red[3 + d][warp] = b; }
-    }
-    __syncthreads();
-    if (tid < 6) {
-      int v = red[tid][0];
-      for (int w = 1; w < BIN_THREADS / 32; ++w)
-        v = tid < 3 ? min(v, red[tid][w]) : max(v, red[tid][w]);
-      bounds[tid] = v;
-    }
-    __syncthreads();
-    const int bx = bounds[0], by = bounds[1], bz = bounds[2];
-    // The box spans floor .. floor+1 on every axis.
-    const int64_t ex = (int64_t)bounds[3] - bx + 2;
-    const int64_t ey = (int64_t)bounds[4] - by + 2;
-    const int64_t ez = (int64_t)bounds[5] - bz + 2;
-    const bool fits = ex <= BIN_CAP && ey <= BIN_CAP && ez <= BIN_CAP &&
-                      ex * ey * ez <= BIN_CAP;
-    __syncthreads();  // everyone has read bounds[] before the next chunk
-
-    if (!fits) {
-#pragma unroll
-      for (int j = 0; j < BIN_PER_THREAD; ++j) {
-        int64_t p = base + tid + j * BIN_THREADS;
-        if (p >= np) continue;
-        float wp = weights ? __fmul_rn(wscale, __ldg(weights + p)) : wscale;
-        Axis ax = cic_axis(px[j], nx), ay = cic_axis(py[j], ny), az = cic_axis(pz[j], nz);
-#pragma unroll
-        for (int n = 0; n < 8; ++n) {
-          float w = __fmul_rn(wp, __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0,
-                                                      conn_y(n) ? ay.k1 : ay.k0),
-                                            conn_z(n) ? az.k1 : az.k0));
-          atomicAdd(mesh + cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
-                                      conn_z(n) ? az.i1 : az.i0, ny, nz), w);
-        }
-      }
-      continue;
-    }
-
-    const int vol = (int)(ex * ey * ez), eyz = (int)(ey * ez), ezi = (int)ez;
-    for (int q = tid; q < vol; q += BIN_THREADS) box[q] = 0.0f;
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < BIN_PER_THREAD; ++j) {
-      int64_t p = base + tid + j * BIN_THREADS;
-      if (p >= np) continue;
-      float wp = weights ? __fmul_rn(wscale, __ldg(weights + p)) : wscale;
-      float fx = floorf(px[j]), fy = floorf(py[j]), fz = floorf(pz[j]);
-      Axis ax = cic_axis(px[j], nx), ay = cic_axis(py[j], ny), az = cic_axis(pz[j], nz);
-      int lx = (int)fx - bx, ly = (int)fy - by, lz = (int)fz - bz;
-      int q0 = lx * eyz + ly * ezi + lz;
-#pragma unroll
-      for (int n = 0; n < 8; ++n) {
-        float w = __fmul_rn(wp, __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0,
-                                                    conn_y(n) ? ay.k1 : ay.k0),
-                                          conn_z(n) ? az.k1 : az.k0));
-        atomicAdd(box + q0 + conn_x(n) * eyz + conn_y(n) * ezi + conn_z(n), w);
-      }
-    }
-    __syncthreads();
-    for (int q = tid; q < vol; q += BIN_THREADS) {
-      float v = box[q];
-      if (v != 0.0f) {
-        int a = q / eyz, r = q - a * eyz, b = r / ezi, c = r - b * ezi;
-        int gx = wrap_index(bx + a, nx), gy = wrap_index(by + b, ny), gz = wrap_index(bz + c, nz);
-        atomicAdd(mesh + cell_index(gx, gy, gz, ny, nz), v);
-      }
-    }
-    __syncthreads();  // box is reused by the next chunk
-  }
-}
-
-// ---------------------------------------------------------------------------
 // Deterministic painter: every contribution is rounded to a signed 32.32
 // fixed-point integer and summed with 64-bit integer atomics, which are
 // associative, so the result does not depend on the order of arrival.
@@ -468,23 +340,8 @@ int paint(float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
     PMGB_LAUNCHED("paint_atomic_kernel");
     return PMGB_OK;
   }
-  if (mode == PMGB_PAINT_BINNED) {
-    static bool attr_set[64] = {false};
-    int dev = 0;
-    PMGB_CUDA(cudaGetDevice(&dev));
-    if (dev < 64 && !attr_set[dev]) {
-      PMGB_CUDA(cudaFuncSetAttribute(paint_binned_kernel,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     BIN_CAP * (int)sizeof(float)));
-      attr_set[dev] = true;
-    }
-    int64_t chunks = (np + BIN_CHUNK - 1) / BIN_CHUNK;
-    unsigned grid = (unsigned)std::min<int64_t>(chunks, (int64_t)sm_count() * 3);
-    paint_binned_kernel<<<grid, BIN_THREADS, BIN_CAP * sizeof(float), s>>>(
-        mesh, nx, ny, nz, pos, np, weights, wscale);
-    PMGB_LAUNCHED("paint_binned_kernel");
-    return PMGB_OK;
-  }
+  if (mode == PMGB_PAINT_BINNED) return paint_box(mesh, nx, ny, nz, pos, np, weights, wscale,
+                                                  nullptr, s);
   return fail(PMGB_ERR_INVALID_ARGUMENT, "unknown paint mode " + std::to_string(mode));
 }
 

@@ -1,0 +1,666 @@
+// Tile-sorted particle kernels: counting sort by mesh tile, shared-memory
+// box painting and box-staged gather + kick + drift.
+//
+// Particles are kept physically ordered by the 8^3-cell mesh tile that holds
+// them (tiles in Morton order), so a CTA's chunk of consecutive particles
+// covers a compact box of cells.  The painter accumulates that box in shared
+// memory and flushes it with 16-byte vector atomics; the gather stages the
+// box of the three force meshes in shared memory and interpolates from
+// there.  The sort is a counting sort: the gather kernel, which computes the
+// new positions, also counts them per tile and records each particle's rank
+// in its tile (warp-aggregated atomics); an exclusive scan turns counts into
+// offsets; a scatter pass moves (pos, vel, id) to offset + rank.
+//
+// Reference semantics are unchanged: every particle's CIC indices and
+// weights are computed exactly as in jaxpm/painting.py:21-37 (common.cuh)
+// from its own unwrapped position; the box only changes where partial sums
+// are accumulated and where mesh values are read from.
+#include <algorithm>
+
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace pmgb {
+
+constexpr int TILE = 8;               // cells per tile edge
+constexpr int BOX_THREADS = 256;
+constexpr int PAINT_PER_THREAD = 8;   // paint chunk: 2048 particles
+constexpr int PAINT_CHUNK = BOX_THREADS * PAINT_PER_THREAD;
+constexpr int PAINT_CAP = 16384;      // cells of the paint box (64 KB)
+constexpr int READ_PER_THREAD = 4;    // gather chunk: 1024 particles
+constexpr int READ_CHUNK = BOX_THREADS * READ_PER_THREAD;
+constexpr int READ_CAP = 6144;        // cells of the gather box (float4 each, 96 KB)
+
+// ---------------------------------------------------------------------------
+// tile keys
+// ---------------------------------------------------------------------------
+__host__ __device__ inline int tile_bits(int nx, int ny, int nz) {
+  int t = std::max(std::max((nx + TILE - 1) / TILE, (ny + TILE - 1) / TILE), (nz + TILE - 1) / TILE);
+  int b = 0;
+  while ((1 << b) < t) ++b;
+  return b;
+}
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+  v &= 0x3ff;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+// Morton key of the tile holding the (wrapped) cell of position (x, y, z).
+__device__ __forceinline__ uint32_t tile_key(float x, float y, float z, int nx, int ny, int nz) {
+  uint32_t tx = wrap_index((int)floorf(x), nx) / TILE;
+  uint32_t ty = wrap_index((int)floorf(y), ny) / TILE;
+  uint32_t tz = wrap_index((int)floorf(z), nz) / TILE;
+  return (spread3(tx) << 2) | (spread3(ty) << 1) | spread3(tz);
+}
+
+// Warp-aggregated count of `key` (valid lanes only); returns the lane's rank
+// among the particles of that key counted so far.
+__device__ __forceinline__ uint32_t count_and_rank(unsigned *__restrict__ counts, uint32_t key,
+                                                   unsigned active) {
+  const int lane = threadIdx.x & 31;
+  unsigned peers = __match_any_sync(active, key);
+  int leader = __ffs(peers) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(counts + key, (unsigned)__popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+// ---------------------------------------------------------------------------
+// chunk boxes in coordinates relative to a reference cell (so a chunk that
+// straddles the periodic boundary, or whose particles carry different
+// numbers of box lengths, stays compact)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int rel_coord(int f, int r, int n) {
+  int d = (f - r) % n;
+  if (d < 0) d += n;
+  if (d >= (n + 1) / 2) d -= n;  // into [-(n/2), (n+1)/2)
+  return d;
+}
+
+struct BoxGeom {
+  int rx, ry, rz;  // reference cell (unwrapped floor of the chunk's first particle)
+  int lx, ly, lz;  // relative coordinate of box cell 0
+  int ex, ey, ez;  // extents
+  bool fits;
+};
+
+template <int NWARPS>
+__device__ BoxGeom chunk_box(int lo0, int lo1, int lo2, int hi0, int hi1, int hi2, int rx,
+                             int ry, int rz, int cap, int zalign, int nz) {
+  __shared__ int red[6][NWARPS];
+  __shared__ int fin[6];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int v[6] = {lo0, lo1, lo2, hi0, hi1, hi2};
+#pragma unroll
+  for (int d = 0; d < 6; ++d) {
+    int x = v[d];
+    for (int o = 16; o > 0; o >>= 1) {
+      int y = __shfl_xor_sync(0xffffffffu, x, o);
+      x = d < 3 ? min(x, y) : max(x, y);
+    }
+    if (lane == 0) red[d][warp] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    int d = threadIdx.x, x = red[d][0];
+    for (int w = 1; w < NWARPS; ++w) x = d < 3 ? min(x, red[d][w]) : max(x, red[d][w]);
+    fin[d] = x;
+  }
+  __syncthreads();
+  BoxGeom g;
+  g.rx = rx; g.ry = ry; g.rz = rz;
+  g.lx = fin[0]; g.ly = fin[1]; g.lz = fin[2];
+  if (zalign > 1) {  // start the box on a z-cell that is a multiple of zalign
+    int gz = ((rz + g.lz) % nz + nz) % nz;
+    g.lz -= gz % zalign;
+  }
+  int64_t ex = (int64_t)fin[3] - g.lx + 2, ey = (int64_t)fin[4] - g.ly + 2,
+          ez = (int64_t)fin[5] - g.lz + 2;
+  if (zalign > 1) ez = (ez + zalign - 1) / zalign * zalign;
+  g.fits = ex <= cap && ey <= cap && ez <= cap && ex * ey * ez <= cap;
+  g.ex = (int)(ex < cap ? ex : cap);
+  g.ey = (int)(ey < cap ? ey : cap);
+  g.ez = (int)(ez < cap ? ez : cap);
+  __syncthreads();  // red/fin are reused by the next call
+  return g;
+}
+
+// Relative floor coordinates of a particle w.r.t. the reference cell; a
+// non-finite or huge coordinate forces the chunk out of the box path.
+__device__ __forceinline__ void rel_bounds(float x, int r, int n, int &lo, int &hi, int &rel) {
+  float f = floorf(x);
+  if (fabsf(f) < 1e9f) {
+    rel = rel_coord((int)f, r, n);
+    lo = min(lo, rel);
+    hi = max(hi, rel);
+  } else {
+    rel = 0;
+    lo = INT_MIN / 4;
+    hi = INT_MAX / 4;
+  }
+}
+
+__device__ __forceinline__ int ref_floor(float x) {
+  float f = floorf(x);
+  return fabsf(f) < 1e9f ? (int)f : 0;
+}
+
+// ---------------------------------------------------------------------------
+// Box painter (PMGB_PAINT_BINNED).  Works for particles in any order; it is
+// fast when they are tile sorted, because a chunk's box is then small.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(BOX_THREADS)
+paint_box_kernel(float *__restrict__ mesh, int nx, int ny, int nz, const float *__restrict__ pos,
+                 int64_t np, const float *__restrict__ weights, float wscale,
+                 unsigned *__restrict__ stats, int zal) {
+  // zal = 4: flush with 16-byte atomics (nz % 4 == 0, mesh 16-byte aligned)
+  extern __shared__ float box[];
+  const int tid = threadIdx.x;
+  for (int64_t chunk = blockIdx.x; chunk * PAINT_CHUNK < np; chunk += gridDim.x) {
+    const int64_t base = chunk * PAINT_CHUNK;
+    const int rx = ref_floor(__ldg(pos + 3 * base)), ry = ref_floor(__ldg(pos + 3 * base + 1)),
+              rz = ref_floor(__ldg(pos + 3 * base + 2));
+    float px[PAINT_PER_THREAD], py[PAINT_PER_THREAD], pz[PAINT_PER_THREAD];
+    int qx[PAINT_PER_THREAD], qy[PAINT_PER_THREAD], qz[PAINT_PER_THREAD];
+    int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
+#pragma unroll
+    for (int j = 0; j < PAINT_PER_THREAD; ++j) {
+      int64_t p = base + tid + j * BOX_THREADS;
+      if (p < np) {
+        load3(pos, p, px[j], py[j], pz[j]);
+        rel_bounds(px[j], rx, nx, lo[0], hi[0], qx[j]);
+        rel_bounds(py[j], ry, ny, lo[1], hi[1], qy[j]);
+        rel_bounds(pz[j], rz, nz, lo[2], hi[2], qz[j]);
+      }
+    }
+    BoxGeom g = chunk_box<BOX_THREADS / 32>(lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], rx, ry, rz,
+                                            PAINT_CAP, zal, nz);
+    if (!g.fits) {
+      if (stats && tid == 0) atomicAdd(stats, 1u);
+#pragma unroll
+      for (int j = 0; j < PAINT_PER_THREAD; ++j) {
+        int64_t p = base + tid + j * BOX_THREADS;
+        if (p >= np) continue;
+        float wp = weights ? __fmul_rn(wscale, __ldg(weights + p)) : wscale;
+        Axis ax = cic_axis(px[j], nx), ay = cic_axis(py[j], ny), az = cic_axis(pz[j], nz);
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          float w = __fmul_rn(wp, __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0,
+                                                      conn_y(n) ? ay.k1 : ay.k0),
+                                            conn_z(n) ? az.k1 : az.k0));
+          atomicAdd(mesh + cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
+                                      conn_z(n) ? az.i1 : az.i0, ny, nz), w);
+        }
+      }
+      continue;
+    }
+    const int eyz = g.ey * g.ez, vol = g.ex * eyz;
+    for (int q = tid; q < vol; q += BOX_THREADS) box[q] = 0.0f;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < PAINT_PER_THREAD; ++j) {
+      int64_t p = base + tid + j * BOX_THREADS;
+      if (p >= np) continue;
+      float wp = weights ? __fmul_rn(wscale, __ldg(weights + p)) : wscale;
+      Axis ax = cic_axis(px[j], nx), ay = cic_axis(py[j], ny), az = cic_axis(pz[j], nz);
+      int q0 = ((qx[j] - g.lx) * g.ey + (qy[j] - g.ly)) * g.ez + (qz[j] - g.lz);
+#pragma unroll
+      for (int n = 0; n < 8; ++n) {
+        float w = __fmul_rn(wp, __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0,
+                                                    conn_y(n) ? ay.k1 : ay.k0),
+                                          conn_z(n) ? az.k1 : az.k0));
+        atomicAdd(box + q0 + conn_x(n) * eyz + conn_y(n) * g.ez + conn_z(n), w);
+      }
+    }
+    __syncthreads();
+    if (zal == 4) {
+      // flush groups of four z-consecutive cells with one 16-byte atomic
+      const int ez4 = g.ez >> 2, groups = g.ex * g.ey * ez4;
+      for (int q = tid; q < groups; q += BOX_THREADS) {
+        int c4 = q % ez4, r = q / ez4, b = r % g.ey, a = r / g.ey;
+        const float4 v = *reinterpret_cast<const float4 *>(box + (a * g.ey + b) * g.ez + 4 * c4);
+        if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
+          int gx = wrap_index(rx + g.lx + a, nx), gy = wrap_index(ry + g.ly + b, ny);
+          int gz = wrap_index(rz + g.lz + 4 * c4, nz);
+          atomicAdd(reinterpret_cast<float4 *>(mesh + cell_index(gx, gy, gz, ny, nz)), v);
+        }
+      }
+    } else {
+      for (int q = tid; q < vol; q += BOX_THREADS) {
+        float v = box[q];
+        if (v != 0.0f) {
+          int c = q % g.ez, r = q / g.ez, b = r % g.ey, a = r / g.ey;
+          atomicAdd(mesh + cell_index(wrap_index(rx + g.lx + a, nx), wrap_index(ry + g.ly + b, ny),
+                                      wrap_index(rz + g.lz + c, nz), ny, nz), v);
+        }
+      }
+    }
+    __syncthreads();  // the box is reused by the next chunk
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Box-staged gather + kick + drift, with the tile histogram of the new
+// positions and each particle's rank in its new tile.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(BOX_THREADS)
+rkd_box_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int nz,
+               float *__restrict__ pos, float *__restrict__ vel, int64_t np, float kick,
+               float drift, unsigned *__restrict__ counts, unsigned *__restrict__ rank,
+               unsigned *__restrict__ stats) {
+  extern __shared__ float4 fbox[];
+  const int tid = threadIdx.x;
+  for (int64_t chunk = blockIdx.x; chunk * READ_CHUNK < np; chunk += gridDim.x) {
+    const int64_t base = chunk * READ_CHUNK;
+    const int rx = ref_floor(pos[3 * base]), ry = ref_floor(pos[3 * base + 1]),
+              rz = ref_floor(pos[3 * base + 2]);
+    float px[READ_PER_THREAD], py[READ_PER_THREAD], pz[READ_PER_THREAD];
+    int qx[READ_PER_THREAD], qy[READ_PER_THREAD], qz[READ_PER_THREAD];
+    int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
+#pragma unroll
+    for (int j = 0; j < READ_PER_THREAD; ++j) {
+      int64_t p = base + tid + j * BOX_THREADS;
+      if (p < np) {
+        px[j] = pos[3 * p]; py[j] = pos[3 * p + 1]; pz[j] = pos[3 * p + 2];
+        rel_bounds(px[j], rx, nx, lo[0], hi[0], qx[j]);
+        rel_bounds(py[j], ry, ny, lo[1], hi[1], qy[j]);
+        rel_bounds(pz[j], rz, nz, lo[2], hi[2], qz[j]);
+      }
+    }
+    BoxGeom g = chunk_box<BOX_THREADS / 32>(lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], rx, ry, rz,
+                                            READ_CAP, 1, nz);
+    const int eyz = g.ey * g.ez, vol = g.ex * eyz;
+    if (g.fits) {
+      for (int q = tid; q < vol; q += BOX_THREADS) {
+        int c = q % g.ez, r = q / g.ez, b = r % g.ey, a = r / g.ey;
+        int64_t cell = cell_index(wrap_index(rx + g.lx + a, nx), wrap_index(ry + g.ly + b, ny),
+                                  wrap_index(rz + g.lz + c, nz), ny, nz);
+        fbox[q] = make_float4(__ldg(f3 + cell), __ldg(f3 + cs + cell), __ldg(f3 + 2 * cs + cell),
+                              0.f);
+      }
+    } else if (stats && tid == 0) {
+      atomicAdd(stats + 1, 1u);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < READ_PER_THREAD; ++j) {
+      const int64_t p = base + tid + j * BOX_THREADS;
+      const bool valid = p < np;
+      uint32_t key = 0;
+      if (valid) {
+        Axis ax = cic_axis(px[j], nx), ay = cic_axis(py[j], ny), az = cic_axis(pz[j], nz);
+        float f0 = 0.f, f1 = 0.f, f2 = 0.f;
+        if (g.fits) {
+          int q0 = ((qx[j] - g.lx) * g.ey + (qy[j] - g.ly)) * g.ez + (qz[j] - g.lz);
+#pragma unroll
+          for (int n = 0; n < 8; ++n) {
+            float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                                conn_z(n) ? az.k1 : az.k0);
+            float4 f = fbox[q0 + conn_x(n) * eyz + conn_y(n) * g.ez + conn_z(n)];
+            f0 += f.x * w;
+            f1 += f.y * w;
+            f2 += f.z * w;
+          }
+        } else {
+#pragma unroll
+          for (int n = 0; n < 8; ++n) {
+            float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                                conn_z(n) ? az.k1 : az.k0);
+            int64_t c = cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
+                                   conn_z(n) ? az.i1 : az.i0, ny, nz);
+            f0 += __ldg(f3 + c) * w;
+            f1 += __ldg(f3 + cs + c) * w;
+            f2 += __ldg(f3 + 2 * cs + c) * w;
+          }
+        }
+        float vx = vel[3 * p] + kick * f0, vy = vel[3 * p + 1] + kick * f1,
+              vz = vel[3 * p + 2] + kick * f2;
+        vel[3 * p] = vx;
+        vel[3 * p + 1] = vy;
+        vel[3 * p + 2] = vz;
+        float x = px[j] + drift * vx, y = py[j] + drift * vy, z = pz[j] + drift * vz;
+        pos[3 * p] = x;
+        pos[3 * p + 1] = y;
+        pos[3 * p + 2] = z;
+        key = tile_key(x, y, z, nx, ny, nz);
+      }
+      if (counts) {
+        unsigned active = __ballot_sync(0xffffffffu, valid);
+        if (valid) rank[p] = count_and_rank(counts, key, active);
+      }
+    }
+    __syncthreads();  // fbox is reused by the next chunk
+  }
+}
+
+// Histogram + rank of the current positions (the first sort of a run).
+__global__ void __launch_bounds__(256)
+tile_rank_kernel(const float *__restrict__ pos, int64_t np, int nx, int ny, int nz,
+                 unsigned *__restrict__ counts, unsigned *__restrict__ rank) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  // every lane of a warp runs the same number of iterations (match/shfl)
+  for (int64_t p0 = blockIdx.x * (int64_t)blockDim.x; p0 < np; p0 += stride) {
+    int64_t p = p0 + threadIdx.x;
+    bool valid = p < np;
+    uint32_t key = 0;
+    if (valid) key = tile_key(__ldg(pos + 3 * p), __ldg(pos + 3 * p + 1), __ldg(pos + 3 * p + 2),
+                              nx, ny, nz);
+    unsigned active = __ballot_sync(0xffffffffu, valid);
+    if (valid) rank[p] = count_and_rank(counts, key, active);
+  }
+}
+
+// Moves particle p to offsets[key] + rank[p] (pos, vel, id).
+__global__ void __launch_bounds__(256)
+scatter_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
+               const unsigned *__restrict__ id, const unsigned *__restrict__ rank, int64_t np,
+               int nx, int ny, int nz, const unsigned *__restrict__ offsets,
+               float *__restrict__ pos2, float *__restrict__ vel2, unsigned *__restrict__ id2) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    float x = __ldg(pos + 3 * p), y = __ldg(pos + 3 * p + 1), z = __ldg(pos + 3 * p + 2);
+    uint32_t key = tile_key(x, y, z, nx, ny, nz);
+    int64_t d = (int64_t)__ldg(offsets + key) + __ldg(rank + p);
+    pos2[3 * d] = x;
+    pos2[3 * d + 1] = y;
+    pos2[3 * d + 2] = z;
+    if (vel) {
+      vel2[3 * d] = __ldg(vel + 3 * p);
+      vel2[3 * d + 1] = __ldg(vel + 3 * p + 1);
+      vel2[3 * d + 2] = __ldg(vel + 3 * p + 2);
+    }
+    id2[d] = id ? __ldg(id + p) : (unsigned)p;
+  }
+}
+
+// out[id[p]] = in[p] for [np][3] arrays (back to the caller's order).
+__global__ void unpermute3_kernel(const float *__restrict__ in, const unsigned *__restrict__ id,
+                                  int64_t np, float *__restrict__ out) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    int64_t d = __ldg(id + p);
+    if (d >= np) continue;  // not a permutation entry: skipped
+    out[3 * d] = __ldg(in + 3 * p);
+    out[3 * d + 1] = __ldg(in + 3 * p + 1);
+    out[3 * d + 2] = __ldg(in + 3 * p + 2);
+  }
+}
+
+// out[p] = in[id[p]] for [np][3] arrays (caller's order -> tile order).
+__global__ void permute3_kernel(const float *__restrict__ in, const unsigned *__restrict__ id,
+                                int64_t np, float *__restrict__ out) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    int64_t s = __ldg(id + p);
+    if (s >= np) continue;  // not a permutation entry: skipped
+    out[3 * p] = __ldg(in + 3 * s);
+    out[3 * p + 1] = __ldg(in + 3 * s + 1);
+    out[3 * p + 2] = __ldg(in + 3 * s + 2);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan of the tile counts (two levels: 4096 per block, then the
+// block totals in one block).
+// ---------------------------------------------------------------------------
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_PER_THREAD = 4;
+constexpr int SCAN_BLOCK = SCAN_THREADS * SCAN_PER_THREAD;
+
+__device__ unsigned block_exclusive_scan(unsigned v, unsigned *total) {
+  __shared__ unsigned warp_sums[SCAN_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned s = lane < SCAN_THREADS / 32 ? warp_sums[lane] : 0u;
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned y = __shfl_up_sync(0xffffffffu, s, o);
+      if (lane >= o) s += y;
+    }
+    if (lane < SCAN_THREADS / 32) warp_sums[lane] = s;
+  }
+  __syncthreads();
+  unsigned before = (warp > 0 ? warp_sums[warp - 1] : 0u) + x - v;
+  *total = warp_sums[SCAN_THREADS / 32 - 1];
+  __syncthreads();
+  return before;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+scan_blocks_kernel(const unsigned *__restrict__ in, unsigned *__restrict__ out, int64_t n,
+                   unsigned *__restrict__ sums) {
+  const int64_t b0 = (int64_t)blockIdx.x * SCAN_BLOCK + threadIdx.x * SCAN_PER_THREAD;
+  unsigned v[SCAN_PER_THREAD], s = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_PER_THREAD; ++i) {
+    v[i] = b0 + i < n ? in[b0 + i] : 0u;
+    s += v[i];
+  }
+  unsigned total;
+  unsigned run = block_exclusive_scan(s, &total);
+#pragma unroll
+  for (int i = 0; i < SCAN_PER_THREAD; ++i) {
+    if (b0 + i < n) out[b0 + i] = run;
+    run += v[i];
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+scan_sums_kernel(unsigned *__restrict__ sums, int nb) {
+  unsigned v[SCAN_PER_THREAD], s = 0;
+  const int b0 = threadIdx.x * SCAN_PER_THREAD;
+#pragma unroll
+  for (int i = 0; i < SCAN_PER_THREAD; ++i) {
+    v[i] = b0 + i < nb ? sums[b0 + i] : 0u;
+    s += v[i];
+  }
+  unsigned total;
+  unsigned run = block_exclusive_scan(s, &total);
+#pragma unroll
+  for (int i = 0; i < SCAN_PER_THREAD; ++i) {
+    if (b0 + i < nb) sums[b0 + i] = run;
+    run += v[i];
+  }
+}
+
+__global__ void scan_add_kernel(unsigned *__restrict__ out, int64_t n,
+                                const unsigned *__restrict__ sums) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] += sums[i / SCAN_BLOCK];
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+int64_t tile_key_count(int nx, int ny, int nz) { return (int64_t)1 << (3 * tile_bits(nx, ny, nz)); }
+
+static int set_smem(const void *fn, int bytes) {
+  PMGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  return PMGB_OK;
+}
+
+int paint_box(float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
+              const float *weights, float wscale, unsigned *stats, cudaStream_t s) {
+  static bool ready[64] = {false};
+  int dev = 0;
+  PMGB_CUDA(cudaGetDevice(&dev));
+  if (dev >= 64 || !ready[dev]) {
+    PMGB_TRY(set_smem((const void *)paint_box_kernel, PAINT_CAP * (int)sizeof(float)));
+    if (dev < 64) ready[dev] = true;
+  }
+  if (np == 0) return PMGB_OK;
+  const int zal = (nz % 4 == 0 && reinterpret_cast<uintptr_t>(mesh) % 16 == 0) ? 4 : 1;
+  int64_t chunks = (np + PAINT_CHUNK - 1) / PAINT_CHUNK;
+  unsigned grid = (unsigned)std::min<int64_t>(chunks, (int64_t)sm_count() * 3);
+  paint_box_kernel<<<grid, BOX_THREADS, PAINT_CAP * sizeof(float), s>>>(
+      mesh, nx, ny, nz, pos, np, weights, wscale, stats, zal);
+  PMGB_LAUNCHED("paint_box_kernel");
+  return PMGB_OK;
+}
+
+int rkd_box(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos, float *vel,
+            int64_t np, float kick, float drift, unsigned *counts, unsigned *rank,
+            unsigned *stats, cudaStream_t s) {
+  static bool ready[64] = {false};
+  int dev = 0;
+  PMGB_CUDA(cudaGetDevice(&dev));
+  if (dev >= 64 || !ready[dev]) {
+    PMGB_TRY(set_smem((const void *)rkd_box_kernel, READ_CAP * (int)sizeof(float4)));
+    if (dev < 64) ready[dev] = true;
+  }
+  if (np == 0) return PMGB_OK;
+  int64_t chunks = (np + READ_CHUNK - 1) / READ_CHUNK;
+  unsigned grid = (unsigned)std::min<int64_t>(chunks, (int64_t)sm_count() * 2);
+  rkd_box_kernel<<<grid, BOX_THREADS, READ_CAP * sizeof(float4), s>>>(
+      f3, cs, nx, ny, nz, pos, vel, np, kick, drift, counts, rank, stats);
+  PMGB_LAUNCHED("rkd_box_kernel");
+  return PMGB_OK;
+}
+
+int exclusive_scan(const unsigned *in, unsigned *out, int64_t n, unsigned *sums, cudaStream_t s) {
+  int64_t nb = (n + SCAN_BLOCK - 1) / SCAN_BLOCK;
+  if (nb > SCAN_BLOCK) return fail(PMGB_ERR_UNSUPPORTED, "too many tiles for the scan");
+  scan_blocks_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n, sums);
+  PMGB_LAUNCHED("scan_blocks_kernel");
+  if (nb > 1) {
+    scan_sums_kernel<<<1, SCAN_THREADS, 0, s>>>(sums, (int)nb);
+    PMGB_LAUNCHED("scan_sums_kernel");
+    scan_add_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, n, sums);
+    PMGB_LAUNCHED("scan_add_kernel");
+  }
+  return PMGB_OK;
+}
+
+// Scratch of the sort: counts, offsets, block sums (keys) and ranks (np).
+size_t sort_workspace_size(int nx, int ny, int nz, int64_t np) {
+  const size_t keys = (size_t)tile_key_count(nx, ny, nz);
+  auto a = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  return a(keys * 4) * 2 + a(((keys + SCAN_BLOCK - 1) / SCAN_BLOCK) * 4) + a((size_t)np * 4);
+}
+
+struct SortScratch {
+  unsigned *counts, *offsets, *sums, *rank;
+};
+
+static SortScratch sort_scratch(void *ws, int nx, int ny, int nz, int64_t np) {
+  const size_t keys = (size_t)tile_key_count(nx, ny, nz);
+  auto a = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  char *c = static_cast<char *>(ws);
+  SortScratch sc;
+  sc.counts = reinterpret_cast<unsigned *>(c);
+  c += a(keys * 4);
+  sc.offsets = reinterpret_cast<unsigned *>(c);
+  c += a(keys * 4);
+  sc.sums = reinterpret_cast<unsigned *>(c);
+  c += a(((keys + SCAN_BLOCK - 1) / SCAN_BLOCK) * 4);
+  sc.rank = reinterpret_cast<unsigned *>(c);
+  (void)np;
+  return sc;
+}
+
+int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np, int nx, int ny,
+              int nz, float *pos2, float *vel2, unsigned *id2, void *ws, size_t bytes,
+              cudaStream_t s) {
+  if (!ws || bytes < sort_workspace_size(nx, ny, nz, np))
+    return fail(PMGB_ERR_WORKSPACE, "tile sort needs " +
+                                        std::to_string(sort_workspace_size(nx, ny, nz, np)) +
+                                        " workspace bytes");
+  if (np == 0) return PMGB_OK;
+  const int64_t keys = tile_key_count(nx, ny, nz);
+  SortScratch sc = sort_scratch(ws, nx, ny, nz, np);
+  PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
+  tile_rank_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, np, nx, ny, nz, sc.counts, sc.rank);
+  PMGB_LAUNCHED("tile_rank_kernel");
+  PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, s));
+  scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
+                                                    sc.offsets, pos2, vel2, id2);
+  PMGB_LAUNCHED("scatter_kernel");
+  return PMGB_OK;
+}
+
+int unpermute3(const float *in, const unsigned *id, int64_t np, float *out, cudaStream_t s) {
+  if (np == 0) return PMGB_OK;
+  unpermute3_kernel<<<grid_for(np, 256), 256, 0, s>>>(in, id, np, out);
+  PMGB_LAUNCHED("unpermute3_kernel");
+  return PMGB_OK;
+}
+
+int permute3(const float *in, const unsigned *id, int64_t np, float *out, cudaStream_t s) {
+  if (np == 0) return PMGB_OK;
+  permute3_kernel<<<grid_for(np, 256), 256, 0, s>>>(in, id, np, out);
+  PMGB_LAUNCHED("permute3_kernel");
+  return PMGB_OK;
+}
+
+static int check_sort_ws(void *ws, size_t bytes, int nx, int ny, int nz, int64_t np) {
+  if (!ws || bytes < sort_workspace_size(nx, ny, nz, np))
+    return fail(PMGB_ERR_WORKSPACE, "the sorted path needs " +
+                                        std::to_string(sort_workspace_size(nx, ny, nz, np)) +
+                                        " sort workspace bytes");
+  return PMGB_OK;
+}
+
+// Box-staged gather + kick + drift; with a sort workspace it also counts the
+// new positions per tile and records each particle's rank in its tile.
+int rkd_binned(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos, float *vel,
+               int64_t np, float kick, float drift, void *sort_ws, size_t sort_bytes,
+               unsigned *stats, cudaStream_t s) {
+  unsigned *counts = nullptr, *rank = nullptr;
+  if (sort_ws) {
+    PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
+    SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
+    PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, tile_key_count(nx, ny, nz) * 4, s));
+    counts = sc.counts;
+    rank = sc.rank;
+  }
+  return rkd_box(f3, cs, nx, ny, nz, pos, vel, np, kick, drift, counts, rank, stats, s);
+}
+
+// Scan of the tile counts left by rkd_binned, then the scatter of
+// (pos, vel, id) to (pos2, vel2, id2) in tile order.
+int tile_scatter(const float *pos, const float *vel, const unsigned *id, int64_t np, int nx,
+                 int ny, int nz, float *pos2, float *vel2, unsigned *id2, void *sort_ws,
+                 size_t sort_bytes, cudaStream_t s) {
+  PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
+  const int64_t keys = tile_key_count(nx, ny, nz);
+  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
+  PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, s));
+  if (np > 0) {
+    scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
+                                                      sc.offsets, pos2, vel2, id2);
+    PMGB_LAUNCHED("scatter_kernel");
+  }
+  return PMGB_OK;
+}
+
+// One FastPM step on tile-sorted particles.  Reads (pos, vel, id), writes
+// the advanced state, sorted by the new positions, to (pos2, vel2, id2).
+// `mesh_ws` is the composite workspace (pm_workspace_size); `sort_ws` the
+// sort scratch; `stats` (nullable) counts chunks that left the box path.
+int fpm_step_sorted(float *pos, float *vel, unsigned *id, float *pos2, float *vel2,
+                    unsigned *id2, int64_t np, int nx, int ny, int nz, float kick, float drift,
+                    float r_split, void *mesh_ws, size_t mesh_bytes, void *sort_ws,
+                    size_t sort_bytes, unsigned *stats, cudaStream_t s) {
+  PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
+  float *f3 = nullptr;
+  PMGB_TRY(force_meshes_binned(pos, np, nx, ny, nz, r_split, mesh_ws, mesh_bytes, stats, &f3, s));
+  PMGB_TRY(rkd_binned(f3, (int64_t)nx * ny * nz, nx, ny, nz, pos, vel, np, kick, drift, sort_ws,
+                      sort_bytes, stats, s));
+  return tile_scatter(pos, vel, id, np, nx, ny, nz, pos2, vel2, id2, sort_ws, sort_bytes, s);
+}
+
+}  // namespace pmgb

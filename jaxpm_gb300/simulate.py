@@ -109,6 +109,135 @@ class FastPM:
         return (x, v), (gx, gv)
 
 
+class SortedFastPM:
+    """The fast FastPM loop: particles kept physically sorted by mesh tile.
+
+    ``load(pos, vel)`` sorts the caller's particles into internal
+    double-buffered arrays; ``step(i)`` runs one ``pmgb_fpm_step_sorted_f32``
+    (box paint, R2C, fused k-space kernel, batched C2R, box-staged gather +
+    kick + drift, tile counting sort); ``state()`` returns positions and
+    velocities in the caller's order.  ``stats`` counts the paint and gather
+    chunks whose cell box did not fit in shared memory."""
+
+    def __init__(self, mesh_shape, cosmo, a0, a1, n_steps, n_particles=None, r_split=0.0,
+                 device="cuda"):
+        self.mesh_shape = tuple(int(s) for s in mesh_shape)
+        self.n_steps = int(n_steps)
+        self.kick, self.drift = fpm_coefficients(cosmo, a0, a1, n_steps)
+        self.r_split = float(r_split)
+        n = int(np.prod(self.mesh_shape)) if n_particles is None else int(n_particles)
+        self.n = n
+        nx, ny, nz = self.mesh_shape
+        lib = _lib.load()
+        self.ws_bytes = lib.pmgb_pm_workspace_size(nx, ny, nz, n, _lib.PAINT_BINNED)
+        self.ws = _ws(self.ws_bytes, device)
+        self.sort_bytes = lib.pmgb_tile_sort_workspace_size(nx, ny, nz, n)
+        self.sort_ws = _ws(self.sort_bytes, device)
+        f = dict(dtype=torch.float32, device=device)
+        self.pos = [torch.empty((n, 3), **f), torch.empty((n, 3), **f)]
+        self.vel = [torch.empty((n, 3), **f), torch.empty((n, 3), **f)]
+        self.ids = [torch.empty(n, dtype=torch.int32, device=device) for _ in range(2)]
+        self.cur = 0
+        self.stats_buf = torch.zeros(2, dtype=torch.int32, device=device)
+
+    def load(self, pos, vel):
+        """Sorts ``pos``/``vel`` ([Np, 3], caller's order) into the engine."""
+        pos, vel = pos.contiguous(), vel.contiguous()
+        _lib.require_cuda(pos, vel)
+        if pos.numel() != 3 * self.n:
+            raise ValueError(f"expected {self.n} particles")
+        nx, ny, nz = self.mesh_shape
+        self.cur = 0
+        _lib.call("pmgb_tile_sort_f32", _lib.ptr(pos), _lib.ptr(vel), None, self.n, nx, ny, nz,
+                  _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]), _lib.ptr(self.ids[0]),
+                  _lib.ptr(self.sort_ws), self.sort_bytes, _lib.stream())
+        self.stats_buf.zero_()
+
+    def step(self, i, stream=None):
+        a, b = self.cur, 1 - self.cur
+        nx, ny, nz = self.mesh_shape
+        s = _lib.stream() if stream is None else stream
+        _lib.call("pmgb_fpm_step_sorted_f32", _lib.ptr(self.pos[a]), _lib.ptr(self.vel[a]),
+                  _lib.ptr(self.ids[a]), _lib.ptr(self.pos[b]), _lib.ptr(self.vel[b]),
+                  _lib.ptr(self.ids[b]), self.n, nx, ny, nz, float(self.kick[i]),
+                  float(self.drift[i]), self.r_split, _lib.ptr(self.ws), self.ws_bytes,
+                  _lib.ptr(self.sort_ws), self.sort_bytes, _lib.ptr(self.stats_buf), s)
+        self.cur = b
+
+    def run(self, steps=None):
+        for i in range(self.n_steps if steps is None else steps):
+            self.step(i)
+
+    @property
+    def positions(self):
+        """Current positions in tile order (for order-independent uses such
+        as painting the density)."""
+        return self.pos[self.cur]
+
+    @property
+    def ids_current(self):
+        return self.ids[self.cur]
+
+    def state(self):
+        """``(pos, vel)`` in the caller's order (new tensors)."""
+        out_p = torch.empty_like(self.pos[self.cur])
+        out_v = torch.empty_like(self.vel[self.cur])
+        s = _lib.stream()
+        for src, dst in ((self.pos[self.cur], out_p), (self.vel[self.cur], out_v)):
+            _lib.call("pmgb_unpermute3_f32", _lib.ptr(src), _lib.ptr(self.ids[self.cur]), self.n,
+                      _lib.ptr(dst), s)
+        return out_p, out_v
+
+    @property
+    def stats(self):
+        c = self.stats_buf.cpu().tolist()
+        return {"paint_chunks_global": c[0], "gather_chunks_global": c[1]}
+
+    def vjp(self, pos, vel, g_pos, g_vel, store=None):
+        """Forward run from ``(pos, vel)`` (caller's order) then the reverse
+        sweep; returns the final state and the cotangents of the initial
+        state, all in the caller's order.  Positions and particle ids before
+        every step are kept (``store``: preallocated ``([n,Np,3] float32,
+        [n,Np] int32)`` or allocated here).  Cotangents stay in the caller's
+        order and are gathered into each step's tile order for its adjoint."""
+        n = self.n_steps
+        nx, ny, nz = self.mesh_shape
+        if store is None:
+            store = (torch.empty((n, self.n, 3), dtype=torch.float32, device=self.ws.device),
+                     torch.empty((n, self.n), dtype=torch.int32, device=self.ws.device))
+        xs, ids = store
+        self.load(pos, vel)
+        for i in range(n):
+            xs[i].copy_(self.pos[self.cur])
+            ids[i].copy_(self.ids[self.cur])
+            self.step(i)
+        final = self.state()
+        gx, gv = g_pos.contiguous().clone(), g_vel.contiguous().clone()
+        if not hasattr(self, "_adj"):
+            e = lambda: torch.empty((self.n, 3), dtype=torch.float32, device=self.ws.device)  # noqa
+            self._adj = (e(), e(), e(), e())
+        sgx, sgv, ku, gp = self._adj
+        s = _lib.stream()
+        for i in reversed(range(n)):
+            _lib.call("pmgb_permute3_f32", _lib.ptr(gx), _lib.ptr(ids[i]), self.n, _lib.ptr(sgx), s)
+            _lib.call("pmgb_permute3_f32", _lib.ptr(gv), _lib.ptr(ids[i]), self.n, _lib.ptr(sgv), s)
+            # u = gv + drift*gx ; ku = kick*u ; gx += (dF/dx)^T ku ; gv = u
+            _lib.call("pmgb_lpt_combine_f32", _lib.ptr(sgv), _lib.ptr(sgx), 3 * self.n, 1.0,
+                      float(self.drift[i]), _lib.ptr(sgv), s)
+            _lib.call("pmgb_lpt_combine_f32", _lib.ptr(sgv), None, 3 * self.n,
+                      float(self.kick[i]), 0.0, _lib.ptr(ku), s)
+            _lib.call("pmgb_pm_forces_vjp_f32", _lib.ptr(xs[i]), self.n, nx, ny, nz, self.r_split,
+                      _lib.PAINT_BINNED, _lib.ptr(ku), _lib.ptr(gp), _lib.ptr(self.ws),
+                      self.ws_bytes, s)
+            _lib.call("pmgb_lpt_combine_f32", _lib.ptr(sgx), _lib.ptr(gp), 3 * self.n, 1.0, 1.0,
+                      _lib.ptr(sgx), s)
+            _lib.call("pmgb_unpermute3_f32", _lib.ptr(sgx), _lib.ptr(ids[i]), self.n,
+                      _lib.ptr(gx), s)
+            _lib.call("pmgb_unpermute3_f32", _lib.ptr(sgv), _lib.ptr(ids[i]), self.n,
+                      _lib.ptr(gv), s)
+        return final, (gx, gv)
+
+
 def _combine(x, y, cx, cy):
     out = torch.empty_like(x)
     _lib.call("pmgb_lpt_combine_f32", _lib.ptr(x), _lib.ptr(y), x.numel(), float(cx), float(cy),
