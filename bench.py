@@ -226,8 +226,12 @@ def run_gb300(args):
         else:
             px, pv = x, v
         rec(0)
-        _lib.call("pmgb_cic_paint_f32", P("mesh"), nx, ny, nz, _lib.ptr(px), Np, None, 1.0, mode,
-                  0, P("det"), det_bytes, s)
+        if engine == "sorted":
+            _lib.call("pmgb_cic_paint_sorted_f32", P("mesh"), nx, ny, nz, _lib.ptr(px), Np,
+                      _lib.ptr(eng.sort_ws), eng.sort_bytes, _lib.ptr(eng.stats_buf), s)
+        else:
+            _lib.call("pmgb_cic_paint_f32", P("mesh"), nx, ny, nz, _lib.ptr(px), Np, None, 1.0,
+                      mode, 0, P("det"), det_bytes, s)
         rec(1)
         _lib.call("pmgb_fft_r2c_f32", P("mesh"), P("dk"), nx, ny, nz, 1, s)
         rec(2)
@@ -307,7 +311,7 @@ def run_gb300(args):
               "phases_ms": phase_ms, "mass_rel_err": mass_err,
               "gpu_launches": launches_per_step * K}
     if engine == "sorted":
-        result["box_fallback_chunks"] = eng.stats
+        result["particles_outside_tile"] = eng.stats
 
     # roofline of the dominant own kernel
     peak, peak_kind = peaks()

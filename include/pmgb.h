@@ -266,12 +266,27 @@ int pmgb_unpermute3_f32(const float *in, const uint32_t *id, int64_t np,
 int pmgb_permute3_f32(const float *in, const uint32_t *id, int64_t np,
                       float *out, pmgb_stream_t stream);
 
-/* Box-staged gather + kick + drift (the sorted loop's read): each CTA
- * stages the cell box of its chunk of particles of the three force meshes
- * in shared memory and interpolates from there (global reads when the box
- * does not fit).  Same results as pmgb_read3_kick_drift_f32.  With a sort
- * workspace it also counts the new positions per tile and records each
- * particle's rank in its tile, for pmgb_tile_scatter_f32. */
+/* Paint of tile-sorted particles (the sorted loop's paint; mesh overwritten):
+ * one CTA per tile accumulates the tile plus a one-cell halo in shared
+ * memory from the particle range recorded in sort_workspace by the last
+ * pmgb_tile_sort_f32 / pmgb_tile_scatter_f32, then adds it to the mesh with
+ * 16-byte vector atomics.  Same result as pmgb_cic_paint_f32 up to the
+ * order of the float sums.  stats[0] (nullable) counts particles found
+ * outside their tile (stale ranges), which are painted with global
+ * atomics. */
+int pmgb_cic_paint_sorted_f32(float *mesh, int nx, int ny, int nz,
+                              const float *pos, int64_t np,
+                              void *sort_workspace,
+                              size_t sort_workspace_bytes, uint32_t *stats,
+                              pmgb_stream_t stream);
+
+/* Tile-staged gather + kick + drift of tile-sorted particles (the sorted
+ * loop's read): one CTA per tile stages the tile plus a one-cell halo of
+ * the three force meshes in shared memory and interpolates from there.
+ * Same results as pmgb_read3_kick_drift_f32.  It also counts the new
+ * positions per tile and records each particle's rank in its new tile in
+ * sort_workspace, for pmgb_tile_scatter_f32.  stats[1] (nullable) counts
+ * particles found outside their tile. */
 int pmgb_read3_kick_drift_binned_f32(const float *force3, int64_t comp_stride,
                                      int nx, int ny, int nz, float *pos,
                                      float *vel, int64_t np, float kick,

@@ -425,8 +425,21 @@ int pmgb_read3_kick_drift_binned_f32(const float *force3, int64_t comp_stride, i
   NEED(force3);
   NEED(pos);
   NEED(vel);
-  return rkd_binned(force3, comp_stride, nx, ny, nz, pos, vel, np, kick, drift, sort_workspace,
+  NEED(sort_workspace);
+  return rkd_sorted(force3, comp_stride, nx, ny, nz, pos, vel, np, kick, drift, sort_workspace,
                     sort_workspace_bytes, stats, stream);
+}
+
+int pmgb_cic_paint_sorted_f32(float *mesh, int nx, int ny, int nz, const float *pos,
+                              int64_t np, void *sort_workspace, size_t sort_workspace_bytes,
+                              uint32_t *stats, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  NEED(mesh);
+  NEED(sort_workspace);
+  if (np > 0) NEED(pos);
+  return paint_sorted(mesh, nx, ny, nz, pos, np, sort_workspace, sort_workspace_bytes, stats,
+                      stream);
 }
 
 int pmgb_tile_scatter_f32(const float *pos, const float *vel, const uint32_t *id, int64_t np,

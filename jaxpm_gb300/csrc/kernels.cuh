@@ -86,9 +86,6 @@ int lpt_combine(const float *a, const float *b, int64_t n, float ca, float cb,
 // sorted.cu
 int paint_box(float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
               const float *weights, float wscale, unsigned *stats, cudaStream_t s);
-int rkd_box(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos,
-            float *vel, int64_t np, float kick, float drift, unsigned *counts,
-            unsigned *rank, unsigned *stats, cudaStream_t s);
 int64_t tile_key_count(int nx, int ny, int nz);
 size_t sort_workspace_size(int nx, int ny, int nz, int64_t np);
 int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np,
@@ -98,7 +95,10 @@ int unpermute3(const float *in, const unsigned *id, int64_t np, float *out,
                cudaStream_t s);
 int permute3(const float *in, const unsigned *id, int64_t np, float *out,
              cudaStream_t s);
-int rkd_binned(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos,
+int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos,
+                 int64_t np, void *sort_ws, size_t sort_bytes, unsigned *stats,
+                 cudaStream_t s);
+int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos,
                float *vel, int64_t np, float kick, float drift, void *sort_ws,
                size_t sort_bytes, unsigned *stats, cudaStream_t s);
 int tile_scatter(const float *pos, const float *vel, const unsigned *id,
@@ -109,11 +109,12 @@ int fpm_step_sorted(float *pos, float *vel, unsigned *id, float *pos2,
                     int nz, float kick, float drift, float r_split,
                     void *mesh_ws, size_t mesh_bytes, void *sort_ws,
                     size_t sort_bytes, unsigned *stats, cudaStream_t s);
-// step.cu: paint (box painter) -> R2C -> k-space -> C2R inside the composite
-// workspace; *f3 receives the three force meshes.
-int force_meshes_binned(const float *pos, int64_t np, int nx, int ny, int nz,
-                        float r_split, void *ws, size_t bytes, unsigned *stats,
-                        float **f3, cudaStream_t s);
+// step.cu: paint of tile-sorted particles -> R2C -> k-space -> C2R inside the
+// composite workspace; *f3 receives the three force meshes.
+int force_meshes_sorted(const float *pos, int64_t np, int nx, int ny, int nz,
+                        float r_split, void *ws, size_t bytes, void *sort_ws,
+                        size_t sort_bytes, unsigned *stats, float **f3,
+                        cudaStream_t s);
 
 // pk.cu
 int power_spectrum(const void *spec, int nx, int ny, int nz, double bx,

@@ -27,9 +27,6 @@ constexpr int BOX_THREADS = 256;
 constexpr int PAINT_PER_THREAD = 8;   // paint chunk: 2048 particles
 constexpr int PAINT_CHUNK = BOX_THREADS * PAINT_PER_THREAD;
 constexpr int PAINT_CAP = 16384;      // cells of the paint box (64 KB)
-constexpr int READ_PER_THREAD = 4;    // gather chunk: 1024 particles
-constexpr int READ_CHUNK = BOX_THREADS * READ_PER_THREAD;
-constexpr int READ_CAP = 6144;        // cells of the gather box (float4 each, 96 KB)
 
 // ---------------------------------------------------------------------------
 // tile keys
@@ -56,6 +53,15 @@ __device__ __forceinline__ uint32_t tile_key(float x, float y, float z, int nx, 
   uint32_t ty = wrap_index((int)floorf(y), ny) / TILE;
   uint32_t tz = wrap_index((int)floorf(z), nz) / TILE;
   return (spread3(tx) << 2) | (spread3(ty) << 1) | spread3(tz);
+}
+
+__device__ __forceinline__ uint32_t compact3(uint32_t v) {
+  v &= 0x09249249u;
+  v = (v | (v >> 2)) & 0x030C30C3u;
+  v = (v | (v >> 4)) & 0x0300F00Fu;
+  v = (v | (v >> 8)) & 0x030000FFu;
+  v = (v | (v >> 16)) & 0x000003FFu;
+  return v;
 }
 
 // Warp-aggregated count of `key` (valid lanes only); returns the lane's rank
@@ -246,96 +252,159 @@ paint_box_kernel(float *__restrict__ mesh, int nx, int ny, int nz, const float *
 }
 
 // ---------------------------------------------------------------------------
-// Box-staged gather + kick + drift, with the tile histogram of the new
-// positions and each particle's rank in its new tile.
+// Tile kernels of the sorted loop.  Right after a sort, particles
+// offsets[k] .. offsets[k+1]-1 all have their (wrapped) cell inside tile k,
+// so one CTA per tile works on the fixed box tile + 1-cell halo:
+// 9 x 9 x 9 cells (the paint pads z to 12 for 16-byte flushes).  A particle
+// found outside its tile (only possible if the ranges are stale) takes the
+// global-memory path and is counted in stats.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(BOX_THREADS)
-rkd_box_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int nz,
-               float *__restrict__ pos, float *__restrict__ vel, int64_t np, float kick,
-               float drift, unsigned *__restrict__ counts, unsigned *__restrict__ rank,
-               unsigned *__restrict__ stats) {
-  extern __shared__ float4 fbox[];
+constexpr int TB = TILE + 1;         // box edge
+constexpr int TBZ_PAINT = 12;        // paint box z extent (multiple of 4)
+constexpr int TILE_THREADS = 256;
+
+__device__ __forceinline__ bool tile_local(float x, float y, float z, int ox, int oy, int oz,
+                                           int nx, int ny, int nz, int &lx, int &ly, int &lz) {
+  lx = wrap_index((int)floorf(x), nx) - ox;
+  ly = wrap_index((int)floorf(y), ny) - oy;
+  lz = wrap_index((int)floorf(z), nz) - oz;
+  return (unsigned)lx < (unsigned)TILE && (unsigned)ly < (unsigned)TILE &&
+         (unsigned)lz < (unsigned)TILE;
+}
+
+__global__ void __launch_bounds__(TILE_THREADS)
+paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
+                   const float *__restrict__ pos, const unsigned *__restrict__ offsets,
+                   uint32_t nkeys, unsigned *__restrict__ stats, int vec) {
+  __shared__ __align__(16) float box[TB * TB * TBZ_PAINT];
   const int tid = threadIdx.x;
-  for (int64_t chunk = blockIdx.x; chunk * READ_CHUNK < np; chunk += gridDim.x) {
-    const int64_t base = chunk * READ_CHUNK;
-    const int rx = ref_floor(pos[3 * base]), ry = ref_floor(pos[3 * base + 1]),
-              rz = ref_floor(pos[3 * base + 2]);
-    float px[READ_PER_THREAD], py[READ_PER_THREAD], pz[READ_PER_THREAD];
-    int qx[READ_PER_THREAD], qy[READ_PER_THREAD], qz[READ_PER_THREAD];
-    int lo[3] = {INT_MAX, INT_MAX, INT_MAX}, hi[3] = {INT_MIN, INT_MIN, INT_MIN};
+  for (uint32_t key = blockIdx.x; key < nkeys; key += gridDim.x) {
+    const unsigned beg = __ldg(offsets + key), end = __ldg(offsets + key + 1);
+    if (beg == end) continue;  // uniform across the CTA
+    const int ox = (int)compact3(key >> 2) * TILE, oy = (int)compact3(key >> 1) * TILE,
+              oz = (int)compact3(key) * TILE;
+    for (int q = tid; q < TB * TB * TBZ_PAINT; q += TILE_THREADS) box[q] = 0.f;
+    __syncthreads();
+    for (unsigned p = beg + tid; p < end; p += TILE_THREADS) {
+      float x = __ldg(pos + 3 * (int64_t)p), y = __ldg(pos + 3 * (int64_t)p + 1),
+            z = __ldg(pos + 3 * (int64_t)p + 2);
+      Axis ax = cic_axis(x, nx), ay = cic_axis(y, ny), az = cic_axis(z, nz);
+      int lx, ly, lz;
+      if (tile_local(x, y, z, ox, oy, oz, nx, ny, nz, lx, ly, lz)) {
+        const int q0 = (lx * TB + ly) * TBZ_PAINT + lz;
 #pragma unroll
-    for (int j = 0; j < READ_PER_THREAD; ++j) {
-      int64_t p = base + tid + j * BOX_THREADS;
-      if (p < np) {
-        px[j] = pos[3 * p]; py[j] = pos[3 * p + 1]; pz[j] = pos[3 * p + 2];
-        rel_bounds(px[j], rx, nx, lo[0], hi[0], qx[j]);
-        rel_bounds(py[j], ry, ny, lo[1], hi[1], qy[j]);
-        rel_bounds(pz[j], rz, nz, lo[2], hi[2], qz[j]);
+        for (int n = 0; n < 8; ++n) {
+          float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                              conn_z(n) ? az.k1 : az.k0);
+          atomicAdd(box + q0 + conn_x(n) * TB * TBZ_PAINT + conn_y(n) * TBZ_PAINT + conn_z(n), w);
+        }
+      } else {
+        if (stats) atomicAdd(stats, 1u);
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                              conn_z(n) ? az.k1 : az.k0);
+          atomicAdd(mesh + cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
+                                      conn_z(n) ? az.i1 : az.i0, ny, nz), w);
+        }
       }
-    }
-    BoxGeom g = chunk_box<BOX_THREADS / 32>(lo[0], lo[1], lo[2], hi[0], hi[1], hi[2], rx, ry, rz,
-                                            READ_CAP, 1, nz);
-    const int eyz = g.ey * g.ez, vol = g.ex * eyz;
-    if (g.fits) {
-      for (int q = tid; q < vol; q += BOX_THREADS) {
-        int c = q % g.ez, r = q / g.ez, b = r % g.ey, a = r / g.ey;
-        int64_t cell = cell_index(wrap_index(rx + g.lx + a, nx), wrap_index(ry + g.ly + b, ny),
-                                  wrap_index(rz + g.lz + c, nz), ny, nz);
-        fbox[q] = make_float4(__ldg(f3 + cell), __ldg(f3 + cs + cell), __ldg(f3 + 2 * cs + cell),
-                              0.f);
-      }
-    } else if (stats && tid == 0) {
-      atomicAdd(stats + 1, 1u);
     }
     __syncthreads();
-#pragma unroll
-    for (int j = 0; j < READ_PER_THREAD; ++j) {
-      const int64_t p = base + tid + j * BOX_THREADS;
-      const bool valid = p < np;
-      uint32_t key = 0;
-      if (valid) {
-        Axis ax = cic_axis(px[j], nx), ay = cic_axis(py[j], ny), az = cic_axis(pz[j], nz);
-        float f0 = 0.f, f1 = 0.f, f2 = 0.f;
-        if (g.fits) {
-          int q0 = ((qx[j] - g.lx) * g.ey + (qy[j] - g.ly)) * g.ez + (qz[j] - g.lz);
-#pragma unroll
-          for (int n = 0; n < 8; ++n) {
-            float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
-                                conn_z(n) ? az.k1 : az.k0);
-            float4 f = fbox[q0 + conn_x(n) * eyz + conn_y(n) * g.ez + conn_z(n)];
-            f0 += f.x * w;
-            f1 += f.y * w;
-            f2 += f.z * w;
-          }
-        } else {
-#pragma unroll
-          for (int n = 0; n < 8; ++n) {
-            float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
-                                conn_z(n) ? az.k1 : az.k0);
-            int64_t c = cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
-                                   conn_z(n) ? az.i1 : az.i0, ny, nz);
-            f0 += __ldg(f3 + c) * w;
-            f1 += __ldg(f3 + cs + c) * w;
-            f2 += __ldg(f3 + 2 * cs + c) * w;
-          }
+    if (vec) {
+      // 9 x 9 rows of three float4 groups; z groups start at oz + 4g
+      for (int q = tid; q < TB * TB * 3; q += TILE_THREADS) {
+        const int g = q % 3, r = q / 3, b = r % TB, a = r / TB;
+        const float4 v = *reinterpret_cast<const float4 *>(box + (a * TB + b) * TBZ_PAINT + 4 * g);
+        if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
+          int gx = wrap_index(ox + a, nx), gy = wrap_index(oy + b, ny),
+              gz = wrap_index(oz + 4 * g, nz);
+          atomicAdd(reinterpret_cast<float4 *>(mesh + cell_index(gx, gy, gz, ny, nz)), v);
         }
-        float vx = vel[3 * p] + kick * f0, vy = vel[3 * p + 1] + kick * f1,
-              vz = vel[3 * p + 2] + kick * f2;
-        vel[3 * p] = vx;
-        vel[3 * p + 1] = vy;
-        vel[3 * p + 2] = vz;
-        float x = px[j] + drift * vx, y = py[j] + drift * vy, z = pz[j] + drift * vz;
-        pos[3 * p] = x;
-        pos[3 * p + 1] = y;
-        pos[3 * p + 2] = z;
-        key = tile_key(x, y, z, nx, ny, nz);
       }
-      if (counts) {
-        unsigned active = __ballot_sync(0xffffffffu, valid);
-        if (valid) rank[p] = count_and_rank(counts, key, active);
+    } else {
+      for (int q = tid; q < TB * TB * TB; q += TILE_THREADS) {
+        const int c = q % TB, r = q / TB, b = r % TB, a = r / TB;
+        const float v = box[(a * TB + b) * TBZ_PAINT + c];
+        if (v != 0.f)
+          atomicAdd(mesh + cell_index(wrap_index(ox + a, nx), wrap_index(oy + b, ny),
+                                      wrap_index(oz + c, nz), ny, nz), v);
       }
     }
-    __syncthreads();  // fbox is reused by the next chunk
+    __syncthreads();  // the box is reused by the next tile
+  }
+}
+
+__global__ void __launch_bounds__(TILE_THREADS)
+rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int nz,
+                 float *__restrict__ pos, float *__restrict__ vel,
+                 const unsigned *__restrict__ offsets, uint32_t nkeys, float kick, float drift,
+                 unsigned *__restrict__ counts, unsigned *__restrict__ rank,
+                 unsigned *__restrict__ stats) {
+  __shared__ float4 fbox[TB * TB * TB];
+  const int tid = threadIdx.x;
+  for (uint32_t key = blockIdx.x; key < nkeys; key += gridDim.x) {
+    const unsigned beg = __ldg(offsets + key), end = __ldg(offsets + key + 1);
+    if (beg == end) continue;
+    const int ox = (int)compact3(key >> 2) * TILE, oy = (int)compact3(key >> 1) * TILE,
+              oz = (int)compact3(key) * TILE;
+    for (int q = tid; q < TB * TB * TB; q += TILE_THREADS) {
+      const int c = q % TB, r = q / TB, b = r % TB, a = r / TB;
+      const int64_t cell = cell_index(wrap_index(ox + a, nx), wrap_index(oy + b, ny),
+                                      wrap_index(oz + c, nz), ny, nz);
+      fbox[q] = make_float4(__ldg(f3 + cell), __ldg(f3 + cs + cell), __ldg(f3 + 2 * cs + cell), 0.f);
+    }
+    __syncthreads();
+    // every lane of a warp runs the same iterations (ballot / match inside)
+    for (unsigned p0 = beg; p0 < end; p0 += TILE_THREADS) {
+      const unsigned p = p0 + tid;
+      const bool valid = p < end;
+      uint32_t k = 0;
+      if (valid) {
+        const float x = pos[3 * (int64_t)p], y = pos[3 * (int64_t)p + 1], z = pos[3 * (int64_t)p + 2];
+        Axis ax = cic_axis(x, nx), ay = cic_axis(y, ny), az = cic_axis(z, nz);
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        int lx, ly, lz;
+        if (tile_local(x, y, z, ox, oy, oz, nx, ny, nz, lx, ly, lz)) {
+          const int q0 = (lx * TB + ly) * TB + lz;
+#pragma unroll
+          for (int n = 0; n < 8; ++n) {
+            float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                                conn_z(n) ? az.k1 : az.k0);
+            const float4 f = fbox[q0 + conn_x(n) * TB * TB + conn_y(n) * TB + conn_z(n)];
+            a0 += f.x * w;
+            a1 += f.y * w;
+            a2 += f.z * w;
+          }
+        } else {
+          if (stats) atomicAdd(stats + 1, 1u);
+#pragma unroll
+          for (int n = 0; n < 8; ++n) {
+            float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                                conn_z(n) ? az.k1 : az.k0);
+            const int64_t c = cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
+                                         conn_z(n) ? az.i1 : az.i0, ny, nz);
+            a0 += __ldg(f3 + c) * w;
+            a1 += __ldg(f3 + cs + c) * w;
+            a2 += __ldg(f3 + 2 * cs + c) * w;
+          }
+        }
+        const float vx = vel[3 * (int64_t)p] + kick * a0, vy = vel[3 * (int64_t)p + 1] + kick * a1,
+                    vz = vel[3 * (int64_t)p + 2] + kick * a2;
+        vel[3 * (int64_t)p] = vx;
+        vel[3 * (int64_t)p + 1] = vy;
+        vel[3 * (int64_t)p + 2] = vz;
+        const float nx_ = x + drift * vx, ny_ = y + drift * vy, nz_ = z + drift * vz;
+        pos[3 * (int64_t)p] = nx_;
+        pos[3 * (int64_t)p + 1] = ny_;
+        pos[3 * (int64_t)p + 2] = nz_;
+        k = tile_key(nx_, ny_, nz_, nx, ny, nz);
+      }
+      if (counts) {
+        const unsigned active = __ballot_sync(0xffffffffu, valid);
+        if (valid) rank[p] = count_and_rank(counts, k, active);
+      }
+    }
+    __syncthreads();  // fbox is reused by the next tile
   }
 }
 
@@ -456,6 +525,7 @@ scan_blocks_kernel(const unsigned *__restrict__ in, unsigned *__restrict__ out, 
     run += v[i];
   }
   if (threadIdx.x == 0) sums[blockIdx.x] = total;
+  if (gridDim.x == 1 && threadIdx.x == 0) out[n] = total;  // one block: the grand total
 }
 
 __global__ void __launch_bounds__(SCAN_THREADS)
@@ -477,10 +547,11 @@ scan_sums_kernel(unsigned *__restrict__ sums, int nb) {
 }
 
 __global__ void scan_add_kernel(unsigned *__restrict__ out, int64_t n,
-                                const unsigned *__restrict__ sums) {
+                                const unsigned *__restrict__ sums, unsigned grand_total) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
     out[i] += sums[i / SCAN_BLOCK];
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = grand_total;
 }
 
 // ---------------------------------------------------------------------------
@@ -512,26 +583,8 @@ int paint_box(float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
   return PMGB_OK;
 }
 
-int rkd_box(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos, float *vel,
-            int64_t np, float kick, float drift, unsigned *counts, unsigned *rank,
-            unsigned *stats, cudaStream_t s) {
-  static bool ready[64] = {false};
-  int dev = 0;
-  PMGB_CUDA(cudaGetDevice(&dev));
-  if (dev >= 64 || !ready[dev]) {
-    PMGB_TRY(set_smem((const void *)rkd_box_kernel, READ_CAP * (int)sizeof(float4)));
-    if (dev < 64) ready[dev] = true;
-  }
-  if (np == 0) return PMGB_OK;
-  int64_t chunks = (np + READ_CHUNK - 1) / READ_CHUNK;
-  unsigned grid = (unsigned)std::min<int64_t>(chunks, (int64_t)sm_count() * 2);
-  rkd_box_kernel<<<grid, BOX_THREADS, READ_CAP * sizeof(float4), s>>>(
-      f3, cs, nx, ny, nz, pos, vel, np, kick, drift, counts, rank, stats);
-  PMGB_LAUNCHED("rkd_box_kernel");
-  return PMGB_OK;
-}
-
-int exclusive_scan(const unsigned *in, unsigned *out, int64_t n, unsigned *sums, cudaStream_t s) {
+int exclusive_scan(const unsigned *in, unsigned *out, int64_t n, unsigned *sums,
+                   unsigned grand_total, cudaStream_t s) {
   int64_t nb = (n + SCAN_BLOCK - 1) / SCAN_BLOCK;
   if (nb > SCAN_BLOCK) return fail(PMGB_ERR_UNSUPPORTED, "too many tiles for the scan");
   scan_blocks_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n, sums);
@@ -539,24 +592,26 @@ int exclusive_scan(const unsigned *in, unsigned *out, int64_t n, unsigned *sums,
   if (nb > 1) {
     scan_sums_kernel<<<1, SCAN_THREADS, 0, s>>>(sums, (int)nb);
     PMGB_LAUNCHED("scan_sums_kernel");
-    scan_add_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, n, sums);
+    scan_add_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, n, sums, grand_total);
     PMGB_LAUNCHED("scan_add_kernel");
   }
   return PMGB_OK;
 }
 
-// Scratch of the sort: counts, offsets, block sums (keys) and ranks (np).
+// Scratch of the sort: tile counts (keys), tile offsets (keys + 1: the last
+// entry is the particle count), scan block sums, one rank per particle.
 size_t sort_workspace_size(int nx, int ny, int nz, int64_t np) {
   const size_t keys = (size_t)tile_key_count(nx, ny, nz);
   auto a = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  return a(keys * 4) * 2 + a(((keys + SCAN_BLOCK - 1) / SCAN_BLOCK) * 4) + a((size_t)np * 4);
+  return a(keys * 4) + a((keys + 1) * 4) + a(((keys + SCAN_BLOCK - 1) / SCAN_BLOCK) * 4) +
+         a((size_t)np * 4);
 }
 
 struct SortScratch {
   unsigned *counts, *offsets, *sums, *rank;
 };
 
-static SortScratch sort_scratch(void *ws, int nx, int ny, int nz, int64_t np) {
+static SortScratch sort_scratch(void *ws, int nx, int ny, int nz) {
   const size_t keys = (size_t)tile_key_count(nx, ny, nz);
   auto a = [](size_t b) { return (b + 255) & ~(size_t)255; };
   char *c = static_cast<char *>(ws);
@@ -564,31 +619,44 @@ static SortScratch sort_scratch(void *ws, int nx, int ny, int nz, int64_t np) {
   sc.counts = reinterpret_cast<unsigned *>(c);
   c += a(keys * 4);
   sc.offsets = reinterpret_cast<unsigned *>(c);
-  c += a(keys * 4);
+  c += a((keys + 1) * 4);
   sc.sums = reinterpret_cast<unsigned *>(c);
   c += a(((keys + SCAN_BLOCK - 1) / SCAN_BLOCK) * 4);
   sc.rank = reinterpret_cast<unsigned *>(c);
-  (void)np;
   return sc;
+}
+
+static int check_sort_ws(void *ws, size_t bytes, int nx, int ny, int nz, int64_t np) {
+  if (!ws || bytes < sort_workspace_size(nx, ny, nz, np))
+    return fail(PMGB_ERR_WORKSPACE, "the sorted path needs " +
+                                        std::to_string(sort_workspace_size(nx, ny, nz, np)) +
+                                        " sort workspace bytes");
+  if (reinterpret_cast<uintptr_t>(ws) % 256 != 0)
+    return fail(PMGB_ERR_WORKSPACE, "the sort workspace must be 256-byte aligned");
+  return PMGB_OK;
+}
+
+static unsigned tile_grid(int64_t keys) {
+  return (unsigned)std::min<int64_t>(keys, (int64_t)sm_count() * 8);
 }
 
 int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np, int nx, int ny,
               int nz, float *pos2, float *vel2, unsigned *id2, void *ws, size_t bytes,
               cudaStream_t s) {
-  if (!ws || bytes < sort_workspace_size(nx, ny, nz, np))
-    return fail(PMGB_ERR_WORKSPACE, "tile sort needs " +
-                                        std::to_string(sort_workspace_size(nx, ny, nz, np)) +
-                                        " workspace bytes");
-  if (np == 0) return PMGB_OK;
+  PMGB_TRY(check_sort_ws(ws, bytes, nx, ny, nz, np));
   const int64_t keys = tile_key_count(nx, ny, nz);
-  SortScratch sc = sort_scratch(ws, nx, ny, nz, np);
+  SortScratch sc = sort_scratch(ws, nx, ny, nz);
   PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
-  tile_rank_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, np, nx, ny, nz, sc.counts, sc.rank);
-  PMGB_LAUNCHED("tile_rank_kernel");
-  PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, s));
-  scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
-                                                    sc.offsets, pos2, vel2, id2);
-  PMGB_LAUNCHED("scatter_kernel");
+  if (np > 0) {
+    tile_rank_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, np, nx, ny, nz, sc.counts, sc.rank);
+    PMGB_LAUNCHED("tile_rank_kernel");
+  }
+  PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
+  if (np > 0) {
+    scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
+                                                      sc.offsets, pos2, vel2, id2);
+    PMGB_LAUNCHED("scatter_kernel");
+  }
   return PMGB_OK;
 }
 
@@ -606,39 +674,48 @@ int permute3(const float *in, const unsigned *id, int64_t np, float *out, cudaSt
   return PMGB_OK;
 }
 
-static int check_sort_ws(void *ws, size_t bytes, int nx, int ny, int nz, int64_t np) {
-  if (!ws || bytes < sort_workspace_size(nx, ny, nz, np))
-    return fail(PMGB_ERR_WORKSPACE, "the sorted path needs " +
-                                        std::to_string(sort_workspace_size(nx, ny, nz, np)) +
-                                        " sort workspace bytes");
+// Paint of tile-sorted particles (ranges from the last sort); the mesh is
+// overwritten.
+int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
+                 void *sort_ws, size_t sort_bytes, unsigned *stats, cudaStream_t s) {
+  PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
+  PMGB_CUDA(cudaMemsetAsync(mesh, 0, (size_t)nx * ny * nz * sizeof(float), s));
+  if (np == 0) return PMGB_OK;
+  const int64_t keys = tile_key_count(nx, ny, nz);
+  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz);
+  const int vec = (nz % 4 == 0 && reinterpret_cast<uintptr_t>(mesh) % 16 == 0) ? 1 : 0;
+  paint_tiles_kernel<<<tile_grid(keys), TILE_THREADS, 0, s>>>(mesh, nx, ny, nz, pos, sc.offsets,
+                                                              (uint32_t)keys, stats, vec);
+  PMGB_LAUNCHED("paint_tiles_kernel");
   return PMGB_OK;
 }
 
-// Box-staged gather + kick + drift; with a sort workspace it also counts the
-// new positions per tile and records each particle's rank in its tile.
-int rkd_binned(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos, float *vel,
+// Tile-staged gather + kick + drift of tile-sorted particles; counts the new
+// positions per tile and records each particle's rank in its new tile.
+int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos, float *vel,
                int64_t np, float kick, float drift, void *sort_ws, size_t sort_bytes,
                unsigned *stats, cudaStream_t s) {
-  unsigned *counts = nullptr, *rank = nullptr;
-  if (sort_ws) {
-    PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
-    SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
-    PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, tile_key_count(nx, ny, nz) * 4, s));
-    counts = sc.counts;
-    rank = sc.rank;
-  }
-  return rkd_box(f3, cs, nx, ny, nz, pos, vel, np, kick, drift, counts, rank, stats, s);
+  PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
+  const int64_t keys = tile_key_count(nx, ny, nz);
+  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz);
+  PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
+  if (np == 0) return PMGB_OK;
+  rkd_tiles_kernel<<<tile_grid(keys), TILE_THREADS, 0, s>>>(f3, cs, nx, ny, nz, pos, vel,
+                                                            sc.offsets, (uint32_t)keys, kick,
+                                                            drift, sc.counts, sc.rank, stats);
+  PMGB_LAUNCHED("rkd_tiles_kernel");
+  return PMGB_OK;
 }
 
-// Scan of the tile counts left by rkd_binned, then the scatter of
+// Scan of the tile counts left by rkd_sorted, then the scatter of
 // (pos, vel, id) to (pos2, vel2, id2) in tile order.
 int tile_scatter(const float *pos, const float *vel, const unsigned *id, int64_t np, int nx,
                  int ny, int nz, float *pos2, float *vel2, unsigned *id2, void *sort_ws,
                  size_t sort_bytes, cudaStream_t s) {
   PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
   const int64_t keys = tile_key_count(nx, ny, nz);
-  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
-  PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, s));
+  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz);
+  PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
   if (np > 0) {
     scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
                                                       sc.offsets, pos2, vel2, id2);
@@ -650,15 +727,17 @@ int tile_scatter(const float *pos, const float *vel, const unsigned *id, int64_t
 // One FastPM step on tile-sorted particles.  Reads (pos, vel, id), writes
 // the advanced state, sorted by the new positions, to (pos2, vel2, id2).
 // `mesh_ws` is the composite workspace (pm_workspace_size); `sort_ws` the
-// sort scratch; `stats` (nullable) counts chunks that left the box path.
+// sort scratch holding the ranges of the current order; `stats` (nullable)
+// counts particles found outside their tile (stale ranges).
 int fpm_step_sorted(float *pos, float *vel, unsigned *id, float *pos2, float *vel2,
                     unsigned *id2, int64_t np, int nx, int ny, int nz, float kick, float drift,
                     float r_split, void *mesh_ws, size_t mesh_bytes, void *sort_ws,
                     size_t sort_bytes, unsigned *stats, cudaStream_t s) {
   PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
   float *f3 = nullptr;
-  PMGB_TRY(force_meshes_binned(pos, np, nx, ny, nz, r_split, mesh_ws, mesh_bytes, stats, &f3, s));
-  PMGB_TRY(rkd_binned(f3, (int64_t)nx * ny * nz, nx, ny, nz, pos, vel, np, kick, drift, sort_ws,
+  PMGB_TRY(force_meshes_sorted(pos, np, nx, ny, nz, r_split, mesh_ws, mesh_bytes, sort_ws,
+                               sort_bytes, stats, &f3, s));
+  PMGB_TRY(rkd_sorted(f3, (int64_t)nx * ny * nz, nx, ny, nz, pos, vel, np, kick, drift, sort_ws,
                       sort_bytes, stats, s));
   return tile_scatter(pos, vel, id, np, nx, ny, nz, pos2, vel2, id2, sort_ws, sort_bytes, s);
 }

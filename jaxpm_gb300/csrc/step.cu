@@ -199,15 +199,15 @@ static int force_meshes(const float *pos, int64_t np, int nx, int ny, int nz, fl
   return PMGB_OK;
 }
 
-int force_meshes_binned(const float *pos, int64_t np, int nx, int ny, int nz, float r_split,
-                        void *ws, size_t bytes, unsigned *stats, float **f3, cudaStream_t s) {
+int force_meshes_sorted(const float *pos, int64_t np, int nx, int ny, int nz, float r_split,
+                        void *ws, size_t bytes, void *sort_ws, size_t sort_bytes,
+                        unsigned *stats, float **f3, cudaStream_t s) {
   Layout L = layout(nx, ny, nz, np, PMGB_PAINT_BINNED);
   PMGB_TRY(check_ws(ws, bytes, L));
   const int64_t ncell = (int64_t)nx * ny * nz;
   const int64_t nhalf = (int64_t)nx * ny * (nz / 2 + 1);
   float *mesh = WS(float, L.mesh);
-  PMGB_CUDA(cudaMemsetAsync(mesh, 0, ncell * sizeof(float), s));
-  if (np > 0) PMGB_TRY(paint_box(mesh, nx, ny, nz, pos, np, nullptr, 1.0f, stats, s));
+  PMGB_TRY(paint_sorted(mesh, nx, ny, nz, pos, np, sort_ws, sort_bytes, stats, s));
   PMGB_TRY(fft_r2c(mesh, WS(void, L.dk), nx, ny, nz, 1, s));
   PMGB_TRY(kspace_forces(WS(void, L.dk), WS(void, L.fk), nhalf, nx, ny, nz, r_split, 1, 0,
                          1.0f / (float)ncell, s));

@@ -117,7 +117,7 @@ class SortedFastPM:
     (box paint, R2C, fused k-space kernel, batched C2R, box-staged gather +
     kick + drift, tile counting sort); ``state()`` returns positions and
     velocities in the caller's order.  ``stats`` counts the paint and gather
-    chunks whose cell box did not fit in shared memory."""
+    particles found outside their tile (zero when the ranges are fresh)."""
 
     def __init__(self, mesh_shape, cosmo, a0, a1, n_steps, n_particles=None, r_split=0.0,
                  device="cuda"):
@@ -190,8 +190,10 @@ class SortedFastPM:
 
     @property
     def stats(self):
+        """Particles found outside their tile by the paint and the gather
+        (0 unless the tile ranges were stale)."""
         c = self.stats_buf.cpu().tolist()
-        return {"paint_chunks_global": c[0], "gather_chunks_global": c[1]}
+        return {"paint": c[0], "gather": c[1]}
 
     def vjp(self, pos, vel, g_pos, g_vel, store=None):
         """Forward run from ``(pos, vel)`` (caller's order) then the reverse
