@@ -268,12 +268,14 @@ int pmgb_permute3_f32(const float *in, const uint32_t *id, int64_t np,
 
 /* Paint of tile-sorted particles (the sorted loop's paint; mesh overwritten):
  * one CTA per tile accumulates the tile plus a one-cell halo in shared
- * memory from the particle range recorded in sort_workspace by the last
- * pmgb_tile_sort_f32 / pmgb_tile_scatter_f32, then adds it to the mesh with
- * 16-byte vector atomics.  Same result as pmgb_cic_paint_f32 up to the
- * order of the float sums.  stats[0] (nullable) counts particles found
- * outside their tile (stale ranges), which are painted with global
- * atomics. */
+ * memory (exact 24-bit fixed point with native 32-bit atomics) from the
+ * particle range recorded in sort_workspace by the last pmgb_tile_sort_f32 /
+ * pmgb_tile_scatter_f32, then adds the box to the mesh with one TMA bulk
+ * reduce-add (tiles whose box wraps around the mesh use 16-byte atomics).
+ * Same result as pmgb_cic_paint_f32 up to the order of the float sums.
+ * stats (nullable, 3 counters): [0] particles found outside their tile
+ * (stale ranges; painted with global atomics), [2] set if a wait on a TMA
+ * transfer reached its spin limit (the work was abandoned). */
 int pmgb_cic_paint_sorted_f32(float *mesh, int nx, int ny, int nz,
                               const float *pos, int64_t np,
                               void *sort_workspace,
@@ -282,11 +284,13 @@ int pmgb_cic_paint_sorted_f32(float *mesh, int nx, int ny, int nz,
 
 /* Tile-staged gather + kick + drift of tile-sorted particles (the sorted
  * loop's read): one CTA per tile stages the tile plus a one-cell halo of
- * the three force meshes in shared memory and interpolates from there.
+ * the three force meshes in shared memory (TMA bulk tensor loads, the next
+ * tile's box prefetched into a second buffer) and interpolates from there.
  * Same results as pmgb_read3_kick_drift_f32.  It also counts the new
  * positions per tile and records each particle's rank in its new tile in
- * sort_workspace, for pmgb_tile_scatter_f32.  stats[1] (nullable) counts
- * particles found outside their tile. */
+ * sort_workspace, for pmgb_tile_scatter_f32.  stats (nullable, 3
+ * counters): [1] particles found outside their tile, [2] set if a TMA wait
+ * reached its spin limit. */
 int pmgb_read3_kick_drift_binned_f32(const float *force3, int64_t comp_stride,
                                      int nx, int ny, int nz, float *pos,
                                      float *vel, int64_t np, float kick,
@@ -310,9 +314,9 @@ int pmgb_tile_scatter_f32(const float *pos, const float *vel,
  * (pos, vel, id) and writes the advanced state, sorted by the new
  * positions, to (pos_out, vel_out, id_out).  `workspace` is sized by
  * pmgb_pm_workspace_size(..., PMGB_PAINT_BINNED), `sort_workspace` by
- * pmgb_tile_sort_workspace_size.  stats (nullable, 2 counters the caller
- * zeroes) accumulates the paint and gather chunks whose cell box did not
- * fit in shared memory and took the global-memory path. */
+ * pmgb_tile_sort_workspace_size.  stats (nullable, 3 counters the caller
+ * zeroes): see pmgb_cic_paint_sorted_f32 and
+ * pmgb_read3_kick_drift_binned_f32. */
 int pmgb_fpm_step_sorted_f32(float *pos, float *vel, uint32_t *id,
                              float *pos_out, float *vel_out, uint32_t *id_out,
                              int64_t np, int nx, int ny, int nz, float kick,

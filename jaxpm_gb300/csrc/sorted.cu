@@ -16,9 +16,11 @@
 // from its own unwrapped position; the box only changes where partial sums
 // are accumulated and where mesh values are read from.
 #include <algorithm>
+#include <cstring>
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "tma.cuh"
 
 namespace pmgb {
 
@@ -254,14 +256,27 @@ paint_box_kernel(float *__restrict__ mesh, int nx, int ny, int nz, const float *
 // ---------------------------------------------------------------------------
 // Tile kernels of the sorted loop.  Right after a sort, particles
 // offsets[k] .. offsets[k+1]-1 all have their (wrapped) cell inside tile k,
-// so one CTA per tile works on the fixed box tile + 1-cell halo:
-// 9 x 9 x 9 cells (the paint pads z to 12 for 16-byte flushes).  A particle
+// so one CTA per tile works on the fixed box tile + 1-cell halo,
+// 9 x 9 x 9 cells, stored with a z stride of 12 so that a box row is a
+// whole number of 16-byte units (the TMA box is 12 x 9 x 9).  A particle
 // found outside its tile (only possible if the ranges are stale) takes the
-// global-memory path and is counted in stats.
+// global-memory path and is counted in stats[0] (paint) / stats[1] (gather).
+// An mbarrier wait that reaches its spin limit sets stats[2] and ends the
+// CTA's work.
+//
+// Interior tiles (box inside the mesh: ox+9 <= nx, oy+9 <= ny, oz+12 <= nz)
+// move their boxes with the Tensor Memory Accelerator: the paint flushes its
+// box with one cp.reduce.async.bulk.tensor add, and the gather prefetches
+// the next tile's force box with cp.async.bulk.tensor into the other of two
+// shared-memory buffers while it works on the current one.  Tiles on the
+// periodic boundary use plain loads and 16-byte atomics with wrapped
+// indices.
 // ---------------------------------------------------------------------------
-constexpr int TB = TILE + 1;         // box edge
-constexpr int TBZ_PAINT = 12;        // paint box z extent (multiple of 4)
+constexpr int TB = TILE + 1;   // box edge (cells)
+constexpr int TBZ = 12;        // z stride of a box row (16-byte multiple)
+constexpr int TBOX = TB * TB * TBZ;
 constexpr int TILE_THREADS = 256;
+constexpr float FIX_SCALE = 16777216.0f;  // 2^24: paint accumulates in 40.24 fixed point
 
 __device__ __forceinline__ bool tile_local(float x, float y, float z, int ox, int oy, int oz,
                                            int nx, int ny, int nz, int &lx, int &ly, int &lz) {
@@ -272,31 +287,53 @@ __device__ __forceinline__ bool tile_local(float x, float y, float z, int ox, in
          (unsigned)lz < (unsigned)TILE;
 }
 
+__device__ __forceinline__ bool box_interior(int ox, int oy, int oz, int nx, int ny, int nz) {
+  return ox + TB <= nx && oy + TB <= ny && oz + TBZ <= nz;
+}
+
+// Adds a signed fixed-point value into a two-word (hi:lo) shared
+// accumulator with native 32-bit atomics; the carry out of the low word is
+// detected from the returned old value, so the 64-bit sum is exact.
+__device__ __forceinline__ void fixed_add(unsigned *lo, int *hi, int c, float w) {
+  const long long q = __float2ll_rn(w * FIX_SCALE);
+  const unsigned ql = (unsigned)q;
+  const int qh = (int)(q >> 32);
+  const unsigned old = atomicAdd(lo + c, ql);
+  const int carry = (old + ql < old) ? 1 : 0;
+  if (qh + carry != 0) atomicAdd(hi + c, qh + carry);
+}
+
 __global__ void __launch_bounds__(TILE_THREADS)
 paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
                    const float *__restrict__ pos, const unsigned *__restrict__ offsets,
-                   uint32_t nkeys, unsigned *__restrict__ stats, int vec) {
-  __shared__ __align__(16) float box[TB * TB * TBZ_PAINT];
+                   uint32_t nkeys, unsigned *__restrict__ stats, int vec,
+                   const __grid_constant__ CUtensorMap tmap, int use_tma) {
+  __shared__ __align__(128) float fbox[TBOX];
+  __shared__ unsigned acc_lo[TBOX];
+  __shared__ int acc_hi[TBOX];
   const int tid = threadIdx.x;
   for (uint32_t key = blockIdx.x; key < nkeys; key += gridDim.x) {
     const unsigned beg = __ldg(offsets + key), end = __ldg(offsets + key + 1);
     if (beg == end) continue;  // uniform across the CTA
     const int ox = (int)compact3(key >> 2) * TILE, oy = (int)compact3(key >> 1) * TILE,
               oz = (int)compact3(key) * TILE;
-    for (int q = tid; q < TB * TB * TBZ_PAINT; q += TILE_THREADS) box[q] = 0.f;
+    for (int q = tid; q < TBOX; q += TILE_THREADS) {
+      acc_lo[q] = 0u;
+      acc_hi[q] = 0;
+    }
     __syncthreads();
     for (unsigned p = beg + tid; p < end; p += TILE_THREADS) {
-      float x = __ldg(pos + 3 * (int64_t)p), y = __ldg(pos + 3 * (int64_t)p + 1),
-            z = __ldg(pos + 3 * (int64_t)p + 2);
+      const float x = __ldg(pos + 3 * (int64_t)p), y = __ldg(pos + 3 * (int64_t)p + 1),
+                  z = __ldg(pos + 3 * (int64_t)p + 2);
       Axis ax = cic_axis(x, nx), ay = cic_axis(y, ny), az = cic_axis(z, nz);
       int lx, ly, lz;
       if (tile_local(x, y, z, ox, oy, oz, nx, ny, nz, lx, ly, lz)) {
-        const int q0 = (lx * TB + ly) * TBZ_PAINT + lz;
+        const int q0 = (lx * TB + ly) * TBZ + lz;
 #pragma unroll
         for (int n = 0; n < 8; ++n) {
           float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
                               conn_z(n) ? az.k1 : az.k0);
-          atomicAdd(box + q0 + conn_x(n) * TB * TBZ_PAINT + conn_y(n) * TBZ_PAINT + conn_z(n), w);
+          fixed_add(acc_lo, acc_hi, q0 + conn_x(n) * TB * TBZ + conn_y(n) * TBZ + conn_z(n), w);
         }
       } else {
         if (stats) atomicAdd(stats, 1u);
@@ -310,28 +347,64 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
       }
     }
     __syncthreads();
-    if (vec) {
-      // 9 x 9 rows of three float4 groups; z groups start at oz + 4g
+    for (int q = tid; q < TBOX; q += TILE_THREADS) {
+      const long long v = (long long)(((unsigned long long)(unsigned)acc_hi[q] << 32) | acc_lo[q]);
+      fbox[q] = (float)((double)v * (1.0 / 16777216.0));
+    }
+    const bool tma = use_tma && box_interior(ox, oy, oz, nx, ny, nz);
+    if (tma) fence_async_shared();  // generic-proxy writes of fbox -> TMA
+    __syncthreads();
+    if (tma) {
+      if (tid == 0) {
+        tma_reduce_add_3d(&tmap, oz, oy, ox, fbox);
+        bulk_commit();
+        bulk_wait_read();  // fbox may be rewritten after this
+      }
+    } else if (vec) {
+      // 9 x 9 rows of three 16-byte groups starting at z = oz, oz+4, oz+8
       for (int q = tid; q < TB * TB * 3; q += TILE_THREADS) {
         const int g = q % 3, r = q / 3, b = r % TB, a = r / TB;
-        const float4 v = *reinterpret_cast<const float4 *>(box + (a * TB + b) * TBZ_PAINT + 4 * g);
+        const float4 v = *reinterpret_cast<const float4 *>(fbox + (a * TB + b) * TBZ + 4 * g);
         if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
-          int gx = wrap_index(ox + a, nx), gy = wrap_index(oy + b, ny),
-              gz = wrap_index(oz + 4 * g, nz);
+          const int gx = wrap_index(ox + a, nx), gy = wrap_index(oy + b, ny),
+                    gz = wrap_index(oz + 4 * g, nz);
           atomicAdd(reinterpret_cast<float4 *>(mesh + cell_index(gx, gy, gz, ny, nz)), v);
         }
       }
     } else {
       for (int q = tid; q < TB * TB * TB; q += TILE_THREADS) {
         const int c = q % TB, r = q / TB, b = r % TB, a = r / TB;
-        const float v = box[(a * TB + b) * TBZ_PAINT + c];
+        const float v = fbox[(a * TB + b) * TBZ + c];
         if (v != 0.f)
           atomicAdd(mesh + cell_index(wrap_index(ox + a, nx), wrap_index(oy + b, ny),
                                       wrap_index(oz + c, nz), ny, nz), v);
       }
     }
-    __syncthreads();  // the box is reused by the next tile
+    __syncthreads();  // the boxes are reused by the next tile
   }
+  if (use_tma && tid == 0) bulk_wait_all();  // reductions complete before the kernel ends
+}
+
+constexpr int FBOX = 3 * TBOX;  // three force components, [c][x][y][z(12)]
+constexpr uint32_t FBOX_BYTES = FBOX * sizeof(float);
+constexpr int FBOX_STRIDE = (FBOX + 31) / 32 * 32;  // buffers 128-byte aligned
+
+struct TileInfo {
+  unsigned beg, end;
+  int ox, oy, oz;
+  bool tma;
+};
+
+__device__ __forceinline__ TileInfo tile_info(const unsigned *__restrict__ offsets, uint32_t key,
+                                              int nx, int ny, int nz, int use_tma) {
+  TileInfo t;
+  t.beg = __ldg(offsets + key);
+  t.end = __ldg(offsets + key + 1);
+  t.ox = (int)compact3(key >> 2) * TILE;
+  t.oy = (int)compact3(key >> 1) * TILE;
+  t.oz = (int)compact3(key) * TILE;
+  t.tma = use_tma && t.beg != t.end && box_interior(t.ox, t.oy, t.oz, nx, ny, nz);
+  return t;
 }
 
 __global__ void __launch_bounds__(TILE_THREADS)
@@ -339,72 +412,116 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
                  float *__restrict__ pos, float *__restrict__ vel,
                  const unsigned *__restrict__ offsets, uint32_t nkeys, float kick, float drift,
                  unsigned *__restrict__ counts, unsigned *__restrict__ rank,
-                 unsigned *__restrict__ stats) {
-  __shared__ float4 fbox[TB * TB * TB];
+                 unsigned *__restrict__ stats, const __grid_constant__ CUtensorMap tmap,
+                 int use_tma) {
+  __shared__ __align__(128) float fb[2][FBOX_STRIDE];
+  __shared__ __align__(8) uint64_t bar[2];
   const int tid = threadIdx.x;
-  for (uint32_t key = blockIdx.x; key < nkeys; key += gridDim.x) {
-    const unsigned beg = __ldg(offsets + key), end = __ldg(offsets + key + 1);
-    if (beg == end) continue;
-    const int ox = (int)compact3(key >> 2) * TILE, oy = (int)compact3(key >> 1) * TILE,
-              oz = (int)compact3(key) * TILE;
-    for (int q = tid; q < TB * TB * TB; q += TILE_THREADS) {
-      const int c = q % TB, r = q / TB, b = r % TB, a = r / TB;
-      const int64_t cell = cell_index(wrap_index(ox + a, nx), wrap_index(oy + b, ny),
-                                      wrap_index(oz + c, nz), ny, nz);
-      fbox[q] = make_float4(__ldg(f3 + cell), __ldg(f3 + cs + cell), __ldg(f3 + 2 * cs + cell), 0.f);
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_async_shared();
+  }
+  __syncthreads();
+  uint32_t phase0 = 0u, phase1 = 0u;  // parity of the next completion of bar[0] / bar[1]
+  const uint32_t stride = gridDim.x;
+  uint32_t key = blockIdx.x;
+  if (key >= nkeys) return;
+  TileInfo cur = tile_info(offsets, key, nx, ny, nz, use_tma);
+  if (cur.tma && tid == 0) {
+    mbar_expect_tx(&bar[0], FBOX_BYTES);
+    tma_load_4d(fb[0], &tmap, cur.oz, cur.oy, cur.ox, 0, &bar[0]);
+  }
+  int buf = 0;
+  for (; key < nkeys; key += stride) {
+    // prefetch the next tile's box into the other buffer (freed by the
+    // barrier at the end of the previous iteration)
+    const uint32_t knext = key + stride;
+    TileInfo nxt;
+    nxt.tma = false;
+    if (knext < nkeys) {
+      nxt = tile_info(offsets, knext, nx, ny, nz, use_tma);
+      if (nxt.tma && tid == 0) {
+        fence_async_shared();
+        mbar_expect_tx(&bar[buf ^ 1], FBOX_BYTES);
+        tma_load_4d(fb[buf ^ 1], &tmap, nxt.oz, nxt.oy, nxt.ox, 0, &bar[buf ^ 1]);
+      }
     }
-    __syncthreads();
-    // every lane of a warp runs the same iterations (ballot / match inside)
-    for (unsigned p0 = beg; p0 < end; p0 += TILE_THREADS) {
-      const unsigned p = p0 + tid;
-      const bool valid = p < end;
-      uint32_t k = 0;
-      if (valid) {
-        const float x = pos[3 * (int64_t)p], y = pos[3 * (int64_t)p + 1], z = pos[3 * (int64_t)p + 2];
-        Axis ax = cic_axis(x, nx), ay = cic_axis(y, ny), az = cic_axis(z, nz);
-        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-        int lx, ly, lz;
-        if (tile_local(x, y, z, ox, oy, oz, nx, ny, nz, lx, ly, lz)) {
-          const int q0 = (lx * TB + ly) * TB + lz;
-#pragma unroll
-          for (int n = 0; n < 8; ++n) {
-            float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
-                                conn_z(n) ? az.k1 : az.k0);
-            const float4 f = fbox[q0 + conn_x(n) * TB * TB + conn_y(n) * TB + conn_z(n)];
-            a0 += f.x * w;
-            a1 += f.y * w;
-            a2 += f.z * w;
-          }
-        } else {
-          if (stats) atomicAdd(stats + 1, 1u);
-#pragma unroll
-          for (int n = 0; n < 8; ++n) {
-            float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
-                                conn_z(n) ? az.k1 : az.k0);
-            const int64_t c = cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
-                                         conn_z(n) ? az.i1 : az.i0, ny, nz);
-            a0 += __ldg(f3 + c) * w;
-            a1 += __ldg(f3 + cs + c) * w;
-            a2 += __ldg(f3 + 2 * cs + c) * w;
-          }
+    if (cur.beg != cur.end) {
+      float *box = fb[buf];
+      if (cur.tma) {
+        const bool ok = mbar_wait(&bar[buf], buf ? phase1 : phase0);
+        if (__syncthreads_or(!ok)) {  // uniform: every thread leaves together
+          if (stats && tid == 0) atomicExch(stats + 2, 1u);
+          if (nxt.tma) mbar_wait(&bar[buf ^ 1], buf ? phase0 : phase1);  // drain the prefetch
+          return;
         }
-        const float vx = vel[3 * (int64_t)p] + kick * a0, vy = vel[3 * (int64_t)p + 1] + kick * a1,
-                    vz = vel[3 * (int64_t)p + 2] + kick * a2;
-        vel[3 * (int64_t)p] = vx;
-        vel[3 * (int64_t)p + 1] = vy;
-        vel[3 * (int64_t)p + 2] = vz;
-        const float nx_ = x + drift * vx, ny_ = y + drift * vy, nz_ = z + drift * vz;
-        pos[3 * (int64_t)p] = nx_;
-        pos[3 * (int64_t)p + 1] = ny_;
-        pos[3 * (int64_t)p + 2] = nz_;
-        k = tile_key(nx_, ny_, nz_, nx, ny, nz);
+        if (buf) phase1 ^= 1u; else phase0 ^= 1u;
+      } else {
+        for (int q = tid; q < 3 * TB * TB * TB; q += TILE_THREADS) {
+          const int c = q % TB, r = q / TB, b = r % TB, r2 = r / TB, a = r2 % TB, comp = r2 / TB;
+          const int64_t cell = cell_index(wrap_index(cur.ox + a, nx), wrap_index(cur.oy + b, ny),
+                                          wrap_index(cur.oz + c, nz), ny, nz);
+          box[((comp * TB + a) * TB + b) * TBZ + c] = __ldg(f3 + comp * cs + cell);
+        }
+        __syncthreads();
       }
-      if (counts) {
-        const unsigned active = __ballot_sync(0xffffffffu, valid);
-        if (valid) rank[p] = count_and_rank(counts, k, active);
+      // every lane of a warp runs the same iterations (ballot / match inside)
+      for (unsigned p0 = cur.beg; p0 < cur.end; p0 += TILE_THREADS) {
+        const unsigned p = p0 + tid;
+        const bool valid = p < cur.end;
+        uint32_t k = 0;
+        if (valid) {
+          const float x = pos[3 * (int64_t)p], y = pos[3 * (int64_t)p + 1],
+                      z = pos[3 * (int64_t)p + 2];
+          const float v0 = vel[3 * (int64_t)p], v1 = vel[3 * (int64_t)p + 1],
+                      v2 = vel[3 * (int64_t)p + 2];
+          Axis ax = cic_axis(x, nx), ay = cic_axis(y, ny), az = cic_axis(z, nz);
+          float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+          int lx, ly, lz;
+          if (tile_local(x, y, z, cur.ox, cur.oy, cur.oz, nx, ny, nz, lx, ly, lz)) {
+            const int q0 = (lx * TB + ly) * TBZ + lz;
+#pragma unroll
+            for (int n = 0; n < 8; ++n) {
+              float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                                  conn_z(n) ? az.k1 : az.k0);
+              const int q = q0 + conn_x(n) * TB * TBZ + conn_y(n) * TBZ + conn_z(n);
+              a0 += box[q] * w;
+              a1 += box[TBOX + q] * w;
+              a2 += box[2 * TBOX + q] * w;
+            }
+          } else {
+            if (stats) atomicAdd(stats + 1, 1u);
+#pragma unroll
+            for (int n = 0; n < 8; ++n) {
+              float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                                  conn_z(n) ? az.k1 : az.k0);
+              const int64_t c = cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
+                                           conn_z(n) ? az.i1 : az.i0, ny, nz);
+              a0 += __ldg(f3 + c) * w;
+              a1 += __ldg(f3 + cs + c) * w;
+              a2 += __ldg(f3 + 2 * cs + c) * w;
+            }
+          }
+          const float vx = v0 + kick * a0, vy = v1 + kick * a1, vz = v2 + kick * a2;
+          vel[3 * (int64_t)p] = vx;
+          vel[3 * (int64_t)p + 1] = vy;
+          vel[3 * (int64_t)p + 2] = vz;
+          const float xn = x + drift * vx, yn = y + drift * vy, zn = z + drift * vz;
+          pos[3 * (int64_t)p] = xn;
+          pos[3 * (int64_t)p + 1] = yn;
+          pos[3 * (int64_t)p + 2] = zn;
+          k = tile_key(xn, yn, zn, nx, ny, nz);
+        }
+        if (counts) {
+          const unsigned active = __ballot_sync(0xffffffffu, valid);
+          if (valid) rank[p] = count_and_rank(counts, k, active);
+        }
       }
     }
-    __syncthreads();  // fbox is reused by the next tile
+    __syncthreads();  // buffer `buf` is free for the prefetch two tiles ahead
+    cur = nxt;
+    buf ^= 1;
   }
 }
 
@@ -684,8 +801,19 @@ int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos, int64_t 
   const int64_t keys = tile_key_count(nx, ny, nz);
   SortScratch sc = sort_scratch(sort_ws, nx, ny, nz);
   const int vec = (nz % 4 == 0 && reinterpret_cast<uintptr_t>(mesh) % 16 == 0) ? 1 : 0;
-  paint_tiles_kernel<<<tile_grid(keys), TILE_THREADS, 0, s>>>(mesh, nx, ny, nz, pos, sc.offsets,
-                                                              (uint32_t)keys, stats, vec);
+  // TMA flush of interior tiles: a 3-D map over the mesh, box 12 x 9 x 9
+  CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  int use_tma = 0;
+  if (vec && nz >= TBZ && ny >= TB && nx >= TB) {
+    const uint64_t dims[3] = {(uint64_t)nz, (uint64_t)ny, (uint64_t)nx};
+    const uint64_t strides[2] = {(uint64_t)nz * 4, (uint64_t)ny * nz * 4};
+    const uint32_t box[3] = {TBZ, TB, TB};
+    use_tma = make_tensor_map(&map, mesh, 3, dims, strides, box) == PMGB_OK ? 1 : 0;
+    clear_error();
+  }
+  paint_tiles_kernel<<<tile_grid(keys), TILE_THREADS, 0, s>>>(
+      mesh, nx, ny, nz, pos, sc.offsets, (uint32_t)keys, stats, vec, map, use_tma);
   PMGB_LAUNCHED("paint_tiles_kernel");
   return PMGB_OK;
 }
@@ -700,9 +828,22 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos, 
   SortScratch sc = sort_scratch(sort_ws, nx, ny, nz);
   PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
   if (np == 0) return PMGB_OK;
-  rkd_tiles_kernel<<<tile_grid(keys), TILE_THREADS, 0, s>>>(f3, cs, nx, ny, nz, pos, vel,
-                                                            sc.offsets, (uint32_t)keys, kick,
-                                                            drift, sc.counts, sc.rank, stats);
+  // TMA prefetch of interior force boxes: a 4-D map (z, y, x, component),
+  // box 12 x 9 x 9 x 3
+  CUtensorMap map;
+  memset(&map, 0, sizeof(map));
+  int use_tma = 0;
+  if (nz % 4 == 0 && cs % 4 == 0 && reinterpret_cast<uintptr_t>(f3) % 16 == 0 && nz >= TBZ &&
+      ny >= TB && nx >= TB) {
+    const uint64_t dims[4] = {(uint64_t)nz, (uint64_t)ny, (uint64_t)nx, 3};
+    const uint64_t strides[3] = {(uint64_t)nz * 4, (uint64_t)ny * nz * 4, (uint64_t)cs * 4};
+    const uint32_t box[4] = {TBZ, TB, TB, 3};
+    use_tma = make_tensor_map(&map, f3, 4, dims, strides, box) == PMGB_OK ? 1 : 0;
+    clear_error();
+  }
+  rkd_tiles_kernel<<<tile_grid(keys), TILE_THREADS, 0, s>>>(
+      f3, cs, nx, ny, nz, pos, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts, sc.rank,
+      stats, map, use_tma);
   PMGB_LAUNCHED("rkd_tiles_kernel");
   return PMGB_OK;
 }

@@ -138,7 +138,7 @@ class SortedFastPM:
         self.vel = [torch.empty((n, 3), **f), torch.empty((n, 3), **f)]
         self.ids = [torch.empty(n, dtype=torch.int32, device=device) for _ in range(2)]
         self.cur = 0
-        self.stats_buf = torch.zeros(2, dtype=torch.int32, device=device)
+        self.stats_buf = torch.zeros(3, dtype=torch.int32, device=device)
 
     def load(self, pos, vel):
         """Sorts ``pos``/``vel`` ([Np, 3], caller's order) into the engine."""
@@ -193,7 +193,7 @@ class SortedFastPM:
         """Particles found outside their tile by the paint and the gather
         (0 unless the tile ranges were stale)."""
         c = self.stats_buf.cpu().tolist()
-        return {"paint": c[0], "gather": c[1]}
+        return {"paint": c[0], "gather": c[1], "tma_wait_timeout": c[2]}
 
     def vjp(self, pos, vel, g_pos, g_vel, store=None):
         """Forward run from ``(pos, vel)`` (caller's order) then the reverse
