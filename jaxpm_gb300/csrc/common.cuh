@@ -69,7 +69,10 @@ inline unsigned grid_for(int64_t n, int threads, int per_sm = 8) {
 //   cell = int32(c) floor-mod n.
 // ---------------------------------------------------------------------------
 
+// Floor-modulo i mod n (n > 0); the integer division only runs for indices
+// outside [0, n), which unwrapped positions rarely are.
 __device__ __forceinline__ int wrap_index(int i, int n) {
+  if ((unsigned)i < (unsigned)n) return i;
   int r = i % n;
   return r < 0 ? r + n : r;
 }
@@ -79,6 +82,8 @@ struct Axis {
   float k0, k1;  // their CIC factors
 };
 
+// The upper neighbour's cell int32(floor(x) + 1) mod n equals
+// (i0 + 1) mod n for every position with |x| < 2^24.
 __device__ __forceinline__ Axis cic_axis(float x, int n) {
   Axis a;
   float f = floorf(x);
@@ -86,7 +91,7 @@ __device__ __forceinline__ Axis cic_axis(float x, int n) {
   a.k0 = __fsub_rn(1.0f, fabsf(__fsub_rn(x, f)));
   a.k1 = __fsub_rn(1.0f, fabsf(__fsub_rn(x, c1)));
   a.i0 = wrap_index((int)f, n);
-  a.i1 = wrap_index((int)c1, n);
+  a.i1 = (fabsf(f) < 16777216.0f) ? (a.i0 + 1 == n ? 0 : a.i0 + 1) : wrap_index((int)c1, n);
   return a;
 }
 

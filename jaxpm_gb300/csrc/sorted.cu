@@ -276,67 +276,77 @@ constexpr int TB = TILE + 1;   // box edge (cells)
 constexpr int TBZ = 12;        // z stride of a box row (16-byte multiple)
 constexpr int TBOX = TB * TB * TBZ;
 constexpr int TILE_THREADS = 256;
-constexpr float FIX_SCALE = 16777216.0f;  // 2^24: paint accumulates in 40.24 fixed point
-
-__device__ __forceinline__ bool tile_local(float x, float y, float z, int ox, int oy, int oz,
-                                           int nx, int ny, int nz, int &lx, int &ly, int &lz) {
-  lx = wrap_index((int)floorf(x), nx) - ox;
-  ly = wrap_index((int)floorf(y), ny) - oy;
-  lz = wrap_index((int)floorf(z), nz) - oz;
-  return (unsigned)lx < (unsigned)TILE && (unsigned)ly < (unsigned)TILE &&
-         (unsigned)lz < (unsigned)TILE;
-}
+constexpr float FIX_SCALE = 16777216.0f;  // 2^24: paint weights in 24-bit fixed point
 
 __device__ __forceinline__ bool box_interior(int ox, int oy, int oz, int nx, int ny, int nz) {
   return ox + TB <= nx && oy + TB <= ny && oz + TBZ <= nz;
 }
 
-// Adds a signed fixed-point value into a two-word (hi:lo) shared
-// accumulator with native 32-bit atomics; the carry out of the low word is
-// detected from the returned old value, so the 64-bit sum is exact.
-__device__ __forceinline__ void fixed_add(unsigned *lo, int *hi, int c, float w) {
-  const long long q = __float2ll_rn(w * FIX_SCALE);
-  const unsigned ql = (unsigned)q;
-  const int qh = (int)(q >> 32);
-  const unsigned old = atomicAdd(lo + c, ql);
-  const int carry = (old + ql < old) ? 1 : 0;
-  if (qh + carry != 0) atomicAdd(hi + c, qh + carry);
+// The paint box accumulates CIC weights (in [0, 1]) as 24-bit fixed point
+// split into two 12-bit halves, each summed with native (fire-and-forget)
+// 32-bit shared atomics.  A cell receives at most one contribution per
+// particle of the tile, so neither half can wrap while the tile holds fewer
+// than 2^20 particles; the sum hi * 2^-12 + lo * 2^-24 is then exact and is
+// converted to float once per cell.  A tile with more particles paints
+// with global float atomics instead.
+constexpr unsigned FIX_SAFE_COUNT = 1u << 20;
+
+__device__ __forceinline__ void fixed_add_split(unsigned *lo, unsigned *hi, int c, float w) {
+  const unsigned q = __float2uint_rn(w * FIX_SCALE);  // <= 2^24
+  atomicAdd(lo + c, q & 0xFFFu);
+  atomicAdd(hi + c, q >> 12);
 }
 
-__global__ void __launch_bounds__(TILE_THREADS)
+// Warp-per-tile painter: each warp of a CTA owns a private box (the two
+// fixed-point halves; the low half is reused as the float box for the
+// flush) and takes tiles from a global counter, so warps never wait on each
+// other and a heavy tile delays only its own warp.
+constexpr int PAINT_WARPS = 8;
+constexpr int WBOX_WORDS = (2 * TBOX + 31) / 32 * 32;  // lo + hi, 128-byte multiple
+constexpr int PAINT_SMEM = PAINT_WARPS * WBOX_WORDS * 4;
+
+__global__ void __launch_bounds__(PAINT_WARPS * 32)
 paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
                    const float *__restrict__ pos, const unsigned *__restrict__ offsets,
-                   uint32_t nkeys, unsigned *__restrict__ stats, int vec,
+                   uint32_t nkeys, unsigned *__restrict__ next_tile,
+                   unsigned *__restrict__ stats, int vec,
                    const __grid_constant__ CUtensorMap tmap, int use_tma) {
-  __shared__ __align__(128) float fbox[TBOX];
-  __shared__ unsigned acc_lo[TBOX];
-  __shared__ int acc_hi[TBOX];
-  const int tid = threadIdx.x;
-  for (uint32_t key = blockIdx.x; key < nkeys; key += gridDim.x) {
+  extern __shared__ __align__(128) unsigned wbox[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned *lo = wbox + warp * WBOX_WORDS;
+  unsigned *hi = lo + TBOX;
+  float *fbox = reinterpret_cast<float *>(lo);
+  for (;;) {
+    uint32_t key = 0;
+    if (lane == 0) key = atomicAdd(next_tile, 1u);
+    key = __shfl_sync(0xffffffffu, key, 0);
+    if (key >= nkeys) break;
     const unsigned beg = __ldg(offsets + key), end = __ldg(offsets + key + 1);
-    if (beg == end) continue;  // uniform across the CTA
+    if (beg == end) continue;  // uniform across the warp
     const int ox = (int)compact3(key >> 2) * TILE, oy = (int)compact3(key >> 1) * TILE,
               oz = (int)compact3(key) * TILE;
-    for (int q = tid; q < TBOX; q += TILE_THREADS) {
-      acc_lo[q] = 0u;
-      acc_hi[q] = 0;
+    const bool boxed = end - beg < FIX_SAFE_COUNT;  // uniform
+    for (int q = lane; q < TBOX; q += 32) {
+      lo[q] = 0u;
+      hi[q] = 0u;
     }
-    __syncthreads();
-    for (unsigned p = beg + tid; p < end; p += TILE_THREADS) {
+    __syncwarp();
+    for (unsigned p = beg + lane; p < end; p += 32) {
       const float x = __ldg(pos + 3 * (int64_t)p), y = __ldg(pos + 3 * (int64_t)p + 1),
                   z = __ldg(pos + 3 * (int64_t)p + 2);
       Axis ax = cic_axis(x, nx), ay = cic_axis(y, ny), az = cic_axis(z, nz);
-      int lx, ly, lz;
-      if (tile_local(x, y, z, ox, oy, oz, nx, ny, nz, lx, ly, lz)) {
+      const int lx = ax.i0 - ox, ly = ay.i0 - oy, lz = az.i0 - oz;
+      if (boxed && (unsigned)lx < (unsigned)TILE && (unsigned)ly < (unsigned)TILE &&
+          (unsigned)lz < (unsigned)TILE) {
         const int q0 = (lx * TB + ly) * TBZ + lz;
 #pragma unroll
         for (int n = 0; n < 8; ++n) {
           float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
                               conn_z(n) ? az.k1 : az.k0);
-          fixed_add(acc_lo, acc_hi, q0 + conn_x(n) * TB * TBZ + conn_y(n) * TBZ + conn_z(n), w);
+          fixed_add_split(lo, hi, q0 + conn_x(n) * TB * TBZ + conn_y(n) * TBZ + conn_z(n), w);
         }
       } else {
-        if (stats) atomicAdd(stats, 1u);
+        if (stats && boxed) atomicAdd(stats, 1u);
 #pragma unroll
         for (int n = 0; n < 8; ++n) {
           float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
@@ -346,23 +356,22 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
         }
       }
     }
-    __syncthreads();
-    for (int q = tid; q < TBOX; q += TILE_THREADS) {
-      const long long v = (long long)(((unsigned long long)(unsigned)acc_hi[q] << 32) | acc_lo[q]);
-      fbox[q] = (float)((double)v * (1.0 / 16777216.0));
-    }
+    __syncwarp();
+    // fixed point -> float in place (each lane reads and rewrites its own cells)
+    for (int q = lane; q < TBOX; q += 32)
+      fbox[q] = fmaf((float)hi[q], 1.0f / 4096.0f, (float)lo[q] * (1.0f / 16777216.0f));
     const bool tma = use_tma && box_interior(ox, oy, oz, nx, ny, nz);
     if (tma) fence_async_shared();  // generic-proxy writes of fbox -> TMA
-    __syncthreads();
+    __syncwarp();
     if (tma) {
-      if (tid == 0) {
+      if (lane == 0) {
         tma_reduce_add_3d(&tmap, oz, oy, ox, fbox);
         bulk_commit();
-        bulk_wait_read();  // fbox may be rewritten after this
+        bulk_wait_read();  // the box may be rewritten after this
       }
     } else if (vec) {
       // 9 x 9 rows of three 16-byte groups starting at z = oz, oz+4, oz+8
-      for (int q = tid; q < TB * TB * 3; q += TILE_THREADS) {
+      for (int q = lane; q < TB * TB * 3; q += 32) {
         const int g = q % 3, r = q / 3, b = r % TB, a = r / TB;
         const float4 v = *reinterpret_cast<const float4 *>(fbox + (a * TB + b) * TBZ + 4 * g);
         if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
@@ -372,7 +381,7 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
         }
       }
     } else {
-      for (int q = tid; q < TB * TB * TB; q += TILE_THREADS) {
+      for (int q = lane; q < TB * TB * TB; q += 32) {
         const int c = q % TB, r = q / TB, b = r % TB, a = r / TB;
         const float v = fbox[(a * TB + b) * TBZ + c];
         if (v != 0.f)
@@ -380,9 +389,9 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
                                       wrap_index(oz + c, nz), ny, nz), v);
       }
     }
-    __syncthreads();  // the boxes are reused by the next tile
+    __syncwarp();  // the box is reused by the warp's next tile
   }
-  if (use_tma && tid == 0) bulk_wait_all();  // reductions complete before the kernel ends
+  if (use_tma && lane == 0) bulk_wait_all();  // reductions complete before the kernel ends
 }
 
 constexpr int FBOX = 3 * TBOX;  // three force components, [c][x][y][z(12)]
@@ -407,7 +416,9 @@ __device__ __forceinline__ TileInfo tile_info(const unsigned *__restrict__ offse
   return t;
 }
 
-__global__ void __launch_bounds__(TILE_THREADS)
+constexpr int RKD_ILP = 2;
+
+__global__ void __launch_bounds__(TILE_THREADS, 4)
 rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int nz,
                  float *__restrict__ pos, float *__restrict__ vel,
                  const unsigned *__restrict__ offsets, uint32_t nkeys, float kick, float drift,
@@ -466,20 +477,35 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
         }
         __syncthreads();
       }
-      // every lane of a warp runs the same iterations (ballot / match inside)
-      for (unsigned p0 = cur.beg; p0 < cur.end; p0 += TILE_THREADS) {
-        const unsigned p = p0 + tid;
+      // every lane of a warp runs the same iterations (ballot / match inside);
+      // each thread loads RKD_ILP particles before computing any of them
+      for (unsigned p0 = cur.beg; p0 < cur.end; p0 += TILE_THREADS * RKD_ILP) {
+       float px[RKD_ILP], py[RKD_ILP], pz[RKD_ILP], pu[RKD_ILP], pv[RKD_ILP], pw[RKD_ILP];
+#pragma unroll
+       for (int j = 0; j < RKD_ILP; ++j) {
+         const unsigned p = p0 + tid + j * TILE_THREADS;
+         if (p < cur.end) {
+           px[j] = pos[3 * (int64_t)p];
+           py[j] = pos[3 * (int64_t)p + 1];
+           pz[j] = pos[3 * (int64_t)p + 2];
+           pu[j] = vel[3 * (int64_t)p];
+           pv[j] = vel[3 * (int64_t)p + 1];
+           pw[j] = vel[3 * (int64_t)p + 2];
+         }
+       }
+#pragma unroll
+       for (int j = 0; j < RKD_ILP; ++j) {
+        const unsigned p = p0 + tid + j * TILE_THREADS;
         const bool valid = p < cur.end;
         uint32_t k = 0;
         if (valid) {
-          const float x = pos[3 * (int64_t)p], y = pos[3 * (int64_t)p + 1],
-                      z = pos[3 * (int64_t)p + 2];
-          const float v0 = vel[3 * (int64_t)p], v1 = vel[3 * (int64_t)p + 1],
-                      v2 = vel[3 * (int64_t)p + 2];
+          const float x = px[j], y = py[j], z = pz[j];
+          const float v0 = pu[j], v1 = pv[j], v2 = pw[j];
           Axis ax = cic_axis(x, nx), ay = cic_axis(y, ny), az = cic_axis(z, nz);
           float a0 = 0.f, a1 = 0.f, a2 = 0.f;
-          int lx, ly, lz;
-          if (tile_local(x, y, z, cur.ox, cur.oy, cur.oz, nx, ny, nz, lx, ly, lz)) {
+          const int lx = ax.i0 - cur.ox, ly = ay.i0 - cur.oy, lz = az.i0 - cur.oz;
+          if ((unsigned)lx < (unsigned)TILE && (unsigned)ly < (unsigned)TILE &&
+              (unsigned)lz < (unsigned)TILE) {
             const int q0 = (lx * TB + ly) * TBZ + lz;
 #pragma unroll
             for (int n = 0; n < 8; ++n) {
@@ -517,6 +543,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
           const unsigned active = __ballot_sync(0xffffffffu, valid);
           if (valid) rank[p] = count_and_rank(counts, k, active);
         }
+       }
       }
     }
     __syncthreads();  // buffer `buf` is free for the prefetch two tiles ahead
@@ -542,26 +569,57 @@ tile_rank_kernel(const float *__restrict__ pos, int64_t np, int nx, int ny, int 
   }
 }
 
-// Moves particle p to offsets[key] + rank[p] (pos, vel, id).
+// Moves particle p to offsets[key] + rank[p] (pos, vel, id).  Each thread
+// carries SCATTER_ILP particles so that their loads are in flight together.
+constexpr int SCATTER_ILP = 4;
+
 __global__ void __launch_bounds__(256)
 scatter_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
                const unsigned *__restrict__ id, const unsigned *__restrict__ rank, int64_t np,
                int nx, int ny, int nz, const unsigned *__restrict__ offsets,
                float *__restrict__ pos2, float *__restrict__ vel2, unsigned *__restrict__ id2) {
-  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    float x = __ldg(pos + 3 * p), y = __ldg(pos + 3 * p + 1), z = __ldg(pos + 3 * p + 2);
-    uint32_t key = tile_key(x, y, z, nx, ny, nz);
-    int64_t d = (int64_t)__ldg(offsets + key) + __ldg(rank + p);
-    pos2[3 * d] = x;
-    pos2[3 * d + 1] = y;
-    pos2[3 * d + 2] = z;
-    if (vel) {
-      vel2[3 * d] = __ldg(vel + 3 * p);
-      vel2[3 * d + 1] = __ldg(vel + 3 * p + 1);
-      vel2[3 * d + 2] = __ldg(vel + 3 * p + 2);
+  const int64_t span = (int64_t)blockDim.x * SCATTER_ILP;
+  for (int64_t base = blockIdx.x * span + threadIdx.x; base < np; base += gridDim.x * span) {
+    float x[SCATTER_ILP], y[SCATTER_ILP], z[SCATTER_ILP], u[SCATTER_ILP], v[SCATTER_ILP],
+        w[SCATTER_ILP];
+    unsigned r[SCATTER_ILP], ident[SCATTER_ILP];
+#pragma unroll
+    for (int j = 0; j < SCATTER_ILP; ++j) {
+      const int64_t p = base + j * (int64_t)blockDim.x;
+      if (p < np) {
+        x[j] = __ldg(pos + 3 * p);
+        y[j] = __ldg(pos + 3 * p + 1);
+        z[j] = __ldg(pos + 3 * p + 2);
+        r[j] = __ldg(rank + p);
+        if (vel) {
+          u[j] = __ldg(vel + 3 * p);
+          v[j] = __ldg(vel + 3 * p + 1);
+          w[j] = __ldg(vel + 3 * p + 2);
+        }
+        ident[j] = id ? __ldg(id + p) : (unsigned)p;
+      }
     }
-    id2[d] = id ? __ldg(id + p) : (unsigned)p;
+#pragma unroll
+    for (int j = 0; j < SCATTER_ILP; ++j) {
+      const int64_t p = base + j * (int64_t)blockDim.x;
+      if (p < np) r[j] += __ldg(offsets + tile_key(x[j], y[j], z[j], nx, ny, nz));
+    }
+#pragma unroll
+    for (int j = 0; j < SCATTER_ILP; ++j) {
+      const int64_t p = base + j * (int64_t)blockDim.x;
+      if (p < np) {
+        const int64_t d = r[j];
+        pos2[3 * d] = x[j];
+        pos2[3 * d + 1] = y[j];
+        pos2[3 * d + 2] = z[j];
+        if (vel) {
+          vel2[3 * d] = u[j];
+          vel2[3 * d + 1] = v[j];
+          vel2[3 * d + 2] = w[j];
+        }
+        id2[d] = ident[j];
+      }
+    }
   }
 }
 
@@ -721,14 +779,14 @@ size_t sort_workspace_size(int nx, int ny, int nz, int64_t np) {
   const size_t keys = (size_t)tile_key_count(nx, ny, nz);
   auto a = [](size_t b) { return (b + 255) & ~(size_t)255; };
   return a(keys * 4) + a((keys + 1) * 4) + a(((keys + SCAN_BLOCK - 1) / SCAN_BLOCK) * 4) +
-         a((size_t)np * 4);
+         a((size_t)np * 4) + 256;
 }
 
 struct SortScratch {
-  unsigned *counts, *offsets, *sums, *rank;
+  unsigned *counts, *offsets, *sums, *rank, *work;
 };
 
-static SortScratch sort_scratch(void *ws, int nx, int ny, int nz) {
+static SortScratch sort_scratch(void *ws, int nx, int ny, int nz, int64_t np) {
   const size_t keys = (size_t)tile_key_count(nx, ny, nz);
   auto a = [](size_t b) { return (b + 255) & ~(size_t)255; };
   char *c = static_cast<char *>(ws);
@@ -740,6 +798,8 @@ static SortScratch sort_scratch(void *ws, int nx, int ny, int nz) {
   sc.sums = reinterpret_cast<unsigned *>(c);
   c += a(((keys + SCAN_BLOCK - 1) / SCAN_BLOCK) * 4);
   sc.rank = reinterpret_cast<unsigned *>(c);
+  c += a((size_t)np * 4);
+  sc.work = reinterpret_cast<unsigned *>(c);
   return sc;
 }
 
@@ -762,7 +822,7 @@ int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np
               cudaStream_t s) {
   PMGB_TRY(check_sort_ws(ws, bytes, nx, ny, nz, np));
   const int64_t keys = tile_key_count(nx, ny, nz);
-  SortScratch sc = sort_scratch(ws, nx, ny, nz);
+  SortScratch sc = sort_scratch(ws, nx, ny, nz, np);
   PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
   if (np > 0) {
     tile_rank_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, np, nx, ny, nz, sc.counts, sc.rank);
@@ -799,7 +859,7 @@ int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos, int64_t 
   PMGB_CUDA(cudaMemsetAsync(mesh, 0, (size_t)nx * ny * nz * sizeof(float), s));
   if (np == 0) return PMGB_OK;
   const int64_t keys = tile_key_count(nx, ny, nz);
-  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz);
+  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
   const int vec = (nz % 4 == 0 && reinterpret_cast<uintptr_t>(mesh) % 16 == 0) ? 1 : 0;
   // TMA flush of interior tiles: a 3-D map over the mesh, box 12 x 9 x 9
   CUtensorMap map;
@@ -812,8 +872,18 @@ int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos, int64_t 
     use_tma = make_tensor_map(&map, mesh, 3, dims, strides, box) == PMGB_OK ? 1 : 0;
     clear_error();
   }
-  paint_tiles_kernel<<<tile_grid(keys), TILE_THREADS, 0, s>>>(
-      mesh, nx, ny, nz, pos, sc.offsets, (uint32_t)keys, stats, vec, map, use_tma);
+  static bool ready[64] = {false};
+  int dev = 0;
+  PMGB_CUDA(cudaGetDevice(&dev));
+  if (dev >= 64 || !ready[dev]) {
+    PMGB_TRY(set_smem((const void *)paint_tiles_kernel, PAINT_SMEM));
+    if (dev < 64) ready[dev] = true;
+  }
+  PMGB_CUDA(cudaMemsetAsync(sc.work, 0, sizeof(unsigned), s));
+  const unsigned grid = (unsigned)std::min<int64_t>((keys + PAINT_WARPS - 1) / PAINT_WARPS,
+                                                    (int64_t)sm_count() * 3);
+  paint_tiles_kernel<<<grid, PAINT_WARPS * 32, PAINT_SMEM, s>>>(
+      mesh, nx, ny, nz, pos, sc.offsets, (uint32_t)keys, sc.work, stats, vec, map, use_tma);
   PMGB_LAUNCHED("paint_tiles_kernel");
   return PMGB_OK;
 }
@@ -825,7 +895,7 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos, 
                unsigned *stats, cudaStream_t s) {
   PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
   const int64_t keys = tile_key_count(nx, ny, nz);
-  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz);
+  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
   PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
   if (np == 0) return PMGB_OK;
   // TMA prefetch of interior force boxes: a 4-D map (z, y, x, component),
@@ -855,7 +925,7 @@ int tile_scatter(const float *pos, const float *vel, const unsigned *id, int64_t
                  size_t sort_bytes, cudaStream_t s) {
   PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
   const int64_t keys = tile_key_count(nx, ny, nz);
-  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz);
+  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
   PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
   if (np > 0) {
     scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
