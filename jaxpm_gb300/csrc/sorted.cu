@@ -302,6 +302,7 @@ __device__ __forceinline__ void fixed_add_split(unsigned *lo, unsigned *hi, int 
 // flush) and takes tiles from a global counter, so warps never wait on each
 // other and a heavy tile delays only its own warp.
 constexpr int PAINT_WARPS = 8;
+constexpr int PAINT_ILP = 4;
 constexpr int WBOX_WORDS = (2 * TBOX + 31) / 32 * 32;  // lo + hi, 128-byte multiple
 constexpr int PAINT_SMEM = PAINT_WARPS * WBOX_WORDS * 4;
 
@@ -331,9 +332,21 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
       hi[q] = 0u;
     }
     __syncwarp();
-    for (unsigned p = beg + lane; p < end; p += 32) {
-      const float x = __ldg(pos + 3 * (int64_t)p), y = __ldg(pos + 3 * (int64_t)p + 1),
-                  z = __ldg(pos + 3 * (int64_t)p + 2);
+    for (unsigned p0 = beg + lane; p0 < end; p0 += 32 * PAINT_ILP) {
+     float px[PAINT_ILP], py[PAINT_ILP], pz[PAINT_ILP];
+#pragma unroll
+     for (int j = 0; j < PAINT_ILP; ++j) {  // loads of several particles in flight
+       const unsigned p = p0 + 32 * j;
+       if (p < end) {
+         px[j] = __ldg(pos + 3 * (int64_t)p);
+         py[j] = __ldg(pos + 3 * (int64_t)p + 1);
+         pz[j] = __ldg(pos + 3 * (int64_t)p + 2);
+       }
+     }
+#pragma unroll
+     for (int j = 0; j < PAINT_ILP; ++j) {
+      if (p0 + 32 * j >= end) break;
+      const float x = px[j], y = py[j], z = pz[j];
       Axis ax = cic_axis(x, nx), ay = cic_axis(y, ny), az = cic_axis(z, nz);
       const int lx = ax.i0 - ox, ly = ay.i0 - oy, lz = az.i0 - oz;
       if (boxed && (unsigned)lx < (unsigned)TILE && (unsigned)ly < (unsigned)TILE &&
@@ -355,6 +368,7 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
                                       conn_z(n) ? az.i1 : az.i0, ny, nz), w);
         }
       }
+     }
     }
     __syncwarp();
     // fixed point -> float in place (each lane reads and rewrites its own cells)
