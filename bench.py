@@ -58,13 +58,21 @@ def dist_env():
 
 
 def max_over_ranks(value, world):
+    """Maximum of a per-rank value (the slowest replica's time)."""
     if world == 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dev = "cpu" if dist.get_backend() == "gloo" else "cuda"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_rate(particles_per_rank, steps, ms_max, world):
+    """Whole-job particle-steps/s of `world` independent replicas, timed by
+    the slowest one."""
+    return world * particles_per_rank * steps / (ms_max / 1e3)
 
 
 def barrier(world):
