@@ -79,6 +79,28 @@ int pmgb_cic_paint_f32(float *mesh, int nx, int ny, int nz, const float *pos,
                        int mode, int accumulate, void *workspace,
                        size_t workspace_bytes, pmgb_stream_t stream);
 
+/* The deterministic paint (PMGB_PAINT_DETERMINISTIC semantics, same result
+ * bit for bit) without any allocation and without a workspace argument.
+ * No counterpart in the reference: it exists for callers that cannot hand
+ * out device memory, such as a custom-call handler that only receives the
+ * buffers its framework's allocator made, or code that must not call
+ * cudaMalloc while another runtime's pool owns the device memory.  The
+ * fixed-point scratch (8 bytes per cell) is a static device array inside
+ * libpmgb, so meshes are limited to 128^3 = 2097152 cells (larger ones are
+ * rejected with PMGB_ERR_INVALID_ARGUMENT); every GPU that loads the
+ * library holds those 16 MiB until the process exits.  The first call on a
+ * device looks the array's address up (cudaGetSymbolAddress) and caches
+ * it: make that first call before any stream capture.  The scratch is
+ * cleared by every call, but all calls share it: calls that overlap on the
+ * GPU (different streams, or different host threads on one device) race
+ * and must be serialised by the caller. */
+int pmgb_cic_paint_deterministic_noalloc_f32(float *mesh, int nx, int ny,
+                                             int nz, const float *pos,
+                                             int64_t np, const float *weights,
+                                             float weight_scale,
+                                             int accumulate,
+                                             pmgb_stream_t stream);
+
 /* out[p] = sum_c W(pos_p, c) * mesh[c].
  * Replaces _cic_read_impl / cic_read, jaxpm/painting.py:78-128. */
 int pmgb_cic_read_f32(const float *mesh, int nx, int ny, int nz,

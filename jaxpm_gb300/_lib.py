@@ -37,6 +37,8 @@ SIGNATURES = {
     "pmgb_cic_paint_workspace_size": (c_size_t, [c_int, c_int, c_int, c_int64, c_int]),
     "pmgb_cic_paint_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P, c_float, c_int, c_int,
                                    P, c_size_t, P]),
+    "pmgb_cic_paint_deterministic_noalloc_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P,
+                                                         c_float, c_int, P]),
     "pmgb_cic_read_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P, P]),
     "pmgb_cic_read3_f32": (c_int, [P, c_int64, c_int, c_int, c_int, P, c_int64, P, P]),
     "pmgb_cic_weights_f32": (c_int, [P, c_int64, c_int, c_int, c_int, P, P, P]),

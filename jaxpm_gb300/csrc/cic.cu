@@ -345,6 +345,24 @@ int paint(float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
   return fail(PMGB_ERR_INVALID_ARGUMENT, "unknown paint mode " + std::to_string(mode));
 }
 
+// Deterministic paint into a caller-provided fixed-point accumulator of
+// nx*ny*nz 64-bit words (cleared here): the kernels of the deterministic
+// mode, for callers that supply the scratch themselves.
+int paint_fixed_into(unsigned long long *acc, float *mesh, int nx, int ny, int nz,
+                     const float *pos, int64_t np, const float *weights, float wscale,
+                     int accumulate, cudaStream_t s) {
+  const int64_t ncell = (int64_t)nx * ny * nz;
+  PMGB_CUDA(cudaMemsetAsync(acc, 0, ncell * sizeof(unsigned long long), s));
+  if (np > 0) {
+    paint_fixed_kernel<<<grid_for(np, 256), 256, 0, s>>>(acc, nx, ny, nz, pos, np, weights,
+                                                          wscale);
+    PMGB_LAUNCHED("paint_fixed_kernel");
+  }
+  fixed_to_float_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(mesh, acc, ncell, accumulate);
+  PMGB_LAUNCHED("fixed_to_float_kernel");
+  return PMGB_OK;
+}
+
 int read(const float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
          float *out, cudaStream_t s) {
   if (np == 0) return PMGB_OK;

@@ -31,6 +31,10 @@ int read_dx(const float *mesh, int nx, int ny, int nz, const float *disp,
             float *out, cudaStream_t s);
 int enmesh(const float *disp, int nx, int ny, int nz, int32_t *idx, float *w,
            cudaStream_t s);
+int paint_fixed_into(unsigned long long *acc, float *mesh, int nx, int ny,
+                     int nz, const float *pos, int64_t np,
+                     const float *weights, float wscale, int accumulate,
+                     cudaStream_t s);
 
 // fft.cu
 int fft_r2c(const float *in, void *out, int nx, int ny, int nz, int batch,
