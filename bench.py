@@ -255,7 +255,7 @@ def run_gb300(args):
             rec(5)
             _lib.call("pmgb_tile_scatter_f32", _lib.ptr(px), _lib.ptr(pv), _lib.ptr(eng.ids[a]),
                       Np, nx, ny, nz, _lib.ptr(eng.pos[b]), _lib.ptr(eng.vel[b]),
-                      _lib.ptr(eng.ids[b]), _lib.ptr(eng.sort_ws), eng.sort_bytes, s)
+                      _lib.ptr(eng.ids[b]), None, _lib.ptr(eng.sort_ws), eng.sort_bytes, s)
             rec(6)
             eng.cur = b
         else:
@@ -338,14 +338,13 @@ def run_gb300(args):
         print(json.dumps(result))
         return
 
-    # forward + adjoint (hand-written adjoint; positions, and for the sorted
-    # loop particle ids, stored before every step)
+    # forward + adjoint (hand-written adjoint; positions stored before every
+    # step, and for the sorted loop also its force meshes and re-sort map)
     if "adjoint" not in skip:
         gx = torch.ones_like(x0) * 1e-3
         gv = torch.zeros_like(v0)
         if engine == "sorted":
-            store = (torch.empty((K, Np, 3), dtype=torch.float32, device=dev),
-                     torch.empty((K, Np), dtype=torch.int32, device=dev))
+            store = eng.alloc_store()
         else:
             store = torch.empty((K, Np, 3), dtype=torch.float32, device=dev)
         eng.vjp(x0, v0, gx, gv, store=store)  # warm-up (plans, buffers)
@@ -407,7 +406,7 @@ def run_gb300(args):
                       _lib.ptr(E.ids[0]), _lib.ptr(E.pos[1]), _lib.ptr(E.vel[1]),
                       _lib.ptr(E.ids[1]), Np, nx, ny, nz, float(E.kick[i]), float(E.drift[i]),
                       0.0, _lib.ptr(E.ws), E.ws_bytes, _lib.ptr(E.sort_ws), E.sort_bytes, None,
-                      s)
+                      None, None, None, s)
             _lib.call("pmgb_unpermute3_f32", _lib.ptr(E.pos[1]), _lib.ptr(E.ids[1]), Np,
                       _lib.ptr(dx_), s)
             _lib.call("pmgb_unpermute3_f32", _lib.ptr(E.vel[1]), _lib.ptr(E.ids[1]), Np,

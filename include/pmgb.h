@@ -322,30 +322,67 @@ int pmgb_read3_kick_drift_binned_f32(const float *force3, int64_t comp_stride,
 
 /* Exclusive scan of the tile counts left in sort_workspace by
  * pmgb_read3_kick_drift_binned_f32, then the scatter of (pos, vel, id) to
- * (pos_out, vel_out, id_out) in tile order. */
+ * (pos_out, vel_out, id_out) in tile order; dest_out (nullable) receives
+ * each particle's new index. */
 int pmgb_tile_scatter_f32(const float *pos, const float *vel,
                           const uint32_t *id, int64_t np, int nx, int ny,
                           int nz, float *pos_out, float *vel_out,
-                          uint32_t *id_out, void *sort_workspace,
-                          size_t sort_workspace_bytes, pmgb_stream_t stream);
+                          uint32_t *id_out, uint32_t *dest_out,
+                          void *sort_workspace, size_t sort_workspace_bytes,
+                          pmgb_stream_t stream);
 
 /* One FastPM step on tile-sorted particles (jaxpm/ode.py:35-58 kick and
  * :20-33 drift, forces of jaxpm/pm.py:12-58): shared-memory box paint,
  * R2C, fused k-space kernel, batched C2R, box-staged gather + kick + drift
  * that also counts the new positions per tile, scan, scatter.  Reads
  * (pos, vel, id) and writes the advanced state, sorted by the new
- * positions, to (pos_out, vel_out, id_out).  `workspace` is sized by
+ * positions, to (pos_out, vel_out, id_out); pos and id are left unchanged
+ * (the drifted positions pass through the workspace), vel holds the kicked
+ * velocities in the old order on return.  `workspace` is sized by
  * pmgb_pm_workspace_size(..., PMGB_PAINT_BINNED), `sort_workspace` by
- * pmgb_tile_sort_workspace_size.  stats (nullable, 3 counters the caller
- * zeroes): see pmgb_cic_paint_sorted_f32 and
- * pmgb_read3_kick_drift_binned_f32. */
-int pmgb_fpm_step_sorted_f32(float *pos, float *vel, uint32_t *id,
+ * pmgb_tile_sort_workspace_size.  What the reverse step needs can be
+ * recorded (each nullable): force3_out [3][nx][ny][nz] receives the force
+ * meshes (computed there in place of the workspace), dest_out [np] each
+ * particle's index after the step, offsets_out the tile ranges of the
+ * order the step started from (pmgb_tile_key_count + 1 entries).  stats
+ * (nullable, 3 counters the caller zeroes): see pmgb_cic_paint_sorted_f32
+ * and pmgb_read3_kick_drift_binned_f32. */
+int pmgb_fpm_step_sorted_f32(const float *pos, float *vel, const uint32_t *id,
                              float *pos_out, float *vel_out, uint32_t *id_out,
                              int64_t np, int nx, int ny, int nz, float kick,
                              float drift, float r_split, void *workspace,
                              size_t workspace_bytes, void *sort_workspace,
-                             size_t sort_workspace_bytes, uint32_t *stats,
-                             pmgb_stream_t stream);
+                             size_t sort_workspace_bytes, float *force3_out,
+                             uint32_t *dest_out, uint32_t *offsets_out,
+                             uint32_t *stats, pmgb_stream_t stream);
+
+/* Number of tile keys of a mesh (the sorted loop's tile ranges have one
+ * more entry). */
+int64_t pmgb_tile_key_count(int nx, int ny, int nz);
+
+/* Reverse (vector-Jacobian) step of pmgb_fpm_step_sorted_f32, on the
+ * quantities that step recorded: pos = the positions it started from (tile
+ * order i), force3 its force meshes, dest where each particle went
+ * (order i -> i+1; NULL = identity), tile_offsets the ranges of order i.
+ * Given the cotangents (g_pos_in, g_vel_in) of its outputs (order i+1), it
+ * writes those of its inputs (order i):
+ *   u = g_vel[dest] + drift * g_pos[dest],   g_vel_out = u,
+ *   g_pos_out = g_pos[dest] + (dF/dx)^T (kick * u),
+ * the force Jacobian-transpose product being a tile-sorted paint of the
+ * three cotangent components (block-scaled fixed point in shared memory,
+ * TMA reduce), three R2C, the conjugate k-space multiply, one C2R, and a
+ * TMA-staged gather of both position terms.  Adjoint of the kick
+ * (ode.py:35-80), the drift (:20-33) and pm_forces (pm.py:12-58); the
+ * reference differentiates these with JAX's autodiff. */
+int pmgb_fpm_step_sorted_vjp_f32(const float *pos, const float *force3,
+                                 const uint32_t *dest,
+                                 const uint32_t *tile_offsets,
+                                 const float *g_pos_in, const float *g_vel_in,
+                                 float *g_pos_out, float *g_vel_out,
+                                 int64_t np, int nx, int ny, int nz,
+                                 float kick, float drift, float r_split,
+                                 void *workspace, size_t workspace_bytes,
+                                 uint32_t *stats, pmgb_stream_t stream);
 
 /* ---- initial conditions (jaxpm/pm.py:61-144) ----------------------------- */
 

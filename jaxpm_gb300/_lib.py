@@ -82,10 +82,14 @@ SIGNATURES = {
     "pmgb_read3_kick_drift_binned_f32": (c_int, [P, c_int64, c_int, c_int, c_int, P, P, c_int64,
                                                  c_float, c_float, P, c_size_t, P, P]),
     "pmgb_cic_paint_sorted_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P, c_size_t, P, P]),
-    "pmgb_tile_scatter_f32": (c_int, [P, P, P, c_int64, c_int, c_int, c_int, P, P, P, P,
+    "pmgb_tile_scatter_f32": (c_int, [P, P, P, c_int64, c_int, c_int, c_int, P, P, P, P, P,
                                       c_size_t, P]),
     "pmgb_fpm_step_sorted_f32": (c_int, [P, P, P, P, P, P, c_int64, c_int, c_int, c_int, c_float,
-                                         c_float, c_float, P, c_size_t, P, c_size_t, P, P]),
+                                         c_float, c_float, P, c_size_t, P, c_size_t, P, P, P, P,
+                                         P]),
+    "pmgb_tile_key_count": (c_int64, [c_int, c_int, c_int]),
+    "pmgb_fpm_step_sorted_vjp_f32": (c_int, [P, P, P, P, P, P, P, P, c_int64, c_int, c_int, c_int,
+                                             c_float, c_float, c_float, P, c_size_t, P, P]),
     "pmgb_power_spectrum_f32": (c_int, [P, c_int, c_int, c_int, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, P, c_int, P, P, P, P]),
 }

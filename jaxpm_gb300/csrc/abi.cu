@@ -426,8 +426,8 @@ int pmgb_read3_kick_drift_binned_f32(const float *force3, int64_t comp_stride, i
   NEED(pos);
   NEED(vel);
   NEED(sort_workspace);
-  return rkd_sorted(force3, comp_stride, nx, ny, nz, pos, vel, np, kick, drift, sort_workspace,
-                    sort_workspace_bytes, stats, stream);
+  return rkd_sorted(force3, comp_stride, nx, ny, nz, pos, pos, vel, np, kick, drift,
+                    sort_workspace, sort_workspace_bytes, stats, stream);
 }
 
 int pmgb_cic_paint_sorted_f32(float *mesh, int nx, int ny, int nz, const float *pos,
@@ -444,8 +444,8 @@ int pmgb_cic_paint_sorted_f32(float *mesh, int nx, int ny, int nz, const float *
 
 int pmgb_tile_scatter_f32(const float *pos, const float *vel, const uint32_t *id, int64_t np,
                           int nx, int ny, int nz, float *pos_out, float *vel_out,
-                          uint32_t *id_out, void *sort_workspace, size_t sort_workspace_bytes,
-                          pmgb_stream_t stream) {
+                          uint32_t *id_out, uint32_t *dest_out, void *sort_workspace,
+                          size_t sort_workspace_bytes, pmgb_stream_t stream) {
   BEGIN();
   PMGB_TRY(check_sortable(nx, ny, nz, np));
   if (np > 0) {
@@ -456,15 +456,17 @@ int pmgb_tile_scatter_f32(const float *pos, const float *vel, const uint32_t *id
     PMGB_REQUIRE(pos != pos_out && (!vel || vel != vel_out) && (!id || id != id_out),
                  "the scatter cannot run in place");
   }
-  return tile_scatter(pos, vel, id, np, nx, ny, nz, pos_out, vel_out, id_out, sort_workspace,
-                      sort_workspace_bytes, stream);
+  return tile_scatter(pos, vel, id, np, nx, ny, nz, pos_out, vel_out, id_out, dest_out,
+                      sort_workspace, sort_workspace_bytes, stream);
 }
 
-int pmgb_fpm_step_sorted_f32(float *pos, float *vel, uint32_t *id, float *pos_out, float *vel_out,
+int pmgb_fpm_step_sorted_f32(const float *pos, float *vel, const uint32_t *id, float *pos_out,
+                             float *vel_out,
                              uint32_t *id_out, int64_t np, int nx, int ny, int nz, float kick,
                              float drift, float r_split, void *workspace, size_t workspace_bytes,
-                             void *sort_workspace, size_t sort_workspace_bytes, uint32_t *stats,
-                             pmgb_stream_t stream) {
+                             void *sort_workspace, size_t sort_workspace_bytes,
+                             float *force3_out, uint32_t *dest_out, uint32_t *offsets_out,
+                             uint32_t *stats, pmgb_stream_t stream) {
   BEGIN();
   PMGB_TRY(check_sortable(nx, ny, nz, np));
   if (np > 0) {
@@ -479,7 +481,36 @@ int pmgb_fpm_step_sorted_f32(float *pos, float *vel, uint32_t *id, float *pos_ou
   }
   return fpm_step_sorted(pos, vel, id, pos_out, vel_out, id_out, np, nx, ny, nz, kick, drift,
                          r_split, workspace, workspace_bytes, sort_workspace,
-                         sort_workspace_bytes, stats, stream);
+                         sort_workspace_bytes, force3_out, dest_out, offsets_out, stats, stream);
+}
+
+int64_t pmgb_tile_key_count(int nx, int ny, int nz) {
+  if (nx <= 0 || ny <= 0 || nz <= 0) return 0;
+  return tile_key_count(nx, ny, nz);
+}
+
+int pmgb_fpm_step_sorted_vjp_f32(const float *pos, const float *force3, const uint32_t *dest,
+                                 const uint32_t *tile_offsets, const float *g_pos_in,
+                                 const float *g_vel_in, float *g_pos_out, float *g_vel_out,
+                                 int64_t np, int nx, int ny, int nz, float kick, float drift,
+                                 float r_split, void *workspace, size_t workspace_bytes,
+                                 uint32_t *stats, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  NEED(force3);
+  NEED(tile_offsets);
+  if (np > 0) {
+    NEED(pos);
+    NEED(g_pos_in);
+    NEED(g_vel_in);
+    NEED(g_pos_out);
+    NEED(g_vel_out);
+    PMGB_REQUIRE(g_pos_in != g_pos_out && g_vel_in != g_vel_out && g_pos_out != g_vel_out,
+                 "the reverse step writes to separate output buffers");
+  }
+  return fpm_step_sorted_vjp(pos, force3, dest, tile_offsets, g_pos_in, g_vel_in, g_pos_out,
+                             g_vel_out, np, nx, ny, nz, kick, drift, r_split, workspace,
+                             workspace_bytes, stats, stream);
 }
 
 int pmgb_linear_field_colour_f32(void *spec, int nx, int ny, int nz, float box_x, float box_y,

@@ -102,23 +102,42 @@ int permute3(const float *in, const unsigned *id, int64_t np, float *out,
 int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos,
                  int64_t np, void *sort_ws, size_t sort_bytes, unsigned *stats,
                  cudaStream_t s);
-int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos,
-               float *vel, int64_t np, float kick, float drift, void *sort_ws,
-               size_t sort_bytes, unsigned *stats, cudaStream_t s);
+int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz,
+               const float *pos, float *pos_out, float *vel, int64_t np,
+               float kick, float drift, void *sort_ws, size_t sort_bytes,
+               unsigned *stats, cudaStream_t s);
 int tile_scatter(const float *pos, const float *vel, const unsigned *id,
                  int64_t np, int nx, int ny, int nz, float *pos2, float *vel2,
-                 unsigned *id2, void *sort_ws, size_t sort_bytes, cudaStream_t s);
-int fpm_step_sorted(float *pos, float *vel, unsigned *id, float *pos2,
+                 unsigned *id2, unsigned *dest, void *sort_ws, size_t sort_bytes,
+                 cudaStream_t s);
+const unsigned *tile_offsets(void *sort_ws, int nx, int ny, int nz, int64_t np);
+int fpm_step_sorted(const float *pos, float *vel, const unsigned *id, float *pos2,
                     float *vel2, unsigned *id2, int64_t np, int nx, int ny,
                     int nz, float kick, float drift, float r_split,
                     void *mesh_ws, size_t mesh_bytes, void *sort_ws,
-                    size_t sort_bytes, unsigned *stats, cudaStream_t s);
+                    size_t sort_bytes, float *force3_out, unsigned *dest_out,
+                    unsigned *offsets_out, unsigned *stats, cudaStream_t s);
+int fpm_step_sorted_vjp(const float *pos, const float *force3,
+                        const unsigned *dest, const unsigned *offsets,
+                        const float *gx_in, const float *gv_in, float *gx_out,
+                        float *gv_out, int64_t np, int nx, int ny, int nz,
+                        float kick, float drift, float r_split, void *mesh_ws,
+                        size_t mesh_bytes, unsigned *stats, cudaStream_t s);
 // step.cu: paint of tile-sorted particles -> R2C -> k-space -> C2R inside the
-// composite workspace; *f3 receives the three force meshes.
+// composite workspace; *f3 receives the three force meshes (f3_out when it
+// is given, else the workspace's region).
 int force_meshes_sorted(const float *pos, int64_t np, int nx, int ny, int nz,
                         float r_split, void *ws, size_t bytes, void *sort_ws,
-                        size_t sort_bytes, unsigned *stats, float **f3,
-                        cudaStream_t s);
+                        size_t sort_bytes, unsigned *stats, float *f3_out,
+                        float **f3, cudaStream_t s);
+// step.cu: the composite workspace's [np][3] particle scratch (nullptr and
+// an error left when the workspace is too small).
+float *pm_workspace_particles(void *ws, size_t bytes, int nx, int ny, int nz,
+                              int64_t np);
+// step.cu: the composite workspace's regions used by the sorted adjoint.
+int pm_workspace_regions(void *ws, size_t bytes, int nx, int ny, int nz,
+                         int64_t np, float **mesh, void **dk, void **fk,
+                         float **f3, float **g3, unsigned **work);
 
 // pk.cu
 int power_spectrum(const void *spec, int nx, int ny, int nz, double bx,

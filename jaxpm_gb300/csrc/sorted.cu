@@ -71,7 +71,14 @@ __device__ __forceinline__ uint32_t compact3(uint32_t v) {
 __device__ __forceinline__ uint32_t count_and_rank(unsigned *__restrict__ counts, uint32_t key,
                                                    unsigned active) {
   const int lane = threadIdx.x & 31;
-  unsigned peers = __match_any_sync(active, key);
+  // common case: every active lane has the same key (vote + shuffle only)
+  const int first = __ffs(active) - 1;
+  const uint32_t k0 = __shfl_sync(active, key, first);
+  unsigned peers;
+  if (__all_sync(active, key == k0))
+    peers = active;
+  else
+    peers = __match_any_sync(active, key);
   int leader = __ffs(peers) - 1;
   unsigned base = 0;
   if (lane == leader) base = atomicAdd(counts + key, (unsigned)__popc(peers));
@@ -297,6 +304,16 @@ __device__ __forceinline__ void fixed_add_split(unsigned *lo, unsigned *hi, int 
   atomicAdd(hi + c, q >> 12);
 }
 
+// Tiles with fewer than 4096 particles use one word per cell with 20
+// fractional bits (a cell's sum stays below 4096 < 2^12): half the shared
+// atomics, quantisation 2^-20 per contribution, sums exact.
+constexpr unsigned FIX1_COUNT = 4096;
+constexpr float FIX1_SCALE = 1048576.0f;  // 2^20
+
+__device__ __forceinline__ void fixed_add_single(unsigned *acc, int c, float w) {
+  atomicAdd(acc + c, __float2uint_rn(w * FIX1_SCALE));
+}
+
 // Warp-per-tile painter: each warp of a CTA owns a private box (the two
 // fixed-point halves; the low half is reused as the float box for the
 // flush) and takes tiles from a global counter, so warps never wait on each
@@ -327,9 +344,11 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
     const int ox = (int)compact3(key >> 2) * TILE, oy = (int)compact3(key >> 1) * TILE,
               oz = (int)compact3(key) * TILE;
     const bool boxed = end - beg < FIX_SAFE_COUNT;  // uniform
-    for (int q = lane; q < TBOX; q += 32) {
-      lo[q] = 0u;
-      hi[q] = 0u;
+    const bool single = end - beg < FIX1_COUNT;     // uniform: one word per cell
+    {
+      uint4 *z4 = reinterpret_cast<uint4 *>(lo);  // lo and hi are contiguous, 16-byte aligned
+      const int words = single ? TBOX : 2 * TBOX;
+      for (int q = lane; q < words / 4; q += 32) z4[q] = make_uint4(0u, 0u, 0u, 0u);
     }
     __syncwarp();
     for (unsigned p0 = beg + lane; p0 < end; p0 += 32 * PAINT_ILP) {
@@ -352,11 +371,20 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
       if (boxed && (unsigned)lx < (unsigned)TILE && (unsigned)ly < (unsigned)TILE &&
           (unsigned)lz < (unsigned)TILE) {
         const int q0 = (lx * TB + ly) * TBZ + lz;
+        if (single) {
 #pragma unroll
-        for (int n = 0; n < 8; ++n) {
-          float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
-                              conn_z(n) ? az.k1 : az.k0);
-          fixed_add_split(lo, hi, q0 + conn_x(n) * TB * TBZ + conn_y(n) * TBZ + conn_z(n), w);
+          for (int n = 0; n < 8; ++n) {
+            float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                                conn_z(n) ? az.k1 : az.k0);
+            fixed_add_single(lo, q0 + conn_x(n) * TB * TBZ + conn_y(n) * TBZ + conn_z(n), w);
+          }
+        } else {
+#pragma unroll
+          for (int n = 0; n < 8; ++n) {
+            float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                                conn_z(n) ? az.k1 : az.k0);
+            fixed_add_split(lo, hi, q0 + conn_x(n) * TB * TBZ + conn_y(n) * TBZ + conn_z(n), w);
+          }
         }
       } else {
         if (stats && boxed) atomicAdd(stats, 1u);
@@ -372,8 +400,12 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
     }
     __syncwarp();
     // fixed point -> float in place (each lane reads and rewrites its own cells)
-    for (int q = lane; q < TBOX; q += 32)
-      fbox[q] = fmaf((float)hi[q], 1.0f / 4096.0f, (float)lo[q] * (1.0f / 16777216.0f));
+    if (single) {
+      for (int q = lane; q < TBOX; q += 32) fbox[q] = (float)lo[q] * (1.0f / FIX1_SCALE);
+    } else {
+      for (int q = lane; q < TBOX; q += 32)
+        fbox[q] = fmaf((float)hi[q], 1.0f / 4096.0f, (float)lo[q] * (1.0f / 16777216.0f));
+    }
     const bool tma = use_tma && box_interior(ox, oy, oz, nx, ny, nz);
     if (tma) fence_async_shared();  // generic-proxy writes of fbox -> TMA
     __syncwarp();
@@ -434,7 +466,7 @@ constexpr int RKD_ILP = 2;
 
 __global__ void __launch_bounds__(TILE_THREADS, 4)
 rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int nz,
-                 float *__restrict__ pos, float *__restrict__ vel,
+                 const float *pos, float *pos_out, float *__restrict__ vel,
                  const unsigned *__restrict__ offsets, uint32_t nkeys, float kick, float drift,
                  unsigned *__restrict__ counts, unsigned *__restrict__ rank,
                  unsigned *__restrict__ stats, const __grid_constant__ CUtensorMap tmap,
@@ -548,10 +580,18 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
           vel[3 * (int64_t)p + 1] = vy;
           vel[3 * (int64_t)p + 2] = vz;
           const float xn = x + drift * vx, yn = y + drift * vy, zn = z + drift * vz;
-          pos[3 * (int64_t)p] = xn;
-          pos[3 * (int64_t)p + 1] = yn;
-          pos[3 * (int64_t)p + 2] = zn;
-          k = tile_key(xn, yn, zn, nx, ny, nz);
+          pos_out[3 * (int64_t)p] = xn;
+          pos_out[3 * (int64_t)p + 1] = yn;
+          pos_out[3 * (int64_t)p + 2] = zn;
+          {  // most particles stay in their tile: reuse its key
+            const int cx = wrap_index((int)floorf(xn), nx) - cur.ox,
+                      cy = wrap_index((int)floorf(yn), ny) - cur.oy,
+                      cz = wrap_index((int)floorf(zn), nz) - cur.oz;
+            k = ((unsigned)cx < (unsigned)TILE && (unsigned)cy < (unsigned)TILE &&
+                 (unsigned)cz < (unsigned)TILE)
+                    ? key
+                    : tile_key(xn, yn, zn, nx, ny, nz);
+          }
         }
         if (counts) {
           const unsigned active = __ballot_sync(0xffffffffu, valid);
@@ -591,7 +631,8 @@ __global__ void __launch_bounds__(256)
 scatter_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
                const unsigned *__restrict__ id, const unsigned *__restrict__ rank, int64_t np,
                int nx, int ny, int nz, const unsigned *__restrict__ offsets,
-               float *__restrict__ pos2, float *__restrict__ vel2, unsigned *__restrict__ id2) {
+               float *__restrict__ pos2, float *__restrict__ vel2, unsigned *__restrict__ id2,
+               unsigned *__restrict__ dest) {
   const int64_t span = (int64_t)blockDim.x * SCATTER_ILP;
   for (int64_t base = blockIdx.x * span + threadIdx.x; base < np; base += gridDim.x * span) {
     float x[SCATTER_ILP], y[SCATTER_ILP], z[SCATTER_ILP], u[SCATTER_ILP], v[SCATTER_ILP],
@@ -632,6 +673,7 @@ scatter_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
           vel2[3 * d + 2] = w[j];
         }
         id2[d] = ident[j];
+        if (dest) dest[p] = (unsigned)d;  // where particle p went (for adjoints)
       }
     }
   }
@@ -845,7 +887,7 @@ int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np
   PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
   if (np > 0) {
     scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
-                                                      sc.offsets, pos2, vel2, id2);
+                                                      sc.offsets, pos2, vel2, id2, nullptr);
     PMGB_LAUNCHED("scatter_kernel");
   }
   return PMGB_OK;
@@ -903,9 +945,10 @@ int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos, int64_t 
 }
 
 // Tile-staged gather + kick + drift of tile-sorted particles; counts the new
-// positions per tile and records each particle's rank in its new tile.
-int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos, float *vel,
-               int64_t np, float kick, float drift, void *sort_ws, size_t sort_bytes,
+// positions per tile and records each particle's rank in its new tile.  The
+// drifted positions go to pos_out (pos itself for an in-place update).
+int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float *pos,
+               float *pos_out, float *vel, int64_t np, float kick, float drift, void *sort_ws, size_t sort_bytes,
                unsigned *stats, cudaStream_t s) {
   PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
   const int64_t keys = tile_key_count(nx, ny, nz);
@@ -926,45 +969,402 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, float *pos, 
     clear_error();
   }
   rkd_tiles_kernel<<<tile_grid(keys), TILE_THREADS, 0, s>>>(
-      f3, cs, nx, ny, nz, pos, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts, sc.rank,
+      f3, cs, nx, ny, nz, pos, pos_out, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts,
+      sc.rank,
       stats, map, use_tma);
   PMGB_LAUNCHED("rkd_tiles_kernel");
   return PMGB_OK;
 }
 
 // Scan of the tile counts left by rkd_sorted, then the scatter of
-// (pos, vel, id) to (pos2, vel2, id2) in tile order.
+// (pos, vel, id) to (pos2, vel2, id2) in tile order; dest (nullable)
+// receives each particle's new index.
 int tile_scatter(const float *pos, const float *vel, const unsigned *id, int64_t np, int nx,
-                 int ny, int nz, float *pos2, float *vel2, unsigned *id2, void *sort_ws,
-                 size_t sort_bytes, cudaStream_t s) {
+                 int ny, int nz, float *pos2, float *vel2, unsigned *id2, unsigned *dest,
+                 void *sort_ws, size_t sort_bytes, cudaStream_t s) {
   PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
   const int64_t keys = tile_key_count(nx, ny, nz);
   SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
   PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
   if (np > 0) {
     scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
-                                                      sc.offsets, pos2, vel2, id2);
+                                                      sc.offsets, pos2, vel2, id2, dest);
     PMGB_LAUNCHED("scatter_kernel");
   }
   return PMGB_OK;
+}
+
+// The tile ranges (nkeys + 1 offsets) of the current order.
+const unsigned *tile_offsets(void *sort_ws, int nx, int ny, int nz, int64_t np) {
+  return sort_scratch(sort_ws, nx, ny, nz, np).offsets;
 }
 
 // One FastPM step on tile-sorted particles.  Reads (pos, vel, id), writes
 // the advanced state, sorted by the new positions, to (pos2, vel2, id2).
 // `mesh_ws` is the composite workspace (pm_workspace_size); `sort_ws` the
 // sort scratch holding the ranges of the current order; `stats` (nullable)
-// counts particles found outside their tile (stale ranges).
-int fpm_step_sorted(float *pos, float *vel, unsigned *id, float *pos2, float *vel2,
+// counts particles found outside their tile (stale ranges).  For adjoints
+// the step can record (each nullable): the force meshes [3][nx][ny][nz]
+// (written there instead of the workspace), each particle's index after the
+// step (dest), and the tile ranges of the order it started from (offsets).
+int fpm_step_sorted(const float *pos, float *vel, const unsigned *id, float *pos2, float *vel2,
                     unsigned *id2, int64_t np, int nx, int ny, int nz, float kick, float drift,
                     float r_split, void *mesh_ws, size_t mesh_bytes, void *sort_ws,
-                    size_t sort_bytes, unsigned *stats, cudaStream_t s) {
+                    size_t sort_bytes, float *force3_out, unsigned *dest_out,
+                    unsigned *offsets_out, unsigned *stats, cudaStream_t s) {
   PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
+  if (offsets_out)
+    PMGB_CUDA(cudaMemcpyAsync(offsets_out, tile_offsets(sort_ws, nx, ny, nz, np),
+                              (tile_key_count(nx, ny, nz) + 1) * sizeof(unsigned),
+                              cudaMemcpyDeviceToDevice, s));
   float *f3 = nullptr;
   PMGB_TRY(force_meshes_sorted(pos, np, nx, ny, nz, r_split, mesh_ws, mesh_bytes, sort_ws,
-                               sort_bytes, stats, &f3, s));
-  PMGB_TRY(rkd_sorted(f3, (int64_t)nx * ny * nz, nx, ny, nz, pos, vel, np, kick, drift, sort_ws,
-                      sort_bytes, stats, s));
-  return tile_scatter(pos, vel, id, np, nx, ny, nz, pos2, vel2, id2, sort_ws, sort_bytes, s);
+                               sort_bytes, stats, force3_out, &f3, s));
+  // the drifted positions go to workspace scratch, so pos keeps the
+  // positions the step started from (the reverse step needs them)
+  float *drifted = pm_workspace_particles(mesh_ws, mesh_bytes, nx, ny, nz, np);
+  if (!drifted) return PMGB_ERR_WORKSPACE;
+  PMGB_TRY(rkd_sorted(f3, (int64_t)nx * ny * nz, nx, ny, nz, pos, drifted, vel, np, kick, drift,
+                      sort_ws, sort_bytes, stats, s));
+  return tile_scatter(drifted, vel, id, np, nx, ny, nz, pos2, vel2, id2, dest_out, sort_ws,
+                      sort_bytes, s);
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint of the sorted step.
+//
+// Forward step (particles in tile order i): v' = v + kick F(x),
+// x' = x + drift v', then the sort moves particle p to dest[p] (order i+1).
+// Given the cotangents (g, h) of (x', v') in order i+1, the cotangents of
+// (x, v) in order i are
+//   u = h[dest] + drift g[dest],   gv = u,
+//   gx = g[dest] + (dF/dx)^T (kick u),
+// with (dF/dx)^T w = sum_c w_c grad F_c(x) + grad rho_bar(x) and
+// rho_bar = sum_c A_c^T paint(w_c) (A_c the k-space operator of force
+// component c, A_c^T its conjugate multiplier between an R2C and a C2R).
+// ---------------------------------------------------------------------------
+constexpr int ADJ_WARPS = 4;
+constexpr int ADJ_BOX_WORDS = (3 * TBOX + 31) / 32 * 32;  // three components, 128-byte multiple
+constexpr int ADJ_PAINT_SMEM = ADJ_WARPS * ADJ_BOX_WORDS * 4;
+constexpr unsigned ADJ_BOX_COUNT = 8192;  // larger tiles paint with global atomics
+
+__device__ __forceinline__ void adj_cotangent(const float *__restrict__ gx,
+                                              const float *__restrict__ gv,
+                                              const unsigned *__restrict__ dest, unsigned p,
+                                              float kick, float drift, float g[3], float u[3],
+                                              float w[3]) {
+  const int64_t d = dest ? (int64_t)__ldg(dest + p) : (int64_t)p;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    g[c] = __ldg(gx + 3 * d + c);
+    u[c] = __ldg(gv + 3 * d + c) + drift * g[c];
+    w[c] = kick * u[c];
+  }
+}
+
+// Paint of the three components of w = kick * u, one warp per tile.  The
+// cotangents have no fixed range, so each tile uses block floating point:
+// a first pass finds max |w| over the tile, the box then accumulates
+// round(W * w * S) in int32 with native shared atomics, S a power of two
+// chosen so that no cell can overflow (|sum| <= count * max * S <= 2^30).
+__global__ void __launch_bounds__(ADJ_WARPS * 32)
+adj_paint3_tiles_kernel(float *__restrict__ g3, int64_t cs, int nx, int ny, int nz,
+                        const float *__restrict__ pos, const unsigned *__restrict__ dest,
+                        const float *__restrict__ gx, const float *__restrict__ gv, float kick,
+                        float drift, const unsigned *__restrict__ offsets, uint32_t nkeys,
+                        unsigned *__restrict__ next_tile, unsigned *__restrict__ stats, int vec,
+                        const __grid_constant__ CUtensorMap tmap, int use_tma) {
+  extern __shared__ __align__(128) int abox[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int *acc = abox + warp * ADJ_BOX_WORDS;
+  float *fb = reinterpret_cast<float *>(acc);
+  for (;;) {
+    uint32_t key = 0;
+    if (lane == 0) key = atomicAdd(next_tile, 1u);
+    key = __shfl_sync(0xffffffffu, key, 0);
+    if (key >= nkeys) break;
+    const unsigned beg = __ldg(offsets + key), end = __ldg(offsets + key + 1);
+    if (beg == end) continue;
+    const int ox = (int)compact3(key >> 2) * TILE, oy = (int)compact3(key >> 1) * TILE,
+              oz = (int)compact3(key) * TILE;
+    const unsigned count = end - beg;
+    // pass 1: the tile's largest cotangent component
+    float m = 0.f;
+    for (unsigned p = beg + lane; p < end; p += 32) {
+      float g[3], u[3], w[3];
+      adj_cotangent(gx, gv, dest, p, kick, drift, g, u, w);
+      m = fmaxf(m, fmaxf(fabsf(w[0]), fmaxf(fabsf(w[1]), fabsf(w[2]))));
+      if (isnan(w[0] + w[1] + w[2])) m = INFINITY;  // fmaxf drops NaN: keep it visible
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (m == 0.f) continue;  // nothing to paint (uniform across the warp)
+    // non-finite cotangents skip the box and propagate through global atomics
+    const bool boxed = count < ADJ_BOX_COUNT && isfinite(m);
+    int e = 0;
+    if (boxed) {
+      // S = 2^e with m * S * count <= 2^30
+      e = (int)floorf(30.0f - log2f((float)count) - log2f(m));
+      e = max(-120, min(120, e));
+      for (int q = lane; q < 3 * TBOX; q += 32) acc[q] = 0;
+    }
+    const float S = ldexpf(1.0f, e);
+    __syncwarp();
+    for (unsigned p = beg + lane; p < end; p += 32) {
+      float g[3], u[3], w[3];
+      adj_cotangent(gx, gv, dest, p, kick, drift, g, u, w);
+      const float x = __ldg(pos + 3 * (int64_t)p), y = __ldg(pos + 3 * (int64_t)p + 1),
+                  z = __ldg(pos + 3 * (int64_t)p + 2);
+      Axis ax = cic_axis(x, nx), ay = cic_axis(y, ny), az = cic_axis(z, nz);
+      const int lx = ax.i0 - ox, ly = ay.i0 - oy, lz = az.i0 - oz;
+      if (boxed && (unsigned)lx < (unsigned)TILE && (unsigned)ly < (unsigned)TILE &&
+          (unsigned)lz < (unsigned)TILE) {
+        const int q0 = (lx * TB + ly) * TBZ + lz;
+        const float ws0 = w[0] * S, ws1 = w[1] * S, ws2 = w[2] * S;
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          const float W = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                                    conn_z(n) ? az.k1 : az.k0);
+          const int q = q0 + conn_x(n) * TB * TBZ + conn_y(n) * TBZ + conn_z(n);
+          atomicAdd(acc + q, __float2int_rn(W * ws0));
+          atomicAdd(acc + TBOX + q, __float2int_rn(W * ws1));
+          atomicAdd(acc + 2 * TBOX + q, __float2int_rn(W * ws2));
+        }
+      } else {
+        if (stats && boxed) atomicAdd(stats, 1u);
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          const float W = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                                    conn_z(n) ? az.k1 : az.k0);
+          const int64_t c = cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
+                                       conn_z(n) ? az.i1 : az.i0, ny, nz);
+          atomicAdd(g3 + c, W * w[0]);
+          atomicAdd(g3 + cs + c, W * w[1]);
+          atomicAdd(g3 + 2 * cs + c, W * w[2]);
+        }
+      }
+    }
+    if (!boxed) continue;
+    __syncwarp();
+    const float inv = ldexpf(1.0f, -e);
+    for (int q = lane; q < 3 * TBOX; q += 32) fb[q] = (float)acc[q] * inv;
+    const bool tma = use_tma && box_interior(ox, oy, oz, nx, ny, nz);
+    if (tma) fence_async_shared();
+    __syncwarp();
+    if (tma) {
+      if (lane == 0) {
+        tma_reduce_add_4d(&tmap, oz, oy, ox, 0, fb);
+        bulk_commit();
+        bulk_wait_read();
+      }
+    } else if (vec) {
+      for (int q = lane; q < 3 * TB * TB * 3; q += 32) {
+        const int gq = q % 3, r = q / 3, b = r % TB, r2 = r / TB, a = r2 % TB, c = r2 / TB;
+        const float4 v =
+            *reinterpret_cast<const float4 *>(fb + c * TBOX + (a * TB + b) * TBZ + 4 * gq);
+        if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f) {
+          const int64_t cell = cell_index(wrap_index(ox + a, nx), wrap_index(oy + b, ny),
+                                          wrap_index(oz + 4 * gq, nz), ny, nz);
+          atomicAdd(reinterpret_cast<float4 *>(g3 + c * cs + cell), v);
+        }
+      }
+    } else {
+      for (int q = lane; q < 3 * TB * TB * TB; q += 32) {
+        const int cz = q % TB, r = q / TB, b = r % TB, r2 = r / TB, a = r2 % TB, c = r2 / TB;
+        const float v = fb[c * TBOX + (a * TB + b) * TBZ + cz];
+        if (v != 0.f)
+          atomicAdd(g3 + c * cs + cell_index(wrap_index(ox + a, nx), wrap_index(oy + b, ny),
+                                             wrap_index(oz + cz, nz), ny, nz), v);
+      }
+    }
+    __syncwarp();
+  }
+  if (use_tma && lane == 0) bulk_wait_all();
+}
+
+// Both position terms of the adjoint in one tile-staged gather (one CTA per
+// tile, the boxes of the three force meshes and of rho_bar fetched by TMA
+// and double buffered), plus the cotangent update:
+// gx_out = g + sum_n (rho_bar + w . F)(c_n) dW_n/dx,  gv_out = u.
+constexpr int RBOX_STRIDE = (TBOX + 31) / 32 * 32;
+constexpr uint32_t RBOX_BYTES = TBOX * sizeof(float);
+
+__global__ void __launch_bounds__(TILE_THREADS)
+adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *__restrict__ rbar,
+                        int nx, int ny, int nz, const float *__restrict__ pos,
+                        const unsigned *__restrict__ dest, const float *__restrict__ gx,
+                        const float *__restrict__ gv, float *__restrict__ gx_out,
+                        float *__restrict__ gv_out, float kick, float drift,
+                        const unsigned *__restrict__ offsets, uint32_t nkeys,
+                        unsigned *__restrict__ stats, const __grid_constant__ CUtensorMap fmap,
+                        const __grid_constant__ CUtensorMap rmap, int use_tma) {
+  __shared__ __align__(128) float fb[2][FBOX_STRIDE];
+  __shared__ __align__(128) float rb[2][RBOX_STRIDE];
+  __shared__ __align__(8) uint64_t bar[2];
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_async_shared();
+  }
+  __syncthreads();
+  uint32_t phase0 = 0u, phase1 = 0u;
+  const uint32_t stride = gridDim.x;
+  uint32_t key = blockIdx.x;
+  if (key >= nkeys) return;
+  TileInfo cur = tile_info(offsets, key, nx, ny, nz, use_tma);
+  if (cur.tma && tid == 0) {
+    mbar_expect_tx(&bar[0], FBOX_BYTES + RBOX_BYTES);
+    tma_load_4d(fb[0], &fmap, cur.oz, cur.oy, cur.ox, 0, &bar[0]);
+    tma_load_3d(rb[0], &rmap, cur.oz, cur.oy, cur.ox, &bar[0]);
+  }
+  int buf = 0;
+  for (; key < nkeys; key += stride) {
+    const uint32_t knext = key + stride;
+    TileInfo nxt;
+    nxt.tma = false;
+    if (knext < nkeys) {
+      nxt = tile_info(offsets, knext, nx, ny, nz, use_tma);
+      if (nxt.tma && tid == 0) {
+        fence_async_shared();
+        mbar_expect_tx(&bar[buf ^ 1], FBOX_BYTES + RBOX_BYTES);
+        tma_load_4d(fb[buf ^ 1], &fmap, nxt.oz, nxt.oy, nxt.ox, 0, &bar[buf ^ 1]);
+        tma_load_3d(rb[buf ^ 1], &rmap, nxt.oz, nxt.oy, nxt.ox, &bar[buf ^ 1]);
+      }
+    }
+    if (cur.beg != cur.end) {
+      float *box = fb[buf];
+      float *rbox = rb[buf];
+      if (cur.tma) {
+        const bool ok = mbar_wait(&bar[buf], buf ? phase1 : phase0);
+        if (__syncthreads_or(!ok)) {
+          if (stats && tid == 0) atomicExch(stats + 2, 1u);
+          if (nxt.tma) mbar_wait(&bar[buf ^ 1], buf ? phase0 : phase1);
+          return;
+        }
+        if (buf) phase1 ^= 1u; else phase0 ^= 1u;
+      } else {
+        for (int q = tid; q < 4 * TB * TB * TB; q += TILE_THREADS) {
+          const int c = q % TB, r = q / TB, b = r % TB, r2 = r / TB, a = r2 % TB, comp = r2 / TB;
+          const int64_t cell = cell_index(wrap_index(cur.ox + a, nx), wrap_index(cur.oy + b, ny),
+                                          wrap_index(cur.oz + c, nz), ny, nz);
+          const int li = (a * TB + b) * TBZ + c;
+          if (comp < 3) box[comp * TBOX + li] = __ldg(f3 + comp * cs + cell);
+          else rbox[li] = __ldg(rbar + cell);
+        }
+        __syncthreads();
+      }
+      for (unsigned p = cur.beg + tid; p < cur.end; p += TILE_THREADS) {
+        float g[3], u[3], w[3];
+        adj_cotangent(gx, gv, dest, p, kick, drift, g, u, w);
+        const float x = __ldg(pos + 3 * (int64_t)p), y = __ldg(pos + 3 * (int64_t)p + 1),
+                    z = __ldg(pos + 3 * (int64_t)p + 2);
+        Axis ax = cic_axis(x, nx), ay = cic_axis(y, ny), az = cic_axis(z, nz);
+        AxisGrad dx = cic_axis_grad(x), dy = cic_axis_grad(y), dz = cic_axis_grad(z);
+        const int lx = ax.i0 - cur.ox, ly = ay.i0 - cur.oy, lz = az.i0 - cur.oz;
+        const bool in = (unsigned)lx < (unsigned)TILE && (unsigned)ly < (unsigned)TILE &&
+                        (unsigned)lz < (unsigned)TILE;
+        if (!in && stats) atomicAdd(stats + 1, 1u);
+        float o0 = 0.f, o1 = 0.f, o2 = 0.f;
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          const float kx = conn_x(n) ? ax.k1 : ax.k0, ky = conn_y(n) ? ay.k1 : ay.k0,
+                      kz = conn_z(n) ? az.k1 : az.k0;
+          const float ddx = conn_x(n) ? dx.d1 : dx.d0, ddy = conn_y(n) ? dy.d1 : dy.d0,
+                      ddz = conn_z(n) ? dz.d1 : dz.d0;
+          float v;
+          if (in) {
+            const int q = ((lx + conn_x(n)) * TB + ly + conn_y(n)) * TBZ + lz + conn_z(n);
+            v = rbox[q] + w[0] * box[q] + w[1] * box[TBOX + q] + w[2] * box[2 * TBOX + q];
+          } else {
+            const int64_t c = cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
+                                         conn_z(n) ? az.i1 : az.i0, ny, nz);
+            v = __ldg(rbar + c) + w[0] * __ldg(f3 + c) + w[1] * __ldg(f3 + cs + c) +
+                w[2] * __ldg(f3 + 2 * cs + c);
+          }
+          o0 += v * ddx * ky * kz;
+          o1 += v * kx * ddy * kz;
+          o2 += v * kx * ky * ddz;
+        }
+        gx_out[3 * (int64_t)p] = g[0] + o0;
+        gx_out[3 * (int64_t)p + 1] = g[1] + o1;
+        gx_out[3 * (int64_t)p + 2] = g[2] + o2;
+        gv_out[3 * (int64_t)p] = u[0];
+        gv_out[3 * (int64_t)p + 1] = u[1];
+        gv_out[3 * (int64_t)p + 2] = u[2];
+      }
+    }
+    __syncthreads();
+    cur = nxt;
+    buf ^= 1;
+  }
+}
+
+// One reverse step of the sorted loop (see the block comment above).
+// pos: the positions the step started from (order i); force3: the force
+// meshes the step used; dest: where each particle went (order i -> i+1;
+// NULL = identity); offsets: the tile ranges of order i (nkeys + 1
+// entries); (gx_in, gv_in) in order i+1 -> (gx_out, gv_out) in order i.
+int fpm_step_sorted_vjp(const float *pos, const float *force3, const unsigned *dest,
+                        const unsigned *offsets, const float *gx_in, const float *gv_in,
+                        float *gx_out, float *gv_out, int64_t np, int nx, int ny, int nz,
+                        float kick, float drift, float r_split, void *mesh_ws, size_t mesh_bytes,
+                        unsigned *stats, cudaStream_t s) {
+  float *mesh, *f3w, *g3;
+  void *dk, *fk;
+  unsigned *work;
+  PMGB_TRY(pm_workspace_regions(mesh_ws, mesh_bytes, nx, ny, nz, np, &mesh, &dk, &fk, &f3w, &g3,
+                                &work));
+  (void)f3w;
+  const int64_t ncell = (int64_t)nx * ny * nz, nhalf = (int64_t)nx * ny * (nz / 2 + 1);
+  const int64_t keys = tile_key_count(nx, ny, nz);
+  PMGB_CUDA(cudaMemsetAsync(g3, 0, 3 * ncell * sizeof(float), s));
+  if (np == 0) return PMGB_OK;
+  const bool aligned = nz % 4 == 0 && ncell % 4 == 0 &&
+                       reinterpret_cast<uintptr_t>(g3) % 16 == 0 &&
+                       reinterpret_cast<uintptr_t>(force3) % 16 == 0 &&
+                       reinterpret_cast<uintptr_t>(mesh) % 16 == 0 && nz >= TBZ && ny >= TB &&
+                       nx >= TB;
+  const uint64_t dims4[4] = {(uint64_t)nz, (uint64_t)ny, (uint64_t)nx, 3};
+  const uint64_t strides4[3] = {(uint64_t)nz * 4, (uint64_t)ny * nz * 4, (uint64_t)ncell * 4};
+  const uint32_t box4[4] = {TBZ, TB, TB, 3};
+  const uint64_t dims3[3] = {(uint64_t)nz, (uint64_t)ny, (uint64_t)nx};
+  const uint32_t box3[3] = {TBZ, TB, TB};
+  CUtensorMap gmap, fmap, rmap;
+  memset(&gmap, 0, sizeof(gmap));
+  memset(&fmap, 0, sizeof(fmap));
+  memset(&rmap, 0, sizeof(rmap));
+  int use_tma = 0;
+  if (aligned) {
+    use_tma = make_tensor_map(&gmap, g3, 4, dims4, strides4, box4) == PMGB_OK &&
+              make_tensor_map(&fmap, force3, 4, dims4, strides4, box4) == PMGB_OK &&
+              make_tensor_map(&rmap, mesh, 3, dims3, strides4, box3) == PMGB_OK;
+    clear_error();
+  }
+  static bool ready[64] = {false};
+  int dev = 0;
+  PMGB_CUDA(cudaGetDevice(&dev));
+  if (dev >= 64 || !ready[dev]) {
+    PMGB_TRY(set_smem((const void *)adj_paint3_tiles_kernel, ADJ_PAINT_SMEM));
+    if (dev < 64) ready[dev] = true;
+  }
+  // 1. paint of the cotangent-weighted forces
+  PMGB_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
+  const unsigned pgrid = (unsigned)std::min<int64_t>((keys + ADJ_WARPS - 1) / ADJ_WARPS,
+                                                     (int64_t)sm_count() * 4);
+  adj_paint3_tiles_kernel<<<pgrid, ADJ_WARPS * 32, ADJ_PAINT_SMEM, s>>>(
+      g3, ncell, nx, ny, nz, pos, dest, gx_in, gv_in, kick, drift, offsets, (uint32_t)keys, work,
+      stats, aligned ? 1 : 0, gmap, use_tma);
+  PMGB_LAUNCHED("adj_paint3_tiles_kernel");
+  // 2. rho_bar = sum_c A_c^T (painted component c)
+  PMGB_TRY(fft_r2c(g3, fk, nx, ny, nz, 3, s));
+  PMGB_TRY(kspace_forces_vjp(fk, nhalf, dk, nx, ny, nz, r_split, 1, 0, 1.0f / (float)ncell, s));
+  PMGB_TRY(fft_c2r(dk, mesh, nx, ny, nz, 1, s));
+  // 3. gather of both position terms and the cotangent update
+  adj_gather_tiles_kernel<<<tile_grid(keys), TILE_THREADS, 0, s>>>(
+      force3, ncell, mesh, nx, ny, nz, pos, dest, gx_in, gv_in, gx_out, gv_out, kick, drift,
+      offsets, (uint32_t)keys, stats, fmap, rmap, use_tma);
+  PMGB_LAUNCHED("adj_gather_tiles_kernel");
+  return PMGB_OK;
 }
 
 }  // namespace pmgb

@@ -146,7 +146,7 @@ forces_vjp_gather_kernel(const float *__restrict__ f3, int64_t cs,
 // Workspace of the composite calls (every region 256-byte aligned).
 // ---------------------------------------------------------------------------
 struct Layout {
-  size_t mesh, dk, fk, f3, g3, forces, det, total;
+  size_t mesh, dk, fk, f3, g3, forces, work, det, total;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -162,6 +162,7 @@ static Layout layout(int nx, int ny, int nz, int64_t np, int mode) {
   L.f3 = o; o = align256(o + 3 * ncell * 4);
   L.g3 = o; o = align256(o + 3 * ncell * 4);
   L.forces = o; o = align256(o + (size_t)np * 12);
+  L.work = o; o = align256(o + 16);  // tile counter of the dynamically scheduled kernels
   L.det = o;
   if (mode == PMGB_PAINT_DETERMINISTIC) o = align256(o + ncell * 8);
   L.total = o;
@@ -199,9 +200,29 @@ static int force_meshes(const float *pos, int64_t np, int nx, int ny, int nz, fl
   return PMGB_OK;
 }
 
+int pm_workspace_regions(void *ws, size_t bytes, int nx, int ny, int nz, int64_t np,
+                         float **mesh, void **dk, void **fk, float **f3, float **g3,
+                         unsigned **work) {
+  Layout L = layout(nx, ny, nz, np, PMGB_PAINT_BINNED);
+  PMGB_TRY(check_ws(ws, bytes, L));
+  *mesh = WS(float, L.mesh);
+  *dk = WS(void, L.dk);
+  *fk = WS(void, L.fk);
+  *f3 = WS(float, L.f3);
+  *g3 = WS(float, L.g3);
+  *work = WS(unsigned, L.work);
+  return PMGB_OK;
+}
+
+float *pm_workspace_particles(void *ws, size_t bytes, int nx, int ny, int nz, int64_t np) {
+  Layout L = layout(nx, ny, nz, np, PMGB_PAINT_BINNED);
+  if (check_ws(ws, bytes, L) != PMGB_OK) return nullptr;
+  return WS(float, L.forces);
+}
+
 int force_meshes_sorted(const float *pos, int64_t np, int nx, int ny, int nz, float r_split,
                         void *ws, size_t bytes, void *sort_ws, size_t sort_bytes,
-                        unsigned *stats, float **f3, cudaStream_t s) {
+                        unsigned *stats, float *f3_out, float **f3, cudaStream_t s) {
   Layout L = layout(nx, ny, nz, np, PMGB_PAINT_BINNED);
   PMGB_TRY(check_ws(ws, bytes, L));
   const int64_t ncell = (int64_t)nx * ny * nz;
@@ -211,8 +232,8 @@ int force_meshes_sorted(const float *pos, int64_t np, int nx, int ny, int nz, fl
   PMGB_TRY(fft_r2c(mesh, WS(void, L.dk), nx, ny, nz, 1, s));
   PMGB_TRY(kspace_forces(WS(void, L.dk), WS(void, L.fk), nhalf, nx, ny, nz, r_split, 1, 0,
                          1.0f / (float)ncell, s));
-  PMGB_TRY(fft_c2r(WS(void, L.fk), WS(float, L.f3), nx, ny, nz, 3, s));
-  *f3 = WS(float, L.f3);
+  *f3 = f3_out ? f3_out : WS(float, L.f3);
+  PMGB_TRY(fft_c2r(WS(void, L.fk), *f3, nx, ny, nz, 3, s));
   return PMGB_OK;
 }
 

@@ -81,6 +81,26 @@ __device__ __forceinline__ void tma_reduce_add_3d(const CUtensorMap *map, int c0
       : "memory");
 }
 
+// 4-D tiled reduce-add of a shared-memory box into global memory.
+__device__ __forceinline__ void tma_reduce_add_4d(const CUtensorMap *map, int c0, int c1, int c2,
+                                                  int c3, const void *src) {
+  asm volatile(
+      "cp.reduce.async.bulk.tensor.4d.global.shared::cta.add.tile.bulk_group"
+      " [%0, {%1, %2, %3, %4}], [%5];" ::"l"(reinterpret_cast<uint64_t>(map)),
+      "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_addr(src))
+      : "memory");
+}
+
+// 3-D tiled load of the tensor-map box at (c0, c1, c2), completing on `bar`.
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1,
+                                            int c2, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_addr(bar))
+      : "memory");
+}
+
 __device__ __forceinline__ void bulk_commit() {
   asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }

@@ -153,15 +153,21 @@ class SortedFastPM:
                   _lib.ptr(self.sort_ws), self.sort_bytes, _lib.stream())
         self.stats_buf.zero_()
 
-    def step(self, i, stream=None):
+    def step(self, i, stream=None, pos_in=None, pos_out=None, record=None):
+        """Runs step ``i``.  ``pos_in``/``pos_out`` replace the internal
+        position buffers of this step; ``record = (force3, dest, offsets)``
+        keeps what the reverse step needs."""
         a, b = self.cur, 1 - self.cur
         nx, ny, nz = self.mesh_shape
         s = _lib.stream() if stream is None else stream
-        _lib.call("pmgb_fpm_step_sorted_f32", _lib.ptr(self.pos[a]), _lib.ptr(self.vel[a]),
-                  _lib.ptr(self.ids[a]), _lib.ptr(self.pos[b]), _lib.ptr(self.vel[b]),
-                  _lib.ptr(self.ids[b]), self.n, nx, ny, nz, float(self.kick[i]),
-                  float(self.drift[i]), self.r_split, _lib.ptr(self.ws), self.ws_bytes,
-                  _lib.ptr(self.sort_ws), self.sort_bytes, _lib.ptr(self.stats_buf), s)
+        f3, dest, offs = record if record is not None else (None, None, None)
+        _lib.call("pmgb_fpm_step_sorted_f32",
+                  _lib.ptr(self.pos[a] if pos_in is None else pos_in), _lib.ptr(self.vel[a]),
+                  _lib.ptr(self.ids[a]), _lib.ptr(self.pos[b] if pos_out is None else pos_out),
+                  _lib.ptr(self.vel[b]), _lib.ptr(self.ids[b]), self.n, nx, ny, nz,
+                  float(self.kick[i]), float(self.drift[i]), self.r_split, _lib.ptr(self.ws),
+                  self.ws_bytes, _lib.ptr(self.sort_ws), self.sort_bytes, _lib.ptr(f3),
+                  _lib.ptr(dest), _lib.ptr(offs), _lib.ptr(self.stats_buf), s)
         self.cur = b
 
     def run(self, steps=None):
@@ -195,48 +201,63 @@ class SortedFastPM:
         c = self.stats_buf.cpu().tolist()
         return {"paint": c[0], "gather": c[1], "tma_wait_timeout": c[2]}
 
+    def alloc_store(self):
+        """Buffers of what the forward run records for the reverse sweep:
+        ``(positions [n,Np,3], force meshes [n,3,nx,ny,nz], dest [n,Np],
+        tile ranges [n,keys+1])``."""
+        n, dev = self.n_steps, self.ws.device
+        nx, ny, nz = self.mesh_shape
+        keys = _lib.load().pmgb_tile_key_count(nx, ny, nz)
+        return (torch.empty((n, self.n, 3), dtype=torch.float32, device=dev),
+                torch.empty((n, 3, nx, ny, nz), dtype=torch.float32, device=dev),
+                torch.empty((n, self.n), dtype=torch.int32, device=dev),
+                torch.empty((n, keys + 1), dtype=torch.int32, device=dev))
+
     def vjp(self, pos, vel, g_pos, g_vel, store=None):
         """Forward run from ``(pos, vel)`` (caller's order) then the reverse
         sweep; returns the final state and the cotangents of the initial
-        state, all in the caller's order.  Positions and particle ids before
-        every step are kept (``store``: preallocated ``([n,Np,3] float32,
-        [n,Np] int32)`` or allocated here).  Cotangents stay in the caller's
-        order and are gathered into each step's tile order for its adjoint."""
+        state, all in the caller's order.
+
+        Each forward step records the positions it starts from, its force
+        meshes, where each particle moved in the re-sort and the tile ranges
+        (``store`` from ``alloc_store()``, or allocated here).  The reverse
+        sweep then runs in tile order throughout: the cotangents are put in
+        the final tile order once, each ``pmgb_fpm_step_sorted_vjp_f32``
+        pulls them one re-sort back, and the result is returned to the
+        caller's order once."""
         n = self.n_steps
         nx, ny, nz = self.mesh_shape
         if store is None:
-            store = (torch.empty((n, self.n, 3), dtype=torch.float32, device=self.ws.device),
-                     torch.empty((n, self.n), dtype=torch.int32, device=self.ws.device))
-        xs, ids = store
+            store = self.alloc_store()
+        xs, f3s, dests, offs = store
         self.load(pos, vel)
+        ids0 = self.ids[self.cur].clone()
+        if n:
+            xs[0].copy_(self.pos[self.cur])
         for i in range(n):
-            xs[i].copy_(self.pos[self.cur])
-            ids[i].copy_(self.ids[self.cur])
-            self.step(i)
+            out = xs[i + 1] if i + 1 < n else None
+            self.step(i, pos_in=xs[i], pos_out=out, record=(f3s[i], dests[i], offs[i]))
         final = self.state()
-        gx, gv = g_pos.contiguous().clone(), g_vel.contiguous().clone()
         if not hasattr(self, "_adj"):
             e = lambda: torch.empty((self.n, 3), dtype=torch.float32, device=self.ws.device)  # noqa
             self._adj = (e(), e(), e(), e())
-        sgx, sgv, ku, gp = self._adj
+        gxa, gva, gxb, gvb = self._adj
         s = _lib.stream()
+        idn = self.ids[self.cur]
+        _lib.call("pmgb_permute3_f32", _lib.ptr(g_pos.contiguous()), _lib.ptr(idn), self.n,
+                  _lib.ptr(gxa), s)
+        _lib.call("pmgb_permute3_f32", _lib.ptr(g_vel.contiguous()), _lib.ptr(idn), self.n,
+                  _lib.ptr(gva), s)
         for i in reversed(range(n)):
-            _lib.call("pmgb_permute3_f32", _lib.ptr(gx), _lib.ptr(ids[i]), self.n, _lib.ptr(sgx), s)
-            _lib.call("pmgb_permute3_f32", _lib.ptr(gv), _lib.ptr(ids[i]), self.n, _lib.ptr(sgv), s)
-            # u = gv + drift*gx ; ku = kick*u ; gx += (dF/dx)^T ku ; gv = u
-            _lib.call("pmgb_lpt_combine_f32", _lib.ptr(sgv), _lib.ptr(sgx), 3 * self.n, 1.0,
-                      float(self.drift[i]), _lib.ptr(sgv), s)
-            _lib.call("pmgb_lpt_combine_f32", _lib.ptr(sgv), None, 3 * self.n,
-                      float(self.kick[i]), 0.0, _lib.ptr(ku), s)
-            _lib.call("pmgb_pm_forces_vjp_f32", _lib.ptr(xs[i]), self.n, nx, ny, nz, self.r_split,
-                      _lib.PAINT_BINNED, _lib.ptr(ku), _lib.ptr(gp), _lib.ptr(self.ws),
-                      self.ws_bytes, s)
-            _lib.call("pmgb_lpt_combine_f32", _lib.ptr(sgx), _lib.ptr(gp), 3 * self.n, 1.0, 1.0,
-                      _lib.ptr(sgx), s)
-            _lib.call("pmgb_unpermute3_f32", _lib.ptr(sgx), _lib.ptr(ids[i]), self.n,
-                      _lib.ptr(gx), s)
-            _lib.call("pmgb_unpermute3_f32", _lib.ptr(sgv), _lib.ptr(ids[i]), self.n,
-                      _lib.ptr(gv), s)
+            _lib.call("pmgb_fpm_step_sorted_vjp_f32", _lib.ptr(xs[i]), _lib.ptr(f3s[i]),
+                      _lib.ptr(dests[i]), _lib.ptr(offs[i]), _lib.ptr(gxa), _lib.ptr(gva),
+                      _lib.ptr(gxb), _lib.ptr(gvb), self.n, nx, ny, nz, float(self.kick[i]),
+                      float(self.drift[i]), self.r_split, _lib.ptr(self.ws), self.ws_bytes,
+                      _lib.ptr(self.stats_buf), s)
+            gxa, gxb, gva, gvb = gxb, gxa, gvb, gva
+        gx, gv = torch.empty_like(gxa), torch.empty_like(gva)
+        _lib.call("pmgb_unpermute3_f32", _lib.ptr(gxa), _lib.ptr(ids0), self.n, _lib.ptr(gx), s)
+        _lib.call("pmgb_unpermute3_f32", _lib.ptr(gva), _lib.ptr(ids0), self.n, _lib.ptr(gv), s)
         return final, (gx, gv)
 
 

@@ -164,3 +164,65 @@ def test_sorted_adjoint_matches_lattice_adjoint(cuda, golden):
     (_, _), (bx, bv) = eng.vjp(x0, v0, gx, gv)
     assert rel_l2(bx.cpu(), ax.cpu()) < 1e-4
     assert rel_l2(bv.cpu(), av.cpu()) < 1e-4
+
+
+@pytest.mark.parametrize("shape", [(32, 32, 32), (24, 40, 16)])
+def test_sorted_adjoint_clustered(cuda, shape):
+    """Reverse sweep of the sorted loop on a clustered distribution: one tile
+    holds more than the shared-memory box limit (global-atomic path), others
+    sit on the periodic edges (wrapped boxes), the rest is a perturbed
+    lattice.  Reference: the lattice-order adjoint (pm_forces_vjp)."""
+    from jaxpm_gb300 import cosmology, simulate
+    n = int(np.prod(shape))
+    rng = np.random.default_rng(11)
+    lat = cic.lattice(shape).reshape(-1, 3).astype(np.float64)
+    pos = lat + rng.normal(0, 0.3, lat.shape)
+    k = 9000
+    pos[:k] = rng.uniform(8.0, 15.99, (k, 3))           # one 8^3 tile, > 8192 particles
+    pos[k:k + 2000] = rng.uniform(-0.5, 0.5, (2000, 3))  # straddles the periodic corner
+    vel = rng.normal(0, 0.2, lat.shape)
+    x0, v0 = T(pos.astype(np.float32), cuda), T(vel.astype(np.float32), cuda)
+    g = torch.Generator(device=cuda).manual_seed(5)
+    gx = torch.randn(x0.shape, device=cuda, generator=g)
+    gv = torch.randn(x0.shape, device=cuda, generator=g)
+    cosmo = cosmology.Planck15()
+    ref = simulate.FastPM(shape, cosmo, 0.5, 1.0, 2, n_particles=n, device=cuda)
+    (ax_f, av_f), (ax, av) = ref.vjp(x0, v0, gx, gv)
+    eng = simulate.SortedFastPM(shape, cosmo, 0.5, 1.0, 2, n_particles=n, device=cuda)
+    (bx_f, bv_f), (bx, bv) = eng.vjp(x0, v0, gx, gv)
+    assert rel_l2(bx_f.cpu(), ax_f.cpu()) < 1e-5
+    assert rel_l2(bx.cpu(), ax.cpu()) < 1e-4
+    assert rel_l2(bv.cpu(), av.cpu()) < 1e-4
+    assert eng.stats["tma_wait_timeout"] == 0
+
+
+def test_sorted_reverse_step_identity_dest(cuda, lib):
+    """pmgb_fpm_step_sorted_vjp_f32 with dest = NULL (no re-sort) on the
+    quantities recorded by one sorted step equals the generic adjoint
+    u = gv + drift gx, gx += (dF/dx)^T (kick u), gv = u."""
+    from jaxpm_gb300 import _lib, cosmology, simulate
+    n = 16
+    shape = (n,) * 3
+    np_ = n ** 3
+    rng = np.random.default_rng(2)
+    lat = cic.lattice(shape).reshape(-1, 3)
+    x = T((lat + rng.normal(0, 0.4, lat.shape)).astype(np.float32), cuda)
+    v = T(rng.normal(0, 0.1, lat.shape).astype(np.float32), cuda)
+    eng = simulate.SortedFastPM(shape, cosmology.Planck15(), 0.3, 1.0, 1, device=cuda)
+    eng.load(x, v)
+    xs = eng.pos[eng.cur].clone()
+    f3, dest, offs = [t[0] for t in eng.alloc_store()[1:]]
+    eng.step(0, record=(f3, dest, offs))
+    gx = torch.randn((np_, 3), device=cuda)
+    gv = torch.randn((np_, 3), device=cuda)
+    gxo, gvo = torch.empty_like(gx), torch.empty_like(gv)
+    kick, drift = float(eng.kick[0]), float(eng.drift[0])
+    s = _lib.stream()
+    _lib.call("pmgb_fpm_step_sorted_vjp_f32", _lib.ptr(xs), _lib.ptr(f3), None, _lib.ptr(offs),
+              _lib.ptr(gx), _lib.ptr(gv), _lib.ptr(gxo), _lib.ptr(gvo), np_, n, n, n, kick,
+              drift, 0.0, _lib.ptr(eng.ws), eng.ws_bytes, None, s)
+    ref = simulate.FastPM(shape, cosmology.Planck15(), 0.3, 1.0, 1, device=cuda)
+    rx, rv = gx.clone(), gv.clone()
+    ref.step_vjp(xs, rx, rv, 0)
+    assert rel_l2(gvo.cpu(), rv.cpu()) < 1e-6
+    assert rel_l2(gxo.cpu(), rx.cpu()) < 1e-4
