@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--skip", default="", help="comma list of legs to skip: "
                     "adjoint,plain,e2e,cpu,clocks")
     ap.add_argument("--phases-only", action="store_true")
+    ap.add_argument("--fft", default=None, choices=["cufft", "fused"],
+                    help="FFT path of the force evaluation (library default if omitted)")
     return ap.parse_args()
 
 
@@ -179,6 +181,9 @@ def run_gb300(args):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     lib = _lib.load()
+    if args.fft is not None:
+        from jaxpm_gb300 import distributed
+        distributed.set_fft_path(args.fft)
     skip = set(filter(None, args.skip.split(",")))
     n = args.mesh
     Np = n**3
@@ -192,12 +197,12 @@ def run_gb300(args):
     s = _lib.stream(dev)
     nx = ny = nz = n
     ncell = n**3
-    nh = n * n * (n // 2 + 1)
+    mf_bytes = lib.pmgb_mesh_forces_workspace_size(nx, ny, nz)
+    spectral = bool(lib.pmgb_fft3_supported(nx, ny, nz)) and lib.pmgb_fft_path() == 1
     # buffers of the phase-by-phase step: the same C-ABI calls the composite
     # step makes, issued separately so that each phase is timed on the stream
     buf = {"mesh": torch.empty(ncell, dtype=torch.float32, device=dev),
-           "dk": torch.empty(nh, dtype=torch.complex64, device=dev),
-           "fk": torch.empty(3 * nh, dtype=torch.complex64, device=dev),
+           "mfws": torch.empty(mf_bytes, dtype=torch.uint8, device=dev),
            "f3": torch.empty(3 * ncell, dtype=torch.float32, device=dev),
            "det": torch.empty(ncell * 8 if mode == _lib.PAINT_DETERMINISTIC else 1,
                               dtype=torch.uint8, device=dev)}
@@ -207,12 +212,12 @@ def run_gb300(args):
     if engine == "sorted":
         eng = simulate.SortedFastPM((n,) * 3, cosmo, 0.1, 1.0, K, device=dev)
         kick, drift = eng.kick, eng.drift
-        phase_names = ["paint", "r2c", "kspace", "c2r", "read_kick_drift", "sort"]
+        phase_names = ["paint", "forces", "read_kick_drift", "sort"]
     else:
         eng = simulate.FastPM((n,) * 3, cosmo, 0.1, 1.0, K, paint_mode=mode, device=dev)
         kick, drift = eng.kick, eng.drift
         x, v = x0.clone(), v0.clone()
-        phase_names = ["paint", "r2c", "kspace", "c2r", "read_kick_drift"]
+        phase_names = ["paint", "forces", "read_kick_drift"]
     events = [[torch.cuda.Event(enable_timing=True) for _ in range(len(phase_names) + 1)]
               for _ in range(K)]
 
@@ -241,27 +246,24 @@ def run_gb300(args):
             _lib.call("pmgb_cic_paint_f32", P("mesh"), nx, ny, nz, _lib.ptr(px), Np, None, 1.0,
                       mode, 0, P("det"), det_bytes, s)
         rec(1)
-        _lib.call("pmgb_fft_r2c_f32", P("mesh"), P("dk"), nx, ny, nz, 1, s)
+        # density -> three force meshes (fused FFT pipeline, or cuFFT)
+        _lib.call("pmgb_mesh_forces_f32", P("mesh"), P("f3"), nx, ny, nz, 0.0, P("mfws"),
+                  mf_bytes, s)
         rec(2)
-        _lib.call("pmgb_kspace_forces_f32", P("dk"), P("fk"), nh, nx, ny, nz, 0.0, 1, 0,
-                  1.0 / ncell, s)
-        rec(3)
-        _lib.call("pmgb_fft_c2r_f32", P("fk"), P("f3"), nx, ny, nz, 3, 0, s)
-        rec(4)
         if engine == "sorted":
             _lib.call("pmgb_read3_kick_drift_binned_f32", P("f3"), ncell, nx, ny, nz,
                       _lib.ptr(px), _lib.ptr(pv), Np, float(kick[i]), float(drift[i]),
                       _lib.ptr(eng.sort_ws), eng.sort_bytes, _lib.ptr(eng.stats_buf), s)
-            rec(5)
+            rec(3)
             _lib.call("pmgb_tile_scatter_f32", _lib.ptr(px), _lib.ptr(pv), _lib.ptr(eng.ids[a]),
                       Np, nx, ny, nz, _lib.ptr(eng.pos[b]), _lib.ptr(eng.vel[b]),
                       _lib.ptr(eng.ids[b]), None, _lib.ptr(eng.sort_ws), eng.sort_bytes, s)
-            rec(6)
+            rec(4)
             eng.cur = b
         else:
             _lib.call("pmgb_read3_kick_drift_f32", P("f3"), ncell, nx, ny, nz, _lib.ptr(px),
                       _lib.ptr(pv), Np, float(kick[i]), float(drift[i]), None, s)
-            rec(5)
+            rec(3)
 
     # warm-up on the initial state, then reset
     reset()
@@ -298,7 +300,10 @@ def run_gb300(args):
                          mode="deterministic")
     mass_err = abs(rho.double().sum().item() - Np) / Np
     del rho
-    launches_per_step = {"sorted": 7, "lattice": 3}[engine]
+    # own kernels per step: paint (1); forces (3 with the fused FFT pipeline:
+    # plane R2C, x pass with the k-space multiply, plane C2R; else 1 k-space
+    # kernel between cuFFT's); gather (1); sort (3 scan + 1 scatter)
+    launches_per_step = (1 + (3 if spectral else 1) + 1 + (4 if engine == "sorted" else 0))
     if mode == _lib.PAINT_DETERMINISTIC:
         launches_per_step += 1
 
@@ -311,7 +316,8 @@ def run_gb300(args):
               "config": {"workload": f"FastPM {n}^3 particles on {n}^3 mesh, box {n} Mpc/h, "
                                      f"2LPT a=0.1, {K} steps to a=1",
                          "particles": Np, "mesh": [n, n, n], "box_mpc_h": n * BOX_PER_CELL,
-                         "engine": engine, "paint_mode": {0: "atomic", 1: "binned",
+                         "engine": engine, "fft": "fused" if spectral else "cufft",
+                         "paint_mode": {0: "atomic", 1: "binned",
                                                           2: "deterministic"}[mode],
                          "parallelism": "replicas" if world > 1 else "single",
                          "l2": "inputs larger than L2 (positions+velocities 3.2 GB, "
@@ -323,7 +329,11 @@ def run_gb300(args):
 
     # roofline of the dominant own kernel
     peak, peak_kind = peaks()
-    alg = {"paint": 16.0, "read_kick_drift": 60.0, "kspace": 16.0}
+    # algorithmic bytes per particle (Np = mesh cells): paint 12 read + 4
+    # write; forces 4 read + 12 write + the half spectra in and out of each
+    # of its three passes (4 + 4, 4 + 12, 12 + 12 at nz/2+1 of nz); gather
+    # 12 force + 24 read + 24 write
+    alg = {"paint": 16.0, "forces": 48.0, "read_kick_drift": 60.0}
     own = {k: phase_ms[k] for k in alg}
     dom = max(own, key=own.get)
     achieved = alg[dom] * Np / (phase_ms[dom] / 1e3) / 1e9

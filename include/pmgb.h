@@ -167,7 +167,53 @@ int pmgb_fft_r2c_f32(const float *in, void *out, int nx, int ny, int nz,
 int pmgb_fft_c2r_f32(void *in, float *out, int nx, int ny, int nz, int batch,
                      int normalize, pmgb_stream_t stream);
 
+/* The library's own 3-D FFT (power-of-two nx in [8,1024], ny in [64,512],
+ * nz in [16,512]): a cluster-of-CTAs y-z plane transform and an x-column
+ * transform, in-place radix-8 stages in shared memory.  Its half spectra
+ * use padded rows: [nx][ny][pmgb_fft3_pitch(nz)] complex, modes
+ * kz < nz/2+1 meaningful (the forward transform zeroes the padding).  The
+ * composite force calls (pmgb_pm_forces_f32, the FastPM steps and their
+ * adjoints) use it, fused with the k-space kernel, whenever the mesh shape
+ * allows; otherwise cuFFT.  No reference counterpart: the reference's
+ * fft3d (distributed.py:37-42) is XLA's FFT. */
+int pmgb_fft3_supported(int nx, int ny, int nz);
+int pmgb_fft3_pitch(int nz);
+
+/* Forward R2C, unnormalised, of `batch` meshes (16-byte aligned input):
+ * in + b*nx*ny*nz -> out + b*nx*ny*pitch. */
+int pmgb_fft3_r2c_f32(const float *in, void *out, int nx, int ny, int nz,
+                      int batch, pmgb_stream_t stream);
+
+/* Inverse C2R, unnormalised, of `batch` padded half spectra (overwritten)
+ * into 16-byte aligned meshes.  The imaginary parts of the kz = 0 and
+ * kz = nz/2 modes are ignored. */
+int pmgb_fft3_c2r_f32(void *in, float *out, int nx, int ny, int nz, int batch,
+                      pmgb_stream_t stream);
+
+/* FFT path of the composite calls (process-wide): PMGB_FFT_CUFFT (default)
+ * or PMGB_FFT_FUSED (the library's FFT pipeline, fused with the k-space
+ * kernel, where pmgb_fft3_supported; cuFFT for other shapes). */
+enum pmgb_fft_path { PMGB_FFT_CUFFT = 0, PMGB_FFT_FUSED = 1 };
+int pmgb_set_fft_path(int path);
+int pmgb_fft_path(void);
+
 /* ---- Fourier-space force kernel (jaxpm/pm.py:49-56) --------------------- */
+
+/* The spectral part of pm_forces on a real density mesh (pm.py:30-56 from
+ * delta to the three force meshes, before the read):
+ * force3[i] = ifft3d(-grad_i * invlaplace * longrange * fft3d(mesh)),
+ * [3][nx][ny][nz].  Through the library's FFT pipeline where
+ * pmgb_fft3_supported and the pointers are 16-byte aligned, else cuFFT
+ * R2C + pmgb_kspace_forces_f32 + C2R.  mesh is not modified. */
+size_t pmgb_mesh_forces_workspace_size(int nx, int ny, int nz);
+int pmgb_mesh_forces_f32(const float *mesh, float *force3, int nx, int ny,
+                         int nz, float r_split, void *workspace,
+                         size_t workspace_bytes, pmgb_stream_t stream);
+
+/* Adjoint: g_mesh = sum_i (ifft3d K_i fft3d)^T g_force3[i]. */
+int pmgb_mesh_forces_vjp_f32(const float *g_force3, float *g_mesh, int nx,
+                             int ny, int nz, float r_split, void *workspace,
+                             size_t workspace_bytes, pmgb_stream_t stream);
 
 /* One pass from delta_k to the three force spectra:
  * force_k[i] = -grad_i(k) * invlaplace(k) * longrange(k) * delta_k * scale,

@@ -49,6 +49,15 @@ SIGNATURES = {
     "pmgb_enmesh_f32": (c_int, [P, c_int, c_int, c_int, P, P, P]),
     "pmgb_fft_r2c_f32": (c_int, [P, P, c_int, c_int, c_int, c_int, P]),
     "pmgb_fft_c2r_f32": (c_int, [P, P, c_int, c_int, c_int, c_int, c_int, P]),
+    "pmgb_fft3_supported": (c_int, [c_int, c_int, c_int]),
+    "pmgb_fft3_pitch": (c_int, [c_int]),
+    "pmgb_fft3_r2c_f32": (c_int, [P, P, c_int, c_int, c_int, c_int, P]),
+    "pmgb_fft3_c2r_f32": (c_int, [P, P, c_int, c_int, c_int, c_int, P]),
+    "pmgb_set_fft_path": (c_int, [c_int]),
+    "pmgb_fft_path": (c_int, []),
+    "pmgb_mesh_forces_workspace_size": (c_size_t, [c_int, c_int, c_int]),
+    "pmgb_mesh_forces_f32": (c_int, [P, P, c_int, c_int, c_int, c_float, P, c_size_t, P]),
+    "pmgb_mesh_forces_vjp_f32": (c_int, [P, P, c_int, c_int, c_int, c_float, P, c_size_t, P]),
     "pmgb_kspace_forces_f32": (c_int, [P, P, c_int64, c_int, c_int, c_int, c_float, c_int, c_int,
                                        c_float, P]),
     "pmgb_kspace_forces_vjp_f32": (c_int, [P, c_int64, P, c_int, c_int, c_int, c_float, c_int,

@@ -202,11 +202,74 @@ int pmgb_fft_c2r_f32(void *in, float *out, int nx, int ny, int nz, int batch, in
   return PMGB_OK;
 }
 
+int pmgb_fft3_supported(int nx, int ny, int nz) {
+  return spectral_supported(nx, ny, nz) ? 1 : 0;
+}
+
+int pmgb_fft3_pitch(int nz) { return nz > 0 ? spectral_pitch(nz) : 0; }
+
+int pmgb_set_fft_path(int path) {
+  BEGIN();
+  PMGB_REQUIRE(path == PMGB_FFT_FUSED || path == PMGB_FFT_CUFFT, "unknown FFT path");
+  set_spectral(path == PMGB_FFT_FUSED);
+  return PMGB_OK;
+}
+
+int pmgb_fft_path(void) { return spectral_enabled() ? PMGB_FFT_FUSED : PMGB_FFT_CUFFT; }
+
+int pmgb_fft3_r2c_f32(const float *in, void *out, int nx, int ny, int nz, int batch,
+                      pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  PMGB_REQUIRE(batch >= 1, "batch must be >= 1");
+  NEED(in);
+  NEED(out);
+  PMGB_REQUIRE(reinterpret_cast<uintptr_t>(in) % 16 == 0, "input must be 16-byte aligned");
+  return spectral_r2c(in, out, nx, ny, nz, batch, stream);
+}
+
+int pmgb_fft3_c2r_f32(void *in, float *out, int nx, int ny, int nz, int batch,
+                      pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  PMGB_REQUIRE(batch >= 1, "batch must be >= 1");
+  NEED(in);
+  NEED(out);
+  PMGB_REQUIRE(reinterpret_cast<uintptr_t>(out) % 16 == 0, "output must be 16-byte aligned");
+  return spectral_c2r(in, out, nx, ny, nz, batch, stream);
+}
+
 static int check_kspace(int nx, int ny, int nz, int grad_order, int fd) {
   PMGB_TRY(check_mesh(nx, ny, nz));
   PMGB_REQUIRE(grad_order == 0 || grad_order == 1, "grad_order must be 0 or 1");
   PMGB_REQUIRE(fd == 0 || fd == 1, "fd_laplace must be 0 or 1");
   return PMGB_OK;
+}
+
+size_t pmgb_mesh_forces_workspace_size(int nx, int ny, int nz) {
+  if (nx <= 0 || ny <= 0 || nz <= 0) return 0;
+  return mesh_forces_workspace_size(nx, ny, nz);
+}
+
+int pmgb_mesh_forces_f32(const float *mesh, float *force3, int nx, int ny, int nz,
+                         float r_split, void *workspace, size_t workspace_bytes,
+                         pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NEED(mesh);
+  NEED(force3);
+  return mesh_forces_ws(mesh, force3, nx, ny, nz, r_split, workspace, workspace_bytes, stream);
+}
+
+int pmgb_mesh_forces_vjp_f32(const float *g_force3, float *g_mesh, int nx, int ny, int nz,
+                             float r_split, void *workspace, size_t workspace_bytes,
+                             pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NEED(g_force3);
+  NEED(g_mesh);
+  return mesh_forces_vjp_ws(g_force3, g_mesh, nx, ny, nz, r_split, workspace, workspace_bytes,
+                            stream);
 }
 
 int pmgb_kspace_forces_f32(const void *delta_k, void *force_k, int64_t comp_stride, int nx,

@@ -130,6 +130,17 @@ int force_meshes_sorted(const float *pos, int64_t np, int nx, int ny, int nz,
                         float r_split, void *ws, size_t bytes, void *sort_ws,
                         size_t sort_bytes, unsigned *stats, float *f3_out,
                         float **f3, cudaStream_t s);
+// step.cu: density mesh -> the three force meshes (the spectral part of
+// pm_forces), with caller workspace (mesh_forces_workspace_size).
+size_t mesh_forces_workspace_size(int nx, int ny, int nz);
+int mesh_forces_ws(const float *mesh, float *f3, int nx, int ny, int nz,
+                   float r_split, void *ws, size_t bytes, cudaStream_t s);
+int mesh_forces_vjp_ws(const float *g3, float *rbar, int nx, int ny, int nz,
+                       float r_split, void *ws, size_t bytes, cudaStream_t s);
+// step.cu: the three force-mesh cotangents g3 -> the density cotangent
+// rbar (spectral pipeline or cuFFT; dk/fk are the workspace's spectra).
+int mesh_forces_vjp(const float *g3, int nx, int ny, int nz, float r_split,
+                    void *dk, void *fk, float *rbar, cudaStream_t s);
 // step.cu: the composite workspace's [np][3] particle scratch (nullptr and
 // an error left when the workspace is too small).
 float *pm_workspace_particles(void *ws, size_t bytes, int nx, int ny, int nz,
@@ -138,6 +149,30 @@ float *pm_workspace_particles(void *ws, size_t bytes, int nx, int ny, int nz,
 int pm_workspace_regions(void *ws, size_t bytes, int nx, int ny, int nz,
                          int64_t np, float **mesh, void **dk, void **fk,
                          float **f3, float **g3, unsigned **work);
+
+// spectral.cu: hand-written three-pass FFT pipeline for power-of-two
+// meshes (nx in [8,1024], ny in [64,512], nz in [16,512]).  Spectra use the
+// layout [nx][ny][spectral_pitch(nz)] complex (kz < nz/2+1 meaningful).
+bool spectral_supported(int nx, int ny, int nz);
+// Process-wide choice: the composite calls use the spectral pipeline when
+// enabled (default) and supported, else cuFFT.  set_spectral returns the
+// previous setting.
+bool spectral_enabled();
+int set_spectral(int enabled);
+int spectral_pitch(int nz);
+int spectral_r2c(const float *in, void *out, int nx, int ny, int nz, int batch,
+                 cudaStream_t s);
+int spectral_c2r(void *in, float *out, int nx, int ny, int nz, int batch,
+                 cudaStream_t s);
+// mesh -> spec (density spectrum, plane-transformed) -> fspec (3 components)
+// -> f3 [3][nx][ny][nz]: the force meshes of kspace_forces + C2R.
+int spectral_forces(const float *mesh, void *spec, void *fspec, float *f3,
+                    int nx, int ny, int nz, float r_split, int order, int fd,
+                    float scale, cudaStream_t s);
+// g3 [3][nx][ny][nz] -> spec3 -> dspec -> rbar: the adjoint of the above.
+int spectral_forces_vjp(const float *g3, void *spec3, void *dspec, float *rbar,
+                        int nx, int ny, int nz, float r_split, int order,
+                        int fd, float scale, cudaStream_t s);
 
 // pk.cu
 int power_spectrum(const void *spec, int nx, int ny, int nz, double bx,

@@ -16,18 +16,10 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "kspace.cuh"
 
 namespace pmgb {
 namespace {
-
-struct AxisEntry {
-  float w;     // 2*pi*fftfreq(n)[i], radians per cell
-  float k2;    // w*w
-  float g1;    // (8 sin w - sin 2w)/6, order-1 gradient factor
-  float g0;    // w with the Nyquist entry zeroed, order-0 gradient factor
-  float fdk2;  // (w * sinc(w / 2pi))^2, finite-difference Laplacian term
-  float pad[3];
-};
 
 std::mutex g_mu;
 std::map<std::pair<int, int>, AxisEntry *> g_tables;
@@ -79,21 +71,6 @@ int axis_table(int n, const AxisEntry **out) {
   return PMGB_OK;
 }
 
-struct Tables {
-  const AxisEntry *x, *y, *z;
-};
-
-int tables(int nx, int ny, int nz, Tables *t) {
-  PMGB_TRY(axis_table(nx, &t->x));
-  PMGB_TRY(axis_table(ny, &t->y));
-  PMGB_TRY(axis_table(nz, &t->z));
-  return PMGB_OK;
-}
-
-struct Elem {
-  AxisEntry X, Y, Z;
-};
-
 __device__ __forceinline__ Elem element(const Tables &t, uint32_t e, uint32_t ny, uint32_t nzh) {
   uint32_t k = e % nzh, r = e / nzh, j = r % ny, i = r / ny;
   Elem el;
@@ -103,40 +80,16 @@ __device__ __forceinline__ Elem element(const Tables &t, uint32_t e, uint32_t ny
   return el;
 }
 
-// -1/k^2 with k=0 -> 0 (kernels.py:87-92): kk summed as ((0 + kx^2) + ky^2) + kz^2.
-__device__ __forceinline__ float inv_laplace(const Elem &el, int fd) {
-  float kk = fd ? __fadd_rn(__fadd_rn(el.X.fdk2, el.Y.fdk2), el.Z.fdk2)
-                : __fadd_rn(__fadd_rn(el.X.k2, el.Y.k2), el.Z.k2);
-  return kk == 0.0f ? 0.0f : -__frcp_rn(kk);
-}
-
-// exp(-k^2 r^2) or 1 (kernels.py:111-115).
-__device__ __forceinline__ float long_range(const Elem &el, float r2) {
-  if (r2 == 0.0f) return 1.0f;
-  float kk = __fadd_rn(__fadd_rn(el.X.k2, el.Y.k2), el.Z.k2);
-  return expf(-kk * r2);
-}
-
 __global__ void __launch_bounds__(256)
 forces_kernel(const float2 *__restrict__ dk, float2 *__restrict__ fk, int64_t cs,
               Tables t, uint32_t ny, uint32_t nzh, uint32_t total, float r2, int order,
               int fd, float scale) {
   for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += gridDim.x * blockDim.x) {
-    Elem el = element(t, e, ny, nzh);
-    float inv = inv_laplace(el, fd);
-    float L = long_range(el, r2);
-    float2 d = dk[e];
-    // pot = (delta * invlaplace) * longrange
-    float px = __fmul_rn(__fmul_rn(d.x, inv), L), py = __fmul_rn(__fmul_rn(d.y, inv), L);
-    float g[3] = {order ? el.X.g1 : el.X.g0, order ? el.Y.g1 : el.Y.g0,
-                  order ? el.Z.g1 : el.Z.g0};
+    float2 f[3];
+    force_modes(element(t, e, ny, nzh), dk[e], r2, order, fd, scale, f);
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      // -(i g) * (px + i py) = g*py - i g*px
-      float2 f = make_float2(__fmul_rn(g[c], py) * scale, -__fmul_rn(g[c], px) * scale);
-      fk[c * cs + e] = f;
-    }
+    for (int c = 0; c < 3; ++c) fk[c * cs + e] = f[c];
   }
 }
 
@@ -146,19 +99,8 @@ forces_vjp_kernel(const float2 *__restrict__ gfk, int64_t cs, float2 *__restrict
                   int fd, float scale) {
   for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += gridDim.x * blockDim.x) {
-    Elem el = element(t, e, ny, nzh);
-    float m = inv_laplace(el, fd) * long_range(el, r2) * scale;
-    float g[3] = {order ? el.X.g1 : el.X.g0, order ? el.Y.g1 : el.Y.g0,
-                  order ? el.Z.g1 : el.Z.g0};
-    float ax = 0.f, ay = 0.f;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      float2 v = gfk[c * cs + e];
-      // conj(K_c) * v with conj(K_c) = (i g_c) * m: (i g)(vx + i vy) = -g vy + i g vx
-      ax -= g[c] * v.y;
-      ay += g[c] * v.x;
-    }
-    gdk[e] = make_float2(ax * m, ay * m);
+    const float2 v[3] = {gfk[e], gfk[cs + e], gfk[2 * cs + e]};
+    gdk[e] = force_modes_adjoint(element(t, e, ny, nzh), v, r2, order, fd, scale);
   }
 }
 
@@ -208,6 +150,13 @@ int geometry(int nx, int ny, int nz, uint32_t *total, uint32_t *nzh) {
 }
 
 }  // namespace
+
+int tables(int nx, int ny, int nz, Tables *t) {
+  PMGB_TRY(axis_table(nx, &t->x));
+  PMGB_TRY(axis_table(ny, &t->y));
+  PMGB_TRY(axis_table(nz, &t->z));
+  return PMGB_OK;
+}
 
 int kspace_forces(const void *dk, void *fk, int64_t cs, int nx, int ny, int nz, float r_split,
                   int order, int fd, float scale, cudaStream_t s) {

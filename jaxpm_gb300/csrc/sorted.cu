@@ -1315,7 +1315,7 @@ int fpm_step_sorted_vjp(const float *pos, const float *force3, const unsigned *d
   PMGB_TRY(pm_workspace_regions(mesh_ws, mesh_bytes, nx, ny, nz, np, &mesh, &dk, &fk, &f3w, &g3,
                                 &work));
   (void)f3w;
-  const int64_t ncell = (int64_t)nx * ny * nz, nhalf = (int64_t)nx * ny * (nz / 2 + 1);
+  const int64_t ncell = (int64_t)nx * ny * nz;
   const int64_t keys = tile_key_count(nx, ny, nz);
   PMGB_CUDA(cudaMemsetAsync(g3, 0, 3 * ncell * sizeof(float), s));
   if (np == 0) return PMGB_OK;
@@ -1356,9 +1356,7 @@ int fpm_step_sorted_vjp(const float *pos, const float *force3, const unsigned *d
       stats, aligned ? 1 : 0, gmap, use_tma);
   PMGB_LAUNCHED("adj_paint3_tiles_kernel");
   // 2. rho_bar = sum_c A_c^T (painted component c)
-  PMGB_TRY(fft_r2c(g3, fk, nx, ny, nz, 3, s));
-  PMGB_TRY(kspace_forces_vjp(fk, nhalf, dk, nx, ny, nz, r_split, 1, 0, 1.0f / (float)ncell, s));
-  PMGB_TRY(fft_c2r(dk, mesh, nx, ny, nz, 1, s));
+  PMGB_TRY(mesh_forces_vjp(g3, nx, ny, nz, r_split, dk, fk, mesh, s));
   // 3. gather of both position terms and the cotangent update
   adj_gather_tiles_kernel<<<tile_grid(keys), TILE_THREADS, 0, s>>>(
       force3, ncell, mesh, nx, ny, nz, pos, dest, gx_in, gv_in, gx_out, gv_out, kick, drift,

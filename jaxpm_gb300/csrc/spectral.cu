@@ -1,0 +1,706 @@
+// The spectral part of the PM force (jaxpm/pm.py:30-56: fft3d of the
+// density, the k-space kernels, three ifft3d) and of its adjoint, as
+// hand-written FFTs in three passes over HBM for power-of-two meshes:
+//
+//   plane pass (forward): each x-plane [ny][nz] of a real mesh is transformed
+//     along z (real-to-complex, nz/2+1 modes) and y by one thread-block
+//     cluster of PLANE_CL CTAs.  CTA r holds the rows y = r + CL*l
+//     (l < M = ny/CL) in shared memory, transforms them along z, then along
+//     l (an M-point DFT per column); the last radix-CL step of the y
+//     transform reads the CL partial results of every column from the
+//     cluster's shared memories (DSMEM) and writes the plane's spectrum
+//     [ky][kz] (row pitch `pitch` complex) to HBM.
+//   x pass: one CTA per (ky, XW consecutive kz) transforms the nx values of
+//     each column along x; in the force pipeline it also multiplies by the
+//     three force kernels and transforms each product back along x, so the
+//     density spectrum and the three force spectra never exist in HBM in
+//     full-3-D transformed form.
+//   plane pass (inverse): the mirror of the forward plane pass, per
+//     component, writing the real force meshes.
+//
+// Each pass reads and writes its data once: 6.5 GB per force evaluation at
+// 512^3 against about 16 GB through cuFFT plus a separate k-space kernel.
+//
+// The 1-D transforms are in-place radix-8 Cooley-Tukey: forward stages are
+// decimation in frequency (natural order in, digit-reversed order out),
+// inverse stages decimation in time (digit-reversed in, natural out), so no
+// reordering pass is needed between a forward and an inverse transform.
+// Twiddles come from float32 tables exp(-2 pi i k / n) computed in double
+// precision on the host.  Inverse transforms are unnormalised (as cuFFT's
+// and the 1/N^3 of the force pipeline is folded into the k-space multiply).
+#include <cooperative_groups.h>
+
+#include <atomic>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "kspace.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace pmgb {
+namespace {
+
+constexpr int PLANE_CL = 8;         // CTAs per cluster in the plane passes
+constexpr int PLANE_THREADS = 512;  // threads per plane-pass CTA
+constexpr int XW = 8;               // kz columns per x-pass CTA (64-byte segments)
+constexpr int XPASS_THREADS = 256;
+
+// ---- complex helpers ------------------------------------------------------
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+  return make_float2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  return make_float2(a.x - b.x, a.y - b.y);
+}
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+  return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// a * (-i) (forward) or a * (+i) (inverse)
+template <bool INV>
+__device__ __forceinline__ float2 mul_ni(float2 a) {
+  return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// ---- small DFTs: y[k] = sum_m v[m] exp(-+2 pi i m k / R), in place ------------
+
+template <bool INV>
+__device__ __forceinline__ void dft2(float2 *v) {
+  const float2 a = v[0];
+  v[0] = cadd(a, v[1]);
+  v[1] = csub(a, v[1]);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4(float2 *v) {
+  const float2 t0 = cadd(v[0], v[2]), t1 = csub(v[0], v[2]);
+  const float2 t2 = cadd(v[1], v[3]), t3 = mul_ni<INV>(csub(v[1], v[3]));
+  v[0] = cadd(t0, t2);
+  v[2] = csub(t0, t2);
+  v[1] = cadd(t1, t3);
+  v[3] = csub(t1, t3);
+}
+
+// radix 2 x 4: u_m = v_m + v_{m+4} feed the even outputs, (v_m - v_{m+4}) w8^m
+// the odd ones.
+template <bool INV>
+__device__ __forceinline__ void dft8(float2 *v) {
+  const float r = 0.70710678118654752f;
+  float2 u[4], w[4];
+#pragma unroll
+  for (int m = 0; m < 4; ++m) {
+    u[m] = cadd(v[m], v[m + 4]);
+    w[m] = csub(v[m], v[m + 4]);
+  }
+  {
+    const float2 d = w[1];
+    w[1] = INV ? make_float2(r * (d.x - d.y), r * (d.x + d.y))
+               : make_float2(r * (d.x + d.y), r * (d.y - d.x));
+  }
+  w[2] = mul_ni<INV>(w[2]);
+  {
+    const float2 d = w[3];
+    w[3] = INV ? make_float2(-r * (d.x + d.y), r * (d.x - d.y))
+               : make_float2(r * (d.y - d.x), -r * (d.x + d.y));
+  }
+  dft4<INV>(u);
+  dft4<INV>(w);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    v[2 * j] = u[j];
+    v[2 * j + 1] = w[j];
+  }
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void dft(float2 *v) {
+  if (R == 8) dft8<INV>(v);
+  else if (R == 4) dft4<INV>(v);
+  else dft2<INV>(v);
+}
+
+// ---- in-place radix-8 stages ------------------------------------------------
+//
+// A transform of length n = 2^lgn runs stages with block length L = 2^lg
+// (lg = lgn first), radix R = 2^rb (rb = min(3, lg)) and span S = L / R.
+// Forward (DIF) butterfly (block, j < S): elements base + S m, m < R:
+// DFT_R, then output k2 times w_L^(j k2).  Inverse (DIT) butterfly: the
+// conjugate twiddles first, then the inverse DFT_R; its stages run in the
+// opposite order.  The forward transform leaves frequency k at position
+// dif_pos(k).
+
+__device__ __forceinline__ int dif_pos(int k, int lgn) {
+  int p = 0;
+  for (int lg = lgn; lg > 0;) {
+    const int rb = lg >= 3 ? 3 : lg, sb = lg - rb;
+    p |= (k & ((1 << rb) - 1)) << sb;
+    k >>= rb;
+    lg = sb;
+  }
+  return p;
+}
+
+__device__ __forceinline__ int dif_freq(int p, int lgn) {
+  int k = 0, sh = 0;
+  for (int lg = lgn; lg > 0;) {
+    const int rb = lg >= 3 ? 3 : lg, sb = lg - rb;
+    k |= (p >> sb) << sh;
+    p &= (1 << sb) - 1;
+    sh += rb;
+    lg = sb;
+  }
+  return k;
+}
+
+// One butterfly; `tw` is a table of 2^lgtw entries exp(-2 pi i t / 2^lgtw).
+template <bool INV, int R>
+__device__ __forceinline__ void butterfly(float2 *base, int sstride, int j, int lg,
+                                          const float2 *__restrict__ tw, int lgtw) {
+  float2 v[R];
+#pragma unroll
+  for (int m = 0; m < R; ++m) v[m] = base[m * sstride];
+  const int sh = lgtw - lg;
+  if (INV) {
+#pragma unroll
+    for (int m = 1; m < R; ++m) v[m] = cmulc(v[m], __ldg(tw + ((j * m) << sh)));
+    dft<R, true>(v);
+  } else {
+    dft<R, false>(v);
+#pragma unroll
+    for (int m = 1; m < R; ++m) v[m] = cmul(v[m], __ldg(tw + ((j * m) << sh)));
+  }
+#pragma unroll
+  for (int m = 0; m < R; ++m) base[m * sstride] = v[m];
+}
+
+// One stage over `batch` sequences: element e of sequence q at d[q*qs + e*es].
+// Threads tid, tid+nth, ... take the butterflies, sequence index fastest.
+template <bool INV>
+__device__ __forceinline__ void stage(float2 *d, int lgn, int lg, int es, int qs, int batch,
+                                      const float2 *__restrict__ tw, int lgtw, int tid,
+                                      int nth) {
+  const int rb = lg >= 3 ? 3 : lg, sb = lg - rb;
+  const int total = batch << (lgn - rb);
+  for (int t = tid; t < total; t += nth) {
+    const int b = t / batch, q = t - b * batch;
+    const int blk = b >> sb, j = b & ((1 << sb) - 1);
+    float2 *base = d + q * qs + ((blk << lg) + j) * es;
+    if (rb == 3) butterfly<INV, 8>(base, es << sb, j, lg, tw, lgtw);
+    else if (rb == 2) butterfly<INV, 4>(base, es << sb, j, lg, tw, lgtw);
+    else butterfly<INV, 2>(base, es << sb, j, lg, tw, lgtw);
+  }
+}
+
+// Whole transforms; SYNC is __syncwarp or __syncthreads between stages.
+template <bool CTA>
+__device__ __forceinline__ void group_sync() {
+  if (CTA) __syncthreads();
+  else __syncwarp();
+}
+
+template <bool CTA>
+__device__ void fft_forward(float2 *d, int lgn, int es, int qs, int batch,
+                            const float2 *__restrict__ tw, int lgtw, int tid, int nth) {
+  for (int lg = lgn; lg > 0;) {
+    stage<false>(d, lgn, lg, es, qs, batch, tw, lgtw, tid, nth);
+    group_sync<CTA>();
+    lg -= lg >= 3 ? 3 : lg;
+  }
+}
+
+template <bool CTA>
+__device__ void fft_inverse(float2 *d, int lgn, int es, int qs, int batch,
+                            const float2 *__restrict__ tw, int lgtw, int tid, int nth) {
+  if (lgn == 0) return;
+  int lg = lgn % 3 == 0 ? 3 : lgn % 3;
+  for (;;) {
+    stage<true>(d, lgn, lg, es, qs, batch, tw, lgtw, tid, nth);
+    group_sync<CTA>();
+    if (lg == lgn) break;
+    lg += 3;
+  }
+}
+
+// ---- real <-> half-complex rows (z axis), one warp per row ---------------------
+//
+// A real row x[0..nz) is packed as z[m] = x[2m] + i x[2m+1] (H = nz/2
+// complex).  After the forward H-point transform (digit-reversed Z), the
+// modes X[k], k = 0..H, are E + w^k O and conj(E - w^k O) for the pair
+// (k, H-k), E = (Z[k] + conj Z[H-k])/2, O = -i (Z[k] - conj Z[H-k])/2,
+// w = exp(-2 pi i / nz).  They are written in natural order (H+1 slots).
+
+constexpr int ROW_PAIRS = (256 / 2 + 1 + 31) / 32;  // pairs per lane for H <= 256
+
+__device__ void row_r2c_finish(float2 *row, int lgh, const float2 *__restrict__ twz, int lane) {
+  const int H = 1 << lgh;
+  float2 xa[ROW_PAIRS], xb[ROW_PAIRS];
+#pragma unroll
+  for (int i = 0; i < ROW_PAIRS; ++i) {
+    const int j = lane + 32 * i;
+    if (j <= H / 2) {
+      const float2 a = row[dif_pos(j, lgh)];
+      const float2 b = conjf2(row[dif_pos((H - j) & (H - 1), lgh)]);
+      const float2 e = cscale(cadd(a, b), 0.5f);
+      const float2 o = cscale(mul_ni<false>(csub(a, b)), 0.5f);
+      const float2 t = cmul(__ldg(twz + j), o);
+      xa[i] = cadd(e, t);
+      xb[i] = conjf2(csub(e, t));
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < ROW_PAIRS; ++i) {
+    const int j = lane + 32 * i;
+    if (j <= H / 2) {
+      row[j] = xa[i];
+      row[H - j] = xb[i];
+    }
+  }
+  __syncwarp();
+}
+
+// Inverse: natural X[0..H] -> packed Z'[k] = P + T, Z'[H-k] = conj(P - T),
+// P = X[k] + conj X[H-k], T = i w^-k (X[k] - conj X[H-k]), written at the
+// digit-reversed positions the inverse H-point transform expects; the
+// imaginary parts of X[0] and X[H] are dropped (a real row's modes 0 and
+// nz/2 are real).
+__device__ void row_c2r_start(float2 *row, int lgh, const float2 *__restrict__ twz, int lane) {
+  const int H = 1 << lgh;
+  float2 za[ROW_PAIRS], zb[ROW_PAIRS];
+#pragma unroll
+  for (int i = 0; i < ROW_PAIRS; ++i) {
+    const int j = lane + 32 * i;
+    if (j <= H / 2) {
+      float2 a = row[j], b = row[H - j];
+      if (j == 0) {
+        a.y = 0.f;
+        b.y = 0.f;
+      }
+      const float2 p = cadd(a, conjf2(b));
+      const float2 q = csub(a, conjf2(b));
+      const float2 t = mul_ni<true>(cmulc(q, __ldg(twz + j)));
+      za[i] = cadd(p, t);
+      zb[i] = conjf2(csub(p, t));
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int i = 0; i < ROW_PAIRS; ++i) {
+    const int j = lane + 32 * i;
+    if (j <= H / 2) {
+      row[dif_pos(j, lgh)] = za[i];
+      if (j > 0 && j < H / 2) row[dif_pos(H - j, lgh)] = zb[i];
+    }
+  }
+  __syncwarp();
+}
+
+// ---- plane passes -------------------------------------------------------------
+
+struct PlaneGeom {
+  int ny, nz, lgy, lgz;  // plane size
+  int M, lgm;            // rows per CTA (ny / CL)
+  int sp;                // shared row pitch (complex), even, >= nz/2 + 1
+  int pitch;             // HBM spectrum row pitch (complex), >= nz/2 + 1
+};
+
+// Forward: real planes in[plane][ny][nz] -> out[plane][ky][kz] (pitch),
+// padding columns kz > nz/2 zeroed.
+__global__ void __cluster_dims__(PLANE_CL, 1, 1) __launch_bounds__(PLANE_THREADS, 1)
+plane_r2c_kernel(const float *__restrict__ in, float2 *__restrict__ out, PlaneGeom g,
+                 const float2 *__restrict__ twy, const float2 *__restrict__ twz) {
+  extern __shared__ __align__(16) float2 sm[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int64_t plane = blockIdx.x / PLANE_CL;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = PLANE_THREADS / 32;
+  const int lgh = g.lgz - 1, H = 1 << lgh;
+  // 1. rows y = r + CL*l: load, H-point forward transform, real finish
+  for (int l = warp; l < g.M; l += nwarp) {
+    const int y = r + PLANE_CL * l;
+    const float4 *src =
+        reinterpret_cast<const float4 *>(in + (plane * g.ny + y) * (int64_t)g.nz);
+    float4 *dst = reinterpret_cast<float4 *>(sm + l * g.sp);
+    for (int i = lane; i < g.nz / 4; i += 32) dst[i] = __ldg(src + i);
+    __syncwarp();
+    fft_forward<false>(sm + l * g.sp, lgh, 1, 0, 1, twz, g.lgz, lane, 32);
+    row_r2c_finish(sm + l * g.sp, lgh, twz, lane);
+  }
+  __syncthreads();
+  // 2. M-point forward transform along l of the H+1 columns (w_M = w_ny^CL)
+  fft_forward<true>(sm, g.lgm, g.sp, 1, H + 1, twy, g.lgy, tid, PLANE_THREADS);
+  cluster.sync();
+  // 3. the last radix-CL step: X[k2 + M k1] = sum_s w_CL^(s k1) w_ny^(s k2) Y_s[k2]
+  const int kb = g.M / PLANE_CL;
+  for (int t = tid; t < kb * g.pitch; t += PLANE_THREADS) {
+    const int kk = t / g.pitch, kz = t - kk * g.pitch;
+    const int k2 = r * kb + kk;
+    float2 v[PLANE_CL];
+    if (kz <= H) {
+      const int row = dif_pos(k2, g.lgm);
+#pragma unroll
+      for (int s = 0; s < PLANE_CL; ++s) {
+        const float2 *rem = cluster.map_shared_rank(sm, s);
+        v[s] = cmul(rem[row * g.sp + kz], __ldg(twy + s * k2));
+      }
+      dft8<false>(v);
+    } else {
+#pragma unroll
+      for (int s = 0; s < PLANE_CL; ++s) v[s] = make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < PLANE_CL; ++k1)
+      out[(plane * g.ny + k2 + g.M * k1) * (int64_t)g.pitch + kz] = v[k1];
+  }
+  cluster.sync();  // keep this CTA's shared memory alive while others read it
+}
+
+// Inverse: in[plane][ky][kz] (pitch) -> real planes out[plane][ny][nz]
+// (unnormalised).
+__global__ void __cluster_dims__(PLANE_CL, 1, 1) __launch_bounds__(PLANE_THREADS, 1)
+plane_c2r_kernel(const float2 *__restrict__ in, float *__restrict__ out, PlaneGeom g,
+                 const float2 *__restrict__ twy, const float2 *__restrict__ twz) {
+  extern __shared__ __align__(16) float2 sm[];
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int64_t plane = blockIdx.x / PLANE_CL;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = PLANE_THREADS / 32;
+  const int lgh = g.lgz - 1, H = 1 << lgh;
+  cluster.sync();  // every CTA of the cluster runs before any remote store
+  // 1. first radix-CL step of the inverse y transform, scattered to the
+  //    cluster: V_s[k2] = w_ny^(-s k2) sum_k1 w_CL^(-s k1) X[k2 + M k1]
+  const int kb = g.M / PLANE_CL;
+  for (int t = tid; t < kb * (H + 1); t += PLANE_THREADS) {
+    const int kk = t / (H + 1), kz = t - kk * (H + 1);
+    const int k2 = r * kb + kk;
+    float2 v[PLANE_CL];
+#pragma unroll
+    for (int k1 = 0; k1 < PLANE_CL; ++k1)
+      v[k1] = __ldg(in + (plane * g.ny + k2 + g.M * k1) * (int64_t)g.pitch + kz);
+    dft8<true>(v);
+    const int row = dif_pos(k2, g.lgm);
+#pragma unroll
+    for (int s = 0; s < PLANE_CL; ++s) {
+      float2 *rem = cluster.map_shared_rank(sm, s);
+      rem[row * g.sp + kz] = cmulc(v[s], __ldg(twy + s * k2));
+    }
+  }
+  cluster.sync();
+  // 2. inverse M-point transform along the columns -> natural l
+  fft_inverse<true>(sm, g.lgm, g.sp, 1, H + 1, twy, g.lgy, tid, PLANE_THREADS);
+  // 3. rows: half-complex -> packed, inverse H-point transform, store
+  for (int l = warp; l < g.M; l += nwarp) {
+    const int y = r + PLANE_CL * l;
+    float2 *row = sm + l * g.sp;
+    row_c2r_start(row, lgh, twz, lane);
+    fft_inverse<false>(row, lgh, 1, 0, 1, twz, g.lgz, lane, 32);
+    float4 *dst = reinterpret_cast<float4 *>(out + (plane * g.ny + y) * (int64_t)g.nz);
+    const float4 *src = reinterpret_cast<const float4 *>(row);
+    for (int i = lane; i < g.nz / 4; i += 32) dst[i] = src[i];
+  }
+}
+
+// ---- x pass -------------------------------------------------------------------
+
+enum XMode { X_FORWARD = 0, X_INVERSE = 1, X_FORCES = 2, X_FORCES_ADJ = 3 };
+
+struct XGeom {
+  int nx, ny, lgx, nzh, pitch, chunks;
+  int64_t cs_in, cs_out;  // component strides (complex elements)
+};
+
+// CTA per (ky, chunk of XW columns); buf[x][w].  X_FORWARD: natural x ->
+// natural kx (in place allowed).  X_INVERSE: natural kx -> natural x
+// (unnormalised).  X_FORCES: forward, then for each force component the
+// k-space product and the inverse transform, out + c*cs_out.
+// X_FORCES_ADJ: for each component the forward transform of in + c*cs_in,
+// the conjugate products summed, then the inverse transform.
+template <int MODE>
+__global__ void __launch_bounds__(XPASS_THREADS)
+xpass_kernel(const float2 *in, float2 *out, XGeom g, const float2 *__restrict__ twx, Tables t,
+             float r2, int order, int fd, float scale) {
+  extern __shared__ __align__(16) float2 xs[];
+  float2 *b0 = xs, *b1 = xs + g.nx * XW;
+  const int tid = threadIdx.x;
+  const int ky = blockIdx.x / g.chunks, kz0 = (blockIdx.x - ky * g.chunks) * XW;
+  const int n = g.nx * XW;
+  auto gidx = [&](int x, int w) -> int64_t {
+    return ((int64_t)x * g.ny + ky) * g.pitch + kz0 + w;
+  };
+  if (MODE == X_FORCES_ADJ) {
+    for (int c = 0; c < 3; ++c) {
+      for (int i = tid; i < n; i += XPASS_THREADS)
+        b1[i] = in[c * g.cs_in + gidx(i / XW, i % XW)];
+      __syncthreads();
+      fft_forward<true>(b1, g.lgx, XW, 1, XW, twx, g.lgx, tid, XPASS_THREADS);
+      const AxisEntry Y = t.y[ky];
+      for (int i = tid; i < n; i += XPASS_THREADS) {
+        const int p = i / XW, w = i % XW, kz = kz0 + w;
+        if (kz >= g.nzh) {
+          b0[i] = make_float2(0.f, 0.f);
+          continue;
+        }
+        const AxisEntry X = t.x[dif_freq(p, g.lgx)], Z = t.z[kz];
+        const float gc = c == 0 ? (order ? X.g1 : X.g0)
+                                : (c == 1 ? (order ? Y.g1 : Y.g0) : (order ? Z.g1 : Z.g0));
+        const float2 v = b1[i];
+        float2 acc = c == 0 ? make_float2(0.f, 0.f) : b0[i];
+        acc.x -= gc * v.y;
+        acc.y += gc * v.x;
+        if (c == 2) {
+          Elem el;
+          el.X = X;
+          el.Y = Y;
+          el.Z = Z;
+          const float m = inv_laplace(el, fd) * long_range(el, r2) * scale;
+          acc = make_float2(acc.x * m, acc.y * m);
+        }
+        b0[i] = acc;
+      }
+      __syncthreads();
+    }
+    fft_inverse<true>(b0, g.lgx, XW, 1, XW, twx, g.lgx, tid, XPASS_THREADS);
+    for (int i = tid; i < n; i += XPASS_THREADS) out[gidx(i / XW, i % XW)] = b0[i];
+    return;
+  }
+  // load (X_INVERSE: natural kx into digit-reversed positions)
+  for (int i = tid; i < n; i += XPASS_THREADS) {
+    const int x = i / XW, w = i % XW;
+    const int p = MODE == X_INVERSE ? dif_pos(x, g.lgx) : x;
+    b0[p * XW + w] = in[gidx(x, w)];
+  }
+  __syncthreads();
+  if (MODE == X_INVERSE) {
+    fft_inverse<true>(b0, g.lgx, XW, 1, XW, twx, g.lgx, tid, XPASS_THREADS);
+    for (int i = tid; i < n; i += XPASS_THREADS) out[gidx(i / XW, i % XW)] = b0[i];
+    return;
+  }
+  fft_forward<true>(b0, g.lgx, XW, 1, XW, twx, g.lgx, tid, XPASS_THREADS);
+  if (MODE == X_FORWARD) {
+    for (int i = tid; i < n; i += XPASS_THREADS) {
+      const int kx = i / XW, w = i % XW;
+      out[gidx(kx, w)] = b0[dif_pos(kx, g.lgx) * XW + w];
+    }
+    return;
+  }
+  // X_FORCES
+  const AxisEntry Y = t.y[ky];
+  for (int c = 0; c < 3; ++c) {
+    for (int i = tid; i < n; i += XPASS_THREADS) {
+      const int p = i / XW, w = i % XW, kz = kz0 + w;
+      float2 f[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+      if (kz < g.nzh) {
+        Elem el;
+        el.X = t.x[dif_freq(p, g.lgx)];
+        el.Y = Y;
+        el.Z = t.z[kz];
+        force_modes(el, b0[i], r2, order, fd, scale, f);
+      }
+      b1[i] = c == 0 ? f[0] : (c == 1 ? f[1] : f[2]);
+    }
+    __syncthreads();
+    fft_inverse<true>(b1, g.lgx, XW, 1, XW, twx, g.lgx, tid, XPASS_THREADS);
+    for (int i = tid; i < n; i += XPASS_THREADS)
+      out[c * g.cs_out + gidx(i / XW, i % XW)] = b1[i];
+    __syncthreads();
+  }
+}
+
+// ---- host side ----------------------------------------------------------------
+
+std::mutex g_tw_mu;
+std::map<std::pair<int, int>, float2 *> g_twiddles;
+
+// exp(-2 pi i k / n), k < n, per (device, n).
+int twiddles(int n, const float2 **out) {
+  int dev = 0;
+  PMGB_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_tw_mu);
+  auto key = std::make_pair(dev, n);
+  auto it = g_twiddles.find(key);
+  if (it != g_twiddles.end()) {
+    *out = it->second;
+    return PMGB_OK;
+  }
+  std::vector<float2> h(n);
+  for (int k = 0; k < n; ++k) {
+    const double a = -2.0 * M_PI * (double)k / (double)n;
+    h[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  float2 *d = nullptr;
+  PMGB_CUDA(cudaMalloc(&d, n * sizeof(float2)));
+  cudaError_t err = cudaMemcpy(d, h.data(), n * sizeof(float2), cudaMemcpyHostToDevice);
+  if (err != cudaSuccess) {
+    cudaFree(d);
+    return fail(PMGB_ERR_CUDA, std::string("twiddle upload: ") + cudaGetErrorString(err));
+  }
+  g_twiddles[key] = d;
+  *out = d;
+  return PMGB_OK;
+}
+
+int ilog2(int n) {
+  int l = 0;
+  while ((1 << l) < n) ++l;
+  return l;
+}
+
+bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+PlaneGeom plane_geom(int ny, int nz, int pitch) {
+  PlaneGeom g;
+  g.ny = ny;
+  g.nz = nz;
+  g.lgy = ilog2(ny);
+  g.lgz = ilog2(nz);
+  g.M = ny / PLANE_CL;
+  g.lgm = ilog2(g.M);
+  g.sp = (nz / 2 + 2) & ~1;
+  g.pitch = pitch;
+  return g;
+}
+
+size_t plane_smem(const PlaneGeom &g) { return (size_t)g.M * g.sp * sizeof(float2); }
+
+int set_dyn_smem(const void *fn, size_t bytes) {
+  PMGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return PMGB_OK;
+}
+
+int plane_r2c(const float *in, float2 *out, int nplanes, int ny, int nz, int pitch,
+              cudaStream_t s) {
+  const PlaneGeom g = plane_geom(ny, nz, pitch);
+  const float2 *twy, *twz;
+  PMGB_TRY(twiddles(ny, &twy));
+  PMGB_TRY(twiddles(nz, &twz));
+  const size_t smem = plane_smem(g);
+  PMGB_TRY(set_dyn_smem((const void *)plane_r2c_kernel, smem));
+  plane_r2c_kernel<<<nplanes * PLANE_CL, PLANE_THREADS, smem, s>>>(in, out, g, twy, twz);
+  PMGB_LAUNCHED("plane_r2c_kernel");
+  return PMGB_OK;
+}
+
+int plane_c2r(const float2 *in, float *out, int nplanes, int ny, int nz, int pitch,
+              cudaStream_t s) {
+  const PlaneGeom g = plane_geom(ny, nz, pitch);
+  const float2 *twy, *twz;
+  PMGB_TRY(twiddles(ny, &twy));
+  PMGB_TRY(twiddles(nz, &twz));
+  const size_t smem = plane_smem(g);
+  PMGB_TRY(set_dyn_smem((const void *)plane_c2r_kernel, smem));
+  plane_c2r_kernel<<<nplanes * PLANE_CL, PLANE_THREADS, smem, s>>>(in, out, g, twy, twz);
+  PMGB_LAUNCHED("plane_c2r_kernel");
+  return PMGB_OK;
+}
+
+template <int MODE>
+int xpass(const float2 *in, float2 *out, int nx, int ny, int nz, int pitch, int64_t cs_in,
+          int64_t cs_out, float r_split, int order, int fd, float scale, cudaStream_t s) {
+  XGeom g;
+  g.nx = nx;
+  g.ny = ny;
+  g.lgx = ilog2(nx);
+  g.nzh = nz / 2 + 1;
+  g.pitch = pitch;
+  g.chunks = (g.nzh + XW - 1) / XW;
+  g.cs_in = cs_in;
+  g.cs_out = cs_out;
+  const float2 *twx;
+  PMGB_TRY(twiddles(nx, &twx));
+  Tables t{nullptr, nullptr, nullptr};
+  if (MODE == X_FORCES || MODE == X_FORCES_ADJ) PMGB_TRY(tables(nx, ny, nz, &t));
+  const size_t smem = 2 * (size_t)nx * XW * sizeof(float2);
+  PMGB_TRY(set_dyn_smem((const void *)xpass_kernel<MODE>, smem));
+  xpass_kernel<MODE><<<ny * g.chunks, XPASS_THREADS, smem, s>>>(in, out, g, twx, t,
+                                                                  r_split * r_split, order, fd,
+                                                                  scale);
+  PMGB_LAUNCHED("xpass_kernel");
+  return PMGB_OK;
+}
+
+}  // namespace
+
+static std::atomic<int> g_spectral{0};
+
+bool spectral_enabled() { return g_spectral.load() != 0; }
+
+int set_spectral(int enabled) { return g_spectral.exchange(enabled ? 1 : 0); }
+
+int spectral_pitch(int nz) { return (nz / 2 + 1 + XW - 1) / XW * XW; }
+
+bool spectral_supported(int nx, int ny, int nz) {
+  return pow2(nx) && pow2(ny) && pow2(nz) && nx >= 8 && nx <= 1024 &&
+         ny >= PLANE_CL * PLANE_CL && ny <= 512 && nz >= 16 && nz <= 512;
+}
+
+static int check_spectral(int nx, int ny, int nz) {
+  if (!spectral_supported(nx, ny, nz))
+    return fail(PMGB_ERR_UNSUPPORTED,
+                "the spectral pipeline needs power-of-two nx in [8,1024], ny in [64,512], "
+                "nz in [16,512]");
+  return PMGB_OK;
+}
+
+int spectral_r2c(const float *in, void *out, int nx, int ny, int nz, int batch,
+                 cudaStream_t s) {
+  PMGB_TRY(check_spectral(nx, ny, nz));
+  const int pitch = spectral_pitch(nz);
+  float2 *o = static_cast<float2 *>(out);
+  PMGB_TRY(plane_r2c(in, o, nx * batch, ny, nz, pitch, s));
+  const int64_t cs = (int64_t)nx * ny * pitch;
+  for (int b = 0; b < batch; ++b)
+    PMGB_TRY(xpass<X_FORWARD>(o + b * cs, o + b * cs, nx, ny, nz, pitch, cs, cs, 0.f, 1, 0,
+                              1.f, s));
+  return PMGB_OK;
+}
+
+int spectral_c2r(void *in, float *out, int nx, int ny, int nz, int batch, cudaStream_t s) {
+  PMGB_TRY(check_spectral(nx, ny, nz));
+  const int pitch = spectral_pitch(nz);
+  float2 *i2 = static_cast<float2 *>(in);
+  const int64_t cs = (int64_t)nx * ny * pitch;
+  for (int b = 0; b < batch; ++b)
+    PMGB_TRY(xpass<X_INVERSE>(i2 + b * cs, i2 + b * cs, nx, ny, nz, pitch, cs, cs, 0.f, 1, 0,
+                              1.f, s));
+  PMGB_TRY(plane_c2r(i2, out, nx * batch, ny, nz, pitch, s));
+  return PMGB_OK;
+}
+
+int spectral_forces(const float *mesh, void *spec, void *fspec, float *f3, int nx, int ny,
+                    int nz, float r_split, int order, int fd, float scale, cudaStream_t s) {
+  PMGB_TRY(check_spectral(nx, ny, nz));
+  const int pitch = spectral_pitch(nz);
+  const int64_t cs = (int64_t)nx * ny * pitch;
+  float2 *d = static_cast<float2 *>(spec), *f = static_cast<float2 *>(fspec);
+  PMGB_TRY(plane_r2c(mesh, d, nx, ny, nz, pitch, s));
+  PMGB_TRY(xpass<X_FORCES>(d, f, nx, ny, nz, pitch, cs, cs, r_split, order, fd, scale, s));
+  PMGB_TRY(plane_c2r(f, f3, 3 * nx, ny, nz, pitch, s));
+  return PMGB_OK;
+}
+
+int spectral_forces_vjp(const float *g3, void *spec3, void *dspec, float *rbar, int nx, int ny,
+                        int nz, float r_split, int order, int fd, float scale,
+                        cudaStream_t s) {
+  PMGB_TRY(check_spectral(nx, ny, nz));
+  const int pitch = spectral_pitch(nz);
+  const int64_t cs = (int64_t)nx * ny * pitch;
+  float2 *a = static_cast<float2 *>(spec3), *d = static_cast<float2 *>(dspec);
+  PMGB_TRY(plane_r2c(g3, a, 3 * nx, ny, nz, pitch, s));
+  PMGB_TRY(xpass<X_FORCES_ADJ>(a, d, nx, ny, nz, pitch, cs, cs, r_split, order, fd, scale, s));
+  PMGB_TRY(plane_c2r(d, rbar, nx, ny, nz, pitch, s));
+  return PMGB_OK;
+}
+
+}  // namespace pmgb

@@ -153,12 +153,14 @@ static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 static Layout layout(int nx, int ny, int nz, int64_t np, int mode) {
   const size_t ncell = (size_t)nx * ny * nz;
-  const size_t nhalf = (size_t)nx * ny * (nz / 2 + 1);
+  // spectra sized for the padded rows of the spectral pipeline (a superset
+  // of cuFFT's [nx][ny][nz/2+1])
+  const size_t nspec = (size_t)nx * ny * spectral_pitch(nz);
   Layout L;
   size_t o = 0;
   L.mesh = o; o = align256(o + ncell * 4);
-  L.dk = o; o = align256(o + nhalf * 8);
-  L.fk = o; o = align256(o + 3 * nhalf * 8);
+  L.dk = o; o = align256(o + nspec * 8);
+  L.fk = o; o = align256(o + 3 * nspec * 8);
   L.f3 = o; o = align256(o + 3 * ncell * 4);
   L.g3 = o; o = align256(o + 3 * ncell * 4);
   L.forces = o; o = align256(o + (size_t)np * 12);
@@ -184,20 +186,82 @@ static int check_ws(void *ws, size_t bytes, const Layout &L) {
 
 #define WS(T, off) reinterpret_cast<T *>(static_cast<char *>(ws) + (off))
 
-// paint -> R2C -> fused k-space -> batched C2R: leaves the three force
-// meshes at WS(float, L.f3).
+static bool aligned16(const void *p) { return reinterpret_cast<uintptr_t>(p) % 16 == 0; }
+
+static bool use_spectral(int nx, int ny, int nz, const void *in, const void *out) {
+  return spectral_enabled() && spectral_supported(nx, ny, nz) && aligned16(in) && aligned16(out);
+}
+
+// density mesh -> the three force meshes f3: the spectral pipeline where
+// the mesh shape allows it (and it is enabled), else R2C -> fused k-space
+// kernel -> batched C2R through cuFFT.  dk / fk: one and three spectra of
+// spectral_pitch rows.
+int mesh_forces(const float *mesh, int nx, int ny, int nz, float r_split, void *dk, void *fk,
+                float *f3, cudaStream_t s) {
+  const int64_t ncell = (int64_t)nx * ny * nz;
+  const int64_t nhalf = (int64_t)nx * ny * (nz / 2 + 1);
+  if (use_spectral(nx, ny, nz, mesh, f3))
+    return spectral_forces(mesh, dk, fk, f3, nx, ny, nz, r_split, 1, 0, 1.0f / (float)ncell, s);
+  PMGB_TRY(fft_r2c(mesh, dk, nx, ny, nz, 1, s));
+  PMGB_TRY(kspace_forces(dk, fk, nhalf, nx, ny, nz, r_split, 1, 0, 1.0f / (float)ncell, s));
+  return fft_c2r(fk, f3, nx, ny, nz, 3, s);
+}
+
+// Adjoint of mesh_forces: the three force-mesh cotangents g3 (read only)
+// -> the density-mesh cotangent rbar.
+int mesh_forces_vjp(const float *g3, int nx, int ny, int nz, float r_split, void *dk,
+                    void *fk, float *rbar, cudaStream_t s) {
+  const int64_t ncell = (int64_t)nx * ny * nz;
+  const int64_t nhalf = (int64_t)nx * ny * (nz / 2 + 1);
+  if (use_spectral(nx, ny, nz, g3, rbar))
+    return spectral_forces_vjp(g3, fk, dk, rbar, nx, ny, nz, r_split, 1, 0,
+                               1.0f / (float)ncell, s);
+  PMGB_TRY(fft_r2c(g3, fk, nx, ny, nz, 3, s));
+  PMGB_TRY(kspace_forces_vjp(fk, nhalf, dk, nx, ny, nz, r_split, 1, 0, 1.0f / (float)ncell, s));
+  return fft_c2r(dk, rbar, nx, ny, nz, 1, s);
+}
+
+// Workspace of the standalone mesh-force calls: one spectrum then three.
+size_t mesh_forces_workspace_size(int nx, int ny, int nz) {
+  const size_t nspec = (size_t)nx * ny * spectral_pitch(nz);
+  return align256(nspec * 8) + align256(3 * nspec * 8);
+}
+
+static int mesh_ws(void *ws, size_t bytes, int nx, int ny, int nz, void **dk, void **fk) {
+  const size_t need = mesh_forces_workspace_size(nx, ny, nz);
+  if (!ws || bytes < need)
+    return fail(PMGB_ERR_WORKSPACE, "mesh-force call needs " + std::to_string(need) +
+                                        " workspace bytes, got " + std::to_string(bytes));
+  if (reinterpret_cast<uintptr_t>(ws) % 256 != 0)
+    return fail(PMGB_ERR_WORKSPACE, "workspace must be 256-byte aligned");
+  *dk = ws;
+  *fk = static_cast<char *>(ws) + align256((size_t)nx * ny * spectral_pitch(nz) * 8);
+  return PMGB_OK;
+}
+
+int mesh_forces_ws(const float *mesh, float *f3, int nx, int ny, int nz, float r_split,
+                   void *ws, size_t bytes, cudaStream_t s) {
+  void *dk, *fk;
+  PMGB_TRY(mesh_ws(ws, bytes, nx, ny, nz, &dk, &fk));
+  return mesh_forces(mesh, nx, ny, nz, r_split, dk, fk, f3, s);
+}
+
+int mesh_forces_vjp_ws(const float *g3, float *rbar, int nx, int ny, int nz, float r_split,
+                       void *ws, size_t bytes, cudaStream_t s) {
+  void *dk, *fk;
+  PMGB_TRY(mesh_ws(ws, bytes, nx, ny, nz, &dk, &fk));
+  return mesh_forces_vjp(g3, nx, ny, nz, r_split, dk, fk, rbar, s);
+}
+
+// paint -> the three force meshes at WS(float, L.f3).
 static int force_meshes(const float *pos, int64_t np, int nx, int ny, int nz, float r_split,
                         int mode, void *ws, const Layout &L, cudaStream_t s) {
   const int64_t ncell = (int64_t)nx * ny * nz;
-  const int64_t nhalf = (int64_t)nx * ny * (nz / 2 + 1);
   float *mesh = WS(float, L.mesh);
   PMGB_TRY(paint(mesh, nx, ny, nz, pos, np, nullptr, 1.0f, mode, 0, WS(void, L.det),
                  mode == PMGB_PAINT_DETERMINISTIC ? (size_t)ncell * 8 : 0, s));
-  PMGB_TRY(fft_r2c(mesh, WS(void, L.dk), nx, ny, nz, 1, s));
-  PMGB_TRY(kspace_forces(WS(void, L.dk), WS(void, L.fk), nhalf, nx, ny, nz, r_split, 1, 0,
-                         1.0f / (float)ncell, s));
-  PMGB_TRY(fft_c2r(WS(void, L.fk), WS(float, L.f3), nx, ny, nz, 3, s));
-  return PMGB_OK;
+  return mesh_forces(mesh, nx, ny, nz, r_split, WS(void, L.dk), WS(void, L.fk),
+                     WS(float, L.f3), s);
 }
 
 int pm_workspace_regions(void *ws, size_t bytes, int nx, int ny, int nz, int64_t np,
@@ -225,16 +289,10 @@ int force_meshes_sorted(const float *pos, int64_t np, int nx, int ny, int nz, fl
                         unsigned *stats, float *f3_out, float **f3, cudaStream_t s) {
   Layout L = layout(nx, ny, nz, np, PMGB_PAINT_BINNED);
   PMGB_TRY(check_ws(ws, bytes, L));
-  const int64_t ncell = (int64_t)nx * ny * nz;
-  const int64_t nhalf = (int64_t)nx * ny * (nz / 2 + 1);
   float *mesh = WS(float, L.mesh);
   PMGB_TRY(paint_sorted(mesh, nx, ny, nz, pos, np, sort_ws, sort_bytes, stats, s));
-  PMGB_TRY(fft_r2c(mesh, WS(void, L.dk), nx, ny, nz, 1, s));
-  PMGB_TRY(kspace_forces(WS(void, L.dk), WS(void, L.fk), nhalf, nx, ny, nz, r_split, 1, 0,
-                         1.0f / (float)ncell, s));
   *f3 = f3_out ? f3_out : WS(float, L.f3);
-  PMGB_TRY(fft_c2r(WS(void, L.fk), *f3, nx, ny, nz, 3, s));
-  return PMGB_OK;
+  return mesh_forces(mesh, nx, ny, nz, r_split, WS(void, L.dk), WS(void, L.fk), *f3, s);
 }
 
 int pm_forces(const float *pos, int64_t np, int nx, int ny, int nz, float r_split, int mode,
@@ -317,7 +375,6 @@ int pm_forces_vjp(const float *pos, int64_t np, int nx, int ny, int nz, float r_
   Layout L = layout(nx, ny, nz, np, mode);
   PMGB_TRY(check_ws(ws, bytes, L));
   const int64_t ncell = (int64_t)nx * ny * nz;
-  const int64_t nhalf = (int64_t)nx * ny * (nz / 2 + 1);
   PMGB_TRY(force_meshes(pos, np, nx, ny, nz, r_split, mode, ws, L, s));
   float *g3 = WS(float, L.g3);
   PMGB_CUDA(cudaMemsetAsync(g3, 0, 3 * ncell * sizeof(float), s));
@@ -325,11 +382,8 @@ int pm_forces_vjp(const float *pos, int64_t np, int nx, int ny, int nz, float r_
     paint3_kernel<<<grid_for(np, 256), 256, 0, s>>>(g3, ncell, nx, ny, nz, pos, np, g);
     PMGB_LAUNCHED("paint3_kernel");
   }
-  PMGB_TRY(fft_r2c(g3, WS(void, L.fk), nx, ny, nz, 3, s));
-  PMGB_TRY(kspace_forces_vjp(WS(void, L.fk), nhalf, WS(void, L.dk), nx, ny, nz, r_split, 1, 0,
-                             1.0f / (float)ncell, s));
   float *rbar = WS(float, L.mesh);
-  PMGB_TRY(fft_c2r(WS(void, L.dk), rbar, nx, ny, nz, 1, s));
+  PMGB_TRY(mesh_forces_vjp(g3, nx, ny, nz, r_split, WS(void, L.dk), WS(void, L.fk), rbar, s));
   if (np > 0) {
     forces_vjp_gather_kernel<<<grid_for(np, 256), 256, 0, s>>>(WS(float, L.f3), ncell, rbar, nx,
                                                                 ny, nz, pos, np, g, gpos);

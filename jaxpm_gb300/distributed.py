@@ -91,6 +91,29 @@ def ifft3d(x, nz=None):
     return _C2R.apply(x, nz)
 
 
+FFT_PATHS = {"cufft": 0, "fused": 1}
+
+
+def fft_path():
+    """FFT path of the composite force calls: ``"cufft"`` (default) or
+    ``"fused"`` (the library's own FFT pipeline, fused with the k-space
+    kernel, for the mesh shapes it supports; cuFFT otherwise)."""
+    return {v: k for k, v in FFT_PATHS.items()}[_lib.load().pmgb_fft_path()]
+
+
+def set_fft_path(path):
+    """Selects the FFT path of the composite force calls (process-wide);
+    returns the previous one."""
+    prev = fft_path()
+    _lib.call("pmgb_set_fft_path", FFT_PATHS[path])
+    return prev
+
+
+def fft3_supported(mesh_shape):
+    """Whether the library's own FFT pipeline handles this mesh shape."""
+    return bool(_lib.load().pmgb_fft3_supported(*(int(s) for s in mesh_shape)))
+
+
 def uniform_particles(mesh_shape, sharding=None, device="cuda"):
     """Lattice positions ``[*mesh_shape, 3]`` (``jaxpm/distributed.py:168-190``)."""
     _single_device(0, sharding)

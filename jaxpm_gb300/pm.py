@@ -57,21 +57,18 @@ class _PMForces(torch.autograd.Function):
 
 class _ForceMeshes(torch.autograd.Function):
     """Real density mesh -> three real force meshes [3, nx, ny, nz]
-    (R2C, fused k-space kernel, batched C2R).  Linear; the adjoint is R2C of
-    the cotangents, the conjugate k-space kernel and one C2R."""
+    (``pmgb_mesh_forces_f32``: the library's fused FFT pipeline, or R2C +
+    fused k-space kernel + batched C2R).  Linear; the adjoint is
+    ``pmgb_mesh_forces_vjp_f32``."""
 
     @staticmethod
     def forward(ctx, rho, r_split):
         nx, ny, nz = rho.shape
-        nh = nx * ny * (nz // 2 + 1)
-        dk = torch.empty(nh, dtype=torch.complex64, device=rho.device)
-        fk = torch.empty(3 * nh, dtype=torch.complex64, device=rho.device)
+        nb = _lib.load().pmgb_mesh_forces_workspace_size(nx, ny, nz)
+        ws = torch.empty(nb, dtype=torch.uint8, device=rho.device)
         out = torch.empty((3, nx, ny, nz), dtype=torch.float32, device=rho.device)
-        s = _lib.stream()
-        _lib.call("pmgb_fft_r2c_f32", _lib.ptr(rho), _lib.ptr(dk), nx, ny, nz, 1, s)
-        _lib.call("pmgb_kspace_forces_f32", _lib.ptr(dk), _lib.ptr(fk), nh, nx, ny, nz,
-                  float(r_split), 1, 0, 1.0 / (nx * ny * nz), s)
-        _lib.call("pmgb_fft_c2r_f32", _lib.ptr(fk), _lib.ptr(out), nx, ny, nz, 3, 0, s)
+        _lib.call("pmgb_mesh_forces_f32", _lib.ptr(rho), _lib.ptr(out), nx, ny, nz,
+                  float(r_split), _lib.ptr(ws), nb, _lib.stream())
         ctx.r_split = float(r_split)
         return out
 
@@ -79,15 +76,11 @@ class _ForceMeshes(torch.autograd.Function):
     def backward(ctx, g):
         g = g.contiguous()
         _, nx, ny, nz = g.shape
-        nh = nx * ny * (nz // 2 + 1)
-        gk = torch.empty(3 * nh, dtype=torch.complex64, device=g.device)
-        dk = torch.empty(nh, dtype=torch.complex64, device=g.device)
+        nb = _lib.load().pmgb_mesh_forces_workspace_size(nx, ny, nz)
+        ws = torch.empty(nb, dtype=torch.uint8, device=g.device)
         out = torch.empty((nx, ny, nz), dtype=torch.float32, device=g.device)
-        s = _lib.stream()
-        _lib.call("pmgb_fft_r2c_f32", _lib.ptr(g), _lib.ptr(gk), nx, ny, nz, 3, s)
-        _lib.call("pmgb_kspace_forces_vjp_f32", _lib.ptr(gk), nh, _lib.ptr(dk), nx, ny, nz,
-                  ctx.r_split, 1, 0, 1.0 / (nx * ny * nz), s)
-        _lib.call("pmgb_fft_c2r_f32", _lib.ptr(dk), _lib.ptr(out), nx, ny, nz, 1, 0, s)
+        _lib.call("pmgb_mesh_forces_vjp_f32", _lib.ptr(g), _lib.ptr(out), nx, ny, nz,
+                  ctx.r_split, _lib.ptr(ws), nb, _lib.stream())
         return out, None
 
 
