@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--skip", default="", help="comma list of legs to skip: "
                     "adjoint,plain,e2e,cpu,clocks")
     ap.add_argument("--phases-only", action="store_true")
-    ap.add_argument("--fft", default=None, choices=["cufft", "fused"],
+    ap.add_argument("--fft", default=None, choices=["cufft", "fused", "own"],
                     help="FFT path of the force evaluation (library default if omitted)")
     return ap.parse_args()
 
@@ -198,7 +198,7 @@ def run_gb300(args):
     nx = ny = nz = n
     ncell = n**3
     mf_bytes = lib.pmgb_mesh_forces_workspace_size(nx, ny, nz)
-    spectral = bool(lib.pmgb_fft3_supported(nx, ny, nz)) and lib.pmgb_fft_path() == 1
+    fft_path = lib.pmgb_fft_path() if lib.pmgb_fft3_supported(nx, ny, nz) else 0
     # buffers of the phase-by-phase step: the same C-ABI calls the composite
     # step makes, issued separately so that each phase is timed on the stream
     buf = {"mesh": torch.empty(ncell, dtype=torch.float32, device=dev),
@@ -221,7 +221,13 @@ def run_gb300(args):
     events = [[torch.cuda.Event(enable_timing=True) for _ in range(len(phase_names) + 1)]
               for _ in range(K)]
 
+    # sorted loop: every step's gather also paints the next step's density
+    # (pmgb_read3_kick_drift_paint_binned_f32), so only the first step of a
+    # run has a paint phase
+    density_ready = [False]
+
     def reset():
+        density_ready[0] = False
         if engine == "sorted":
             eng.load(x0, v0)
         else:
@@ -240,8 +246,9 @@ def run_gb300(args):
             px, pv = x, v
         rec(0)
         if engine == "sorted":
-            _lib.call("pmgb_cic_paint_sorted_f32", P("mesh"), nx, ny, nz, _lib.ptr(px), Np,
-                      _lib.ptr(eng.sort_ws), eng.sort_bytes, _lib.ptr(eng.stats_buf), s)
+            if not density_ready[0]:
+                _lib.call("pmgb_cic_paint_sorted_f32", P("mesh"), nx, ny, nz, _lib.ptr(px), Np,
+                          _lib.ptr(eng.sort_ws), eng.sort_bytes, _lib.ptr(eng.stats_buf), s)
         else:
             _lib.call("pmgb_cic_paint_f32", P("mesh"), nx, ny, nz, _lib.ptr(px), Np, None, 1.0,
                       mode, 0, P("det"), det_bytes, s)
@@ -251,9 +258,16 @@ def run_gb300(args):
                   mf_bytes, s)
         rec(2)
         if engine == "sorted":
-            _lib.call("pmgb_read3_kick_drift_binned_f32", P("f3"), ncell, nx, ny, nz,
-                      _lib.ptr(px), _lib.ptr(pv), Np, float(kick[i]), float(drift[i]),
-                      _lib.ptr(eng.sort_ws), eng.sort_bytes, _lib.ptr(eng.stats_buf), s)
+            if i + 1 < K:  # gather + kick + drift + paint of the next density
+                _lib.call("pmgb_read3_kick_drift_paint_binned_f32", P("f3"), ncell, nx, ny, nz,
+                          _lib.ptr(px), _lib.ptr(pv), Np, float(kick[i]), float(drift[i]),
+                          P("mesh"), _lib.ptr(eng.sort_ws), eng.sort_bytes,
+                          _lib.ptr(eng.stats_buf), s)
+            else:
+                _lib.call("pmgb_read3_kick_drift_binned_f32", P("f3"), ncell, nx, ny, nz,
+                          _lib.ptr(px), _lib.ptr(pv), Np, float(kick[i]), float(drift[i]),
+                          _lib.ptr(eng.sort_ws), eng.sort_bytes, _lib.ptr(eng.stats_buf), s)
+            density_ready[0] = i + 1 < K
             rec(3)
             _lib.call("pmgb_tile_scatter_f32", _lib.ptr(px), _lib.ptr(pv), _lib.ptr(eng.ids[a]),
                       Np, nx, ny, nz, _lib.ptr(eng.pos[b]), _lib.ptr(eng.vel[b]),
@@ -300,12 +314,17 @@ def run_gb300(args):
                          mode="deterministic")
     mass_err = abs(rho.double().sum().item() - Np) / Np
     del rho
-    # own kernels per step: paint (1); forces (3 with the fused FFT pipeline:
-    # plane R2C, x pass with the k-space multiply, plane C2R; else 1 k-space
-    # kernel between cuFFT's); gather (1); sort (3 scan + 1 scatter)
-    launches_per_step = (1 + (3 if spectral else 1) + 1 + (4 if engine == "sorted" else 0))
-    if mode == _lib.PAINT_DETERMINISTIC:
-        launches_per_step += 1
+    # own kernels: forces (the k-space kernel between cuFFT's transforms, or
+    # the fused x kernel between cuFFT's plane transforms: 1; with the
+    # library's plane kernels too: 3) and the gather every step; the sorted
+    # loop adds the sort (3 scan + 1 scatter) per step and one paint per run
+    # (the gather paints every later density), the lattice loop a paint per
+    # step (two kernels when deterministic)
+    forces_own = 3 if fft_path == 2 else 1
+    if engine == "sorted":
+        gpu_launches = 1 + K * (forces_own + 1 + 4)
+    else:
+        gpu_launches = K * ((2 if mode == _lib.PAINT_DETERMINISTIC else 1) + forces_own + 1)
 
     result = {"metric": "particle-steps/s (FastPM PM step, 512^3 particles on 512^3 mesh)",
               "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": K,
@@ -316,14 +335,14 @@ def run_gb300(args):
               "config": {"workload": f"FastPM {n}^3 particles on {n}^3 mesh, box {n} Mpc/h, "
                                      f"2LPT a=0.1, {K} steps to a=1",
                          "particles": Np, "mesh": [n, n, n], "box_mpc_h": n * BOX_PER_CELL,
-                         "engine": engine, "fft": "fused" if spectral else "cufft",
+                         "engine": engine, "fft": ["cufft", "fused", "own"][fft_path],
                          "paint_mode": {0: "atomic", 1: "binned",
                                                           2: "deterministic"}[mode],
                          "parallelism": "replicas" if world > 1 else "single",
                          "l2": "inputs larger than L2 (positions+velocities 3.2 GB, "
                                "meshes 0.54 GB each)"},
               "phases_ms": phase_ms, "mass_rel_err": mass_err,
-              "gpu_launches": launches_per_step * K}
+              "gpu_launches": gpu_launches}
     if engine == "sorted":
         result["particles_outside_tile"] = eng.stats
 
@@ -332,8 +351,13 @@ def run_gb300(args):
     # algorithmic bytes per particle (Np = mesh cells): paint 12 read + 4
     # write; forces 4 read + 12 write + the half spectra in and out of each
     # of its three passes (4 + 4, 4 + 12, 12 + 12 at nz/2+1 of nz); gather
-    # 12 force + 24 read + 24 write
-    alg = {"paint": 16.0, "forces": 48.0, "read_kick_drift": 60.0}
+    # 12 force + 24 read + 24 write, + 4 for the sorted loop's paint of the
+    # next density (its paint phase runs once per run, so it has no per-step
+    # roofline)
+    if engine == "sorted":
+        alg = {"forces": 48.0, "read_kick_drift": 64.0}
+    else:
+        alg = {"paint": 16.0, "forces": 48.0, "read_kick_drift": 60.0}
     own = {k: phase_ms[k] for k in alg}
     dom = max(own, key=own.get)
     achieved = alg[dom] * Np / (phase_ms[dom] / 1e3) / 1e9

@@ -190,10 +190,13 @@ int pmgb_fft3_r2c_f32(const float *in, void *out, int nx, int ny, int nz,
 int pmgb_fft3_c2r_f32(void *in, float *out, int nx, int ny, int nz, int batch,
                       pmgb_stream_t stream);
 
-/* FFT path of the composite calls (process-wide): PMGB_FFT_CUFFT (default)
- * or PMGB_FFT_FUSED (the library's FFT pipeline, fused with the k-space
- * kernel, where pmgb_fft3_supported; cuFFT for other shapes). */
-enum pmgb_fft_path { PMGB_FFT_CUFFT = 0, PMGB_FFT_FUSED = 1 };
+/* FFT path of the composite calls (process-wide): PMGB_FFT_CUFFT (cuFFT
+ * 3-D R2C, pmgb_kspace_forces_f32, batched C2R), PMGB_FFT_FUSED (default:
+ * cuFFT's batched 2-D plane transforms around the library's x-direction
+ * kernel that fuses the forward x transform, the k-space multiply and the
+ * inverse x transforms) or PMGB_FFT_OWN (the library's plane kernels too).
+ * The last two apply where pmgb_fft3_supported; other shapes use cuFFT. */
+enum pmgb_fft_path { PMGB_FFT_CUFFT = 0, PMGB_FFT_FUSED = 1, PMGB_FFT_OWN = 2 };
 int pmgb_set_fft_path(int path);
 int pmgb_fft_path(void);
 
@@ -366,6 +369,23 @@ int pmgb_read3_kick_drift_binned_f32(const float *force3, int64_t comp_stride,
                                      size_t sort_workspace_bytes,
                                      uint32_t *stats, pmgb_stream_t stream);
 
+/* pmgb_read3_kick_drift_binned_f32 that also paints the new positions into
+ * mesh_next (overwritten): the density of the next step, from a per-tile
+ * box (the tile plus the cell the particles may have moved into) in shared
+ * memory added with one TMA reduce per tile, so that the next step needs no
+ * separate paint pass.  Same density as pmgb_cic_paint_sorted_f32 of the
+ * new positions up to the order of the float sums; stats [0] counts
+ * particles that moved beyond the box (painted with global atomics). */
+int pmgb_read3_kick_drift_paint_binned_f32(const float *force3,
+                                           int64_t comp_stride, int nx, int ny,
+                                           int nz, float *pos, float *vel,
+                                           int64_t np, float kick, float drift,
+                                           float *mesh_next,
+                                           void *sort_workspace,
+                                           size_t sort_workspace_bytes,
+                                           uint32_t *stats,
+                                           pmgb_stream_t stream);
+
 /* Exclusive scan of the tile counts left in sort_workspace by
  * pmgb_read3_kick_drift_binned_f32, then the scatter of (pos, vel, id) to
  * (pos_out, vel_out, id_out) in tile order; dest_out (nullable) receives
@@ -401,6 +421,25 @@ int pmgb_fpm_step_sorted_f32(const float *pos, float *vel, const uint32_t *id,
                              size_t sort_workspace_bytes, float *force3_out,
                              uint32_t *dest_out, uint32_t *offsets_out,
                              uint32_t *stats, pmgb_stream_t stream);
+
+/* n_steps FastPM steps of tile-sorted particles (the time loop of
+ * jaxpm/ode.py driven over a_i = a0 + i da): each step as
+ * pmgb_fpm_step_sorted_f32, except that the density of every step after the
+ * first is painted by the previous step's gather
+ * (pmgb_read3_kick_drift_paint_binned_f32), so each step reads the
+ * particles once.  The sort_workspace must hold the tile ranges of
+ * (pos_a, ...) (as left by pmgb_tile_sort_f32 or a previous step).  kick and
+ * drift are HOST arrays of n_steps coefficients.  The state ping-pongs
+ * between the a and b buffers: after the call it is in a when n_steps is
+ * even, in b when odd. */
+int pmgb_fpm_run_sorted_f32(float *pos_a, float *vel_a, uint32_t *id_a,
+                            float *pos_b, float *vel_b, uint32_t *id_b,
+                            int64_t np, int nx, int ny, int nz, int n_steps,
+                            const float *kick, const float *drift,
+                            float r_split, void *workspace,
+                            size_t workspace_bytes, void *sort_workspace,
+                            size_t sort_workspace_bytes, uint32_t *stats,
+                            pmgb_stream_t stream);
 
 /* Number of tile keys of a mesh (the sorted loop's tile ranges have one
  * more entry). */

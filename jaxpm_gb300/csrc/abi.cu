@@ -210,12 +210,13 @@ int pmgb_fft3_pitch(int nz) { return nz > 0 ? spectral_pitch(nz) : 0; }
 
 int pmgb_set_fft_path(int path) {
   BEGIN();
-  PMGB_REQUIRE(path == PMGB_FFT_FUSED || path == PMGB_FFT_CUFFT, "unknown FFT path");
-  set_spectral(path == PMGB_FFT_FUSED);
+  PMGB_REQUIRE(path == PMGB_FFT_CUFFT || path == PMGB_FFT_FUSED || path == PMGB_FFT_OWN,
+               "unknown FFT path");
+  set_spectral(path);
   return PMGB_OK;
 }
 
-int pmgb_fft_path(void) { return spectral_enabled() ? PMGB_FFT_FUSED : PMGB_FFT_CUFFT; }
+int pmgb_fft_path(void) { return spectral_mode(); }
 
 int pmgb_fft3_r2c_f32(const float *in, void *out, int nx, int ny, int nz, int batch,
                       pmgb_stream_t stream) {
@@ -491,6 +492,55 @@ int pmgb_read3_kick_drift_binned_f32(const float *force3, int64_t comp_stride, i
   NEED(sort_workspace);
   return rkd_sorted(force3, comp_stride, nx, ny, nz, pos, pos, vel, np, kick, drift,
                     sort_workspace, sort_workspace_bytes, stats, stream);
+}
+
+int pmgb_read3_kick_drift_paint_binned_f32(const float *force3, int64_t comp_stride, int nx,
+                                           int ny, int nz, float *pos, float *vel, int64_t np,
+                                           float kick, float drift, float *mesh_next,
+                                           void *sort_workspace, size_t sort_workspace_bytes,
+                                           uint32_t *stats, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  PMGB_REQUIRE(comp_stride >= (int64_t)nx * ny * nz, "comp_stride smaller than the mesh");
+  NEED(mesh_next);
+  if (np == 0) {
+    PMGB_CUDA(cudaMemsetAsync(mesh_next, 0, (size_t)nx * ny * nz * sizeof(float), stream));
+    return PMGB_OK;
+  }
+  NEED(force3);
+  NEED(pos);
+  NEED(vel);
+  NEED(sort_workspace);
+  PMGB_REQUIRE(mesh_next != force3, "mesh_next must not alias the force meshes");
+  return rkd_sorted(force3, comp_stride, nx, ny, nz, pos, pos, vel, np, kick, drift,
+                    sort_workspace, sort_workspace_bytes, stats, stream, mesh_next);
+}
+
+int pmgb_fpm_run_sorted_f32(float *pos_a, float *vel_a, uint32_t *id_a, float *pos_b,
+                            float *vel_b, uint32_t *id_b, int64_t np, int nx, int ny, int nz,
+                            int n_steps, const float *kick, const float *drift, float r_split,
+                            void *workspace, size_t workspace_bytes, void *sort_workspace,
+                            size_t sort_workspace_bytes, uint32_t *stats,
+                            pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  PMGB_REQUIRE(n_steps >= 0, "n_steps is negative");
+  if (n_steps == 0) return PMGB_OK;
+  NEED(kick);
+  NEED(drift);
+  if (np > 0) {
+    NEED(pos_a);
+    NEED(vel_a);
+    NEED(id_a);
+    NEED(pos_b);
+    NEED(vel_b);
+    NEED(id_b);
+    PMGB_REQUIRE(pos_a != pos_b && vel_a != vel_b && id_a != id_b,
+                 "the two state buffers must be distinct");
+  }
+  return fpm_run_sorted(pos_a, vel_a, id_a, pos_b, vel_b, id_b, np, nx, ny, nz, n_steps, kick,
+                        drift, r_split, workspace, workspace_bytes, sort_workspace,
+                        sort_workspace_bytes, stats, stream);
 }
 
 int pmgb_cic_paint_sorted_f32(float *mesh, int nx, int ny, int nz, const float *pos,

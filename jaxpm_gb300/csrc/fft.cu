@@ -20,7 +20,8 @@
 namespace pmgb {
 namespace {
 
-using Key = std::tuple<int, int, int, int, int, int>;  // dev, nx, ny, nz, batch, type
+// dev, nx (0 for a batch of 2-D plane transforms), ny, nz, batch, type, pitch
+using Key = std::tuple<int, int, int, int, int, int, int>;
 
 std::mutex g_mu;
 std::map<Key, cufftHandle> g_plans;
@@ -43,7 +44,7 @@ const char *cufft_name(cufftResult r) {
 int plan_for(int nx, int ny, int nz, int batch, cufftType type, cufftHandle *out) {
   int dev = 0;
   PMGB_CUDA(cudaGetDevice(&dev));
-  Key k{dev, nx, ny, nz, batch, (int)type};
+  Key k{dev, nx, ny, nz, batch, (int)type, 0};
   auto it = g_plans.find(k);
   if (it != g_plans.end()) {
     *out = it->second;
@@ -58,6 +59,36 @@ int plan_for(int nx, int ny, int nz, int batch, cufftType type, cufftHandle *out
   if (r != CUFFT_SUCCESS) {
     cufftDestroy(h);
     return fail(PMGB_ERR_CUFFT, std::string("cufftMakePlanMany: ") + cufft_name(r));
+  }
+  g_plans[k] = h;
+  *out = h;
+  return PMGB_OK;
+}
+
+// Batched 2-D (y, z) transforms of x-planes with padded half-spectrum rows
+// ([plane][ny][pitch] complex); g_mu must be held.
+int plane_plan_for(int nplanes, int ny, int nz, int pitch, cufftType type, cufftHandle *out) {
+  int dev = 0;
+  PMGB_CUDA(cudaGetDevice(&dev));
+  Key k{dev, 0, ny, nz, nplanes, (int)type, pitch};
+  auto it = g_plans.find(k);
+  if (it != g_plans.end()) {
+    *out = it->second;
+    return PMGB_OK;
+  }
+  cufftHandle h;
+  cufftResult r = cufftCreate(&h);
+  if (r != CUFFT_SUCCESS) return fail(PMGB_ERR_CUFFT, std::string("cufftCreate: ") + cufft_name(r));
+  int n[2] = {ny, nz};
+  int real_embed[2] = {ny, nz}, spec_embed[2] = {ny, pitch};
+  const bool fwd = type == CUFFT_R2C;
+  size_t work = 0;
+  r = cufftMakePlanMany(h, 2, n, fwd ? real_embed : spec_embed, 1,
+                        fwd ? ny * nz : ny * pitch, fwd ? spec_embed : real_embed, 1,
+                        fwd ? ny * pitch : ny * nz, type, nplanes, &work);
+  if (r != CUFFT_SUCCESS) {
+    cufftDestroy(h);
+    return fail(PMGB_ERR_CUFFT, std::string("cufftMakePlanMany (planes): ") + cufft_name(r));
   }
   g_plans[k] = h;
   *out = h;
@@ -87,6 +118,29 @@ int fft_c2r(void *in, float *out, int nx, int ny, int nz, int batch, cudaStream_
   std::lock_guard<std::mutex> lk(g_mu);
   cufftHandle h;
   PMGB_TRY(plan_for(nx, ny, nz, batch, CUFFT_C2R, &h));
+  cufftResult r = cufftSetStream(h, s);
+  if (r == CUFFT_SUCCESS) r = cufftExecC2R(h, static_cast<cufftComplex *>(in), out);
+  if (r != CUFFT_SUCCESS) return fail(PMGB_ERR_CUFFT, std::string("cufftExecC2R: ") + cufft_name(r));
+  return PMGB_OK;
+}
+
+int fft_planes_r2c(const float *in, void *out, int nplanes, int ny, int nz, int pitch,
+                   cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  cufftHandle h;
+  PMGB_TRY(plane_plan_for(nplanes, ny, nz, pitch, CUFFT_R2C, &h));
+  cufftResult r = cufftSetStream(h, s);
+  if (r == CUFFT_SUCCESS)
+    r = cufftExecR2C(h, const_cast<cufftReal *>(in), static_cast<cufftComplex *>(out));
+  if (r != CUFFT_SUCCESS) return fail(PMGB_ERR_CUFFT, std::string("cufftExecR2C: ") + cufft_name(r));
+  return PMGB_OK;
+}
+
+int fft_planes_c2r(void *in, float *out, int nplanes, int ny, int nz, int pitch,
+                   cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  cufftHandle h;
+  PMGB_TRY(plane_plan_for(nplanes, ny, nz, pitch, CUFFT_C2R, &h));
   cufftResult r = cufftSetStream(h, s);
   if (r == CUFFT_SUCCESS) r = cufftExecC2R(h, static_cast<cufftComplex *>(in), out);
   if (r != CUFFT_SUCCESS) return fail(PMGB_ERR_CUFFT, std::string("cufftExecC2R: ") + cufft_name(r));

@@ -42,6 +42,11 @@ int fft_r2c(const float *in, void *out, int nx, int ny, int nz, int batch,
 int fft_c2r(void *in, float *out, int nx, int ny, int nz, int batch,
             cudaStream_t s);
 int scale_inplace(float *x, int64_t n, float scale, cudaStream_t s);
+// batched 2-D (y, z) transforms of x-planes, spectra [plane][ny][pitch]
+int fft_planes_r2c(const float *in, void *out, int nplanes, int ny, int nz,
+                   int pitch, cudaStream_t s);
+int fft_planes_c2r(void *in, float *out, int nplanes, int ny, int nz, int pitch,
+                   cudaStream_t s);
 
 // kspace.cu
 int kspace_forces(const void *dk, void *fk, int64_t cs, int nx, int ny, int nz,
@@ -105,7 +110,20 @@ int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos,
 int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz,
                const float *pos, float *pos_out, float *vel, int64_t np,
                float kick, float drift, void *sort_ws, size_t sort_bytes,
-               unsigned *stats, cudaStream_t s);
+               unsigned *stats, cudaStream_t s, float *mesh_next = nullptr);
+// n_steps sorted steps with the paint of each next density fused into the
+// gather; the state ping-pongs between the a and b buffers (in a after an
+// even number of steps).  kick/drift: host arrays of n_steps.
+int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b,
+                   float *vel_b, unsigned *id_b, int64_t np, int nx, int ny,
+                   int nz, int n_steps, const float *kick, const float *drift,
+                   float r_split, void *mesh_ws, size_t mesh_bytes,
+                   void *sort_ws, size_t sort_bytes, unsigned *stats,
+                   cudaStream_t s);
+// step.cu: density mesh -> force meshes inside the composite workspace's
+// spectra (dk, fk) by the selected FFT path.
+int mesh_forces(const float *mesh, int nx, int ny, int nz, float r_split,
+                void *dk, void *fk, float *f3, cudaStream_t s);
 int tile_scatter(const float *pos, const float *vel, const unsigned *id,
                  int64_t np, int nx, int ny, int nz, float *pos2, float *vel2,
                  unsigned *id2, unsigned *dest, void *sort_ws, size_t sort_bytes,
@@ -154,11 +172,12 @@ int pm_workspace_regions(void *ws, size_t bytes, int nx, int ny, int nz,
 // meshes (nx in [8,1024], ny in [64,512], nz in [16,512]).  Spectra use the
 // layout [nx][ny][spectral_pitch(nz)] complex (kz < nz/2+1 meaningful).
 bool spectral_supported(int nx, int ny, int nz);
-// Process-wide choice: the composite calls use the spectral pipeline when
-// enabled (default) and supported, else cuFFT.  set_spectral returns the
-// previous setting.
+// Process-wide choice of the composite calls' FFT path (the pmgb_fft_path
+// values): 0 cuFFT 3-D, 1 cuFFT planes + fused x pass, 2 own planes + fused
+// x pass (1 and 2 only where spectral_supported).  Returns the previous.
 bool spectral_enabled();
-int set_spectral(int enabled);
+int spectral_mode();
+int set_spectral(int mode);
 int spectral_pitch(int nz);
 int spectral_r2c(const float *in, void *out, int nx, int ny, int nz, int batch,
                  cudaStream_t s);

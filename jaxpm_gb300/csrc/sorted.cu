@@ -464,22 +464,56 @@ __device__ __forceinline__ TileInfo tile_info(const unsigned *__restrict__ offse
 
 constexpr int RKD_ILP = 2;
 
+// Paint box of the fused gather (the next step's density from the new
+// positions, which may leave their tile by about a cell): x and y cover
+// o-1 .. o+9, z covers o-4 .. o+11 so that the TMA box starts on a 16-byte
+// boundary.  Two boxes in turn (the TMA reduce of one drains while the next
+// tile paints the other), each with the two fixed-point halves.
+constexpr int NB = TILE + 3;
+constexpr int NBZ = 16;
+constexpr int NBOX = NB * NB * NBZ;
+constexpr int NBOX_WORDS = (2 * NBOX + 31) / 32 * 32;
+constexpr int RKDP_SMEM = 2 * NBOX_WORDS * 4;
+
+__device__ __forceinline__ bool nbox_interior(int ox, int oy, int oz, int nx, int ny, int nz) {
+  return ox >= 1 && oy >= 1 && oz >= 4 && ox + NB - 1 <= nx && oy + NB - 1 <= ny &&
+         oz + NBZ - 4 <= nz;
+}
+
+// c - o taken periodically into (-n/2, n/2]
+__device__ __forceinline__ int periodic_offset(int c, int o, int n) {
+  int d = c - o;
+  if (d > n / 2) d -= n;
+  else if (d < -(n / 2)) d += n;
+  return d;
+}
+
+__device__ __forceinline__ void zero_words(unsigned *p, int words, int tid) {
+  uint4 *z4 = reinterpret_cast<uint4 *>(p);
+  for (int q = tid; q < words / 4; q += TILE_THREADS) z4[q] = make_uint4(0u, 0u, 0u, 0u);
+}
+
+template <bool PAINT>
 __global__ void __launch_bounds__(TILE_THREADS, 4)
 rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int nz,
                  const float *pos, float *pos_out, float *__restrict__ vel,
                  const unsigned *__restrict__ offsets, uint32_t nkeys, float kick, float drift,
                  unsigned *__restrict__ counts, unsigned *__restrict__ rank,
                  unsigned *__restrict__ stats, const __grid_constant__ CUtensorMap tmap,
-                 int use_tma) {
+                 int use_tma, float *__restrict__ mesh_next, int pvec,
+                 const __grid_constant__ CUtensorMap pmap, int use_ptma) {
   __shared__ __align__(128) float fb[2][FBOX_STRIDE];
   __shared__ __align__(8) uint64_t bar[2];
+  extern __shared__ __align__(128) unsigned pbox[];  // PAINT: 2 x NBOX_WORDS
   const int tid = threadIdx.x;
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
     fence_async_shared();
   }
+  if (PAINT) zero_words(pbox, 2 * NBOX, tid);
   __syncthreads();
+  int pbuf = 0;
   uint32_t phase0 = 0u, phase1 = 0u;  // parity of the next completion of bar[0] / bar[1]
   const uint32_t stride = gridDim.x;
   uint32_t key = blockIdx.x;
@@ -511,6 +545,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
         if (__syncthreads_or(!ok)) {  // uniform: every thread leaves together
           if (stats && tid == 0) atomicExch(stats + 2, 1u);
           if (nxt.tma) mbar_wait(&bar[buf ^ 1], buf ? phase0 : phase1);  // drain the prefetch
+          if (PAINT && use_ptma && tid == 0) bulk_wait_all();  // paint reductions in flight
           return;
         }
         if (buf) phase1 ^= 1u; else phase0 ^= 1u;
@@ -592,6 +627,39 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
                     ? key
                     : tile_key(xn, yn, zn, nx, ny, nz);
           }
+          if (PAINT) {  // the next step's density: the new position into the paint box
+            const unsigned cnt = cur.end - cur.beg;
+            const Axis bx = cic_axis(xn, nx), by = cic_axis(yn, ny), bz = cic_axis(zn, nz);
+            const int qx = periodic_offset(bx.i0, cur.ox, nx) + 1,
+                      qy = periodic_offset(by.i0, cur.oy, ny) + 1,
+                      qz = periodic_offset(bz.i0, cur.oz, nz) + 4;
+            unsigned *plo = pbox + pbuf * NBOX_WORDS;
+            if (cnt < FIX_SAFE_COUNT && (unsigned)qx <= NB - 2 && (unsigned)qy <= NB - 2 &&
+                (unsigned)qz <= NBZ - 2) {
+              const int q0 = (qx * NB + qy) * NBZ + qz;
+#pragma unroll
+              for (int n = 0; n < 8; ++n) {
+                const float w =
+                    __fmul_rn(__fmul_rn(conn_x(n) ? bx.k1 : bx.k0, conn_y(n) ? by.k1 : by.k0),
+                              conn_z(n) ? bz.k1 : bz.k0);
+                const int q = q0 + conn_x(n) * NB * NBZ + conn_y(n) * NBZ + conn_z(n);
+                if (cnt < FIX1_COUNT) fixed_add_single(plo, q, w);
+                else fixed_add_split(plo, plo + NBOX, q, w);
+              }
+            } else {
+              if (stats && cnt < FIX_SAFE_COUNT) atomicAdd(stats, 1u);
+#pragma unroll
+              for (int n = 0; n < 8; ++n) {
+                const float w =
+                    __fmul_rn(__fmul_rn(conn_x(n) ? bx.k1 : bx.k0, conn_y(n) ? by.k1 : by.k0),
+                              conn_z(n) ? bz.k1 : bz.k0);
+                atomicAdd(mesh_next + cell_index(conn_x(n) ? bx.i1 : bx.i0,
+                                                 conn_y(n) ? by.i1 : by.i0,
+                                                 conn_z(n) ? bz.i1 : bz.i0, ny, nz),
+                          w);
+              }
+            }
+          }
         }
         if (counts) {
           const unsigned active = __ballot_sync(0xffffffffu, valid);
@@ -601,9 +669,56 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
       }
     }
     __syncthreads();  // buffer `buf` is free for the prefetch two tiles ahead
+    if (PAINT && cur.beg != cur.end) {
+      // flush the paint box: fixed point -> float in place, then one TMA
+      // reduce-add into the mesh (16-byte atomics where the box wraps)
+      const unsigned cnt = cur.end - cur.beg;
+      unsigned *plo = pbox + pbuf * NBOX_WORDS, *phi = plo + NBOX;
+      float *pf = reinterpret_cast<float *>(plo);
+      if (cnt < FIX1_COUNT) {
+        for (int q = tid; q < NBOX; q += TILE_THREADS) pf[q] = (float)plo[q] * (1.0f / FIX1_SCALE);
+      } else {
+        for (int q = tid; q < NBOX; q += TILE_THREADS)
+          pf[q] = fmaf((float)phi[q], 1.0f / 4096.0f, (float)plo[q] * (1.0f / 16777216.0f));
+      }
+      const bool ptma = use_ptma && nbox_interior(cur.ox, cur.oy, cur.oz, nx, ny, nz);
+      if (ptma) fence_async_shared();
+      if (use_ptma && tid == 0) bulk_wait_read();  // the other box's reduce has read it
+      __syncthreads();
+      if (ptma) {
+        if (tid == 0) {
+          tma_reduce_add_3d(&pmap, cur.oz - 4, cur.oy - 1, cur.ox - 1, pf);
+          bulk_commit();
+        }
+      } else if (pvec) {
+        for (int q = tid; q < NB * NB * (NBZ / 4); q += TILE_THREADS) {
+          const int g = q % (NBZ / 4), r = q / (NBZ / 4), b = r % NB, a = r / NB;
+          const float4 v = *reinterpret_cast<const float4 *>(pf + (a * NB + b) * NBZ + 4 * g);
+          if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f)
+            atomicAdd(reinterpret_cast<float4 *>(
+                          mesh_next + cell_index(wrap_index(cur.ox - 1 + a, nx),
+                                                 wrap_index(cur.oy - 1 + b, ny),
+                                                 wrap_index(cur.oz - 4 + 4 * g, nz), ny, nz)),
+                      v);
+        }
+      } else {
+        for (int q = tid; q < NBOX; q += TILE_THREADS) {
+          const int c = q % NBZ, r = q / NBZ, b = r % NB, a = r / NB;
+          const float v = pf[q];
+          if (v != 0.f)
+            atomicAdd(mesh_next + cell_index(wrap_index(cur.ox - 1 + a, nx),
+                                             wrap_index(cur.oy - 1 + b, ny),
+                                             wrap_index(cur.oz - 4 + c, nz), ny, nz),
+                      v);
+        }
+      }
+      zero_words(pbox + (pbuf ^ 1) * NBOX_WORDS, 2 * NBOX, tid);  // for the next tile
+      pbuf ^= 1;
+    }
     cur = nxt;
     buf ^= 1;
   }
+  if (PAINT && use_ptma && tid == 0) bulk_wait_all();  // reductions complete before exit
 }
 
 // Histogram + rank of the current positions (the first sort of a run).
@@ -946,10 +1061,12 @@ int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos, int64_t 
 
 // Tile-staged gather + kick + drift of tile-sorted particles; counts the new
 // positions per tile and records each particle's rank in its new tile.  The
-// drifted positions go to pos_out (pos itself for an in-place update).
+// drifted positions go to pos_out (pos itself for an in-place update).  With
+// mesh_next, the new positions are also painted there (overwritten): the
+// density of the next step.
 int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float *pos,
-               float *pos_out, float *vel, int64_t np, float kick, float drift, void *sort_ws, size_t sort_bytes,
-               unsigned *stats, cudaStream_t s) {
+               float *pos_out, float *vel, int64_t np, float kick, float drift, void *sort_ws,
+               size_t sort_bytes, unsigned *stats, cudaStream_t s, float *mesh_next) {
   PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
   const int64_t keys = tile_key_count(nx, ny, nz);
   SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
@@ -968,11 +1085,38 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float 
     use_tma = make_tensor_map(&map, f3, 4, dims, strides, box) == PMGB_OK ? 1 : 0;
     clear_error();
   }
-  rkd_tiles_kernel<<<tile_grid(keys), TILE_THREADS, 0, s>>>(
+  CUtensorMap pmap;
+  memset(&pmap, 0, sizeof(pmap));
+  if (!mesh_next) {
+    rkd_tiles_kernel<false><<<tile_grid(keys), TILE_THREADS, 0, s>>>(
+        f3, cs, nx, ny, nz, pos, pos_out, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts,
+        sc.rank, stats, map, use_tma, nullptr, 0, pmap, 0);
+    PMGB_LAUNCHED("rkd_tiles_kernel");
+    return PMGB_OK;
+  }
+  const int64_t ncell = (int64_t)nx * ny * nz;
+  PMGB_CUDA(cudaMemsetAsync(mesh_next, 0, ncell * sizeof(float), s));
+  const bool aligned = nz % 4 == 0 && reinterpret_cast<uintptr_t>(mesh_next) % 16 == 0;
+  int use_ptma = 0;
+  if (aligned && nz >= NBZ && ny >= NB && nx >= NB) {
+    // 3-D map of the density mesh, box 16 x 11 x 11 (the paint box)
+    const uint64_t dims[3] = {(uint64_t)nz, (uint64_t)ny, (uint64_t)nx};
+    const uint64_t strides[2] = {(uint64_t)nz * 4, (uint64_t)ny * nz * 4};
+    const uint32_t box[3] = {NBZ, NB, NB};
+    use_ptma = make_tensor_map(&pmap, mesh_next, 3, dims, strides, box) == PMGB_OK ? 1 : 0;
+    clear_error();
+  }
+  static bool ready[64] = {false};
+  int dev = 0;
+  PMGB_CUDA(cudaGetDevice(&dev));
+  if (dev >= 64 || !ready[dev]) {
+    PMGB_TRY(set_smem((const void *)rkd_tiles_kernel<true>, RKDP_SMEM));
+    if (dev < 64) ready[dev] = true;
+  }
+  rkd_tiles_kernel<true><<<tile_grid(keys), TILE_THREADS, RKDP_SMEM, s>>>(
       f3, cs, nx, ny, nz, pos, pos_out, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts,
-      sc.rank,
-      stats, map, use_tma);
-  PMGB_LAUNCHED("rkd_tiles_kernel");
+      sc.rank, stats, map, use_tma, mesh_next, aligned ? 1 : 0, pmap, use_ptma);
+  PMGB_LAUNCHED("rkd_tiles_kernel<paint>");
   return PMGB_OK;
 }
 
@@ -1028,6 +1172,41 @@ int fpm_step_sorted(const float *pos, float *vel, const unsigned *id, float *pos
                       sort_ws, sort_bytes, stats, s));
   return tile_scatter(drifted, vel, id, np, nx, ny, nz, pos2, vel2, id2, dest_out, sort_ws,
                       sort_bytes, s);
+}
+
+// A run of sorted steps: the density of the first step is painted from the
+// tile ranges in sort_ws; every later density is painted by the previous
+// step's gather (rkd_tiles_kernel<true>) from the new positions, before the
+// re-sort, so each step reads the particles once.
+int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, float *vel_b,
+                   unsigned *id_b, int64_t np, int nx, int ny, int nz, int n_steps,
+                   const float *kick, const float *drift, float r_split, void *mesh_ws,
+                   size_t mesh_bytes, void *sort_ws, size_t sort_bytes, unsigned *stats,
+                   cudaStream_t s) {
+  PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
+  float *mesh, *f3, *g3;
+  void *dk, *fk;
+  unsigned *work;
+  PMGB_TRY(pm_workspace_regions(mesh_ws, mesh_bytes, nx, ny, nz, np, &mesh, &dk, &fk, &f3, &g3,
+                                &work));
+  (void)g3;
+  (void)work;
+  float *drifted = pm_workspace_particles(mesh_ws, mesh_bytes, nx, ny, nz, np);
+  if (!drifted) return PMGB_ERR_WORKSPACE;
+  if (n_steps <= 0) return PMGB_OK;
+  float *P[2] = {pos_a, pos_b}, *V[2] = {vel_a, vel_b};
+  unsigned *I[2] = {id_a, id_b};
+  PMGB_TRY(paint_sorted(mesh, nx, ny, nz, pos_a, np, sort_ws, sort_bytes, stats, s));
+  for (int i = 0; i < n_steps; ++i) {
+    const int a = i & 1, b = a ^ 1;
+    PMGB_TRY(mesh_forces(mesh, nx, ny, nz, r_split, dk, fk, f3, s));
+    PMGB_TRY(rkd_sorted(f3, (int64_t)nx * ny * nz, nx, ny, nz, P[a], drifted, V[a], np, kick[i],
+                        drift[i], sort_ws, sort_bytes, stats, s,
+                        i + 1 < n_steps ? mesh : nullptr));
+    PMGB_TRY(tile_scatter(drifted, V[a], I[a], np, nx, ny, nz, P[b], V[b], I[b], nullptr,
+                          sort_ws, sort_bytes, s));
+  }
+  return PMGB_OK;
 }
 
 // ---------------------------------------------------------------------------

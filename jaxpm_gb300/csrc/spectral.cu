@@ -518,6 +518,294 @@ xpass_kernel(const float2 *in, float2 *out, XGeom g, const float2 *__restrict__ 
   }
 }
 
+// ---- x pass, register-resident transforms (nx = 2^LG, 64 <= nx <= 1024) --------
+//
+// Each column of nx values is transformed by nx/8 threads holding 8
+// elements each; a CTA takes XW columns (w fastest in the thread index, so
+// each warp reads and writes 64-byte segments).  A stage's butterfly is
+// computed in registers; between stages the values move through a padded
+// shared buffer (two buffers used in turn, one barrier per exchange).  The
+// first forward stage reads HBM directly, the last inverse stage writes it,
+// and the last forward stage and the first inverse stage work on the same
+// 8 positions, so the k-space multiply happens in registers.
+
+// float2 of padding per 8 positions: with 8, every exchange pattern of every
+// stage reads and writes in the minimum two wavefronts per warp
+constexpr int XPAD = 8;
+
+template <int LG>
+struct XPlan {
+  static constexpr int N = 1 << LG;
+  static constexpr int T = N / 8;                   // threads per column
+  static constexpr int NS = (LG + 2) / 3;           // stages
+  static constexpr int BUF = N * XW + (N / 8) * XPAD;  // one exchange buffer (float2)
+};
+
+__device__ __forceinline__ int xaddr(int p, int w) { return p * XW + w + (p >> 3) * XPAD; }
+
+// position of element m of thread b in stage s (block length 2^(LG-3s))
+template <int LG, int S_>
+__device__ __forceinline__ int xpos(int b, int m) {
+  constexpr int lg = LG - 3 * S_;
+  if constexpr (lg >= 3) {
+    constexpr int sb = lg - 3;
+    return ((b >> sb) << lg) + (b & ((1 << sb) - 1)) + (m << sb);
+  } else {
+    return 8 * b + m;
+  }
+}
+
+// frequency held at DIF output position p
+template <int LG>
+__device__ __forceinline__ int xfreq(int p) {
+  int k = 0, sh = 0;
+#pragma unroll
+  for (int lg = LG; lg > 0;) {
+    const int rb = lg >= 3 ? 3 : lg, sb = lg - rb;
+    k |= (p >> sb) << sh;
+    p &= (1 << sb) - 1;
+    sh += rb;
+    lg = sb;
+  }
+  return k;
+}
+
+// Twiddles of the radix-8 stages with span S > 1, packed per stage as
+// [j][m-1] = w_L^(j m) (j < S, m = 1..7) so a thread reads its seven at
+// consecutive addresses; xtw_offset(s) is where stage s's table starts.
+template <int LG>
+__host__ __device__ constexpr int xtw_offset(int s) {
+  int off = 0;
+  for (int q = 0; q < s; ++q) {
+    const int lg = LG - 3 * q;
+    if (lg >= 4) off += 7 << (lg - 3);
+  }
+  return off;
+}
+
+template <int LG, int S_ = 0>
+__device__ __forceinline__ void xload_twiddles(float2 *tw, const float2 *__restrict__ twx,
+                                               int tid, int nth) {
+  constexpr int lg = LG - 3 * S_;
+  if constexpr (lg >= 4) {
+    constexpr int S = 1 << (lg - 3), sh = LG - lg, off = xtw_offset<LG>(S_);
+    for (int i = tid; i < 7 * S; i += nth) {
+      const int j = i / 7, m = i - 7 * j + 1;
+      tw[off + i] = __ldg(twx + ((j * m) << sh));
+    }
+    xload_twiddles<LG, S_ + 1>(tw, twx, tid, nth);
+  }
+}
+
+template <int LG, int S_, bool INV>
+__device__ __forceinline__ void xstage(float2 *v, int b, const float2 *tw) {
+  constexpr int lg = LG - 3 * S_;
+  if constexpr (lg >= 3) {
+    constexpr int sb = lg - 3;
+    if constexpr (sb > 0) {
+      const int j = b & ((1 << sb) - 1);
+      const float2 *tj = tw + xtw_offset<LG>(S_) + 7 * j;
+      if (INV) {
+#pragma unroll
+        for (int m = 1; m < 8; ++m) v[m] = cmulc(v[m], tj[m - 1]);
+        dft8<true>(v);
+      } else {
+        dft8<false>(v);
+#pragma unroll
+        for (int m = 1; m < 8; ++m) v[m] = cmul(v[m], tj[m - 1]);
+      }
+    } else {
+      dft8<INV>(v);
+    }
+  } else if constexpr (lg == 2) {
+    dft4<INV>(v);
+    dft4<INV>(v + 4);
+  } else {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) dft2<INV>(v + 2 * q);
+  }
+}
+
+// Exchange addresses of stage S_: element m of thread b sits at
+// xaddr(base + m*S) = xaddr(base) + m*S*XW + ((m*S) >> 3)*XPAD, base =
+// xpos(b, 0): the low three bits of base plus (m*S mod 8) never carry
+// (base's low bits are j < S when S < 8, zero otherwise), so the per-m part
+// is a compile-time offset.
+template <int LG, int S_>
+__device__ __forceinline__ int xbase(int b, int w) {
+  return xaddr(xpos<LG, S_>(b, 0), w);
+}
+
+template <int LG, int S_>
+__device__ __forceinline__ constexpr int xoff(int m) {
+  constexpr int lg = LG - 3 * S_;
+  constexpr int S = lg >= 3 ? 1 << (lg - 3) : 1;
+  return m * S * XW + ((m * S) >> 3) * XPAD;
+}
+
+// write the values at stage A's positions, read them at stage B's
+template <int LG, int SA, int SB>
+__device__ __forceinline__ void xexchange(float2 *v, int b, int w, float2 *buf) {
+  float2 *pa = buf + xbase<LG, SA>(b, w);
+#pragma unroll
+  for (int m = 0; m < 8; ++m) pa[xoff<LG, SA>(m)] = v[m];
+  __syncthreads();
+  const float2 *pb = buf + xbase<LG, SB>(b, w);
+#pragma unroll
+  for (int m = 0; m < 8; ++m) v[m] = pb[xoff<LG, SB>(m)];
+}
+
+// Forward transform from natural order (v at stage-0 positions) to the last
+// stage's positions; `flip` tracks which exchange buffer is next.
+template <int LG, int S_ = 0>
+__device__ __forceinline__ void xforward(float2 *v, int b, int w, const float2 *tw, float2 *buf0,
+                                         float2 *buf1, int &flip) {
+  xstage<LG, S_, false>(v, b, tw);
+  if constexpr (S_ + 1 < XPlan<LG>::NS) {
+    xexchange<LG, S_, S_ + 1>(v, b, w, flip ? buf1 : buf0);
+    flip ^= 1;
+    xforward<LG, S_ + 1>(v, b, w, tw, buf0, buf1, flip);
+  }
+}
+
+// Inverse transform from the last stage's positions to natural order.
+template <int LG, int S_ = XPlan<LG>::NS - 1>
+__device__ __forceinline__ void xinverse(float2 *v, int b, int w, const float2 *tw, float2 *buf0,
+                                         float2 *buf1, int &flip) {
+  xstage<LG, S_, true>(v, b, tw);
+  if constexpr (S_ > 0) {
+    xexchange<LG, S_, S_ - 1>(v, b, w, flip ? buf1 : buf0);
+    flip ^= 1;
+    xinverse<LG, S_ - 1>(v, b, w, tw, buf0, buf1, flip);
+  }
+}
+
+template <int LG, int MODE>
+__global__ void __launch_bounds__(XPlan<LG>::T * XW, 1024 / (XPlan<LG>::T * XW))
+xpass_reg_kernel(const float2 *in, float2 *out, XGeom g, const float2 *__restrict__ twx,
+                 Tables t, float r2, int order, int fd, float scale) {
+  using PL = XPlan<LG>;
+  constexpr int N = PL::N, T = PL::T, NS = PL::NS;
+  extern __shared__ __align__(16) float2 xsm[];
+  float2 *tw = xsm;  // per-stage twiddle tables (xtw_offset), fewer than N entries
+  float2 *buf0 = xsm + N, *buf1 = buf0 + PL::BUF;
+  float2 *xk = buf1 + PL::BUF;  // per kx: (k2 or fd k2, gradient factor) for the k-space modes
+  const int tid = threadIdx.x, w = tid % XW, b = tid / XW;
+  const int ky = blockIdx.x / g.chunks, kz0 = (blockIdx.x - ky * g.chunks) * XW;
+  const int kz = kz0 + w;
+  xload_twiddles<LG>(tw, twx, tid, T * XW);
+  if (MODE == X_FORCES || MODE == X_FORCES_ADJ) {
+    for (int i = tid; i < N; i += T * XW) {
+      const AxisEntry X = t.x[i];
+      xk[i] = make_float2(fd ? X.fdk2 : X.k2, order ? X.g1 : X.g0);
+    }
+  }
+  __syncthreads();
+  auto gidx = [&](int x) -> int64_t { return ((int64_t)x * g.ny + ky) * g.pitch + kz; };
+  int flip = 0;
+  float2 v[8];
+  if (MODE == X_FORWARD || MODE == X_FORCES) {
+#pragma unroll
+    for (int m = 0; m < 8; ++m) v[m] = in[gidx(b + T * m)];
+    xforward<LG>(v, b, w, tw, buf0, buf1, flip);
+  }
+  if (MODE == X_FORWARD) {
+#pragma unroll
+    for (int m = 0; m < 8; ++m) out[gidx(xfreq<LG>(xpos<LG, NS - 1>(b, m)))] = v[m];
+    return;
+  }
+  if (MODE == X_INVERSE) {
+#pragma unroll
+    for (int m = 0; m < 8; ++m) v[m] = in[gidx(xfreq<LG>(xpos<LG, NS - 1>(b, m)))];
+    xinverse<LG>(v, b, w, tw, buf0, buf1, flip);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) out[gidx(b + T * m)] = v[m];
+    return;
+  }
+  const bool live = kz < g.nzh;
+  const AxisEntry Y = t.y[ky];
+  const AxisEntry Z = t.z[live ? kz : 0];
+  const float yk2 = fd ? Y.fdk2 : Y.k2, zk2 = fd ? Z.fdk2 : Z.k2;
+  const float gy = order ? Y.g1 : Y.g0, gz = order ? Z.g1 : Z.g0;
+  // per element: the inverse Laplacian times the long-range factor, as in
+  // inv_laplace / long_range (kk = ((kx^2 + ky^2) + kz^2); r2 uses k^2)
+  auto kfactor = [&](int kx, float &inv, float &L) {
+    const float2 xe = xk[kx];
+    const float kk = __fadd_rn(__fadd_rn(xe.x, yk2), zk2);
+    inv = kk == 0.0f ? 0.0f : -__frcp_rn(kk);
+    L = 1.0f;
+    if (r2 != 0.0f) {
+      const float k2 = fd ? __fadd_rn(__fadd_rn(t.x[kx].k2, Y.k2), Z.k2) : kk;
+      L = expf(-k2 * r2);
+    }
+  };
+  if (MODE == X_FORCES) {
+    // pot = (delta * invlaplace) * longrange.  F_c = -(i g_c) pot: the x
+    // component needs its own inverse x transform; g_y and g_z are constant
+    // along x, so F_y and F_z are -(i g_y) and -(i g_z) times one inverse
+    // transform of pot.  pot is kept (times the normalisation) in v after
+    // the x component is written.
+    float2 pot[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const int kx = xfreq<LG>(xpos<LG, NS - 1>(b, m));
+      float inv, L;
+      kfactor(kx, inv, L);
+      pot[m] = make_float2(__fmul_rn(__fmul_rn(v[m].x, inv), L),
+                           __fmul_rn(__fmul_rn(v[m].y, inv), L));
+      if (!live) pot[m] = make_float2(0.f, 0.f);
+      const float gc = xk[kx].y;
+      // -(i g) * (px + i py) = g*py - i g*px
+      v[m] = make_float2(__fmul_rn(gc, pot[m].y) * scale, -__fmul_rn(gc, pot[m].x) * scale);
+    }
+    xinverse<LG>(v, b, w, tw, buf0, buf1, flip);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      out[gidx(b + T * m)] = v[m];
+      v[m] = make_float2(pot[m].x * scale, pot[m].y * scale);
+    }
+    xinverse<LG>(v, b, w, tw, buf0, buf1, flip);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      out[g.cs_out + gidx(b + T * m)] = make_float2(gy * v[m].y, -gy * v[m].x);
+      out[2 * g.cs_out + gidx(b + T * m)] = make_float2(gz * v[m].y, -gz * v[m].x);
+    }
+    return;
+  }
+  // X_FORCES_ADJ: acc = sum_c (i g_c) V_c, then times invlaplace * longrange
+  // * scale.  g_y and g_z are constant along x, so the y and z cotangents
+  // are combined before one forward transform: (i g_y) V_y + (i g_z) V_z =
+  // FFT_x((i g_y) G_y + (i g_z) G_z).
+  float2 acc[8];
+#pragma unroll
+  for (int m = 0; m < 8; ++m) v[m] = in[gidx(b + T * m)];
+  xforward<LG>(v, b, w, tw, buf0, buf1, flip);
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    const float gc = xk[xfreq<LG>(xpos<LG, NS - 1>(b, m))].y;
+    acc[m] = make_float2(-gc * v[m].y, gc * v[m].x);
+  }
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    const float2 a = in[g.cs_in + gidx(b + T * m)], c = in[2 * g.cs_in + gidx(b + T * m)];
+    // (i g_y) a + (i g_z) c
+    v[m] = make_float2(-(gy * a.y + gz * c.y), gy * a.x + gz * c.x);
+  }
+  xforward<LG>(v, b, w, tw, buf0, buf1, flip);
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    const int kx = xfreq<LG>(xpos<LG, NS - 1>(b, m));
+    float inv, L;
+    kfactor(kx, inv, L);
+    const float mm = inv * L * scale;
+    const float ax = acc[m].x + v[m].x, ay = acc[m].y + v[m].y;
+    v[m] = live ? make_float2(ax * mm, ay * mm) : make_float2(0.f, 0.f);
+  }
+  xinverse<LG>(v, b, w, tw, buf0, buf1, flip);
+#pragma unroll
+  for (int m = 0; m < 8; ++m) out[gidx(b + T * m)] = v[m];
+}
+
 // ---- host side ----------------------------------------------------------------
 
 std::mutex g_tw_mu;
@@ -605,6 +893,18 @@ int plane_c2r(const float2 *in, float *out, int nplanes, int ny, int nz, int pit
   return PMGB_OK;
 }
 
+template <int LG, int MODE>
+int xpass_reg(const float2 *in, float2 *out, const XGeom &g, const float2 *twx, const Tables &t,
+              float r2, int order, int fd, float scale, cudaStream_t s) {
+  using PL = XPlan<LG>;
+  const size_t smem = (2 * (size_t)PL::N + 2 * (size_t)PL::BUF) * sizeof(float2);
+  PMGB_TRY(set_dyn_smem((const void *)xpass_reg_kernel<LG, MODE>, smem));
+  xpass_reg_kernel<LG, MODE><<<g.ny * g.chunks, PL::T * XW, smem, s>>>(in, out, g, twx, t, r2,
+                                                                       order, fd, scale);
+  PMGB_LAUNCHED("xpass_reg_kernel");
+  return PMGB_OK;
+}
+
 template <int MODE>
 int xpass(const float2 *in, float2 *out, int nx, int ny, int nz, int pitch, int64_t cs_in,
           int64_t cs_out, float r_split, int order, int fd, float scale, cudaStream_t s) {
@@ -621,6 +921,15 @@ int xpass(const float2 *in, float2 *out, int nx, int ny, int nz, int pitch, int6
   PMGB_TRY(twiddles(nx, &twx));
   Tables t{nullptr, nullptr, nullptr};
   if (MODE == X_FORCES || MODE == X_FORCES_ADJ) PMGB_TRY(tables(nx, ny, nz, &t));
+  const float r2 = r_split * r_split;
+  switch (g.lgx) {
+    case 6: return xpass_reg<6, MODE>(in, out, g, twx, t, r2, order, fd, scale, s);
+    case 7: return xpass_reg<7, MODE>(in, out, g, twx, t, r2, order, fd, scale, s);
+    case 8: return xpass_reg<8, MODE>(in, out, g, twx, t, r2, order, fd, scale, s);
+    case 9: return xpass_reg<9, MODE>(in, out, g, twx, t, r2, order, fd, scale, s);
+    case 10: return xpass_reg<10, MODE>(in, out, g, twx, t, r2, order, fd, scale, s);
+    default: break;
+  }
   const size_t smem = 2 * (size_t)nx * XW * sizeof(float2);
   PMGB_TRY(set_dyn_smem((const void *)xpass_kernel<MODE>, smem));
   xpass_kernel<MODE><<<ny * g.chunks, XPASS_THREADS, smem, s>>>(in, out, g, twx, t,
@@ -632,11 +941,28 @@ int xpass(const float2 *in, float2 *out, int nx, int ny, int nz, int pitch, int6
 
 }  // namespace
 
-static std::atomic<int> g_spectral{0};
+// 0: cuFFT 3-D + k-space kernel; 1 (default): cuFFT 2-D planes + the fused
+// x pass; 2: the library's plane kernels + the fused x pass.
+static std::atomic<int> g_spectral{1};
 
 bool spectral_enabled() { return g_spectral.load() != 0; }
 
-int set_spectral(int enabled) { return g_spectral.exchange(enabled ? 1 : 0); }
+int spectral_mode() { return g_spectral.load(); }
+
+int set_spectral(int mode) { return g_spectral.exchange(mode); }
+
+// plane transforms of the composite pipeline: cuFFT's batched 2-D or ours
+static int planes_r2c(const float *in, float2 *out, int nplanes, int ny, int nz, int pitch,
+                      cudaStream_t s) {
+  if (g_spectral.load() == 2) return plane_r2c(in, out, nplanes, ny, nz, pitch, s);
+  return fft_planes_r2c(in, out, nplanes, ny, nz, pitch, s);
+}
+
+static int planes_c2r(float2 *in, float *out, int nplanes, int ny, int nz, int pitch,
+                      cudaStream_t s) {
+  if (g_spectral.load() == 2) return plane_c2r(in, out, nplanes, ny, nz, pitch, s);
+  return fft_planes_c2r(in, out, nplanes, ny, nz, pitch, s);
+}
 
 int spectral_pitch(int nz) { return (nz / 2 + 1 + XW - 1) / XW * XW; }
 
@@ -684,9 +1010,9 @@ int spectral_forces(const float *mesh, void *spec, void *fspec, float *f3, int n
   const int pitch = spectral_pitch(nz);
   const int64_t cs = (int64_t)nx * ny * pitch;
   float2 *d = static_cast<float2 *>(spec), *f = static_cast<float2 *>(fspec);
-  PMGB_TRY(plane_r2c(mesh, d, nx, ny, nz, pitch, s));
+  PMGB_TRY(planes_r2c(mesh, d, nx, ny, nz, pitch, s));
   PMGB_TRY(xpass<X_FORCES>(d, f, nx, ny, nz, pitch, cs, cs, r_split, order, fd, scale, s));
-  PMGB_TRY(plane_c2r(f, f3, 3 * nx, ny, nz, pitch, s));
+  PMGB_TRY(planes_c2r(f, f3, 3 * nx, ny, nz, pitch, s));
   return PMGB_OK;
 }
 
@@ -697,9 +1023,9 @@ int spectral_forces_vjp(const float *g3, void *spec3, void *dspec, float *rbar, 
   const int pitch = spectral_pitch(nz);
   const int64_t cs = (int64_t)nx * ny * pitch;
   float2 *a = static_cast<float2 *>(spec3), *d = static_cast<float2 *>(dspec);
-  PMGB_TRY(plane_r2c(g3, a, 3 * nx, ny, nz, pitch, s));
+  PMGB_TRY(planes_r2c(g3, a, 3 * nx, ny, nz, pitch, s));
   PMGB_TRY(xpass<X_FORCES_ADJ>(a, d, nx, ny, nz, pitch, cs, cs, r_split, order, fd, scale, s));
-  PMGB_TRY(plane_c2r(d, rbar, nx, ny, nz, pitch, s));
+  PMGB_TRY(planes_c2r(d, rbar, nx, ny, nz, pitch, s));
   return PMGB_OK;
 }
 

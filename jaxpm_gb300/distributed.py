@@ -91,13 +91,16 @@ def ifft3d(x, nz=None):
     return _C2R.apply(x, nz)
 
 
-FFT_PATHS = {"cufft": 0, "fused": 1}
+FFT_PATHS = {"cufft": 0, "fused": 1, "own": 2}
 
 
 def fft_path():
-    """FFT path of the composite force calls: ``"cufft"`` (default) or
-    ``"fused"`` (the library's own FFT pipeline, fused with the k-space
-    kernel, for the mesh shapes it supports; cuFFT otherwise)."""
+    """FFT path of the composite force calls: ``"cufft"`` (cuFFT 3-D
+    transforms around the k-space kernel), ``"fused"`` (default: cuFFT's 2-D
+    plane transforms around the library's x-direction kernel, which fuses
+    the forward x transform, the force multiplies and the inverse x
+    transforms) or ``"own"`` (the library's plane kernels as well).  The
+    last two apply to the mesh shapes ``fft3_supported`` accepts."""
     return {v: k for k, v in FFT_PATHS.items()}[_lib.load().pmgb_fft_path()]
 
 

@@ -7,6 +7,8 @@ call, ``pmgb_fpm_step_f32``: paint -> R2C -> fused k-space -> batched C2R ->
 gather + kick + drift in one kernel.  Positions and velocities are
 ``[Np, 3]`` float32 CUDA tensors updated in place.
 """
+import ctypes
+
 import numpy as np
 import torch
 from torch.utils.checkpoint import checkpoint
@@ -170,9 +172,25 @@ class SortedFastPM:
                   _lib.ptr(dest), _lib.ptr(offs), _lib.ptr(self.stats_buf), s)
         self.cur = b
 
-    def run(self, steps=None):
-        for i in range(self.n_steps if steps is None else steps):
-            self.step(i)
+    def run(self, steps=None, start=0, stream=None):
+        """Runs steps ``start .. start+steps-1`` (default: all remaining) with
+        one ``pmgb_fpm_run_sorted_f32`` call: each step's gather also paints
+        the next step's density."""
+        n = (self.n_steps - start) if steps is None else int(steps)
+        if n <= 0:
+            return
+        nx, ny, nz = self.mesh_shape
+        a, b = self.cur, 1 - self.cur
+        kick = np.ascontiguousarray(self.kick[start:start + n], dtype=np.float32)
+        drift = np.ascontiguousarray(self.drift[start:start + n], dtype=np.float32)
+        fp = ctypes.POINTER(ctypes.c_float)
+        s = _lib.stream() if stream is None else stream
+        _lib.call("pmgb_fpm_run_sorted_f32", _lib.ptr(self.pos[a]), _lib.ptr(self.vel[a]),
+                  _lib.ptr(self.ids[a]), _lib.ptr(self.pos[b]), _lib.ptr(self.vel[b]),
+                  _lib.ptr(self.ids[b]), self.n, nx, ny, nz, n, kick.ctypes.data_as(fp),
+                  drift.ctypes.data_as(fp), self.r_split, _lib.ptr(self.ws), self.ws_bytes,
+                  _lib.ptr(self.sort_ws), self.sort_bytes, _lib.ptr(self.stats_buf), s)
+        self.cur = a if n % 2 == 0 else b
 
     @property
     def positions(self):

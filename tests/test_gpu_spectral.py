@@ -13,11 +13,13 @@ pytestmark = pytest.mark.gpu
 SHAPES = [(64, 64, 64), (8, 64, 16), (32, 128, 256), (128, 64, 32), (16, 512, 512)]
 
 
-@pytest.fixture()
-def fft_fused(lib):
+@pytest.fixture(params=["fused", "own"])
+def fft_fused(lib, request):
+    """The two library FFT paths of the composite calls: cuFFT planes around
+    the fused x kernel, and the library's plane kernels as well."""
     from jaxpm_gb300 import distributed
-    prev = distributed.set_fft_path("fused")
-    yield
+    prev = distributed.set_fft_path(request.param)
+    yield request.param
     distributed.set_fft_path(prev)
 
 
@@ -93,7 +95,7 @@ def test_force_pipeline_matches_cufft_and_oracle(cuda, fft_fused, shape):
     distributed.set_fft_path("cufft")
     f_cufft = pm.pm_forces(x, shape, r_split=0.0).cpu()
     f_cufft_rs = pm.pm_forces(x, shape, r_split=1.5).cpu()
-    distributed.set_fft_path("fused")
+    distributed.set_fft_path(fft_fused)
     # two float32 FFT implementations: rounding differences only
     assert rel_l2(f_auto, f_cufft) < 1e-5
     assert rel_l2(f_auto_rs, f_cufft_rs) < 1e-5
@@ -118,7 +120,7 @@ def test_force_adjoint_matches_cufft(cuda, fft_fused):
     a = grad()
     distributed.set_fft_path("cufft")
     b = grad()
-    distributed.set_fft_path("fused")
+    distributed.set_fft_path(fft_fused)
     assert rel_l2(a, b) < 1e-5
 
 
@@ -134,7 +136,7 @@ def test_sorted_run_spectral_matches_cufft(cuda, fft_fused):
     gx = torch.randn(x0.shape, device=cuda)
     gv = torch.randn(x0.shape, device=cuda)
     res = {}
-    for path in ("fused", "cufft"):
+    for path in (fft_fused, "cufft"):
         distributed.set_fft_path(path)
         eng = simulate.SortedFastPM(shape, cosmology.Planck15(), 0.1, 1.0, 10, device=cuda)
         eng.load(x0, v0)
@@ -142,6 +144,6 @@ def test_sorted_run_spectral_matches_cufft(cuda, fft_fused):
         xf, vf = eng.state()
         (_, _), (ax, av) = eng.vjp(x0, v0, gx, gv)
         res[path] = (xf.cpu(), vf.cpu(), ax.cpu(), av.cpu())
-    distributed.set_fft_path("fused")
-    for a, b in zip(res["fused"], res["cufft"]):
+    distributed.set_fft_path(fft_fused)
+    for a, b in zip(res[fft_fused], res["cufft"]):
         assert rel_l2(a, b) < 1e-4
