@@ -339,7 +339,7 @@ int pmgb_permute3_f32(const float *in, const uint32_t *id, int64_t np,
 
 /* Paint of tile-sorted particles (the sorted loop's paint; mesh overwritten):
  * one CTA per tile accumulates the tile plus a one-cell halo in shared
- * memory (exact 24-bit fixed point with native 32-bit atomics) from the
+ * memory (exact fixed point with native 32-bit atomics) from the
  * particle range recorded in sort_workspace by the last pmgb_tile_sort_f32 /
  * pmgb_tile_scatter_f32, then adds the box to the mesh with one TMA bulk
  * reduce-add (tiles whose box wraps around the mesh use 16-byte atomics).

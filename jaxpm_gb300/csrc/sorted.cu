@@ -86,6 +86,38 @@ __device__ __forceinline__ uint32_t count_and_rank(unsigned *__restrict__ counts
   return base + __popc(peers & ((1u << lane) - 1u));
 }
 
+// count_and_rank for the gather, where most particles stay in the tile being
+// processed (`home`): those take their ranks from one warp-level atomic,
+// the few that left count one atomic each.  All 32 lanes call it; the
+// result is meaningful on lanes with `valid`.
+__device__ __forceinline__ uint32_t count_and_rank_home(unsigned *__restrict__ counts,
+                                                        uint32_t key, uint32_t home,
+                                                        bool valid) {
+  const int lane = threadIdx.x & 31;
+  const unsigned stay = __ballot_sync(0xffffffffu, valid && key == home);
+  uint32_t r = 0;
+  if (stay) {
+    const int leader = __ffs(stay) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(counts + home, (unsigned)__popc(stay));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    r = base + __popc(stay & ((1u << lane) - 1u));
+  }
+  if (valid && key != home) r = atomicAdd(counts + key, 1u);
+  return r;
+}
+
+// Fixed-point scale of a paint box whose tile holds `count` (< 2^20)
+// particles: 2^s with s = min(24, clz(count)), so that count * 2^s < 2^32
+// (a cell receives at most one contribution, <= 2^s, per particle) and the
+// box sums stay exact in one 32-bit word.
+__device__ __forceinline__ int paint_shift(unsigned count) {
+  const int s = __clz(count);
+  return s < 24 ? s : 24;
+}
+
+__device__ __forceinline__ float pow2f(int e) { return __int_as_float((127 + e) << 23); }
+
 // ---------------------------------------------------------------------------
 // chunk boxes in coordinates relative to a reference cell (so a chunk that
 // straddles the periodic boundary, or whose particles carry different
@@ -283,44 +315,25 @@ constexpr int TB = TILE + 1;   // box edge (cells)
 constexpr int TBZ = 12;        // z stride of a box row (16-byte multiple)
 constexpr int TBOX = TB * TB * TBZ;
 constexpr int TILE_THREADS = 256;
-constexpr float FIX_SCALE = 16777216.0f;  // 2^24: paint weights in 24-bit fixed point
 
 __device__ __forceinline__ bool box_interior(int ox, int oy, int oz, int nx, int ny, int nz) {
   return ox + TB <= nx && oy + TB <= ny && oz + TBZ <= nz;
 }
 
-// The paint box accumulates CIC weights (in [0, 1]) as 24-bit fixed point
-// split into two 12-bit halves, each summed with native (fire-and-forget)
-// 32-bit shared atomics.  A cell receives at most one contribution per
-// particle of the tile, so neither half can wrap while the tile holds fewer
-// than 2^20 particles; the sum hi * 2^-12 + lo * 2^-24 is then exact and is
-// converted to float once per cell.  A tile with more particles paints
-// with global float atomics instead.
+// The paint boxes accumulate CIC weights (in [0, 1]) in fixed point with
+// native (fire-and-forget) 32-bit shared atomics: round(w * 2^s) with s =
+// paint_shift(count of the tile's particles), which keeps every cell's sum
+// exact and below 2^32 (2^22 for a tile of 512 particles, 2^20 below 4096).
+// Each box is converted to float once per cell.  Tiles of 2^20 particles or
+// more paint with global float atomics instead.
 constexpr unsigned FIX_SAFE_COUNT = 1u << 20;
 
-__device__ __forceinline__ void fixed_add_split(unsigned *lo, unsigned *hi, int c, float w) {
-  const unsigned q = __float2uint_rn(w * FIX_SCALE);  // <= 2^24
-  atomicAdd(lo + c, q & 0xFFFu);
-  atomicAdd(hi + c, q >> 12);
-}
-
-// Tiles with fewer than 4096 particles use one word per cell with 20
-// fractional bits (a cell's sum stays below 4096 < 2^12): half the shared
-// atomics, quantisation 2^-20 per contribution, sums exact.
-constexpr unsigned FIX1_COUNT = 4096;
-constexpr float FIX1_SCALE = 1048576.0f;  // 2^20
-
-__device__ __forceinline__ void fixed_add_single(unsigned *acc, int c, float w) {
-  atomicAdd(acc + c, __float2uint_rn(w * FIX1_SCALE));
-}
-
-// Warp-per-tile painter: each warp of a CTA owns a private box (the two
-// fixed-point halves; the low half is reused as the float box for the
-// flush) and takes tiles from a global counter, so warps never wait on each
-// other and a heavy tile delays only its own warp.
+// Warp-per-tile painter: each warp of a CTA owns a private box (reused as
+// the float box for the flush) and takes tiles from a global counter, so
+// warps never wait on each other and a heavy tile delays only its own warp.
 constexpr int PAINT_WARPS = 8;
 constexpr int PAINT_ILP = 4;
-constexpr int WBOX_WORDS = (2 * TBOX + 31) / 32 * 32;  // lo + hi, 128-byte multiple
+constexpr int WBOX_WORDS = (TBOX + 31) / 32 * 32;  // one word per cell, 128-byte multiple
 constexpr int PAINT_SMEM = PAINT_WARPS * WBOX_WORDS * 4;
 
 __global__ void __launch_bounds__(PAINT_WARPS * 32)
@@ -332,7 +345,6 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
   extern __shared__ __align__(128) unsigned wbox[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned *lo = wbox + warp * WBOX_WORDS;
-  unsigned *hi = lo + TBOX;
   float *fbox = reinterpret_cast<float *>(lo);
   for (;;) {
     uint32_t key = 0;
@@ -344,11 +356,11 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
     const int ox = (int)compact3(key >> 2) * TILE, oy = (int)compact3(key >> 1) * TILE,
               oz = (int)compact3(key) * TILE;
     const bool boxed = end - beg < FIX_SAFE_COUNT;  // uniform
-    const bool single = end - beg < FIX1_COUNT;     // uniform: one word per cell
+    const int shift = paint_shift(end - beg);
+    const float S = pow2f(shift);
     {
-      uint4 *z4 = reinterpret_cast<uint4 *>(lo);  // lo and hi are contiguous, 16-byte aligned
-      const int words = single ? TBOX : 2 * TBOX;
-      for (int q = lane; q < words / 4; q += 32) z4[q] = make_uint4(0u, 0u, 0u, 0u);
+      uint4 *z4 = reinterpret_cast<uint4 *>(lo);  // 16-byte aligned
+      for (int q = lane; q < TBOX / 4; q += 32) z4[q] = make_uint4(0u, 0u, 0u, 0u);
     }
     __syncwarp();
     for (unsigned p0 = beg + lane; p0 < end; p0 += 32 * PAINT_ILP) {
@@ -371,20 +383,12 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
       if (boxed && (unsigned)lx < (unsigned)TILE && (unsigned)ly < (unsigned)TILE &&
           (unsigned)lz < (unsigned)TILE) {
         const int q0 = (lx * TB + ly) * TBZ + lz;
-        if (single) {
 #pragma unroll
-          for (int n = 0; n < 8; ++n) {
-            float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
-                                conn_z(n) ? az.k1 : az.k0);
-            fixed_add_single(lo, q0 + conn_x(n) * TB * TBZ + conn_y(n) * TBZ + conn_z(n), w);
-          }
-        } else {
-#pragma unroll
-          for (int n = 0; n < 8; ++n) {
-            float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
-                                conn_z(n) ? az.k1 : az.k0);
-            fixed_add_split(lo, hi, q0 + conn_x(n) * TB * TBZ + conn_y(n) * TBZ + conn_z(n), w);
-          }
+        for (int n = 0; n < 8; ++n) {
+          float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                              conn_z(n) ? az.k1 : az.k0);
+          atomicAdd(lo + q0 + conn_x(n) * TB * TBZ + conn_y(n) * TBZ + conn_z(n),
+                    __float2uint_rn(w * S));
         }
       } else {
         if (stats && boxed) atomicAdd(stats, 1u);
@@ -400,11 +404,9 @@ paint_tiles_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
     }
     __syncwarp();
     // fixed point -> float in place (each lane reads and rewrites its own cells)
-    if (single) {
-      for (int q = lane; q < TBOX; q += 32) fbox[q] = (float)lo[q] * (1.0f / FIX1_SCALE);
-    } else {
-      for (int q = lane; q < TBOX; q += 32)
-        fbox[q] = fmaf((float)hi[q], 1.0f / 4096.0f, (float)lo[q] * (1.0f / 16777216.0f));
+    {
+      const float inv = pow2f(-shift);
+      for (int q = lane; q < TBOX; q += 32) fbox[q] = (float)lo[q] * inv;
     }
     const bool tma = use_tma && box_interior(ox, oy, oz, nx, ny, nz);
     if (tma) fence_async_shared();  // generic-proxy writes of fbox -> TMA
@@ -468,11 +470,11 @@ constexpr int RKD_ILP = 2;
 // positions, which may leave their tile by about a cell): x and y cover
 // o-1 .. o+9, z covers o-4 .. o+11 so that the TMA box starts on a 16-byte
 // boundary.  Two boxes in turn (the TMA reduce of one drains while the next
-// tile paints the other), each with the two fixed-point halves.
+// tile paints the other), one fixed-point word per cell (paint_shift).
 constexpr int NB = TILE + 3;
 constexpr int NBZ = 16;
 constexpr int NBOX = NB * NB * NBZ;
-constexpr int NBOX_WORDS = (2 * NBOX + 31) / 32 * 32;
+constexpr int NBOX_WORDS = (NBOX + 31) / 32 * 32;
 constexpr int RKDP_SMEM = 2 * NBOX_WORDS * 4;
 
 __device__ __forceinline__ bool nbox_interior(int ox, int oy, int oz, int nx, int ny, int nz) {
@@ -511,7 +513,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
     mbar_init(&bar[1], 1);
     fence_async_shared();
   }
-  if (PAINT) zero_words(pbox, 2 * NBOX, tid);
+  if (PAINT) zero_words(pbox, NBOX_WORDS, tid);
   __syncthreads();
   int pbuf = 0;
   uint32_t phase0 = 0u, phase1 = 0u;  // parity of the next completion of bar[0] / bar[1]
@@ -637,14 +639,14 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
             if (cnt < FIX_SAFE_COUNT && (unsigned)qx <= NB - 2 && (unsigned)qy <= NB - 2 &&
                 (unsigned)qz <= NBZ - 2) {
               const int q0 = (qx * NB + qy) * NBZ + qz;
+              const float S = pow2f(paint_shift(cnt));
 #pragma unroll
               for (int n = 0; n < 8; ++n) {
                 const float w =
                     __fmul_rn(__fmul_rn(conn_x(n) ? bx.k1 : bx.k0, conn_y(n) ? by.k1 : by.k0),
                               conn_z(n) ? bz.k1 : bz.k0);
                 const int q = q0 + conn_x(n) * NB * NBZ + conn_y(n) * NBZ + conn_z(n);
-                if (cnt < FIX1_COUNT) fixed_add_single(plo, q, w);
-                else fixed_add_split(plo, plo + NBOX, q, w);
+                atomicAdd(plo + q, __float2uint_rn(w * S));
               }
             } else {
               if (stats && cnt < FIX_SAFE_COUNT) atomicAdd(stats, 1u);
@@ -662,8 +664,8 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
           }
         }
         if (counts) {
-          const unsigned active = __ballot_sync(0xffffffffu, valid);
-          if (valid) rank[p] = count_and_rank(counts, k, active);
+          const uint32_t r = count_and_rank_home(counts, k, key, valid);
+          if (valid) rank[p] = r;
         }
        }
       }
@@ -673,14 +675,10 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
       // flush the paint box: fixed point -> float in place, then one TMA
       // reduce-add into the mesh (16-byte atomics where the box wraps)
       const unsigned cnt = cur.end - cur.beg;
-      unsigned *plo = pbox + pbuf * NBOX_WORDS, *phi = plo + NBOX;
+      unsigned *plo = pbox + pbuf * NBOX_WORDS;
       float *pf = reinterpret_cast<float *>(plo);
-      if (cnt < FIX1_COUNT) {
-        for (int q = tid; q < NBOX; q += TILE_THREADS) pf[q] = (float)plo[q] * (1.0f / FIX1_SCALE);
-      } else {
-        for (int q = tid; q < NBOX; q += TILE_THREADS)
-          pf[q] = fmaf((float)phi[q], 1.0f / 4096.0f, (float)plo[q] * (1.0f / 16777216.0f));
-      }
+      const float inv = pow2f(-paint_shift(cnt));
+      for (int q = tid; q < NBOX; q += TILE_THREADS) pf[q] = (float)plo[q] * inv;
       const bool ptma = use_ptma && nbox_interior(cur.ox, cur.oy, cur.oz, nx, ny, nz);
       if (ptma) fence_async_shared();
       if (use_ptma && tid == 0) bulk_wait_read();  // the other box's reduce has read it
@@ -712,7 +710,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
                       v);
         }
       }
-      zero_words(pbox + (pbuf ^ 1) * NBOX_WORDS, 2 * NBOX, tid);  // for the next tile
+      zero_words(pbox + (pbuf ^ 1) * NBOX_WORDS, NBOX_WORDS, tid);  // for the next tile
       pbuf ^= 1;
     }
     cur = nxt;
@@ -1087,7 +1085,14 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float 
   }
   CUtensorMap pmap;
   memset(&pmap, 0, sizeof(pmap));
+  static bool ready[2][64] = {{false}};
+  int dev = 0;
+  PMGB_CUDA(cudaGetDevice(&dev));
   if (!mesh_next) {
+    if (dev >= 64 || !ready[0][dev]) {
+      PMGB_TRY(set_smem((const void *)rkd_tiles_kernel<false>, 0));
+      if (dev < 64) ready[0][dev] = true;
+    }
     rkd_tiles_kernel<false><<<tile_grid(keys), TILE_THREADS, 0, s>>>(
         f3, cs, nx, ny, nz, pos, pos_out, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts,
         sc.rank, stats, map, use_tma, nullptr, 0, pmap, 0);
@@ -1106,12 +1111,9 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float 
     use_ptma = make_tensor_map(&pmap, mesh_next, 3, dims, strides, box) == PMGB_OK ? 1 : 0;
     clear_error();
   }
-  static bool ready[64] = {false};
-  int dev = 0;
-  PMGB_CUDA(cudaGetDevice(&dev));
-  if (dev >= 64 || !ready[dev]) {
+  if (dev >= 64 || !ready[1][dev]) {
     PMGB_TRY(set_smem((const void *)rkd_tiles_kernel<true>, RKDP_SMEM));
-    if (dev < 64) ready[dev] = true;
+    if (dev < 64) ready[1][dev] = true;
   }
   rkd_tiles_kernel<true><<<tile_grid(keys), TILE_THREADS, RKDP_SMEM, s>>>(
       f3, cs, nx, ny, nz, pos, pos_out, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts,
