@@ -86,25 +86,15 @@ __device__ __forceinline__ uint32_t count_and_rank(unsigned *__restrict__ counts
   return base + __popc(peers & ((1u << lane) - 1u));
 }
 
-// count_and_rank for the gather, where most particles stay in the tile being
-// processed (`home`): those take their ranks from one warp-level atomic,
-// the few that left count one atomic each.  All 32 lanes call it; the
-// result is meaningful on lanes with `valid`.
-__device__ __forceinline__ uint32_t count_and_rank_home(unsigned *__restrict__ counts,
-                                                        uint32_t key, uint32_t home,
-                                                        bool valid) {
-  const int lane = threadIdx.x & 31;
+// The gather's tile histogram: particles that stay in the tile being
+// processed (`home`) are added by one warp-level reduction, the others one
+// each; no value is returned, so nothing waits on the atomics (the scatter
+// claims the slots).  All 32 lanes call it.
+__device__ __forceinline__ void count_home(unsigned *__restrict__ counts, uint32_t key,
+                                           uint32_t home, bool valid) {
   const unsigned stay = __ballot_sync(0xffffffffu, valid && key == home);
-  uint32_t r = 0;
-  if (stay) {
-    const int leader = __ffs(stay) - 1;
-    unsigned base = 0;
-    if (lane == leader) base = atomicAdd(counts + home, (unsigned)__popc(stay));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    r = base + __popc(stay & ((1u << lane) - 1u));
-  }
-  if (valid && key != home) r = atomicAdd(counts + key, 1u);
-  return r;
+  if (stay && (threadIdx.x & 31) == __ffs(stay) - 1) atomicAdd(counts + home, (unsigned)__popc(stay));
+  if (valid && key != home) atomicAdd(counts + key, 1u);
 }
 
 // Fixed-point scale of a paint box whose tile holds `count` (< 2^20)
@@ -473,8 +463,8 @@ constexpr int RKD_ILP = 2;
 // tile paints the other), one fixed-point word per cell (paint_shift).
 constexpr int NB = TILE + 3;
 constexpr int NBZ = 16;
-constexpr int NBOX = NB * NB * NBZ;
-constexpr int NBOX_WORDS = (NBOX + 31) / 32 * 32;
+constexpr int NPS = (NB * NBZ + 31) / 32 * 32;  // x-plane stride (128-byte multiple)
+constexpr int NBOX_WORDS = NB * NPS;
 constexpr int RKDP_SMEM = 2 * NBOX_WORDS * 4;
 
 __device__ __forceinline__ bool nbox_interior(int ox, int oy, int oz, int nx, int ny, int nz) {
@@ -547,7 +537,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
         if (__syncthreads_or(!ok)) {  // uniform: every thread leaves together
           if (stats && tid == 0) atomicExch(stats + 2, 1u);
           if (nxt.tma) mbar_wait(&bar[buf ^ 1], buf ? phase0 : phase1);  // drain the prefetch
-          if (PAINT && use_ptma && tid == 0) bulk_wait_all();  // paint reductions in flight
+          if (PAINT && use_ptma && (tid & 31) == 0) bulk_wait_all();  // paint reductions
           return;
         }
         if (buf) phase1 ^= 1u; else phase0 ^= 1u;
@@ -638,14 +628,14 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
             unsigned *plo = pbox + pbuf * NBOX_WORDS;
             if (cnt < FIX_SAFE_COUNT && (unsigned)qx <= NB - 2 && (unsigned)qy <= NB - 2 &&
                 (unsigned)qz <= NBZ - 2) {
-              const int q0 = (qx * NB + qy) * NBZ + qz;
+              const int q0 = qx * NPS + qy * NBZ + qz;
               const float S = pow2f(paint_shift(cnt));
 #pragma unroll
               for (int n = 0; n < 8; ++n) {
                 const float w =
                     __fmul_rn(__fmul_rn(conn_x(n) ? bx.k1 : bx.k0, conn_y(n) ? by.k1 : by.k0),
                               conn_z(n) ? bz.k1 : bz.k0);
-                const int q = q0 + conn_x(n) * NB * NBZ + conn_y(n) * NBZ + conn_z(n);
+                const int q = q0 + conn_x(n) * NPS + conn_y(n) * NBZ + conn_z(n);
                 atomicAdd(plo + q, __float2uint_rn(w * S));
               }
             } else {
@@ -663,60 +653,79 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
             }
           }
         }
-        if (counts) {
-          const uint32_t r = count_and_rank_home(counts, k, key, valid);
-          if (valid) rank[p] = r;
-        }
+        if (counts) count_home(counts, k, key, valid);
        }
       }
     }
     __syncthreads();  // buffer `buf` is free for the prefetch two tiles ahead
     if (PAINT && cur.beg != cur.end) {
-      // flush the paint box: fixed point -> float in place, then one TMA
-      // reduce-add into the mesh (16-byte atomics where the box wraps)
+      // flush the paint box, each warp its x-planes (w and w + 8): fixed
+      // point -> float in place, one TMA reduce-add per plane into the mesh
+      // (16-byte atomics where the box wraps), then the warp zeroes its
+      // planes of the other box for the next tile (once its previous
+      // reduce has read them).  No CTA barrier: the next tile's barrier
+      // orders the zeroing before its atomics.
+      const int lane = tid & 31, warp = tid >> 5;
       const unsigned cnt = cur.end - cur.beg;
-      unsigned *plo = pbox + pbuf * NBOX_WORDS;
-      float *pf = reinterpret_cast<float *>(plo);
+      float *pf = reinterpret_cast<float *>(pbox + pbuf * NBOX_WORDS);
       const float inv = pow2f(-paint_shift(cnt));
-      for (int q = tid; q < NBOX; q += TILE_THREADS) pf[q] = (float)plo[q] * inv;
       const bool ptma = use_ptma && nbox_interior(cur.ox, cur.oy, cur.oz, nx, ny, nz);
-      if (ptma) fence_async_shared();
-      if (use_ptma && tid == 0) bulk_wait_read();  // the other box's reduce has read it
-      __syncthreads();
-      if (ptma) {
-        if (tid == 0) {
-          tma_reduce_add_3d(&pmap, cur.oz - 4, cur.oy - 1, cur.ox - 1, pf);
-          bulk_commit();
-        }
-      } else if (pvec) {
-        for (int q = tid; q < NB * NB * (NBZ / 4); q += TILE_THREADS) {
-          const int g = q % (NBZ / 4), r = q / (NBZ / 4), b = r % NB, a = r / NB;
-          const float4 v = *reinterpret_cast<const float4 *>(pf + (a * NB + b) * NBZ + 4 * g);
-          if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f)
-            atomicAdd(reinterpret_cast<float4 *>(
-                          mesh_next + cell_index(wrap_index(cur.ox - 1 + a, nx),
-                                                 wrap_index(cur.oy - 1 + b, ny),
-                                                 wrap_index(cur.oz - 4 + 4 * g, nz), ny, nz)),
-                      v);
-        }
-      } else {
-        for (int q = tid; q < NBOX; q += TILE_THREADS) {
-          const int c = q % NBZ, r = q / NBZ, b = r % NB, a = r / NB;
-          const float v = pf[q];
-          if (v != 0.f)
-            atomicAdd(mesh_next + cell_index(wrap_index(cur.ox - 1 + a, nx),
-                                             wrap_index(cur.oy - 1 + b, ny),
-                                             wrap_index(cur.oz - 4 + c, nz), ny, nz),
-                      v);
+      for (int a = warp; a < NB; a += TILE_THREADS / 32) {
+        uint4 *pl = reinterpret_cast<uint4 *>(pf + a * NPS);
+        for (int q = lane; q < NB * NBZ / 4; q += 32) {
+          const uint4 u = pl[q];
+          reinterpret_cast<float4 *>(pl)[q] =
+              make_float4((float)u.x * inv, (float)u.y * inv, (float)u.z * inv, (float)u.w * inv);
         }
       }
-      zero_words(pbox + (pbuf ^ 1) * NBOX_WORDS, NBOX_WORDS, tid);  // for the next tile
+      if (ptma) fence_async_shared();
+      __syncwarp();
+      if (ptma) {
+        if (lane == 0) {
+          for (int a = warp; a < NB; a += TILE_THREADS / 32)
+            tma_reduce_add_3d(&pmap, cur.oz - 4, cur.oy - 1, cur.ox - 1 + a, pf + a * NPS);
+          bulk_commit();
+        }
+      } else {
+        for (int a = warp; a < NB; a += TILE_THREADS / 32) {
+          for (int q = lane; q < NB * NBZ / 4; q += 32) {
+            const int g = q % (NBZ / 4), b = q / (NBZ / 4);
+            const float *src = pf + a * NPS + b * NBZ + 4 * g;
+            const int64_t row = cell_index(wrap_index(cur.ox - 1 + a, nx),
+                                           wrap_index(cur.oy - 1 + b, ny), 0, ny, nz);
+            if (pvec) {
+              const float4 v = *reinterpret_cast<const float4 *>(src);
+              if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f)
+                atomicAdd(reinterpret_cast<float4 *>(mesh_next + row +
+                                                     wrap_index(cur.oz - 4 + 4 * g, nz)),
+                          v);
+            } else {
+#pragma unroll
+              for (int c = 0; c < 4; ++c)
+                if (src[c] != 0.f)
+                  atomicAdd(mesh_next + row + wrap_index(cur.oz - 4 + 4 * g + c, nz), src[c]);
+            }
+          }
+        }
+      }
+      // the warp's planes of the other box: free once this lane 0's previous
+      // reduce group has read them
+      if (use_ptma && lane == 0) {
+        if (ptma) bulk_wait_read_prior();  // all but the group just committed
+        else bulk_wait_read();             // nothing committed for this tile
+      }
+      __syncwarp();
+      unsigned *other = pbox + (pbuf ^ 1) * NBOX_WORDS;
+      for (int a = warp; a < NB; a += TILE_THREADS / 32) {
+        uint4 *pl = reinterpret_cast<uint4 *>(other + a * NPS);
+        for (int q = lane; q < NB * NBZ / 4; q += 32) pl[q] = make_uint4(0u, 0u, 0u, 0u);
+      }
       pbuf ^= 1;
     }
     cur = nxt;
     buf ^= 1;
   }
-  if (PAINT && use_ptma && tid == 0) bulk_wait_all();  // reductions complete before exit
+  if (PAINT && use_ptma && (tid & 31) == 0) bulk_wait_all();  // reductions done before exit
 }
 
 // Histogram + rank of the current positions (the first sort of a run).
@@ -736,29 +745,53 @@ tile_rank_kernel(const float *__restrict__ pos, int64_t np, int nx, int ny, int 
   }
 }
 
-// Moves particle p to offsets[key] + rank[p] (pos, vel, id).  Each thread
-// carries SCATTER_ILP particles so that their loads are in flight together.
+// Each scatter thread carries SCATTER_ILP particles so that their loads are
+// in flight together.
 constexpr int SCATTER_ILP = 4;
 
+// Warp-aggregated slot claim: lanes whose key equals the first valid lane's
+// (most of a warp, since neighbouring particles share their tile) take
+// consecutive slots from one atomic; the others claim one each.  All 32
+// lanes call it.
+__device__ __forceinline__ uint32_t claim_slot(unsigned *__restrict__ cursor, uint32_t key,
+                                               bool valid) {
+  const int lane = threadIdx.x & 31;
+  const unsigned act = __ballot_sync(0xffffffffu, valid);
+  if (!act) return 0;
+  const uint32_t lead_key = __shfl_sync(0xffffffffu, key, __ffs(act) - 1);
+  const unsigned same = __ballot_sync(0xffffffffu, valid && key == lead_key);
+  const int leader = __ffs(same) - 1;
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(cursor + lead_key, (unsigned)__popc(same));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  uint32_t r = base + __popc(same & ((1u << lane) - 1u));
+  if (valid && key != lead_key) r = atomicAdd(cursor + key, 1u);
+  return r;
+}
+
+// Moves particle p to offsets[key] + its rank in the tile: rank[p] when the
+// ranks were recorded (the first sort), else a slot claimed from `cursor`
+// (the zeroed tile counters) here, so the gather only counts.  The loop is
+// warp-uniform (the slot claim votes across the warp).
 __global__ void __launch_bounds__(256)
 scatter_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
                const unsigned *__restrict__ id, const unsigned *__restrict__ rank, int64_t np,
                int nx, int ny, int nz, const unsigned *__restrict__ offsets,
-               float *__restrict__ pos2, float *__restrict__ vel2, unsigned *__restrict__ id2,
-               unsigned *__restrict__ dest) {
+               unsigned *__restrict__ cursor, float *__restrict__ pos2,
+               float *__restrict__ vel2, unsigned *__restrict__ id2, unsigned *__restrict__ dest) {
   const int64_t span = (int64_t)blockDim.x * SCATTER_ILP;
-  for (int64_t base = blockIdx.x * span + threadIdx.x; base < np; base += gridDim.x * span) {
+  for (int64_t b0 = blockIdx.x * span; b0 < np; b0 += gridDim.x * span) {
     float x[SCATTER_ILP], y[SCATTER_ILP], z[SCATTER_ILP], u[SCATTER_ILP], v[SCATTER_ILP],
         w[SCATTER_ILP];
     unsigned r[SCATTER_ILP], ident[SCATTER_ILP];
 #pragma unroll
     for (int j = 0; j < SCATTER_ILP; ++j) {
-      const int64_t p = base + j * (int64_t)blockDim.x;
+      const int64_t p = b0 + threadIdx.x + j * (int64_t)blockDim.x;
       if (p < np) {
         x[j] = __ldg(pos + 3 * p);
         y[j] = __ldg(pos + 3 * p + 1);
         z[j] = __ldg(pos + 3 * p + 2);
-        r[j] = __ldg(rank + p);
+        if (rank) r[j] = __ldg(rank + p);
         if (vel) {
           u[j] = __ldg(vel + 3 * p);
           v[j] = __ldg(vel + 3 * p + 1);
@@ -769,12 +802,15 @@ scatter_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
     }
 #pragma unroll
     for (int j = 0; j < SCATTER_ILP; ++j) {
-      const int64_t p = base + j * (int64_t)blockDim.x;
-      if (p < np) r[j] += __ldg(offsets + tile_key(x[j], y[j], z[j], nx, ny, nz));
+      const int64_t p = b0 + threadIdx.x + j * (int64_t)blockDim.x;
+      const bool valid = p < np;
+      const uint32_t k = valid ? tile_key(x[j], y[j], z[j], nx, ny, nz) : 0u;
+      if (!rank) r[j] = claim_slot(cursor, k, valid);
+      if (valid) r[j] += __ldg(offsets + k);
     }
 #pragma unroll
     for (int j = 0; j < SCATTER_ILP; ++j) {
-      const int64_t p = base + j * (int64_t)blockDim.x;
+      const int64_t p = b0 + threadIdx.x + j * (int64_t)blockDim.x;
       if (p < np) {
         const int64_t d = r[j];
         pos2[3 * d] = x[j];
@@ -1000,7 +1036,8 @@ int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np
   PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
   if (np > 0) {
     scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
-                                                      sc.offsets, pos2, vel2, id2, nullptr);
+                                                      sc.offsets, nullptr, pos2, vel2, id2,
+                                                      nullptr);
     PMGB_LAUNCHED("scatter_kernel");
   }
   return PMGB_OK;
@@ -1107,7 +1144,7 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float 
     // 3-D map of the density mesh, box 16 x 11 x 11 (the paint box)
     const uint64_t dims[3] = {(uint64_t)nz, (uint64_t)ny, (uint64_t)nx};
     const uint64_t strides[2] = {(uint64_t)nz * 4, (uint64_t)ny * nz * 4};
-    const uint32_t box[3] = {NBZ, NB, NB};
+    const uint32_t box[3] = {NBZ, NB, 1};  // one x-plane of the paint box
     use_ptma = make_tensor_map(&pmap, mesh_next, 3, dims, strides, box) == PMGB_OK ? 1 : 0;
     clear_error();
   }
@@ -1132,9 +1169,12 @@ int tile_scatter(const float *pos, const float *vel, const unsigned *id, int64_t
   const int64_t keys = tile_key_count(nx, ny, nz);
   SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
   PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
+  // the counts become the per-tile slot cursors of the scatter
+  PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
   if (np > 0) {
-    scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
-                                                      sc.offsets, pos2, vel2, id2, dest);
+    scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, nullptr, np, nx, ny, nz,
+                                                      sc.offsets, sc.counts, pos2, vel2, id2,
+                                                      dest);
     PMGB_LAUNCHED("scatter_kernel");
   }
   return PMGB_OK;
