@@ -370,12 +370,12 @@ int pmgb_read3_kick_drift_binned_f32(const float *force3, int64_t comp_stride,
                                      uint32_t *stats, pmgb_stream_t stream);
 
 /* pmgb_read3_kick_drift_binned_f32 that also paints the new positions into
- * mesh_next (overwritten): the density of the next step, from a per-tile
- * box (the tile plus the cell the particles may have moved into) in shared
- * memory added with one TMA reduce per tile, so that the next step needs no
- * separate paint pass.  Same density as pmgb_cic_paint_sorted_f32 of the
- * new positions up to the order of the float sums; stats [0] counts
- * particles that moved beyond the box (painted with global atomics). */
+ * mesh_next (overwritten): the density of the next step.  Particles that
+ * stay in their tile paint into the tile's box in shared memory, added to
+ * the mesh with TMA reduces; those that left it paint with global atomics.
+ * The next step then needs no separate paint pass.  Same density as
+ * pmgb_cic_paint_sorted_f32 of the new positions up to the order of the
+ * float sums.  stats: as pmgb_read3_kick_drift_binned_f32. */
 int pmgb_read3_kick_drift_paint_binned_f32(const float *force3,
                                            int64_t comp_stride, int nx, int ny,
                                            int nz, float *pos, float *vel,

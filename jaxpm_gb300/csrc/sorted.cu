@@ -457,28 +457,16 @@ __device__ __forceinline__ TileInfo tile_info(const unsigned *__restrict__ offse
 constexpr int RKD_ILP = 2;
 
 // Paint box of the fused gather (the next step's density from the new
-// positions, which may leave their tile by about a cell): x and y cover
-// o-1 .. o+9, z covers o-4 .. o+11 so that the TMA box starts on a 16-byte
-// boundary.  Two boxes in turn (the TMA reduce of one drains while the next
-// tile paints the other), one fixed-point word per cell (paint_shift).
-constexpr int NB = TILE + 3;
-constexpr int NBZ = 16;
+// positions): the tile's own 9 x 9 x 12-cell box, so particles that stay in
+// the tile paint into shared memory and the few that left it paint with
+// global atomics.  Two boxes in turn (the TMA reduce of one drains while
+// the next tile paints the other), one fixed-point word per cell
+// (paint_shift), x-planes padded to 128 bytes for the per-plane reduces.
+constexpr int NB = TB;
+constexpr int NBZ = TBZ;
 constexpr int NPS = (NB * NBZ + 31) / 32 * 32;  // x-plane stride (128-byte multiple)
 constexpr int NBOX_WORDS = NB * NPS;
 constexpr int RKDP_SMEM = 2 * NBOX_WORDS * 4;
-
-__device__ __forceinline__ bool nbox_interior(int ox, int oy, int oz, int nx, int ny, int nz) {
-  return ox >= 1 && oy >= 1 && oz >= 4 && ox + NB - 1 <= nx && oy + NB - 1 <= ny &&
-         oz + NBZ - 4 <= nz;
-}
-
-// c - o taken periodically into (-n/2, n/2]
-__device__ __forceinline__ int periodic_offset(int c, int o, int n) {
-  int d = c - o;
-  if (d > n / 2) d -= n;
-  else if (d < -(n / 2)) d += n;
-  return d;
-}
 
 __device__ __forceinline__ void zero_words(unsigned *p, int words, int tid) {
   uint4 *z4 = reinterpret_cast<uint4 *>(p);
@@ -610,25 +598,19 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
           pos_out[3 * (int64_t)p] = xn;
           pos_out[3 * (int64_t)p + 1] = yn;
           pos_out[3 * (int64_t)p + 2] = zn;
-          {  // most particles stay in their tile: reuse its key
-            const int cx = wrap_index((int)floorf(xn), nx) - cur.ox,
-                      cy = wrap_index((int)floorf(yn), ny) - cur.oy,
-                      cz = wrap_index((int)floorf(zn), nz) - cur.oz;
-            k = ((unsigned)cx < (unsigned)TILE && (unsigned)cy < (unsigned)TILE &&
-                 (unsigned)cz < (unsigned)TILE)
-                    ? key
-                    : tile_key(xn, yn, zn, nx, ny, nz);
-          }
+          // the new cell (cic_axis wraps floor(x) as the tile key does)
+          const Axis bx = cic_axis(xn, nx), by = cic_axis(yn, ny), bz = cic_axis(zn, nz);
+          const int cx = bx.i0 - cur.ox, cy = by.i0 - cur.oy, cz = bz.i0 - cur.oz;
+          const bool stays = (unsigned)cx < (unsigned)TILE && (unsigned)cy < (unsigned)TILE &&
+                             (unsigned)cz < (unsigned)TILE;
+          k = stays ? key  // most particles stay
+                    : (spread3((uint32_t)bx.i0 / TILE) << 2) |
+                          (spread3((uint32_t)by.i0 / TILE) << 1) | spread3((uint32_t)bz.i0 / TILE);
           if (PAINT) {  // the next step's density: the new position into the paint box
             const unsigned cnt = cur.end - cur.beg;
-            const Axis bx = cic_axis(xn, nx), by = cic_axis(yn, ny), bz = cic_axis(zn, nz);
-            const int qx = periodic_offset(bx.i0, cur.ox, nx) + 1,
-                      qy = periodic_offset(by.i0, cur.oy, ny) + 1,
-                      qz = periodic_offset(bz.i0, cur.oz, nz) + 4;
             unsigned *plo = pbox + pbuf * NBOX_WORDS;
-            if (cnt < FIX_SAFE_COUNT && (unsigned)qx <= NB - 2 && (unsigned)qy <= NB - 2 &&
-                (unsigned)qz <= NBZ - 2) {
-              const int q0 = qx * NPS + qy * NBZ + qz;
+            if (stays && cnt < FIX_SAFE_COUNT) {
+              const int q0 = cx * NPS + cy * NBZ + cz;
               const float S = pow2f(paint_shift(cnt));
 #pragma unroll
               for (int n = 0; n < 8; ++n) {
@@ -638,8 +620,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
                 const int q = q0 + conn_x(n) * NPS + conn_y(n) * NBZ + conn_z(n);
                 atomicAdd(plo + q, __float2uint_rn(w * S));
               }
-            } else {
-              if (stats && cnt < FIX_SAFE_COUNT) atomicAdd(stats, 1u);
+            } else {  // left the tile (the normal case for ~1 in 10): global atomics
 #pragma unroll
               for (int n = 0; n < 8; ++n) {
                 const float w =
@@ -669,7 +650,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
       const unsigned cnt = cur.end - cur.beg;
       float *pf = reinterpret_cast<float *>(pbox + pbuf * NBOX_WORDS);
       const float inv = pow2f(-paint_shift(cnt));
-      const bool ptma = use_ptma && nbox_interior(cur.ox, cur.oy, cur.oz, nx, ny, nz);
+      const bool ptma = use_ptma && box_interior(cur.ox, cur.oy, cur.oz, nx, ny, nz);
       for (int a = warp; a < NB; a += TILE_THREADS / 32) {
         uint4 *pl = reinterpret_cast<uint4 *>(pf + a * NPS);
         for (int q = lane; q < NB * NBZ / 4; q += 32) {
@@ -683,7 +664,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
       if (ptma) {
         if (lane == 0) {
           for (int a = warp; a < NB; a += TILE_THREADS / 32)
-            tma_reduce_add_3d(&pmap, cur.oz - 4, cur.oy - 1, cur.ox - 1 + a, pf + a * NPS);
+            tma_reduce_add_3d(&pmap, cur.oz, cur.oy, cur.ox + a, pf + a * NPS);
           bulk_commit();
         }
       } else {
@@ -691,19 +672,19 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
           for (int q = lane; q < NB * NBZ / 4; q += 32) {
             const int g = q % (NBZ / 4), b = q / (NBZ / 4);
             const float *src = pf + a * NPS + b * NBZ + 4 * g;
-            const int64_t row = cell_index(wrap_index(cur.ox - 1 + a, nx),
-                                           wrap_index(cur.oy - 1 + b, ny), 0, ny, nz);
+            const int64_t row = cell_index(wrap_index(cur.ox + a, nx),
+                                           wrap_index(cur.oy + b, ny), 0, ny, nz);
             if (pvec) {
               const float4 v = *reinterpret_cast<const float4 *>(src);
               if (v.x != 0.f || v.y != 0.f || v.z != 0.f || v.w != 0.f)
                 atomicAdd(reinterpret_cast<float4 *>(mesh_next + row +
-                                                     wrap_index(cur.oz - 4 + 4 * g, nz)),
+                                                     wrap_index(cur.oz + 4 * g, nz)),
                           v);
             } else {
 #pragma unroll
               for (int c = 0; c < 4; ++c)
                 if (src[c] != 0.f)
-                  atomicAdd(mesh_next + row + wrap_index(cur.oz - 4 + 4 * g + c, nz), src[c]);
+                  atomicAdd(mesh_next + row + wrap_index(cur.oz + 4 * g + c, nz), src[c]);
             }
           }
         }

