@@ -730,31 +730,14 @@ tile_rank_kernel(const float *__restrict__ pos, int64_t np, int nx, int ny, int 
 // in flight together.
 constexpr int SCATTER_ILP = 4;
 
-// Warp-aggregated slot claim: lanes whose key equals the first valid lane's
-// (most of a warp, since neighbouring particles share their tile) take
-// consecutive slots from one atomic; the others claim one each.  All 32
-// lanes call it.
-__device__ __forceinline__ uint32_t claim_slot(unsigned *__restrict__ cursor, uint32_t key,
-                                               bool valid) {
-  const int lane = threadIdx.x & 31;
-  const unsigned act = __ballot_sync(0xffffffffu, valid);
-  if (!act) return 0;
-  const uint32_t lead_key = __shfl_sync(0xffffffffu, key, __ffs(act) - 1);
-  const unsigned same = __ballot_sync(0xffffffffu, valid && key == lead_key);
-  const int leader = __ffs(same) - 1;
-  unsigned base = 0;
-  if (lane == leader) base = atomicAdd(cursor + lead_key, (unsigned)__popc(same));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  uint32_t r = base + __popc(same & ((1u << lane) - 1u));
-  if (valid && key != lead_key) r = atomicAdd(cursor + key, 1u);
-  return r;
-}
-
 // Moves particle p to offsets[key] + its rank in the tile: rank[p] when the
 // ranks were recorded (the first sort), else a slot claimed from `cursor`
-// (the zeroed tile counters) here, so the gather only counts.  The loop is
-// warp-uniform (the slot claim votes across the warp).
-__global__ void __launch_bounds__(256)
+// (the zeroed tile counters) here, so the gather only counts.  A claim is
+// warp-aggregated: lanes whose key equals the first valid lane's (most of a
+// warp, since neighbouring particles share their tile) take consecutive
+// slots from one atomic, the others claim one each.  The loop is
+// warp-uniform (the claims vote across the warp).
+__global__ void __launch_bounds__(256, 3)
 scatter_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
                const unsigned *__restrict__ id, const unsigned *__restrict__ rank, int64_t np,
                int nx, int ny, int nz, const unsigned *__restrict__ offsets,
@@ -781,13 +764,39 @@ scatter_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
         ident[j] = id ? __ldg(id + p) : (unsigned)p;
       }
     }
+    uint32_t k[SCATTER_ILP];
 #pragma unroll
     for (int j = 0; j < SCATTER_ILP; ++j) {
       const int64_t p = b0 + threadIdx.x + j * (int64_t)blockDim.x;
-      const bool valid = p < np;
-      const uint32_t k = valid ? tile_key(x[j], y[j], z[j], nx, ny, nz) : 0u;
-      if (!rank) r[j] = claim_slot(cursor, k, valid);
-      if (valid) r[j] += __ldg(offsets + k);
+      k[j] = p < np ? tile_key(x[j], y[j], z[j], nx, ny, nz) : 0u;
+    }
+    if (!rank) {
+      // slot claims (see claim_slot), all SCATTER_ILP atomics in flight
+      // before any result is used
+      const int lane = threadIdx.x & 31;
+      unsigned same[SCATTER_ILP], base[SCATTER_ILP];
+      uint32_t lead[SCATTER_ILP];
+#pragma unroll
+      for (int j = 0; j < SCATTER_ILP; ++j) {
+        const bool valid = b0 + threadIdx.x + j * (int64_t)blockDim.x < np;
+        const unsigned act = __ballot_sync(0xffffffffu, valid);
+        lead[j] = __shfl_sync(0xffffffffu, k[j], act ? __ffs(act) - 1 : 0);
+        same[j] = __ballot_sync(0xffffffffu, valid && k[j] == lead[j]);
+        base[j] = 0;
+        if (same[j] && lane == __ffs(same[j]) - 1)
+          base[j] = atomicAdd(cursor + lead[j], (unsigned)__popc(same[j]));
+        r[j] = (valid && k[j] != lead[j]) ? atomicAdd(cursor + k[j], 1u) : 0u;
+      }
+#pragma unroll
+      for (int j = 0; j < SCATTER_ILP; ++j) {
+        const unsigned b = __shfl_sync(0xffffffffu, base[j], same[j] ? __ffs(same[j]) - 1 : 0);
+        if ((same[j] >> lane) & 1u) r[j] = b + __popc(same[j] & ((1u << lane) - 1u));
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < SCATTER_ILP; ++j) {
+      const int64_t p = b0 + threadIdx.x + j * (int64_t)blockDim.x;
+      if (p < np) r[j] += __ldg(offsets + k[j]);
     }
 #pragma unroll
     for (int j = 0; j < SCATTER_ILP; ++j) {
