@@ -511,6 +511,71 @@ int pmgb_power_spectrum_f32(const void *spec, int nx, int ny, int nz,
                             double *pcount, double *ksum,
                             pmgb_stream_t stream);
 
+/* ---- batched simulations (jax.vmap over the step: README.md:29,
+ *      tests/test_distributed_pm.py:335-409) ------------------------------ */
+
+/* One simulation of a batch: its mesh and its particle count.  The batch's
+ * particle arrays are the concatenation, in table order, of every
+ * simulation's [np][3] array (positions in that simulation's cell units). */
+typedef struct pmgb_sim {
+  int32_t nx, ny, nz;
+  int32_t reserved; /* 0 */
+  int64_t np;
+} pmgb_sim;
+
+/* Workspace bytes of the batched calls for this table (0 if the table is
+ * invalid).  Simulations of equal mesh shape share batched FFT plans. */
+size_t pmgb_batch_workspace_size(const pmgb_sim *sims, int n_sims);
+
+/* Prepares a 256-byte aligned workspace for this table: uploads the device
+ * descriptor table (stream ordered) and creates the FFT plans and k-space
+ * tables of every mesh shape, so that the batched steps below only launch
+ * work (and can be captured in a CUDA graph).  Every batched call checks
+ * that its workspace was prepared for the same table. */
+int pmgb_batch_init(const pmgb_sim *sims, int n_sims, void *workspace,
+                    size_t workspace_bytes, pmgb_stream_t stream);
+
+/* Forgets the preparation of a workspace (before freeing it). */
+int pmgb_batch_release(const void *workspace);
+
+/* Totals of a table: particles and mesh cells. */
+int pmgb_batch_counts(const pmgb_sim *sims, int n_sims, int64_t *np_total,
+                      int64_t *cells_total);
+
+/* Unit-mass CIC paint of every simulation (painting.py:15-45): `meshes` is
+ * the table-ordered concatenation of every simulation's [nx][ny][nz] mesh
+ * (cleared here). */
+int pmgb_cic_paint_batched_f32(const pmgb_sim *sims, int n_sims, float *meshes,
+                               const float *pos, void *workspace,
+                               size_t workspace_bytes, pmgb_stream_t stream);
+
+/* pm_forces (pm.py:12-58, r_split as there) of every simulation at its
+ * particles: pos, forces [sum np][3]. */
+int pmgb_pm_forces_batched_f32(const pmgb_sim *sims, int n_sims,
+                               const float *pos, float *forces, float r_split,
+                               void *workspace, size_t workspace_bytes,
+                               pmgb_stream_t stream);
+
+/* One FastPM step of every simulation (as pmgb_fpm_step_f32, ode.py:13-82):
+ * vel += kick[s] F(pos); pos += drift[s] vel, with kick and drift DEVICE
+ * arrays of n_sims coefficients (one cosmology per simulation).  pos_before
+ * (optional, [sum np][3]) receives the positions before the step, the
+ * record the reverse sweep needs. */
+int pmgb_fpm_step_batched_f32(const pmgb_sim *sims, int n_sims, float *pos,
+                              float *vel, const float *kick, const float *drift,
+                              float r_split, float *pos_before, void *workspace,
+                              size_t workspace_bytes, pmgb_stream_t stream);
+
+/* Adjoint of pmgb_fpm_step_batched_f32 from the step's starting positions
+ * `pos`: (g_pos, g_vel) hold the cotangents of the step's outputs and are
+ * overwritten with those of its inputs:
+ * u = g_vel + drift g_pos; g_pos += (dF/dx)^T (kick u); g_vel = u. */
+int pmgb_fpm_step_batched_vjp_f32(const pmgb_sim *sims, int n_sims,
+                                  const float *pos, float *g_pos, float *g_vel,
+                                  const float *kick, const float *drift,
+                                  float r_split, void *workspace,
+                                  size_t workspace_bytes, pmgb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

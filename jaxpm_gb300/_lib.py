@@ -106,7 +106,32 @@ SIGNATURES = {
                                              c_float, c_float, c_float, P, c_size_t, P, P]),
     "pmgb_power_spectrum_f32": (c_int, [P, c_int, c_int, c_int, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, P, c_int, P, P, P, P]),
+    "pmgb_batch_workspace_size": (c_size_t, [P, c_int]),
+    "pmgb_batch_init": (c_int, [P, c_int, P, c_size_t, P]),
+    "pmgb_batch_release": (c_int, [P]),
+    "pmgb_batch_counts": (c_int, [P, c_int, P, P]),
+    "pmgb_cic_paint_batched_f32": (c_int, [P, c_int, P, P, P, c_size_t, P]),
+    "pmgb_pm_forces_batched_f32": (c_int, [P, c_int, P, P, c_float, P, c_size_t, P]),
+    "pmgb_fpm_step_batched_f32": (c_int, [P, c_int, P, P, P, P, c_float, P, P, c_size_t, P]),
+    "pmgb_fpm_step_batched_vjp_f32": (c_int, [P, c_int, P, P, P, P, P, c_float, P, c_size_t,
+                                              P]),
 }
+
+
+class Sim(ctypes.Structure):
+    """``pmgb_sim``: one simulation of a batch (mesh shape, particle count)."""
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("np", ctypes.c_int64)]
+
+
+def sim_table(shapes, counts):
+    """A ctypes ``pmgb_sim`` array for mesh ``shapes`` and particle ``counts``."""
+    arr = (Sim * len(shapes))()
+    for i, (sh, n) in enumerate(zip(shapes, counts)):
+        arr[i].nx, arr[i].ny, arr[i].nz = (int(v) for v in sh)
+        arr[i].reserved = 0
+        arr[i].np = int(n)
+    return arr
 
 
 class PmgbError(RuntimeError):

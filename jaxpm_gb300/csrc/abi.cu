@@ -680,4 +680,73 @@ int pmgb_power_spectrum_f32(const void *spec, int nx, int ny, int nz, double box
                         ksum, stream);
 }
 
+size_t pmgb_batch_workspace_size(const pmgb_sim *sims, int n_sims) {
+  BEGIN();
+  return batch_workspace_size(sims, n_sims);
+}
+
+int pmgb_batch_init(const pmgb_sim *sims, int n_sims, void *workspace, size_t workspace_bytes,
+                    pmgb_stream_t stream) {
+  BEGIN();
+  return batch_init(sims, n_sims, workspace, workspace_bytes, stream);
+}
+
+int pmgb_batch_release(const void *workspace) {
+  BEGIN();
+  return batch_release(workspace);
+}
+
+int pmgb_batch_counts(const pmgb_sim *sims, int n_sims, int64_t *np_total, int64_t *cells_total) {
+  BEGIN();
+  return batch_counts(sims, n_sims, np_total, cells_total);
+}
+
+int pmgb_cic_paint_batched_f32(const pmgb_sim *sims, int n_sims, float *meshes, const float *pos,
+                               void *workspace, size_t workspace_bytes, pmgb_stream_t stream) {
+  BEGIN();
+  NEED(meshes);
+  NEED(pos);
+  return cic_paint_batched(sims, n_sims, meshes, pos, workspace, workspace_bytes, stream);
+}
+
+int pmgb_pm_forces_batched_f32(const pmgb_sim *sims, int n_sims, const float *pos, float *forces,
+                               float r_split, void *workspace, size_t workspace_bytes,
+                               pmgb_stream_t stream) {
+  BEGIN();
+  NEED(pos);
+  NEED(forces);
+  PMGB_REQUIRE(r_split >= 0.0f, "r_split must be non-negative");
+  return pm_forces_batched(sims, n_sims, pos, forces, r_split, workspace, workspace_bytes,
+                           stream);
+}
+
+int pmgb_fpm_step_batched_f32(const pmgb_sim *sims, int n_sims, float *pos, float *vel,
+                              const float *kick, const float *drift, float r_split,
+                              float *pos_before, void *workspace, size_t workspace_bytes,
+                              pmgb_stream_t stream) {
+  BEGIN();
+  NEED(pos);
+  NEED(vel);
+  NEED(kick);
+  NEED(drift);
+  PMGB_REQUIRE(r_split >= 0.0f, "r_split must be non-negative");
+  return fpm_step_batched(sims, n_sims, pos, vel, kick, drift, r_split, pos_before, workspace,
+                          workspace_bytes, stream);
+}
+
+int pmgb_fpm_step_batched_vjp_f32(const pmgb_sim *sims, int n_sims, const float *pos,
+                                  float *g_pos, float *g_vel, const float *kick,
+                                  const float *drift, float r_split, void *workspace,
+                                  size_t workspace_bytes, pmgb_stream_t stream) {
+  BEGIN();
+  NEED(pos);
+  NEED(g_pos);
+  NEED(g_vel);
+  NEED(kick);
+  NEED(drift);
+  PMGB_REQUIRE(r_split >= 0.0f, "r_split must be non-negative");
+  return fpm_step_batched_vjp(sims, n_sims, pos, g_pos, g_vel, kick, drift, r_split, workspace,
+                              workspace_bytes, stream);
+}
+
 }  // extern "C"

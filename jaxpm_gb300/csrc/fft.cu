@@ -114,6 +114,12 @@ int fft_r2c(const float *in, void *out, int nx, int ny, int nz, int batch, cudaS
   return PMGB_OK;
 }
 
+int fft_prepare(int nx, int ny, int nz, int batch, int r2c) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  cufftHandle h;
+  return plan_for(nx, ny, nz, batch, r2c ? CUFFT_R2C : CUFFT_C2R, &h);
+}
+
 int fft_c2r(void *in, float *out, int nx, int ny, int nz, int batch, cudaStream_t s) {
   std::lock_guard<std::mutex> lk(g_mu);
   cufftHandle h;

@@ -42,6 +42,8 @@ int fft_r2c(const float *in, void *out, int nx, int ny, int nz, int batch,
 int fft_c2r(void *in, float *out, int nx, int ny, int nz, int batch,
             cudaStream_t s);
 int scale_inplace(float *x, int64_t n, float scale, cudaStream_t s);
+// Creates (if needed) the cached 3-D plan of fft_r2c (r2c=1) or fft_c2r.
+int fft_prepare(int nx, int ny, int nz, int batch, int r2c);
 // batched 2-D (y, z) transforms of x-planes, spectra [plane][ny][pitch]
 int fft_planes_r2c(const float *in, void *out, int nplanes, int ny, int nz,
                    int pitch, cudaStream_t s);
@@ -197,5 +199,21 @@ int spectral_forces_vjp(const float *g3, void *spec3, void *dspec, float *rbar,
 int power_spectrum(const void *spec, int nx, int ny, int nz, double bx,
                    double by, double bz, const double *edges, int n_edges,
                    double *psum, double *pcount, double *ksum, cudaStream_t s);
+
+// batched.cu
+size_t batch_workspace_size(const pmgb_sim *t, int n);
+int batch_init(const pmgb_sim *t, int n, void *ws, size_t bytes, cudaStream_t s);
+int batch_release(const void *ws);
+int batch_counts(const pmgb_sim *t, int n, int64_t *np_total, int64_t *cells_total);
+int cic_paint_batched(const pmgb_sim *t, int n, float *meshes, const float *pos, void *ws,
+                      size_t bytes, cudaStream_t s);
+int pm_forces_batched(const pmgb_sim *t, int n, const float *pos, float *forces, float r_split,
+                      void *ws, size_t bytes, cudaStream_t s);
+int fpm_step_batched(const pmgb_sim *t, int n, float *pos, float *vel, const float *kick,
+                     const float *drift, float r_split, float *pos_before, void *ws,
+                     size_t bytes, cudaStream_t s);
+int fpm_step_batched_vjp(const pmgb_sim *t, int n, const float *pos, float *gpos, float *gvel,
+                         const float *kick, const float *drift, float r_split, void *ws,
+                         size_t bytes, cudaStream_t s);
 
 }  // namespace pmgb

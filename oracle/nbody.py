@@ -115,6 +115,30 @@ def fpm_step(pos, vel, mesh_shape, kick_c, drift_c, dtype=np.float32):
     return pos, vel
 
 
+def fpm_run_vjp(pos, vel, mesh_shape, kicks, drifts, g_pos, g_vel, r_split=0.0):
+    """Float64 forward run of FastPM steps (``fpm_step`` with the given
+    per-step coefficients) and its reverse sweep, the transpose that
+    ``jax.grad`` takes through ``jaxpm/ode.py:13-82``: per step, from the
+    output cotangents, ``u = g_vel + drift g_pos``,
+    ``g_pos += (dF/dx)^T (kick u)`` at the step's starting positions,
+    ``g_vel = u``.  Returns ``((pos, vel), (g_pos0, g_vel0))``."""
+    x = np.asarray(pos, dtype=np.float64)
+    v = np.asarray(vel, dtype=np.float64)
+    starts = []
+    for k, d in zip(kicks, drifts):
+        starts.append(x)
+        F = fo.pm_forces(x, mesh_shape=mesh_shape, r_split=r_split, dtype=np.float64)
+        v = v + k * F
+        x = x + d * v
+    gx = np.asarray(g_pos, dtype=np.float64)
+    gv = np.asarray(g_vel, dtype=np.float64)
+    for i in reversed(range(len(starts))):
+        u = gv + drifts[i] * gx
+        gx = gx + fo.pm_forces_vjp(starts[i], mesh_shape, kicks[i] * u, r_split=r_split)
+        gv = u
+    return (x, v), (gx, gv)
+
+
 def nbody_ode(cosmo, mesh_shape, state, a, dtype=np.float32):
     """``make_ode_fn(...)(state, a, cosmo)`` (``jaxpm/ode.py:122-147``)."""
     pos, vel = state

@@ -4,6 +4,8 @@ import ctypes
 import os
 import re
 
+import numpy as np
+
 import pytest
 
 from conftest import ROOT
@@ -72,3 +74,33 @@ def test_workspace_queries(lib):
     assert lib.pmgb_cic_paint_workspace_size(8, 8, 8, 10, 2) == 8 * 512
     assert lib.pmgb_cic_paint_workspace_size(8, 8, 8, 10, 0) == 0
     assert lib.pmgb_pm_workspace_size(0, 8, 8, 1, 0) == 0
+
+
+def test_batched_table_queries(lib):
+    """The batched calls' host side: struct layout, workspace sizing (shape
+    groups share pools) and table validation, without a GPU."""
+    from jaxpm_gb300 import _lib
+    assert ctypes.sizeof(_lib.Sim) == 24
+    shapes = [(64,) * 3, (96,) * 3, (64,) * 3, (128,) * 3]
+    t = _lib.sim_table(shapes, [int(np.prod(s)) for s in shapes])
+    nbytes = lib.pmgb_batch_workspace_size(t, len(shapes))
+    cells = sum(int(np.prod(s)) for s in shapes)
+    # density + 3 force meshes + 3 cotangent meshes (f32) and 1 + 3 half spectra (c64)
+    assert nbytes >= cells * 4 * 7 + cells * 8 * 4 // 2
+    assert nbytes < cells * 4 * 7 + cells * 8 * 4 * 2
+    np_total, cells_total = ctypes.c_int64(), ctypes.c_int64()
+    _lib.call("pmgb_batch_counts", t, len(shapes), ctypes.byref(np_total),
+              ctypes.byref(cells_total))
+    assert np_total.value == cells and cells_total.value == cells
+    assert lib.pmgb_batch_workspace_size(t, 0) == 0
+    bad = _lib.sim_table([(16, 16, 16)], [-1])
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_batch_counts", bad, 1, None, None)
+    assert "np is negative" in str(e.value)
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_batch_init", t, len(shapes), None, 0, None)
+    assert "NULL" in str(e.value)
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_fpm_step_batched_f32", t, len(shapes), None, None, None, None, 0.0,
+                  None, None, 0, None)
+    assert "pos is NULL" in str(e.value)
