@@ -38,7 +38,11 @@ BOX_PER_CELL = 1.0  # box 512 Mpc/h on 512^3
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--workload", default="step", choices=["step", "batched", "paint"],
+                    help="step: the 512^3 FastPM step (headline); batched: 64 simulations "
+                         "of 64^3-128^3; paint: cic_paint/cic_read microbenchmarks")
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default 40; 20 for the batched workload)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mesh", type=int, default=N_DEFAULT)
@@ -470,6 +474,315 @@ def run_gb300(args):
 
 
 # ---------------------------------------------------------------------------
+# batched workload: 64 independent simulations of 64^3, 96^3 or 128^3
+# ---------------------------------------------------------------------------
+BATCH_SIMS = 64
+BATCH_MESHES = (64, 96, 128)
+
+
+def batched_table(seed):
+    """Mesh sizes, Omega_c ~ U[0.2, 0.35] and sigma8 ~ U[0.6, 1.0] of the
+    64 simulations (NumPy PCG64 with `seed`); box 2N Mpc/h."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ns = [int(n) for n in rng.choice(BATCH_MESHES, size=BATCH_SIMS)]
+    return ns, rng.uniform(0.2, 0.35, BATCH_SIMS), rng.uniform(0.6, 1.0, BATCH_SIMS)
+
+
+def run_batched(args):
+    import torch
+    from jaxpm_gb300 import batched, cosmology
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    skip = set(filter(None, args.skip.split(",")))
+    K, W = args.steps, args.warmup
+    # replicas: every rank runs its own 64 simulations (seeds offset by rank)
+    ns, ocs, s8s = batched_table(seed=rank)
+    shapes = [(n,) * 3 for n in ns]
+    cosmos = [cosmology.Planck15(Omega_c=float(a), sigma8=float(b)) for a, b in zip(ocs, s8s)]
+    x0, v0 = batched.initial_conditions(shapes, [[2.0 * n] * 3 for n in ns], cosmos,
+                                        [BATCH_SIMS * rank + i for i in range(BATCH_SIMS)],
+                                        device=dev)
+    eng = batched.BatchedFastPM(shapes, cosmos, 0.1, 1.0, K, device=dev)
+    Np = eng.n
+    stream = torch.cuda.current_stream(dev)
+    x, v = x0.clone(), v0.clone()
+    for i in range(W):
+        eng.step(x, v, i % K)
+    graph = eng.capture(x, v)  # the K steps as one CUDA graph
+    x.copy_(x0)
+    v.copy_(v0)
+    graph.replay()  # warm-up of the graph itself
+    x.copy_(x0)
+    v.copy_(v0)
+    torch.cuda.synchronize(dev)
+    clocks = ClockSampler(local) if "clocks" not in skip else None
+    if clocks:
+        clocks.start()
+        time.sleep(0.3)
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    graph.replay()
+    t1.record(stream)
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    clk = clocks.stop() if clocks else None
+    ms = max_over_ranks(t0.elapsed_time(t1), world)
+    value = world * Np * K / (ms / 1e3)
+    masses = [float(m.double().sum()) for m in eng.paint(x)]
+    mass_err = max(abs(m - c) / c for m, c in zip(masses, eng.counts))
+    peak, peak_kind = peaks()
+    achieved = 124.0 * Np / (ms / K / 1e3) / 1e9
+    counts = {n: ns.count(n) for n in BATCH_MESHES}
+    result = {"metric": "particle-steps/s (batched FastPM: 64 simulations of 64^3-128^3)",
+              "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": K,
+              "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+              "vs_baseline": None, "dtype": "f32", "impl": "gb300",
+              "data": "synthetic: per simulation a seeded Gaussian random field (NumPy PCG64 "
+                      "noise, Eisenstein-Hu P(k)), 2LPT to a=0.1",
+              "config": {"workload": f"64 independent FastPM simulations, N in {{64, 96, 128}} "
+                                     f"({counts[64]} x 64^3, {counts[96]} x 96^3, "
+                                     f"{counts[128]} x 128^3), particles = cells, box 2N Mpc/h, "
+                                     f"Omega_c ~ U[0.2,0.35], sigma8 ~ U[0.6,1.0], own seeds, "
+                                     f"{K} steps a=0.1 -> 1, the run captured as one CUDA graph",
+                         "particles": Np, "parallelism": "replicas" if world > 1 else "single",
+                         "l2": f"inputs larger than L2 (positions+velocities "
+                               f"{Np * 24 / 1e9:.1f} GB)"},
+              "mass_rel_err": mass_err,
+              # per step: paint, k-space and gather launches (the FFTs are cuFFT)
+              "gpu_launches": K * 3,
+              "roofline": {"kernel": "whole step", "bound": "hbm", "achieved": achieved,
+                           "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                           "peak_kind": peak_kind, "algorithmic_bytes_per_particle": 124.0,
+                           "traffic": None}}
+    if "adjoint" not in skip:
+        store = eng.alloc_store()
+        gx = torch.ones_like(x0) * 1e-3
+        gv = torch.zeros_like(v0)
+        eng.vjp(x0, v0, gx, gv, store=store)
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        eng.vjp(x0, v0, gx, gv, store=store)
+        a1.record(stream)
+        torch.cuda.synchronize(dev)
+        ams = max_over_ranks(a0.elapsed_time(a1), world)
+        result["fwd_adjoint"] = {"value": world * Np * K / (ams / 1e3),
+                                 "unit": "particle-steps/s", "ms_per_step": ams / K,
+                                 "cost_vs_forward": ams / ms}
+        del store
+    if "e2e" not in skip:
+        hx, hv = x0.cpu().pin_memory(), v0.cpu().pin_memory()
+        dx_, dv_ = torch.empty_like(x0), torch.empty_like(v0)
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(K):
+            dx_.copy_(hx, non_blocking=True)
+            dv_.copy_(hv, non_blocking=True)
+            eng.step(dx_, dv_, i)
+            hx.copy_(dx_, non_blocking=True)
+            hv.copy_(dv_, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ems = max_over_ranks(e0.elapsed_time(e1), world)
+        result["e2e"] = {"value": world * Np * K / (ems / 1e3), "unit": "particle-steps/s",
+                         "h2d_bytes_per_step": 2 * Np * 12, "d2h_bytes_per_step": 2 * Np * 12,
+                         "ms_per_step": ems / K,
+                         "api": "pmgb_fpm_step_batched_f32 (C ABI), pinned host buffers"}
+    if clk is not None:
+        result["clocks"] = clk
+    if rank == 0 and "cpu" not in skip:
+        result["cpu_baseline"] = cpu_batched_sample(ns, ocs, s8s, K)
+    if rank == 0:
+        print(json.dumps(result))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def cpu_batched_sample(ns, ocs, s8s, K):
+    """One oracle FastPM step of the table's first 64^3 simulation."""
+    from oracle import cic, cosmology as oc, nbody as onb
+    i = ns.index(64) if 64 in ns else 0
+    n = ns[i]
+    c = oc.Cosmology(Omega_c=float(ocs[i]), sigma8=float(s8s[i]))
+    k = np.logspace(-4, 1, 128)
+    noise = np.random.Generator(np.random.PCG64(i)).standard_normal((n,) * 3, dtype=np.float32)
+    ic = onb.linear_field(noise, [2.0 * n] * 3, k, oc.linear_matter_power(c, k))
+    lat = cic.lattice((n,) * 3).reshape(-1, 3).astype(np.float32)
+    dx, p, _ = onb.lpt(c, ic, lat, a=0.1, order=2)
+    kc, dc = onb.fpm_coefficients(c, 0.1, 1.0, K)
+    t = time.perf_counter()
+    onb.fpm_step(lat + dx, p, (n,) * 3, kc[0], dc[0])
+    dt = time.perf_counter() - t
+    return {"value": n**3 / dt, "unit": "particle-steps/s", "cores": host_threads(),
+            "kind": "port",
+            "sample": f"one FastPM step of the NumPy oracle on one {n}^3 simulation of the table "
+                      f"({dt:.2f} s)"}
+
+
+# ---------------------------------------------------------------------------
+# paint / read microbenchmarks
+# ---------------------------------------------------------------------------
+def run_paint(args):
+    import torch
+    from jaxpm_gb300 import _lib, painting, simulate, cosmology
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    skip = set(filter(None, args.skip.split(",")))
+    K, W = max(args.steps, 5), max(args.warmup, 3)
+    lib = _lib.load()
+    stream = torch.cuda.current_stream(dev)
+    s = _lib.stream(dev)
+    peak, peak_kind = peaks()
+    n = 256
+    Np = n**3
+    cosmo = cosmology.Planck15()
+
+    # (i) uniform U[0,256)^3, PCG64 seed 1; (ii) the a=1 positions of the
+    # 256^3 run (2LPT to a=0.1, 20 steps), in the caller's (lattice) order
+    uni = torch.from_numpy(np.random.Generator(np.random.PCG64(1)).uniform(
+        0.0, n, (Np, 3)).astype(np.float32)).to(dev)
+    x0, v0 = initial_state(n, cosmo, dev)
+    sim = simulate.SortedFastPM((n,) * 3, cosmo, 0.1, 1.0, 20, device=dev)
+    sim.load(x0, v0)
+    sim.run()
+    clustered = sim.state()[0].contiguous()
+    del sim, x0, v0
+
+    def timed(fn):
+        for _ in range(W):
+            fn()
+        ts = []
+        for _ in range(K):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            ts.append(a.elapsed_time(b))
+        return float(np.median(ts))
+
+    def paint_ops(pos, shape):
+        nx, ny, nz = shape
+        npart = pos.shape[0]
+        mesh = torch.empty(shape, dtype=torch.float32, device=dev)
+        ops = {}
+        for name, mode in [("atomic", _lib.PAINT_ATOMIC), ("binned", _lib.PAINT_BINNED)]:
+            wsb = lib.pmgb_cic_paint_workspace_size(nx, ny, nz, npart, mode)
+            ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=dev)
+            ops[name] = (lambda m=mode, w=ws, b=wsb: _lib.call(
+                "pmgb_cic_paint_f32", _lib.ptr(mesh), nx, ny, nz, _lib.ptr(pos), npart, None,
+                1.0, m, 0, _lib.ptr(w), b, s))
+        # sort by tile, then the shared-memory box paint
+        sb = lib.pmgb_tile_sort_workspace_size(nx, ny, nz, npart)
+        sws = torch.empty(sb, dtype=torch.uint8, device=dev)
+        spos = torch.empty_like(pos)
+        sid = torch.empty(npart, dtype=torch.int32, device=dev)
+
+        def sorted_paint():
+            _lib.call("pmgb_tile_sort_f32", _lib.ptr(pos), None, None, npart, nx, ny, nz,
+                      _lib.ptr(spos), None, _lib.ptr(sid), _lib.ptr(sws), sb, s)
+            _lib.call("pmgb_cic_paint_sorted_f32", _lib.ptr(mesh), nx, ny, nz, _lib.ptr(spos),
+                      npart, _lib.ptr(sws), sb, None, s)
+        ops["sort+box"] = sorted_paint
+        alg = 12.0 * npart + 4.0 * nx * ny * nz
+        out = {}
+        for name, fn in ops.items():
+            ms = timed(fn)
+            total = float(mesh.double().sum())
+            out[name] = {"ms": ms, "particles_per_s": npart / (ms / 1e3),
+                         "achieved_gbs": alg / (ms / 1e3) / 1e9,
+                         "frac": alg / (ms / 1e3) / 1e9 / peak,
+                         "mass_rel_err": abs(total - npart) / npart}
+        del mesh, sws, spos, sid
+        return out
+
+    def read_ops(pos, shape):
+        nx, ny, nz = shape
+        npart = pos.shape[0]
+        g = torch.Generator(device=dev).manual_seed(3)
+        mesh3 = torch.rand((3,) + tuple(shape), generator=g, device=dev)
+        out1 = torch.empty(npart, dtype=torch.float32, device=dev)
+        out3 = torch.empty((npart, 3), dtype=torch.float32, device=dev)
+        ncell = nx * ny * nz
+        res = {}
+        ms = timed(lambda: _lib.call("pmgb_cic_read_f32", _lib.ptr(mesh3), nx, ny, nz,
+                                     _lib.ptr(pos), npart, _lib.ptr(out1), s))
+        alg = 20.0 * npart
+        res["read"] = {"ms": ms, "particles_per_s": npart / (ms / 1e3),
+                       "achieved_gbs": alg / (ms / 1e3) / 1e9,
+                       "frac": alg / (ms / 1e3) / 1e9 / peak}
+        ms = timed(lambda: _lib.call("pmgb_cic_read3_f32", _lib.ptr(mesh3), ncell, nx, ny, nz,
+                                     _lib.ptr(pos), npart, _lib.ptr(out3), s))
+        alg = 36.0 * npart
+        res["read3"] = {"ms": ms, "particles_per_s": npart / (ms / 1e3),
+                        "achieved_gbs": alg / (ms / 1e3) / 1e9,
+                        "frac": alg / (ms / 1e3) / 1e9 / peak}
+        del mesh3, out1, out3
+        return res
+
+    results = {}
+    for dname, pos in [("uniform", uni), ("clustered_a1", clustered)]:
+        results[dname] = {"paint": paint_ops(pos, (n,) * 3), "read": read_ops(pos, (n,) * 3)}
+    del uni
+
+    # paint-only: the 512^3 run's a=1 particles on a 1024^3 mesh
+    if "1024" not in skip:
+        x5, v5 = initial_state(512, cosmo, dev)
+        sim = simulate.SortedFastPM((512,) * 3, cosmo, 0.1, 1.0, 40, device=dev)
+        sim.load(x5, v5)
+        del x5, v5
+        sim.run()
+        big = (sim.state()[0] * 2.0).contiguous()  # cell units of the 1024^3 mesh
+        del sim
+        torch.cuda.empty_cache()
+        results["paint_only_1024"] = paint_ops(big, (1024,) * 3)
+        del big
+        torch.cuda.empty_cache()
+
+    head = results["clustered_a1"]["paint"]
+    best = max(head, key=lambda k: head[k]["particles_per_s"])
+    result = {"metric": "particles/s (cic_paint, 16.7M clustered a=1 particles on 256^3 mesh)",
+              "value": head[best]["particles_per_s"], "unit": "particles/s", "n_gpus": 1,
+              "steps": K, "warmup": W, "ms_per_step": head[best]["ms"],
+              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+              "impl": "gb300",
+              "data": "synthetic: (i) uniform U[0,256)^3 positions, NumPy PCG64 seed 1; (ii) "
+                      "a=1 positions of the 256^3 run (2LPT a=0.1 + 20 FastPM steps) in "
+                      "lattice order",
+              "config": {"workload": "cic_paint / cic_read microbenchmarks: 16,777,216 "
+                                     "particles on a 256^3 mesh, uniform and clustered; "
+                                     "paint-only of the 512^3 run's a=1 particles on 1024^3",
+                         "paint_path": best,
+                         "l2": "positions (201 MB) larger than L2; median of K launches"},
+              "results": results,
+              "roofline": {"kernel": f"paint ({best})", "bound": "hbm",
+                           "achieved": head[best]["achieved_gbs"], "peak": peak, "unit": "GB/s",
+                           "frac": head[best]["frac"], "peak_kind": peak_kind,
+                           "algorithmic_bytes_per_particle": 16.0, "traffic": None},
+              "gpu_launches": K}
+    print(json.dumps(result))
+
+
+# ---------------------------------------------------------------------------
 # CPU: the oracle (NumPy restatement of the reference's algorithm)
 # ---------------------------------------------------------------------------
 def host_threads():
@@ -512,6 +825,10 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
+    if args.workload == "batched":
+        return run_reference_batched(args)
+    if args.workload == "paint":
+        return run_reference_paint(args)
     n_sample = 128
     K, W = args.steps, args.warmup
     from oracle import nbody as onb
@@ -544,10 +861,85 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def run_reference_batched(args):
+    """The oracle on the host cores: each timed step is one FastPM step of
+    one 64^3 simulation of the batch table (a bounded sample of the 64)."""
+    from oracle import cic, cosmology as oc, nbody as onb
+    K, W = args.steps, args.warmup
+    ns, ocs, s8s = batched_table(seed=0)
+    i = ns.index(64) if 64 in ns else 0
+    n = ns[i]
+    c = oc.Cosmology(Omega_c=float(ocs[i]), sigma8=float(s8s[i]))
+    k = np.logspace(-4, 1, 128)
+    noise = np.random.Generator(np.random.PCG64(i)).standard_normal((n,) * 3, dtype=np.float32)
+    ic = onb.linear_field(noise, [2.0 * n] * 3, k, oc.linear_matter_power(c, k))
+    lat = cic.lattice((n,) * 3).reshape(-1, 3).astype(np.float32)
+    dx, p, _ = onb.lpt(c, ic, lat, a=0.1, order=2)
+    kc, dc = onb.fpm_coefficients(c, 0.1, 1.0, K)
+    x, v = lat + dx, p
+    for j in range(W):
+        onb.fpm_step(x, v, (n,) * 3, kc[j % K], dc[j % K])
+    t = time.perf_counter()
+    for j in range(K):
+        x, v = onb.fpm_step(x, v, (n,) * 3, kc[j], dc[j])
+    dt = time.perf_counter() - t
+    value = n**3 * K / dt
+    out = {"metric": "particle-steps/s (batched FastPM: 64 simulations of 64^3-128^3)",
+           "value": value, "unit": "particle-steps/s", "n_gpus": 0, "steps": K, "warmup": W,
+           "ms_per_step": dt / K * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "impl": "reference",
+           "data": "synthetic: seeded Gaussian random field, 2LPT to a=0.1",
+           "config": {"workload": "64 independent FastPM simulations, N in {64, 96, 128}, box "
+                                  "2N Mpc/h"},
+           "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": host_threads(),
+                            "kind": "port",
+                            "sample": f"each timed step is one FastPM step of the NumPy oracle "
+                                      f"on one {n}^3 simulation of the table"},
+           "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_reference_paint(args):
+    """The oracle's cic_paint (np.bincount scatter) on the host: each timed
+    step paints a 2M-particle sample of the uniform distribution."""
+    from oracle import cic
+    K, W = args.steps, args.warmup
+    n, m = 256, 1 << 21
+    pos = np.random.Generator(np.random.PCG64(1)).uniform(0.0, n, (m, 3)).astype(np.float32)
+    for _ in range(min(W, 1)):
+        cic.cic_paint(np.zeros((n,) * 3, np.float32), pos)
+    t = time.perf_counter()
+    steps = min(K, 5)
+    for _ in range(steps):
+        cic.cic_paint(np.zeros((n,) * 3, np.float32), pos)
+    dt = time.perf_counter() - t
+    value = m * steps / dt
+    out = {"metric": "particles/s (cic_paint, 16.7M clustered a=1 particles on 256^3 mesh)",
+           "value": value, "unit": "particles/s", "n_gpus": 0, "steps": steps, "warmup": W,
+           "ms_per_step": dt / steps * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "impl": "reference",
+           "data": "synthetic: uniform U[0,256)^3 positions, NumPy PCG64 seed 1",
+           "config": {"workload": "cic_paint of 2,097,152 particles on a 256^3 mesh"},
+           "cpu_baseline": {"value": value, "unit": "particles/s", "cores": 1, "kind": "port",
+                            "sample": "each timed step is the NumPy oracle's cic_paint of a "
+                                      "2,097,152-particle uniform sample (single-threaded "
+                                      "bincount)"},
+           "e2e": {"value": value, "unit": "particles/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
+    if args.steps is None:
+        args.steps = 20 if args.workload == "batched" else 40
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
+    elif args.workload == "paint":
+        run_paint(args)
     else:
         run_gb300(args)
 

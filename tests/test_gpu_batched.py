@@ -78,6 +78,35 @@ def test_batched_paint_matches_oracle(cuda):
         assert abs(float(m.double().sum()) - len(p)) < 1e-3 * len(p)
 
 
+def test_batched_mixed_distributions(cuda):
+    """One batch holding a slightly perturbed lattice, uniform random
+    positions in lattice storage, a 12^3 lattice and a non-cubic mesh:
+    paint, forces and one step of each against the oracle."""
+    from jaxpm_gb300 import batched
+    shapes = [(16, 16, 16), (16, 16, 16), (12, 12, 12), (16, 24, 32)]
+    rng = np.random.default_rng(11)
+    parts = [perturbed_lattice(shapes[0], 1, sigma=0.3),
+             rng.uniform(0, 16, (16**3, 3)).astype(np.float32),
+             perturbed_lattice(shapes[2], 2, sigma=0.5),
+             perturbed_lattice(shapes[3], 3, sigma=1.2)]
+    b = batched.BatchedFastPM(shapes, cosmos(len(shapes)), 0.1, 1.0, 2, device=cuda)
+    x = T(np.concatenate(parts), cuda)
+    for shape, p, m in zip(shapes, parts, b.paint(x)):
+        ref = cic.cic_paint(np.zeros(shape), p.astype(np.float64))
+        assert rel_l2(m.cpu(), ref) < TOL
+    f = b.forces(x)
+    for shape, p, fs in zip(shapes, parts, b.split(f)):
+        ref = fo.pm_forces(p.astype(np.float64), mesh_shape=shape, dtype=np.float64)
+        assert rel_l2(fs.cpu(), ref) < TOL
+    v = torch.zeros_like(x)
+    xs = x.clone()
+    b.step(xs, v, 0)
+    kick = b.kick[0].cpu().numpy()
+    for s, (shape, p) in enumerate(zip(shapes, parts)):
+        ref = fo.pm_forces(p.astype(np.float64), mesh_shape=shape, dtype=np.float64)
+        assert rel_l2(b.split(v)[s].cpu(), kick[s] * ref) < TOL
+
+
 def test_batched_step_matches_single_simulation_steps(cuda):
     from jaxpm_gb300 import batched, simulate
     cs = cosmos(len(SHAPES), seed=1)
