@@ -485,6 +485,16 @@ int pmgb_linear_field_colour_f32(void *spec, int nx, int ny, int nz,
 /* Scratch bytes for pmgb_lpt2_source_f32. */
 size_t pmgb_lpt2_source_workspace_size(int nx, int ny, int nz);
 
+/* Adjoint of the 2LPT source as a function of the real linear field ic
+ * (R2C then pmgb_lpt2_source_f32): the cotangent g_delta2 of delta2 ->
+ * g_ic.  The maps ic -> phi_ij are real convolutions with even kernels
+ * (self-adjoint), so g_ic = sum_ij phi_ij-operator(d delta2/d phi_ij *
+ * g_delta2).  Workspace: pmgb_lpt2_source_workspace_size bytes. */
+int pmgb_lpt2_source_vjp_f32(const float *ic, const float *g_delta2,
+                             float *g_ic, int nx, int ny, int nz,
+                             void *workspace, size_t workspace_bytes,
+                             pmgb_stream_t stream);
+
 /* Second-order LPT source (jaxpm/pm.py:88-109): from the half spectrum
  * delta_k, delta2 = sum_{i<j} (phi_ii phi_jj - phi_ij^2) with
  * phi_ij = ifft3d(grad_i grad_j * invlaplace * delta_k). */

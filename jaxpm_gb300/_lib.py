@@ -106,6 +106,7 @@ SIGNATURES = {
                                              c_float, c_float, c_float, P, c_size_t, P, P]),
     "pmgb_power_spectrum_f32": (c_int, [P, c_int, c_int, c_int, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, P, c_int, P, P, P, P]),
+    "pmgb_lpt2_source_vjp_f32": (c_int, [P, P, P, c_int, c_int, c_int, P, c_size_t, P]),
     "pmgb_batch_workspace_size": (c_size_t, [P, c_int]),
     "pmgb_batch_init": (c_int, [P, c_int, P, c_size_t, P]),
     "pmgb_batch_release": (c_int, [P]),

@@ -645,6 +645,17 @@ size_t pmgb_lpt2_source_workspace_size(int nx, int ny, int nz) {
   return lpt2_source_workspace_size(nx, ny, nz);
 }
 
+int pmgb_lpt2_source_vjp_f32(const float *ic, const float *g_delta2, float *g_ic, int nx, int ny,
+                             int nz, void *workspace, size_t workspace_bytes,
+                             pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NEED(ic);
+  NEED(g_delta2);
+  NEED(g_ic);
+  return lpt2_source_vjp(ic, g_delta2, g_ic, nx, ny, nz, workspace, workspace_bytes, stream);
+}
+
 int pmgb_lpt2_source_f32(const void *delta_k, float *delta2, int nx, int ny, int nz,
                          void *workspace, size_t workspace_bytes, pmgb_stream_t stream) {
   BEGIN();

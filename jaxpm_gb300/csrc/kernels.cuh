@@ -89,6 +89,9 @@ int linear_field_colour(void *spec, int nx, int ny, int nz, float bx, float by,
                         float bz, const float *tk, const float *tp, int nt,
                         float scale, cudaStream_t s);
 size_t lpt2_source_workspace_size(int nx, int ny, int nz);
+// adjoint of R2C(ic) -> lpt2_source: g = delta2 cotangent -> g_ic (same workspace)
+int lpt2_source_vjp(const float *ic, const float *g, float *g_ic, int nx, int ny, int nz, void *ws,
+                    size_t bytes, cudaStream_t s);
 int lpt2_source(const void *dk, float *delta2, int nx, int ny, int nz,
                 void *ws, size_t bytes, cudaStream_t s);
 int lpt_combine(const float *a, const float *b, int64_t n, float ca, float cb,

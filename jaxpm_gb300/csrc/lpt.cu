@@ -113,6 +113,58 @@ __global__ void combine_kernel(const float *__restrict__ a, const float *__restr
     out[e] = b ? ca * a[e] + cb * b[e] : ca * a[e];
 }
 
+// Adjoint of source_kernel: with d = sum_{i<j}(s_ii s_jj - s_ij^2),
+// s_bar_ii = g * (sum of the other two diagonal entries), s_bar_ij = -2 g s_ij
+// (in place over the six shear meshes).
+__global__ void source_vjp_kernel(float *__restrict__ s, int64_t cs,
+                                  const float *__restrict__ g, int64_t n) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const float s00 = s[e], s01 = s[cs + e], s02 = s[2 * cs + e], s11 = s[3 * cs + e],
+                s12 = s[4 * cs + e], s22 = s[5 * cs + e];
+    const float ge = g[e];
+    s[e] = ge * (s11 + s22);
+    s[cs + e] = -2.0f * ge * s01;
+    s[2 * cs + e] = -2.0f * ge * s02;
+    s[3 * cs + e] = ge * (s00 + s22);
+    s[4 * cs + e] = -2.0f * ge * s12;
+    s[5 * cs + e] = ge * (s00 + s11);
+  }
+}
+
+// Adjoint of shear_kernel + C2R: each map delta -> s_ab is a real circular
+// convolution with an even kernel (multiplier -g_a g_b invlaplace, real and
+// even in k), hence self-adjoint; the six transformed cotangents are
+// combined into one spectrum, in place over the first (elementwise).
+__global__ void shear_vjp_kernel(float2 *__restrict__ spec, int64_t cs, int nx, int ny, int nz,
+                                 float scale) {
+  const int nzh = nz / 2 + 1;
+  const int64_t total = (int64_t)nx * ny * nzh;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    int k = (int)(e % nzh);
+    int64_t r = e / nzh;
+    int j = (int)(r % ny), i = (int)(r / ny);
+    float w[3] = {fftfreq_w(i, nx), fftfreq_w(j, ny), fftfreq_w(k, nz)};
+    float kk = __fadd_rn(__fadd_rn(w[0] * w[0], w[1] * w[1]), w[2] * w[2]);
+    float inv = kk == 0.0f ? 0.0f : -__frcp_rn(kk);
+    float g[3] = {order1_grad(w[0]), order1_grad(w[1]), order1_grad(w[2])};
+    float ax = 0.f, ay = 0.f;
+    int c = 0;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int b = a; b < 3; ++b) {
+        const float m = -(g[a] * g[b]) * scale * inv;
+        const float2 v = spec[c * cs + e];
+        ax += m * v.x;
+        ay += m * v.y;
+        ++c;
+      }
+    spec[e] = make_float2(ax, ay);
+  }
+}
+
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
@@ -150,6 +202,32 @@ int lpt2_source(const void *dk, float *delta2, int nx, int ny, int nz, void *ws,
   source_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(shear, ncell, delta2, ncell);
   PMGB_LAUNCHED("source_kernel");
   return PMGB_OK;
+}
+
+int lpt2_source_vjp(const float *ic, const float *g, float *g_ic, int nx, int ny, int nz, void *ws,
+                    size_t bytes, cudaStream_t s) {
+  const size_t need = lpt2_source_workspace_size(nx, ny, nz);
+  if (!ws || bytes < need)
+    return fail(PMGB_ERR_WORKSPACE, "2LPT source adjoint needs " + std::to_string(need) +
+                                        " workspace bytes");
+  const int64_t ncell = (int64_t)nx * ny * nz;
+  const int64_t nhalf = (int64_t)nx * ny * (nz / 2 + 1);
+  float2 *spec = static_cast<float2 *>(ws);
+  float *shear = reinterpret_cast<float *>(static_cast<char *>(ws) + align256(6 * nhalf * 8));
+  const float scale = 1.0f / (float)ncell;
+  // forward recompute of the six shear meshes (delta_k staged in the shear
+  // meshes' region, which holds one spectrum and is overwritten next)
+  float2 *dk = reinterpret_cast<float2 *>(shear);
+  PMGB_TRY(fft_r2c(ic, dk, nx, ny, nz, 1, s));
+  shear_kernel<<<grid_for(nhalf, 256), 256, 0, s>>>(dk, spec, nhalf, nx, ny, nz, scale);
+  PMGB_LAUNCHED("shear_kernel");
+  PMGB_TRY(fft_c2r(spec, shear, nx, ny, nz, 6, s));
+  source_vjp_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(shear, ncell, g, ncell);
+  PMGB_LAUNCHED("source_vjp_kernel");
+  PMGB_TRY(fft_r2c(shear, spec, nx, ny, nz, 6, s));
+  shear_vjp_kernel<<<grid_for(nhalf, 256), 256, 0, s>>>(spec, nhalf, nx, ny, nz, scale);
+  PMGB_LAUNCHED("shear_vjp_kernel");
+  return fft_c2r(spec, g_ic, nx, ny, nz, 1, s);
 }
 
 int lpt_combine(const float *a, const float *b, int64_t n, float ca, float cb, float *out,

@@ -185,12 +185,21 @@ class _Source2LPT(torch.autograd.Function):
         out = torch.empty_like(ic)
         _lib.call("pmgb_lpt2_source_f32", _lib.ptr(dk), _lib.ptr(out), nx, ny, nz, _lib.ptr(ws),
                   wsb, s)
+        ctx.save_for_backward(ic)
         return out
 
     @staticmethod
     def backward(ctx, g):
-        raise NotImplementedError("the gradient of the 2LPT source is not implemented; "
-                                  "differentiate lpt with order=1")
+        """pmgb_lpt2_source_vjp_f32 (recomputes the six shear meshes)."""
+        (ic,) = ctx.saved_tensors
+        nx, ny, nz = ic.shape
+        g = g.to(torch.float32).contiguous()
+        wsb = _lib.load().pmgb_lpt2_source_workspace_size(nx, ny, nz)
+        ws = _ws(wsb, ic.device)
+        out = torch.empty_like(ic)
+        _lib.call("pmgb_lpt2_source_vjp_f32", _lib.ptr(ic), _lib.ptr(g), _lib.ptr(out), nx, ny,
+                  nz, _lib.ptr(ws), wsb, _lib.stream())
+        return out
 
 
 def lpt(cosmo, initial_conditions, particles=None, a=0.1, halo_size=0, sharding=None, order=1):
@@ -249,18 +258,46 @@ def linear_field(mesh_shape, box_size, pk, seed, sharding=None, noise=None, devi
         tp = np.asarray(pk(tk), dtype=np.float64)
     else:
         tk, tp = (np.asarray(v, dtype=np.float64) for v in pk)
-    tk_d = torch.tensor(tk, dtype=torch.float32, device=noise.device)
-    tp_d = torch.tensor(tp, dtype=torch.float32, device=noise.device)
-    nx, ny, nz = mesh_shape
+    return _Colour.apply(noise, power_table(tk, tp, noise.device), tuple(box))
+
+
+def power_table(tk, tp, device):
+    """A (k, P) table as the two float32 device arrays of the colouring
+    kernel."""
+    return (torch.tensor(np.asarray(tk, dtype=np.float64), dtype=torch.float32, device=device),
+            torch.tensor(np.asarray(tp, dtype=np.float64), dtype=torch.float32, device=device))
+
+
+def colour(noise, table, box):
+    """White noise -> the Gaussian field of power spectrum ``table``:
+    R2C, ``pmgb_linear_field_colour_f32``, C2R (``jaxpm/pm.py:134-143``)."""
+    nx, ny, nz = noise.shape
+    tk_d, tp_d = table
     spec = torch.empty((nx, ny, nz // 2 + 1), dtype=torch.complex64, device=noise.device)
     s = _lib.stream()
     _lib.call("pmgb_fft_r2c_f32", _lib.ptr(noise), _lib.ptr(spec), nx, ny, nz, 1, s)
     _lib.call("pmgb_linear_field_colour_f32", _lib.ptr(spec), nx, ny, nz, *box, _lib.ptr(tk_d),
-              _lib.ptr(tp_d), len(tk), 1.0 / (nx * ny * nz), s)
-    out = torch.empty(mesh_shape, dtype=torch.float32, device=noise.device)
+              _lib.ptr(tp_d), tk_d.numel(), 1.0 / (nx * ny * nz), s)
+    out = torch.empty(noise.shape, dtype=torch.float32, device=noise.device)
     _lib.call("pmgb_fft_c2r_f32", _lib.ptr(spec), _lib.ptr(out), nx, ny, nz, 1, 0, s)
     return out
 
 
-__all__ = ["pm_forces", "lpt", "linear_field", "force_meshes", "pk_table", "fft3d", "ifft3d",
-           "MODES"]
+class _Colour(torch.autograd.Function):
+    """noise -> linear field.  The map is a real circular convolution whose
+    kernel (the inverse transform of sqrt(P(|k|) N/V), real and even in k)
+    is symmetric, so the backward applies the same colouring to the
+    cotangent."""
+
+    @staticmethod
+    def forward(ctx, noise, table, box):
+        ctx.table, ctx.box = table, box
+        return colour(noise.to(torch.float32).contiguous(), table, box)
+
+    @staticmethod
+    def backward(ctx, g):
+        return colour(g.to(torch.float32).contiguous(), ctx.table, ctx.box), None, None
+
+
+__all__ = ["pm_forces", "lpt", "linear_field", "force_meshes", "pk_table", "power_table",
+           "colour", "fft3d", "ifft3d", "MODES"]

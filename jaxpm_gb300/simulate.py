@@ -292,7 +292,9 @@ class _Step(torch.autograd.Function):
 
     Backward, given ``(gx', gv')``: ``u = gv' + drift gx'``,
     ``gx = gx' + (dF/dx)^T (kick u)`` (one ``pmgb_pm_forces_vjp_f32``),
-    ``gv = u``."""
+    ``gv = u``.  ``kick`` and ``drift`` may be 0-dim tensors that require
+    grad (coefficients that depend on the cosmology): their cotangents are
+    ``<u, F(x)>`` (one more force evaluation) and ``<gx', v'>``."""
 
     @staticmethod
     def forward(ctx, x, v, mesh_shape, kick, drift, mode, r_split):
@@ -303,13 +305,16 @@ class _Step(torch.autograd.Function):
         ws = _ws(wsb, x.device)
         _lib.call("pmgb_fpm_step_f32", _lib.ptr(xo), _lib.ptr(vo), n, nx, ny, nz, float(kick),
                   float(drift), float(r_split), mode, _lib.ptr(ws), wsb, _lib.stream())
-        ctx.save_for_backward(x)
+        coef_grad = torch.is_tensor(drift) and drift.requires_grad
+        ctx.save_for_backward(x, vo if coef_grad else None)
+        ctx.coef = (kick if torch.is_tensor(kick) else None,
+                    drift if torch.is_tensor(drift) else None)
         ctx.args = (mesh_shape, float(kick), float(drift), mode, float(r_split))
         return xo, vo
 
     @staticmethod
     def backward(ctx, gx, gv):
-        (x,) = ctx.saved_tensors
+        x, vo = ctx.saved_tensors
         (nx, ny, nz), kick, drift, mode, r_split = ctx.args
         gx = torch.zeros_like(x) if gx is None else gx.contiguous()
         gv = torch.zeros_like(x) if gv is None else gv.contiguous()
@@ -321,7 +326,16 @@ class _Step(torch.autograd.Function):
         gpos = torch.empty_like(x)
         _lib.call("pmgb_pm_forces_vjp_f32", _lib.ptr(x), n, nx, ny, nz, r_split, mode,
                   _lib.ptr(ku), _lib.ptr(gpos), _lib.ptr(ws), wsb, _lib.stream())
-        return _combine(gx, gpos, 1.0, 1.0), u, None, None, None, None, None
+        g_kick = g_drift = None
+        kt, dt = ctx.coef
+        if kt is not None and ctx.needs_input_grad[3]:
+            F = torch.empty_like(x)
+            _lib.call("pmgb_pm_forces_f32", _lib.ptr(x), n, nx, ny, nz, r_split, mode,
+                      _lib.ptr(F), _lib.ptr(ws), wsb, _lib.stream())
+            g_kick = (u.double() * F.double()).sum().to(kt.dtype).to(kt.device)
+        if dt is not None and ctx.needs_input_grad[4] and vo is not None:
+            g_drift = (gx.double() * vo.double()).sum().to(dt.dtype).to(dt.device)
+        return _combine(gx, gpos, 1.0, 1.0), u, None, g_kick, g_drift, None, None
 
 
 def fpm_step(x, v, mesh_shape, kick, drift, paint_mode="atomic", r_split=0.0):
@@ -332,12 +346,18 @@ def fpm_step(x, v, mesh_shape, kick, drift, paint_mode="atomic", r_split=0.0):
 
 
 def nbody(pos, vel, cosmo, mesh_shape, a0, a1, n_steps, paint_mode="atomic", r_split=0.0,
-          checkpoint_every=0):
+          checkpoint_every=0, coefficients=None):
     """Differentiable FastPM integration from ``a0`` to ``a1`` in
     ``n_steps`` steps; returns the final ``(pos, vel)``.  With
     ``checkpoint_every = k > 0`` only every k-th state is kept for the
-    backward pass and the steps in between are recomputed."""
-    kick, drift = fpm_coefficients(cosmo, a0, a1, n_steps)
+    backward pass and the steps in between are recomputed.
+    ``coefficients`` (optional): the per-step ``(kick, drift)`` as 1-D
+    tensors, which may require grad (see ``forward_model``); by default
+    they are computed from ``cosmo``."""
+    if coefficients is None:
+        kick, drift = fpm_coefficients(cosmo, a0, a1, n_steps)
+    else:
+        kick, drift = coefficients
 
     def segment(x, v, lo, hi):
         for i in range(lo, hi):

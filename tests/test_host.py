@@ -77,3 +77,29 @@ def test_kedges_match_reference_rule():
     dk = 2 * np.pi / 256 * 2
     assert np.isclose(e[0], 1.5 * dk) and np.allclose(np.diff(e), dk)
     assert e[-1] < np.pi * 32 / 256
+
+
+def test_forward_model_host_scalar_derivatives():
+    """The cosmology scalars' backward (central differences of host float64
+    functions) agrees with an independent difference at a 10x larger step;
+    sigma8 does not enter the LPT or step scalars."""
+    import torch
+    from jaxpm_gb300 import forward_model as fm
+    th = torch.tensor([0.2589, 0.8159], dtype=torch.float64, requires_grad=True)
+
+    def fn(t):
+        return fm._scalars(t, None, 0.1, 1.0, 8, 2)
+    out = fm._HostScalars.apply(th, fn, 1e-5)
+    w = torch.linspace(0.5, 1.5, out.numel(), dtype=torch.float64)
+    (out * w).sum().backward()
+    h = 1e-4
+    t0 = th.detach().numpy()
+    fd = (fn(t0 + [h, 0]) - fn(t0 - [h, 0])) / (2 * h)
+    ref = float(np.dot(w.numpy(), fd))
+    assert abs(float(th.grad[0]) - ref) < 1e-5 * abs(ref)
+    assert float(th.grad[1]) == 0.0
+    # the scalars reproduce the step coefficients of the plain integrator
+    from jaxpm_gb300 import ode
+    k, d = ode.fpm_coefficients(fm.cosmology_of(t0), 0.1, 1.0, 8)
+    assert np.allclose(out.detach().numpy()[4:12], k, rtol=1e-12)
+    assert np.allclose(out.detach().numpy()[12:], d, rtol=1e-12)
