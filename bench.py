@@ -38,9 +38,10 @@ BOX_PER_CELL = 1.0  # box 512 Mpc/h on 512^3
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--workload", default="step", choices=["step", "batched", "paint"],
+    ap.add_argument("--workload", default="step", choices=["step", "batched", "paint", "grad"],
                     help="step: the 512^3 FastPM step (headline); batched: 64 simulations "
-                         "of 64^3-128^3; paint: cic_paint/cic_read microbenchmarks")
+                         "of 64^3-128^3; paint: cic_paint/cic_read microbenchmarks; grad: "
+                         "gradients w.r.t. noise and cosmology")
     ap.add_argument("--steps", type=int, default=None,
                     help="timed steps (default 40; 20 for the batched workload)")
     ap.add_argument("--warmup", type=int, default=3)
@@ -300,10 +301,12 @@ def run_gb300(args):
     torch.cuda.synchronize(dev)
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
+    launches0 = lib.pmgb_launch_count()
     t0.record(stream)
     for i in range(K):
         step_phased(i, events[i])
     t1.record(stream)
+    launches = lib.pmgb_launch_count() - launches0
     torch.cuda.synchronize(dev)
     barrier(world)
     clk = clocks.stop() if clocks else None
@@ -318,17 +321,9 @@ def run_gb300(args):
                          mode="deterministic")
     mass_err = abs(rho.double().sum().item() - Np) / Np
     del rho
-    # own kernels: forces (the k-space kernel between cuFFT's transforms, or
-    # the fused x kernel between cuFFT's plane transforms: 1; with the
-    # library's plane kernels too: 3) and the gather every step; the sorted
-    # loop adds the sort (3 scan + 1 scatter) per step and one paint per run
-    # (the gather paints every later density), the lattice loop a paint per
-    # step (two kernels when deterministic)
-    forces_own = 3 if fft_path == 2 else 1
-    if engine == "sorted":
-        gpu_launches = 1 + K * (forces_own + 1 + 4)
-    else:
-        gpu_launches = K * ((2 if mode == _lib.PAINT_DETERMINISTIC else 1) + forces_own + 1)
+    # own kernels launched in the timed region, counted by the library
+    # (cuFFT's kernels are not counted)
+    gpu_launches = int(launches)
 
     result = {"metric": "particle-steps/s (FastPM PM step, 512^3 particles on 512^3 mesh)",
               "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": K,
@@ -514,7 +509,10 @@ def run_batched(args):
     x, v = x0.clone(), v0.clone()
     for i in range(W):
         eng.step(x, v, i % K)
+    launches0 = batched._lib.load().pmgb_launch_count()
     graph = eng.capture(x, v)  # the K steps as one CUDA graph
+    # own kernels recorded in the graph (the warm-up step of capture() included)
+    graph_launches = batched._lib.load().pmgb_launch_count() - launches0
     x.copy_(x0)
     v.copy_(v0)
     graph.replay()  # warm-up of the graph itself
@@ -557,8 +555,9 @@ def run_batched(args):
                          "l2": f"inputs larger than L2 (positions+velocities "
                                f"{Np * 24 / 1e9:.1f} GB)"},
               "mass_rel_err": mass_err,
-              # per step: paint, k-space and gather launches (the FFTs are cuFFT)
-              "gpu_launches": K * 3,
+              # own kernels of one replay (the K steps; the FFTs are cuFFT's):
+              # the library's count at capture minus capture()'s warm-up step
+              "gpu_launches": int(graph_launches * K // (K + 1)),
               "roofline": {"kernel": "whole step", "bound": "hbm", "achieved": achieved,
                            "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                            "peak_kind": peak_kind, "algorithmic_bytes_per_particle": 124.0,
@@ -667,9 +666,12 @@ def run_paint(args):
     clustered = sim.state()[0].contiguous()
     del sim, x0, v0
 
-    def timed(fn):
+    launches = {}
+
+    def timed(fn, tag=None):
         for _ in range(W):
             fn()
+        l0 = lib.pmgb_launch_count()
         ts = []
         for _ in range(K):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -678,6 +680,8 @@ def run_paint(args):
             b.record(stream)
             torch.cuda.synchronize(dev)
             ts.append(a.elapsed_time(b))
+        if tag is not None:
+            launches[tag] = lib.pmgb_launch_count() - l0
         return float(np.median(ts))
 
     def paint_ops(pos, shape):
@@ -706,7 +710,7 @@ def run_paint(args):
         alg = 12.0 * npart + 4.0 * nx * ny * nz
         out = {}
         for name, fn in ops.items():
-            ms = timed(fn)
+            ms = timed(fn, (shape, pos.data_ptr(), name))
             total = float(mesh.double().sum())
             out[name] = {"ms": ms, "particles_per_s": npart / (ms / 1e3),
                          "achieved_gbs": alg / (ms / 1e3) / 1e9,
@@ -778,7 +782,123 @@ def run_paint(args):
                            "achieved": head[best]["achieved_gbs"], "peak": peak, "unit": "GB/s",
                            "frac": head[best]["frac"], "peak_kind": peak_kind,
                            "algorithmic_bytes_per_particle": 16.0, "traffic": None},
-              "gpu_launches": K}
+              "gpu_launches": int(launches[((n,) * 3, clustered.data_ptr(), best)])}
+    print(json.dumps(result))
+
+
+# ---------------------------------------------------------------------------
+# gradient workload: d loss / d (noise, Omega_c, sigma8) through LPT + FastPM
+# ---------------------------------------------------------------------------
+def grad_case(n, steps, checkpoint_every, dev, fd_eps=1e-3):
+    """Forward model at n^3 (box 2n Mpc/h, 2LPT a=0.1, `steps` steps to a=1,
+    a checkpoint every `checkpoint_every` steps), MSE of the a=1 density
+    against the seed-2 target; times forward and forward+backward and checks
+    the gradients against central differences (eps = fd_eps)."""
+    import torch
+    from jaxpm_gb300 import _lib, distributed, forward_model as fm, painting
+
+    shape, box = (n,) * 3, (2.0 * n,) * 3
+    theta0 = torch.tensor([0.2589, 0.8159], dtype=torch.float64)
+    noise = distributed.normal_field(1, shape, device=dev)
+    with torch.no_grad():
+        xt, _ = fm.lpt_nbody(distributed.normal_field(2, shape, device=dev), theta0, shape, box,
+                             n_steps=steps, checkpoint_every=0)
+        target = painting.cic_paint(torch.zeros(shape, device=dev), xt)
+        del xt
+
+    def loss(nz, th):
+        x, _ = fm.lpt_nbody(nz, th, shape, box, n_steps=steps, checkpoint_every=checkpoint_every)
+        return fm.density_mse(x, target)
+
+    from jaxpm_gb300 import growth
+    stream = torch.cuda.current_stream(dev)
+    ev = lambda: torch.cuda.Event(enable_timing=True)  # noqa: E731
+    # warm-up forward and backward (FFT plans, k-space tables), then drop the
+    # host growth tables so that the timed pass pays the host scalar work of
+    # a new cosmology
+    nzw = noise.clone().requires_grad_(True)
+    thw = theta0.clone().requires_grad_(True)
+    loss(nzw, thw).backward()
+    del nzw, thw
+    growth._CACHE.clear()
+    torch.cuda.synchronize(dev)
+    a, b = ev(), ev()
+    a.record(stream)
+    with torch.no_grad():
+        l0 = loss(noise, theta0)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    fwd_ms = a.elapsed_time(b)
+    nz = noise.clone().requires_grad_(True)
+    th = theta0.clone().requires_grad_(True)
+    growth._CACHE.clear()
+    torch.cuda.synchronize(dev)
+    lib = _lib.load()
+    l0 = lib.pmgb_launch_count()
+    a, b = ev(), ev()
+    a.record(stream)
+    loss(nz, th).backward()
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    grad_ms = a.elapsed_time(b)
+    launches = lib.pmgb_launch_count() - l0
+    d = torch.randn(shape, generator=torch.Generator(device=dev).manual_seed(5), device=dev)
+    checks = {}
+    with torch.no_grad():
+        for j, name in enumerate(["Omega_c", "sigma8"]):
+            tp, tm = theta0.clone(), theta0.clone()
+            tp[j] += fd_eps
+            tm[j] -= fd_eps
+            fd = (float(loss(noise, tp)) - float(loss(noise, tm))) / (2 * fd_eps)
+            an = float(th.grad[j])
+            checks[name] = {"adjoint": an, "finite_difference": fd,
+                            "rel_err": abs(an - fd) / max(abs(fd), 1e-30)}
+        fd = (float(loss(noise + fd_eps * d, theta0)) -
+              float(loss(noise - fd_eps * d, theta0))) / (2 * fd_eps)
+        an = float((nz.grad.double() * d.double()).sum())
+        checks["noise_direction"] = {"adjoint": an, "finite_difference": fd,
+                                     "rel_err": abs(an - fd) / max(abs(fd), 1e-30)}
+    return {"mesh": n, "steps": steps, "checkpoint_every": checkpoint_every,
+            "loss": float(l0), "forward_ms": fwd_ms, "forward_backward_ms": grad_ms,
+            "backward_vs_forward": (grad_ms - fwd_ms) / fwd_ms, "gpu_launches": int(launches),
+            "grad_check_eps": fd_eps, "grad_check": checks}
+
+
+def run_grad(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    skip = set(filter(None, args.skip.split(",")))
+    K = args.steps if args.steps_given else 32
+    clocks = ClockSampler(local) if "clocks" not in skip else None
+    if clocks:
+        clocks.start()
+    main = grad_case(128, K, 4, dev)
+    clk = clocks.stop() if clocks else None
+    Np = 128**3
+    value = Np * K / (main["forward_backward_ms"] / 1e3)
+    result = {"metric": "particle-steps/s (forward+gradient: 2LPT + FastPM, 128^3, d loss / "
+                        "d (noise, Omega_c, sigma8))",
+              "value": value, "unit": "particle-steps/s", "n_gpus": 1, "steps": K, "warmup": 1,
+              "ms_per_step": main["forward_backward_ms"] / K, "higher_is_better": True,
+              "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "gb300",
+              "data": "synthetic: NumPy PCG64 white noise seeds 1 (model) and 2 (target), "
+                      "Eisenstein-Hu P(k)",
+              "config": {"workload": f"MSE between the a=1 CIC density of 128^3 particles on a "
+                                     f"128^3 mesh (box 256 Mpc/h, 2LPT a=0.1, {K} steps, "
+                                     f"checkpoints every 4) and a seed-2 target; gradient w.r.t. "
+                                     f"the white noise and (Omega_c, sigma8)",
+                         "l2": "one timed pass; working set above L2 at 512^3"},
+              "cases": [main],
+              "gpu_launches": main["gpu_launches"]}
+    if "512" not in skip:
+        result["cases"].append(grad_case(512, 64, 4, dev))
+    if clk is not None:
+        result["clocks"] = clk
     print(json.dumps(result))
 
 
@@ -829,6 +949,8 @@ def run_reference(args):
         return run_reference_batched(args)
     if args.workload == "paint":
         return run_reference_paint(args)
+    if args.workload == "grad":
+        return run_reference_grad(args)
     n_sample = 128
     K, W = args.steps, args.warmup
     from oracle import nbody as onb
@@ -930,8 +1052,39 @@ def run_reference_paint(args):
     print(json.dumps(out))
 
 
+def run_reference_grad(args):
+    """The oracle on the host: forward FastPM steps and their reverse sweep
+    (float64 NumPy) on a 32^3 sample of the 128^3 problem."""
+    from oracle import nbody as onb
+    K = args.steps if args.steps_given else 32
+    n = 32
+    cosmo, x0, v0 = oracle_state(n)
+    kc, dc = onb.fpm_coefficients(cosmo, 0.1, 1.0, K)
+    rng = np.random.default_rng(0)
+    gx, gv = rng.standard_normal(x0.shape), rng.standard_normal(x0.shape)
+    t = time.perf_counter()
+    onb.fpm_run_vjp(x0, v0, (n,) * 3, kc, dc, gx, gv)
+    dt = time.perf_counter() - t
+    value = n**3 * K / dt
+    out = {"metric": "particle-steps/s (forward+gradient: 2LPT + FastPM, 128^3, d loss / "
+                     "d (noise, Omega_c, sigma8))",
+           "value": value, "unit": "particle-steps/s", "n_gpus": 0, "steps": K, "warmup": 0,
+           "ms_per_step": dt / K * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "impl": "reference",
+           "data": "synthetic: seeded Gaussian random field, 2LPT to a=0.1",
+           "config": {"workload": f"forward FastPM run and its reverse sweep, {K} steps"},
+           "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": host_threads(),
+                            "kind": "port",
+                            "sample": f"the NumPy oracle's forward run + reverse sweep of {K} "
+                                      f"FastPM steps on a {n}^3 sub-problem (float64)"},
+           "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
 def main():
     args = parse()
+    args.steps_given = args.steps is not None
     if args.steps is None:
         args.steps = 20 if args.workload == "batched" else 40
     if args.impl == "reference":
@@ -940,6 +1093,8 @@ def main():
         run_batched(args)
     elif args.workload == "paint":
         run_paint(args)
+    elif args.workload == "grad":
+        run_grad(args)
     else:
         run_gb300(args)
 

@@ -63,6 +63,11 @@ int pmgb_version(void);
 /* Message for the last failing call on this thread ("" if none). */
 const char *pmgb_last_error(void);
 
+/* Number of kernels this library has launched in this process (library
+ * kernels only: cuFFT's are not counted; launches recorded into a CUDA
+ * graph count once, at capture). */
+uint64_t pmgb_launch_count(void);
+
 /* ---- CIC mass assignment: absolute positions --------------------------- */
 
 /* Scratch bytes needed by pmgb_cic_paint_f32 for this mode and size. */

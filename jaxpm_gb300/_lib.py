@@ -34,6 +34,7 @@ P = ctypes.c_void_p
 SIGNATURES = {
     "pmgb_version": (c_int, []),
     "pmgb_last_error": (ctypes.c_char_p, []),
+    "pmgb_launch_count": (ctypes.c_uint64, []),
     "pmgb_cic_paint_workspace_size": (c_size_t, [c_int, c_int, c_int, c_int64, c_int]),
     "pmgb_cic_paint_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P, c_float, c_int, c_int,
                                    P, c_size_t, P]),

@@ -1,5 +1,6 @@
 // Exported C ABI of libpmgb (declared in include/pmgb.h): argument checks,
 // per-thread error messages, then a call into the kernels' host code.
+#include <atomic>
 #include <map>
 #include <mutex>
 #include <string>
@@ -14,6 +15,10 @@ thread_local std::string t_err;
 std::mutex g_sm_mu;
 std::map<int, int> g_sm;
 }  // namespace
+
+std::atomic<uint64_t> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 int fail(int code, const std::string &msg) {
   t_err = msg;
@@ -65,6 +70,8 @@ static int check_mode(int mode) {
 extern "C" {
 
 int pmgb_version(void) { return 100; }
+
+uint64_t pmgb_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 const char *pmgb_last_error(void) { return t_err.c_str(); }
 

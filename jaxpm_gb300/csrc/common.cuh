@@ -28,12 +28,17 @@ int sm_count();
                                              cudaGetErrorString(e_));       \
   } while (0)
 
+// Counts the kernels this library has launched (every launch site checks
+// its launch with PMGB_LAUNCHED, which also counts it).
+void count_launch();
+
 #define PMGB_LAUNCHED(name)                                                 \
   do {                                                                      \
     cudaError_t e_ = cudaGetLastError();                                    \
     if (e_ != cudaSuccess)                                                  \
       return ::pmgb::fail(PMGB_ERR_CUDA, std::string(name) + " launch: " + \
                                              cudaGetErrorString(e_));       \
+    ::pmgb::count_launch();                                                 \
   } while (0)
 
 #define PMGB_REQUIRE(cond, msg)                                             \

@@ -132,8 +132,10 @@ def lpt_nbody(noise, theta, mesh_shape, box_size, a0=0.1, a1=1.0, n_steps=32, or
     box = tuple(float(b) for b in box_size)
     theta = torch.as_tensor(theta, dtype=torch.float64)
     ic = _LinearField.apply(noise, theta, box, base, omega_step)
+    # the LPT and step scalars depend on Omega_c only (sigma8 enters P(k) alone)
+    s8 = float(theta[1].detach())
     sc = _HostScalars.apply(
-        theta, lambda th: _scalars(th, base, a0, a1, n_steps, order), scalar_step)
+        theta[:1], lambda om: _scalars([om[0], s8], base, a0, a1, n_steps, order), scalar_step)
     lat = uniform_particles(mesh_shape, device=noise.device).reshape(-1, 3)
     F1 = pm.pm_forces(lat, delta=ic, paint_mode=paint_mode)
     dx = sc[0] * F1

@@ -18,6 +18,8 @@ a = 1.  The table tuple is ``(a, g, f, h, g2, f2, h2)`` with
 ``f = dlnD/dlna`` and ``h = a D''/D``.  Lookups interpolate linearly in a.
 Everything here is float64 host arithmetic: these are per-step scalars.
 """
+import math
+
 import numpy as np
 
 from .cosmology import Esqr, Omega_de_a, Omega_m_a, f_de, w
@@ -39,6 +41,21 @@ def _rhs(c, a, y):
     return np.array([v1, r * d1 - q * v1, v2, r * d2 - q * v2 - r * d1 * d1])
 
 
+def _rhs_lna(c, lna, y):
+    """``a * _rhs(c, a, y)`` at ``a = exp(lna)`` in plain float arithmetic
+    (the same formulas as ``_rhs`` and the background functions; the RK4
+    loop calls it 8192 times per table)."""
+    a = math.exp(lna)
+    d1, v1, d2, v2 = y
+    fde = -3.0 * (1.0 + c.w0) + 3.0 * c.wa * ((a - 1.0) / math.log(a - 1e-5) - 1.0)
+    esq = c.Omega_m / a**3 + c.Omega_k / a**2 + c.Omega_de * a**fde
+    om = c.Omega_m / a**3 / esq
+    ode = c.Omega_de * a**fde / esq
+    q = (2.0 - 0.5 * (om + (1.0 + 3.0 * (c.w0 + (1.0 - a) * c.wa)) * ode)) / a
+    r = 1.5 * om / (a * a)
+    return (a * v1, a * (r * d1 - q * v1), a * v2, a * (r * d2 - q * v2 - r * d1 * d1))
+
+
 def compute_growth_tables(c):
     """``(a, g, f, h, g2, f2, h2)`` on ``logspace(-3, 0, 128)`` (cached per
     cosmology)."""
@@ -47,21 +64,21 @@ def compute_growth_tables(c):
         return hit
     atab = np.logspace(-3.0, 0.0, 128)
     sub = 16
-    y = np.array([atab[0], 1.0, -3.0 / 7.0 * atab[0]**2, -6.0 / 7.0 * atab[0]])
-    ys = [y.copy()]
+    y = (float(atab[0]), 1.0, -3.0 / 7.0 * float(atab[0])**2, -6.0 / 7.0 * float(atab[0]))
+    ys = [y]
     for i in range(len(atab) - 1):
-        la, lb = np.log(atab[i]), np.log(atab[i + 1])
+        la, lb = math.log(atab[i]), math.log(atab[i + 1])
         hstep = (lb - la) / sub
         lna = la
         for _ in range(sub):
-            f = lambda l, yy: np.exp(l) * _rhs(c, np.exp(l), yy)  # noqa: E731
-            k1 = f(lna, y)
-            k2 = f(lna + hstep / 2, y + hstep / 2 * k1)
-            k3 = f(lna + hstep / 2, y + hstep / 2 * k2)
-            k4 = f(lna + hstep, y + hstep * k3)
-            y = y + hstep / 6.0 * (k1 + 2 * k2 + 2 * k3 + k4)
+            k1 = _rhs_lna(c, lna, y)
+            k2 = _rhs_lna(c, lna + hstep / 2, tuple(u + hstep / 2 * k for u, k in zip(y, k1)))
+            k3 = _rhs_lna(c, lna + hstep / 2, tuple(u + hstep / 2 * k for u, k in zip(y, k2)))
+            k4 = _rhs_lna(c, lna + hstep, tuple(u + hstep * k for u, k in zip(y, k3)))
+            y = tuple(u + hstep / 6.0 * (p1 + 2 * p2 + 2 * p3 + p4)
+                      for u, p1, p2, p3, p4 in zip(y, k1, k2, k3, k4))
             lna += hstep
-        ys.append(y.copy())
+        ys.append(y)
     ys = np.array(ys)
     dys = np.array([_rhs(c, a, yy) for a, yy in zip(atab, ys)])
     d1n, d2n = ys[-1, 0], ys[-1, 2]
