@@ -57,6 +57,21 @@ def parse():
     return ap.parse_args()
 
 
+class nvtx:
+    """An NVTX range (for `ncu --nvtx --nvtx-include <name>/`)."""
+
+    def __init__(self, name):
+        self.name = name
+
+    def __enter__(self):
+        import torch
+        torch.cuda.nvtx.range_push(self.name)
+
+    def __exit__(self, *exc):
+        import torch
+        torch.cuda.nvtx.range_pop()
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -303,8 +318,9 @@ def run_gb300(args):
     t1 = torch.cuda.Event(enable_timing=True)
     launches0 = lib.pmgb_launch_count()
     t0.record(stream)
-    for i in range(K):
-        step_phased(i, events[i])
+    with nvtx("timed"):
+        for i in range(K):
+            step_phased(i, events[i])
     t1.record(stream)
     launches = lib.pmgb_launch_count() - launches0
     torch.cuda.synchronize(dev)
@@ -528,7 +544,8 @@ def run_batched(args):
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     t0.record(stream)
-    graph.replay()
+    with nvtx("timed"):
+        graph.replay()
     t1.record(stream)
     torch.cuda.synchronize(dev)
     barrier(world)
@@ -684,7 +701,7 @@ def run_paint(args):
             launches[tag] = lib.pmgb_launch_count() - l0
         return float(np.median(ts))
 
-    def paint_ops(pos, shape):
+    def paint_ops(pos, shape, tag):
         nx, ny, nz = shape
         npart = pos.shape[0]
         mesh = torch.empty(shape, dtype=torch.float32, device=dev)
@@ -710,7 +727,8 @@ def run_paint(args):
         alg = 12.0 * npart + 4.0 * nx * ny * nz
         out = {}
         for name, fn in ops.items():
-            ms = timed(fn, (shape, pos.data_ptr(), name))
+            with nvtx(f"paint_{tag}_{name}"):
+                ms = timed(fn, (shape, pos.data_ptr(), name))
             total = float(mesh.double().sum())
             out[name] = {"ms": ms, "particles_per_s": npart / (ms / 1e3),
                          "achieved_gbs": alg / (ms / 1e3) / 1e9,
@@ -745,7 +763,8 @@ def run_paint(args):
 
     results = {}
     for dname, pos in [("uniform", uni), ("clustered_a1", clustered)]:
-        results[dname] = {"paint": paint_ops(pos, (n,) * 3), "read": read_ops(pos, (n,) * 3)}
+        results[dname] = {"paint": paint_ops(pos, (n,) * 3, dname),
+                          "read": read_ops(pos, (n,) * 3)}
     del uni
 
     # paint-only: the 512^3 run's a=1 particles on a 1024^3 mesh
@@ -758,7 +777,7 @@ def run_paint(args):
         big = (sim.state()[0] * 2.0).contiguous()  # cell units of the 1024^3 mesh
         del sim
         torch.cuda.empty_cache()
-        results["paint_only_1024"] = paint_ops(big, (1024,) * 3)
+        results["paint_only_1024"] = paint_ops(big, (1024,) * 3, "1024")
         del big
         torch.cuda.empty_cache()
 
