@@ -105,13 +105,14 @@ int make_plan(const pmgb_sim *t, int n, Plan *P) {
     P->groups[g].n++;
     key = fnv(fnv(fnv(fnv(key, t[i].nx), t[i].ny), t[i].nz), t[i].np);
   }
-  // group pools
+  // group pools, each group starting on a 256-byte boundary (cuFFT wants
+  // aligned batches; the vector reductions of the painters 16 bytes)
   int64_t mesh = 0, spec = 0;
   for (Group &g : P->groups) {
     g.mesh = mesh;
     g.spec = spec;
-    mesh += (int64_t)g.n * g.nx * g.ny * g.nz;
-    spec += (int64_t)g.n * g.nx * g.ny * (g.nz / 2 + 1);
+    mesh += ((int64_t)g.n * g.nx * g.ny * g.nz + 63) / 64 * 64;
+    spec += ((int64_t)g.n * g.nx * g.ny * (g.nz / 2 + 1) + 31) / 32 * 32;
   }
   P->cells = mesh;
   P->specs = spec;
@@ -214,18 +215,25 @@ __device__ __forceinline__ int64_t corner_cell(const Axis &ax, const Axis &ay, c
 // table-ordered slot when `table_order`).
 __global__ void __launch_bounds__(BT)
 batch_paint_kernel(const BatchSim *__restrict__ sims, int n, float *__restrict__ meshes,
-                   int table_order, const float *__restrict__ pos) {
+                   int table_order, const float *__restrict__ pos, bool vec_ok) {
   int s;
   BatchSim d;
   int64_t p;
   if (!locate(sims, n, s, d, p)) return;
   float x, y, z;
   load3(pos, p, x, y, z);
-  float *m = meshes + (table_order ? d.cell0 : d.mesh);
+  const int64_t off = table_order ? d.cell0 : d.mesh;
+  float *m = meshes + off;
   const Axis ax = cic_axis(x, d.nx), ay = cic_axis(y, d.ny), az = cic_axis(z, d.nz);
+  // vector reductions need every row 16-byte aligned: base, mesh offset and nz
+  const bool vec = vec_ok && (d.nz & 3) == 0 && (off & 3) == 0;
 #pragma unroll
-  for (int c = 0; c < 8; ++c)
-    atomicAdd(m + corner_cell(ax, ay, az, c, d.ny, d.nz), corner_weight(ax, ay, az, c));
+  for (int c = 0; c < 4; ++c) {
+    const int cx = c & 1, cy = c >> 1;
+    const float kxy = __fmul_rn(cx ? ax.k1 : ax.k0, cy ? ay.k1 : ay.k0);
+    red_zpair(m + cell_index(cx ? ax.i1 : ax.i0, cy ? ay.i1 : ay.i0, 0, d.ny, d.nz), az.i0,
+              az.i1, __fmul_rn(kxy, az.k0), __fmul_rn(kxy, az.k1), vec);
+  }
 }
 
 // Three-component read at the particles (forces of pm_forces).
@@ -305,7 +313,7 @@ __global__ void __launch_bounds__(BT)
 batch_adj_paint_kernel(const BatchSim *__restrict__ sims, int n, float *__restrict__ g3pool,
                        const float *__restrict__ pos, const float *__restrict__ gpos,
                        const float *__restrict__ gvel, const float *__restrict__ kick,
-                       const float *__restrict__ drift) {
+                       const float *__restrict__ drift, bool vec_ok) {
   int s;
   BatchSim d;
   int64_t p;
@@ -319,13 +327,17 @@ batch_adj_paint_kernel(const BatchSim *__restrict__ sims, int n, float *__restri
   float *m = g3pool + d.f3;
   const int64_t cs = (int64_t)d.nx * d.ny * d.nz;
   const Axis ax = cic_axis(x, d.nx), ay = cic_axis(y, d.ny), az = cic_axis(z, d.nz);
+  // vector reductions need every row of the three meshes 16-byte aligned
+  const bool vec = vec_ok && (d.nz & 3) == 0 && (d.f3 & 3) == 0;
 #pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const float w = corner_weight(ax, ay, az, c);
-    const int64_t e = corner_cell(ax, ay, az, c, d.ny, d.nz);
-    atomicAdd(m + e, u0 * w);
-    atomicAdd(m + cs + e, u1 * w);
-    atomicAdd(m + 2 * cs + e, u2 * w);
+  for (int c = 0; c < 4; ++c) {
+    const int cx = c & 1, cy = c >> 1;
+    const float kxy = __fmul_rn(cx ? ax.k1 : ax.k0, cy ? ay.k1 : ay.k0);
+    const float wa = __fmul_rn(kxy, az.k0), wb = __fmul_rn(kxy, az.k1);
+    float *row = m + cell_index(cx ? ax.i1 : ax.i0, cy ? ay.i1 : ay.i0, 0, d.ny, d.nz);
+    red_zpair(row, az.i0, az.i1, u0 * wa, u0 * wb, vec);
+    red_zpair(row + cs, az.i0, az.i1, u1 * wa, u1 * wb, vec);
+    red_zpair(row + 2 * cs, az.i0, az.i1, u2 * wa, u2 * wb, vec);
   }
 }
 
@@ -385,6 +397,7 @@ struct KGroup {
   uint32_t ny, nzh, total;  // per-simulation half spectrum
   float scale;              // 1 / ncell
   int64_t start;            // first element of the group in the dk pool
+  int64_t count;            // elements of the group (simulations x total)
 };
 
 struct KGroups {
@@ -417,6 +430,7 @@ batch_forces_kernel(const float2 *__restrict__ dk, float2 *__restrict__ fk, KGro
        e += (int64_t)gridDim.x * blockDim.x) {
     const KGroup &g = G.g[kgroup_of(G, e)];
     const int64_t local = e - g.start;
+    if (local >= g.count) continue;  // padding between groups
     const int64_t inst = local / g.total;
     const uint32_t el = (uint32_t)(local - inst * g.total);
     float2 f[3];
@@ -435,6 +449,7 @@ batch_forces_vjp_kernel(const float2 *__restrict__ gfk, float2 *__restrict__ gdk
        e += (int64_t)gridDim.x * blockDim.x) {
     const KGroup &g = G.g[kgroup_of(G, e)];
     const int64_t local = e - g.start;
+    if (local >= g.count) continue;  // padding between groups
     const int64_t inst = local / g.total;
     const uint32_t el = (uint32_t)(local - inst * g.total);
     const float2 *v3 = gfk + 3 * g.start + inst * 3 * (int64_t)g.total + el;
@@ -459,6 +474,7 @@ int kspace_batched(const Plan &P, const float2 *in, float2 *out, float r_split, 
       kg.total = (uint32_t)((int64_t)gr.nx * gr.ny * kg.nzh);
       kg.scale = 1.0f / (float)((int64_t)gr.nx * gr.ny * gr.nz);
       kg.start = gr.spec;
+      kg.count = (int64_t)gr.n * kg.total;
     }
     G.begin = G.g[0].start;
     const Group &last = P.groups[g0 + G.count - 1];
@@ -508,8 +524,10 @@ int batch_density(const Plan &P, void *ws, const float *pos, cudaStream_t s) {
   float *mesh = BW(float, P.o_mesh);
   PMGB_CUDA(cudaMemsetAsync(mesh, 0, (size_t)P.cells * 4, s));
   if (P.blocks == 0) return PMGB_OK;
+  // scalar reductions: lattice-ordered particles of a warp hit consecutive
+  // cells, which the vector form would serialise (measured slower here)
   batch_paint_kernel<<<(unsigned)P.blocks, BT, 0, s>>>(desc(P, ws), (int)P.sims.size(), mesh, 0,
-                                                       pos);
+                                                       pos, false);
   PMGB_LAUNCHED("batch_paint_kernel");
   return PMGB_OK;
 }
@@ -562,7 +580,8 @@ int cic_paint_batched(const pmgb_sim *t, int n, float *meshes, const float *pos,
   PMGB_TRY(bind(t, n, ws, bytes, &P));
   PMGB_CUDA(cudaMemsetAsync(meshes, 0, (size_t)P.cells * 4, s));
   if (P.blocks == 0) return PMGB_OK;
-  batch_paint_kernel<<<(unsigned)P.blocks, BT, 0, s>>>(desc(P, ws), n, meshes, 1, pos);
+  const bool vec = reinterpret_cast<uintptr_t>(meshes) % 16 == 0;
+  batch_paint_kernel<<<(unsigned)P.blocks, BT, 0, s>>>(desc(P, ws), n, meshes, 1, pos, vec);
   PMGB_LAUNCHED("batch_paint_kernel");
   return PMGB_OK;
 }
@@ -606,7 +625,7 @@ int fpm_step_batched_vjp(const pmgb_sim *t, int n, const float *pos, float *gpos
   PMGB_CUDA(cudaMemsetAsync(g3, 0, (size_t)P.cells * 3 * 4, s));
   if (P.blocks > 0) {
     batch_adj_paint_kernel<<<(unsigned)P.blocks, BT, 0, s>>>(desc(P, ws), n, g3, pos, gpos,
-                                                             gvel, kick, drift);
+                                                             gvel, kick, drift, false);
     PMGB_LAUNCHED("batch_adj_paint_kernel");
   }
   PMGB_TRY(batch_mesh_forces_vjp(P, ws, r_split, s));

@@ -15,10 +15,13 @@ namespace pmgb {
 // ---------------------------------------------------------------------------
 // Plain painter: one thread per particle, eight fp32 global atomics.
 // ---------------------------------------------------------------------------
+// The eight weights are those of the reference's neighbour list; the two
+// z-neighbours of each (x, y) pair go out as one vector reduction when
+// they share a 16-byte group (red_zpair).
 __global__ void __launch_bounds__(256)
 paint_atomic_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
                     const float *__restrict__ pos, int64_t np,
-                    const float *__restrict__ weights, float wscale) {
+                    const float *__restrict__ weights, float wscale, bool vec) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
        p += (int64_t)gridDim.x * blockDim.x) {
     float x, y, z;
@@ -26,15 +29,12 @@ paint_atomic_kernel(float *__restrict__ mesh, int nx, int ny, int nz,
     float wp = weights ? __fmul_rn(wscale, __ldg(weights + p)) : wscale;
     Axis ax = cic_axis(x, nx), ay = cic_axis(y, ny), az = cic_axis(z, nz);
 #pragma unroll
-    for (int n = 0; n < 8; ++n) {
-      float kx = conn_x(n) ? ax.k1 : ax.k0;
-      float ky = conn_y(n) ? ay.k1 : ay.k0;
-      float kz = conn_z(n) ? az.k1 : az.k0;
-      float w = __fmul_rn(wp, __fmul_rn(__fmul_rn(kx, ky), kz));
-      int ix = conn_x(n) ? ax.i1 : ax.i0;
-      int iy = conn_y(n) ? ay.i1 : ay.i0;
-      int iz = conn_z(n) ? az.i1 : az.i0;
-      atomicAdd(mesh + cell_index(ix, iy, iz, ny, nz), w);
+    for (int c = 0; c < 4; ++c) {
+      const int cx = c & 1, cy = c >> 1;
+      const float kxy = __fmul_rn(cx ? ax.k1 : ax.k0, cy ? ay.k1 : ay.k0);
+      float *row = mesh + cell_index(cx ? ax.i1 : ax.i0, cy ? ay.i1 : ay.i0, 0, ny, nz);
+      red_zpair(row, az.i0, az.i1, __fmul_rn(wp, __fmul_rn(kxy, az.k0)),
+                __fmul_rn(wp, __fmul_rn(kxy, az.k1)), vec);
     }
   }
 }
@@ -336,7 +336,8 @@ int paint(float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
   if (np == 0) return PMGB_OK;
   if (mode == PMGB_PAINT_ATOMIC) {
     paint_atomic_kernel<<<grid_for(np, 256), 256, 0, s>>>(mesh, nx, ny, nz, pos, np,
-                                                           weights, wscale);
+                                                           weights, wscale,
+                                                           zpair_vec_ok(mesh, nz));
     PMGB_LAUNCHED("paint_atomic_kernel");
     return PMGB_OK;
   }
@@ -402,7 +403,8 @@ int read_vjp(const float *mesh, int nx, int ny, int nz, const float *pos, int64_
   if (np == 0) return PMGB_OK;
   if (g_mesh) {
     paint_atomic_kernel<<<grid_for(np, 256), 256, 0, s>>>(g_mesh, nx, ny, nz, pos, np,
-                                                           g_out, 1.0f);
+                                                           g_out, 1.0f,
+                                                           zpair_vec_ok(g_mesh, nz));
     PMGB_LAUNCHED("paint_atomic_kernel");
   }
   if (g_pos) {
