@@ -591,6 +591,35 @@ int pmgb_fpm_step_batched_vjp_f32(const pmgb_sim *sims, int n_sims,
                                   float r_split, void *workspace,
                                   size_t workspace_bytes, pmgb_stream_t stream);
 
+/* ---- snapshots (np.save of fields, notebooks/05-MultiHost_PM.py:151-177) - */
+
+typedef struct pmgb_snapshot pmgb_snapshot; /* opaque */
+
+/* The NumPy .npy (format 1.0) header of a C-order array of dtype `descr`
+ * (e.g. "<f4", "<c8", "<u4") and `shape`: writes it to buf when cap is
+ * large enough and returns its length in bytes (a multiple of 64; 0 for
+ * invalid arguments).  Host only. */
+size_t pmgb_npy_header(const char *descr, const int64_t *shape, int ndim,
+                       char *buf, size_t cap);
+
+/* Starts writing the device array `array` (C order, `itemsize` bytes per
+ * element, dtype `descr`) to the .npy file `path` and returns at once.  The
+ * array's state is taken in stream order: with `staging` (device memory of
+ * at least the array's bytes) by a device-to-device copy on `stream`, so the
+ * caller may overwrite the array right away; with staging NULL the caller
+ * must not modify the array until pmgb_snapshot_wait returns.  A host thread
+ * then copies the data through pinned memory on its own stream and writes
+ * the file.  Every started snapshot must be joined with pmgb_snapshot_wait. */
+int pmgb_snapshot_begin_npy(const char *path, const void *array,
+                            const char *descr, int itemsize,
+                            const int64_t *shape, int ndim, void *staging,
+                            size_t staging_bytes, pmgb_stream_t stream,
+                            pmgb_snapshot **snapshot);
+
+/* Waits for the snapshot's file to be complete, releases it and returns its
+ * status (file or CUDA errors of the writer thread). */
+int pmgb_snapshot_wait(pmgb_snapshot *snapshot);
+
 #ifdef __cplusplus
 }
 #endif

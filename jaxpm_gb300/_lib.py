@@ -108,6 +108,10 @@ SIGNATURES = {
     "pmgb_power_spectrum_f32": (c_int, [P, c_int, c_int, c_int, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, P, c_int, P, P, P, P]),
     "pmgb_lpt2_source_vjp_f32": (c_int, [P, P, P, c_int, c_int, c_int, P, c_size_t, P]),
+    "pmgb_npy_header": (c_size_t, [ctypes.c_char_p, P, c_int, P, c_size_t]),
+    "pmgb_snapshot_begin_npy": (c_int, [ctypes.c_char_p, P, ctypes.c_char_p, c_int, P, c_int, P,
+                                        c_size_t, P, P]),
+    "pmgb_snapshot_wait": (c_int, [P]),
     "pmgb_batch_workspace_size": (c_size_t, [P, c_int]),
     "pmgb_batch_init": (c_int, [P, c_int, P, c_size_t, P]),
     "pmgb_batch_release": (c_int, [P]),

@@ -767,4 +767,32 @@ int pmgb_fpm_step_batched_vjp_f32(const pmgb_sim *sims, int n_sims, const float 
                               workspace_bytes, stream);
 }
 
+size_t pmgb_npy_header(const char *descr, const int64_t *shape, int ndim, char *buf,
+                       size_t cap) {
+  BEGIN();
+  if (!descr || ndim < 0 || ndim > 32 || (ndim > 0 && !shape)) return 0;
+  return npy_header(descr, shape, ndim, buf, cap);
+}
+
+int pmgb_snapshot_begin_npy(const char *path, const void *array, const char *descr,
+                            int itemsize, const int64_t *shape, int ndim, void *staging,
+                            size_t staging_bytes, pmgb_stream_t stream,
+                            pmgb_snapshot **snapshot) {
+  BEGIN();
+  NEED(path);
+  NEED(array);
+  NEED(descr);
+  NEED(snapshot);
+  PMGB_REQUIRE(ndim >= 0 && ndim <= 32, "ndim must be in 0..32");
+  PMGB_REQUIRE(ndim == 0 || shape != nullptr, "shape is NULL");
+  PMGB_REQUIRE(itemsize > 0 && itemsize <= 16, "itemsize must be in 1..16");
+  return snapshot_begin_npy(path, array, descr, itemsize, shape, ndim, staging, staging_bytes,
+                            stream, reinterpret_cast<Snapshot **>(snapshot));
+}
+
+int pmgb_snapshot_wait(pmgb_snapshot *snapshot) {
+  BEGIN();
+  return snapshot_wait(reinterpret_cast<Snapshot *>(snapshot));
+}
+
 }  // extern "C"

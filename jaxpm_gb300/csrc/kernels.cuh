@@ -219,4 +219,12 @@ int fpm_step_batched_vjp(const pmgb_sim *t, int n, const float *pos, float *gpos
                          const float *kick, const float *drift, float r_split, void *ws,
                          size_t bytes, cudaStream_t s);
 
+// snapshot.cu
+struct Snapshot;
+size_t npy_header(const char *descr, const int64_t *shape, int ndim, char *buf, size_t cap);
+int snapshot_begin_npy(const char *path, const void *dev, const char *descr, int itemsize,
+                       const int64_t *shape, int ndim, void *staging, size_t staging_bytes,
+                       cudaStream_t s, Snapshot **out);
+int snapshot_wait(Snapshot *snap);
+
 }  // namespace pmgb

@@ -104,3 +104,24 @@ def test_batched_table_queries(lib):
         _lib.call("pmgb_fpm_step_batched_f32", t, len(shapes), None, None, None, None, 0.0,
                   None, None, 0, None)
     assert "pos is NULL" in str(e.value)
+
+
+@pytest.mark.parametrize("shape", [(), (7,), (3, 4), (2, 1000000, 3), (16, 16, 9)])
+@pytest.mark.parametrize("descr", ["<f4", "<c8", "<u4"])
+def test_npy_header_is_read_by_numpy(lib, shape, descr):
+    """The snapshot writer's .npy header (host-only): numpy parses it and
+    finds the dtype and shape, and it is a multiple of 64 bytes."""
+    import io
+    from jaxpm_gb300 import _lib
+    arr = (ctypes.c_int64 * max(len(shape), 1))(*shape)
+    n = lib.pmgb_npy_header(descr.encode(), ctypes.cast(arr, ctypes.c_void_p), len(shape),
+                            None, 0)
+    assert n % 64 == 0 and n > 0
+    buf = ctypes.create_string_buffer(n)
+    assert lib.pmgb_npy_header(descr.encode(), ctypes.cast(arr, ctypes.c_void_p), len(shape),
+                               buf, n) == n
+    f = io.BytesIO(buf.raw)
+    assert np.lib.format.read_magic(f) == (1, 0)
+    got_shape, fortran, dtype = np.lib.format.read_array_header_1_0(f)
+    assert got_shape == tuple(shape) and not fortran and dtype == np.dtype(descr)
+    assert f.tell() == n
