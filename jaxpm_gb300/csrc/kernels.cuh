@@ -115,7 +115,8 @@ int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos,
 int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz,
                const float *pos, float *pos_out, float *vel, int64_t np,
                float kick, float drift, void *sort_ws, size_t sort_bytes,
-               unsigned *stats, cudaStream_t s, float *mesh_next = nullptr);
+               unsigned *stats, cudaStream_t s, float *mesh_next = nullptr,
+               bool pot = false);
 // n_steps sorted steps with the paint of each next density fused into the
 // gather; the state ping-pongs between the a and b buffers (in a after an
 // even number of steps).  kick/drift: host arrays of n_steps.
@@ -193,6 +194,10 @@ int spectral_c2r(void *in, float *out, int nx, int ny, int nz, int batch,
 int spectral_forces(const float *mesh, void *spec, void *fspec, float *f3,
                     int nx, int ny, int nz, float r_split, int order, int fd,
                     float scale, cudaStream_t s);
+// mesh -> spec -> pot [nx][ny][nz]: the potential whose order-1 stencil
+// gradient gives the forces of spectral_forces (order 1, fd 0).
+int spectral_potential(const float *mesh, void *spec, float *pot, int nx, int ny, int nz,
+                       float r_split, float scale, cudaStream_t s);
 // g3 [3][nx][ny][nz] -> spec3 -> dspec -> rbar: the adjoint of the above.
 int spectral_forces_vjp(const float *g3, void *spec3, void *dspec, float *rbar,
                         int nx, int ny, int nz, float r_split, int order,

@@ -437,6 +437,70 @@ constexpr int FBOX = 3 * TBOX;  // three force components, [c][x][y][z(12)]
 constexpr uint32_t FBOX_BYTES = FBOX * sizeof(float);
 constexpr int FBOX_STRIDE = (FBOX + 31) / 32 * 32;  // buffers 128-byte aligned
 
+// Potential box of the gather that derives the forces from the potential
+// (the run loop): the tile's force box needs the potential two cells beyond
+// it on each side along each axis (the order-1 gradient kernel
+// (8 sin w - sin 2w)/6 of jaxpm/kernels.py:41-66 is the transfer function
+// of the stencil (8 (p[+1] - p[-1]) - (p[+2] - p[-2])) / 12), so 13 x 13
+// cells in x and y; in z the box starts 4 cells before the tile (a TMA
+// load's innermost coordinate must be 16-byte aligned) and spans 16.
+constexpr int PBX = TB + 4, PBY = TB + 4, PBZ = 16;
+constexpr int PBOX = PBX * PBY * PBZ;
+constexpr uint32_t PBOX_BYTES = PBOX * sizeof(float);
+static_assert(PBOX <= FBOX_STRIDE, "potential box must fit a force-box buffer");
+
+__device__ __forceinline__ bool pot_interior(int ox, int oy, int oz, int nx, int ny, int nz) {
+  return ox >= 2 && oy >= 2 && oz >= 4 && ox + TB + 2 <= nx && oy + TB + 2 <= ny &&
+         oz + PBZ - 4 <= nz;
+}
+
+// -(i g(w)) applied to the potential along `axis` at box entry q (stride st
+// between neighbours along the axis): the force component.
+__device__ __forceinline__ float stencil_force(const float *p, int q, int st) {
+  const float t1 = p[q + st] - p[q - st];
+  const float t2 = p[q + 2 * st] - p[q - 2 * st];
+  return (t2 - 8.0f * t1) * (1.0f / 12.0f);
+}
+
+// The same at mesh cell (ix, iy, iz) from the potential in global memory
+// (wrapped neighbours), for particles found outside their tile.
+__device__ __forceinline__ float stencil_force_global(const float *__restrict__ pot, int ix,
+                                                      int iy, int iz, int axis, int nx, int ny,
+                                                      int nz) {
+  float v[5];
+#pragma unroll
+  for (int d = -2; d <= 2; ++d) {
+    if (d == 0) continue;
+    const int x = axis == 0 ? wrap_index(ix + d, nx) : ix;
+    const int y = axis == 1 ? wrap_index(iy + d, ny) : iy;
+    const int z = axis == 2 ? wrap_index(iz + d, nz) : iz;
+    v[d + 2] = __ldg(pot + cell_index(x, y, z, ny, nz));
+  }
+  const float t1 = v[3] - v[1], t2 = v[4] - v[0];
+  return (t2 - 8.0f * t1) * (1.0f / 12.0f);
+}
+
+// The CIC-interpolated force of a particle (axes ax, ay, az) from the
+// potential in global memory; out of line, it is the rare path and would
+// otherwise crowd the gather's registers.
+__device__ __noinline__ void pot_gather_global(const float *__restrict__ pot, Axis ax, Axis ay,
+                                               Axis az, int nx, int ny, int nz, float *a) {
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+#pragma unroll 1
+  for (int n = 0; n < 8; ++n) {
+    const float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                              conn_z(n) ? az.k1 : az.k0);
+    const int ix = conn_x(n) ? ax.i1 : ax.i0, iy = conn_y(n) ? ay.i1 : ay.i0,
+              iz = conn_z(n) ? az.i1 : az.i0;
+    a0 += stencil_force_global(pot, ix, iy, iz, 0, nx, ny, nz) * w;
+    a1 += stencil_force_global(pot, ix, iy, iz, 1, nx, ny, nz) * w;
+    a2 += stencil_force_global(pot, ix, iy, iz, 2, nx, ny, nz) * w;
+  }
+  a[0] = a0;
+  a[1] = a1;
+  a[2] = a2;
+}
+
 struct TileInfo {
   unsigned beg, end;
   int ox, oy, oz;
@@ -444,14 +508,17 @@ struct TileInfo {
 };
 
 __device__ __forceinline__ TileInfo tile_info(const unsigned *__restrict__ offsets, uint32_t key,
-                                              int nx, int ny, int nz, int use_tma) {
+                                              int nx, int ny, int nz, int use_tma,
+                                              bool pot = false) {
   TileInfo t;
   t.beg = __ldg(offsets + key);
   t.end = __ldg(offsets + key + 1);
   t.ox = (int)compact3(key >> 2) * TILE;
   t.oy = (int)compact3(key >> 1) * TILE;
   t.oz = (int)compact3(key) * TILE;
-  t.tma = use_tma && t.beg != t.end && box_interior(t.ox, t.oy, t.oz, nx, ny, nz);
+  t.tma = use_tma && t.beg != t.end &&
+          (pot ? pot_interior(t.ox, t.oy, t.oz, nx, ny, nz)
+               : box_interior(t.ox, t.oy, t.oz, nx, ny, nz));
   return t;
 }
 
@@ -474,7 +541,9 @@ __device__ __forceinline__ void zero_words(unsigned *p, int words, int tid) {
   for (int q = tid; q < words / 4; q += TILE_THREADS) z4[q] = make_uint4(0u, 0u, 0u, 0u);
 }
 
-template <bool PAINT>
+// POT: f3 is the potential mesh (cs unused) and tmap its 3-D map; each
+// tile's force box is computed from the staged potential box.
+template <bool PAINT, bool POT = false>
 __global__ void __launch_bounds__(TILE_THREADS, 4)
 rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int nz,
                  const float *pos, float *pos_out, float *__restrict__ vel,
@@ -484,8 +553,10 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
                  int use_tma, float *__restrict__ mesh_next, int pvec,
                  const __grid_constant__ CUtensorMap pmap, int use_ptma) {
   __shared__ __align__(128) float fb[2][FBOX_STRIDE];
+  __shared__ __align__(16) float ff[POT ? FBOX : 4];  // POT: the tile's force box
   __shared__ __align__(8) uint64_t bar[2];
   extern __shared__ __align__(128) unsigned pbox[];  // PAINT: 2 x NBOX_WORDS
+  constexpr uint32_t BOX_BYTES = POT ? PBOX_BYTES : FBOX_BYTES;
   const int tid = threadIdx.x;
   if (tid == 0) {
     mbar_init(&bar[0], 1);
@@ -499,10 +570,11 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
   const uint32_t stride = gridDim.x;
   uint32_t key = blockIdx.x;
   if (key >= nkeys) return;
-  TileInfo cur = tile_info(offsets, key, nx, ny, nz, use_tma);
+  TileInfo cur = tile_info(offsets, key, nx, ny, nz, use_tma, POT);
   if (cur.tma && tid == 0) {
-    mbar_expect_tx(&bar[0], FBOX_BYTES);
-    tma_load_4d(fb[0], &tmap, cur.oz, cur.oy, cur.ox, 0, &bar[0]);
+    mbar_expect_tx(&bar[0], BOX_BYTES);
+    if (POT) tma_load_3d(fb[0], &tmap, cur.oz - 4, cur.oy - 2, cur.ox - 2, &bar[0]);
+    else tma_load_4d(fb[0], &tmap, cur.oz, cur.oy, cur.ox, 0, &bar[0]);
   }
   int buf = 0;
   for (; key < nkeys; key += stride) {
@@ -512,11 +584,14 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
     TileInfo nxt;
     nxt.tma = false;
     if (knext < nkeys) {
-      nxt = tile_info(offsets, knext, nx, ny, nz, use_tma);
+      nxt = tile_info(offsets, knext, nx, ny, nz, use_tma, POT);
       if (nxt.tma && tid == 0) {
         fence_async_shared();
-        mbar_expect_tx(&bar[buf ^ 1], FBOX_BYTES);
-        tma_load_4d(fb[buf ^ 1], &tmap, nxt.oz, nxt.oy, nxt.ox, 0, &bar[buf ^ 1]);
+        mbar_expect_tx(&bar[buf ^ 1], BOX_BYTES);
+        if (POT)
+          tma_load_3d(fb[buf ^ 1], &tmap, nxt.oz - 4, nxt.oy - 2, nxt.ox - 2, &bar[buf ^ 1]);
+        else
+          tma_load_4d(fb[buf ^ 1], &tmap, nxt.oz, nxt.oy, nxt.ox, 0, &bar[buf ^ 1]);
       }
     }
     if (cur.beg != cur.end) {
@@ -530,6 +605,14 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
           return;
         }
         if (buf) phase1 ^= 1u; else phase0 ^= 1u;
+      } else if (POT) {
+        for (int q = tid; q < PBOX; q += TILE_THREADS) {
+          const int zc = q % PBZ, r = q / PBZ, yc = r % PBY, xc = r / PBY;
+          box[q] = __ldg(f3 + cell_index(wrap_index(cur.ox - 2 + xc, nx),
+                                         wrap_index(cur.oy - 2 + yc, ny),
+                                         wrap_index(cur.oz - 4 + zc, nz), ny, nz));
+        }
+        __syncthreads();
       } else {
         for (int q = tid; q < 3 * TB * TB * TB; q += TILE_THREADS) {
           const int c = q % TB, r = q / TB, b = r % TB, r2 = r / TB, a = r2 % TB, comp = r2 / TB;
@@ -538,6 +621,18 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
           box[((comp * TB + a) * TB + b) * TBZ + c] = __ldg(f3 + comp * cs + cell);
         }
         __syncthreads();
+      }
+      if (POT) {
+        // the tile's force box from the potential box (box cell (a, b, c) is
+        // potential entry (a + 2, b + 2, c + 4))
+        for (int q = tid; q < 3 * TB * TB * TB; q += TILE_THREADS) {
+          const int c = q % TB, r = q / TB, b = r % TB, r2 = r / TB, a = r2 % TB, comp = r2 / TB;
+          const int pq = ((a + 2) * PBY + b + 2) * PBZ + c + 4;
+          const int st = comp == 0 ? PBY * PBZ : (comp == 1 ? PBZ : 1);
+          ff[((comp * TB + a) * TB + b) * TBZ + c] = stencil_force(box, pq, st);
+        }
+        __syncthreads();
+        box = ff;
       }
       // every lane of a warp runs the same iterations (ballot / match inside);
       // each thread loads RKD_ILP particles before computing any of them
@@ -578,6 +673,13 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
               a1 += box[TBOX + q] * w;
               a2 += box[2 * TBOX + q] * w;
             }
+          } else if (POT) {
+            if (stats) atomicAdd(stats + 1, 1u);
+            float a[3];
+            pot_gather_global(f3, ax, ay, az, nx, ny, nz, a);
+            a0 = a[0];
+            a1 = a[1];
+            a2 = a[2];
           } else {
             if (stats) atomicAdd(stats + 1, 1u);
 #pragma unroll
@@ -1090,21 +1192,31 @@ int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos, int64_t 
 // drifted positions go to pos_out (pos itself for an in-place update).  With
 // mesh_next, the new positions are also painted there (overwritten): the
 // density of the next step.
+// f3: the three force meshes (component stride cs), or with `pot` the
+// potential mesh from which the gather derives them.
 int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float *pos,
                float *pos_out, float *vel, int64_t np, float kick, float drift, void *sort_ws,
-               size_t sort_bytes, unsigned *stats, cudaStream_t s, float *mesh_next) {
+               size_t sort_bytes, unsigned *stats, cudaStream_t s, float *mesh_next, bool pot) {
   PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
   const int64_t keys = tile_key_count(nx, ny, nz);
   SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
   PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
   if (np == 0) return PMGB_OK;
-  // TMA prefetch of interior force boxes: a 4-D map (z, y, x, component),
-  // box 12 x 9 x 9 x 3
+  // TMA prefetch of interior boxes: forces, a 4-D map (z, y, x, component)
+  // with box 12 x 9 x 9 x 3; potential, a 3-D map with box 16 x 13 x 13
   CUtensorMap map;
   memset(&map, 0, sizeof(map));
   int use_tma = 0;
-  if (nz % 4 == 0 && cs % 4 == 0 && reinterpret_cast<uintptr_t>(f3) % 16 == 0 && nz >= TBZ &&
-      ny >= TB && nx >= TB) {
+  const bool al = nz % 4 == 0 && reinterpret_cast<uintptr_t>(f3) % 16 == 0;
+  if (pot) {
+    if (al && nz >= PBZ && ny >= PBY && nx >= PBX) {
+      const uint64_t dims[3] = {(uint64_t)nz, (uint64_t)ny, (uint64_t)nx};
+      const uint64_t strides[2] = {(uint64_t)nz * 4, (uint64_t)ny * nz * 4};
+      const uint32_t box[3] = {PBZ, PBY, PBX};
+      use_tma = make_tensor_map(&map, f3, 3, dims, strides, box) == PMGB_OK ? 1 : 0;
+      clear_error();
+    }
+  } else if (al && cs % 4 == 0 && nz >= TBZ && ny >= TB && nx >= TB) {
     const uint64_t dims[4] = {(uint64_t)nz, (uint64_t)ny, (uint64_t)nx, 3};
     const uint64_t strides[3] = {(uint64_t)nz * 4, (uint64_t)ny * nz * 4, (uint64_t)cs * 4};
     const uint32_t box[4] = {TBZ, TB, TB, 3};
@@ -1113,40 +1225,46 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float 
   }
   CUtensorMap pmap;
   memset(&pmap, 0, sizeof(pmap));
-  static bool ready[2][64] = {{false}};
+  static bool ready[4][64] = {{false}};
   int dev = 0;
   PMGB_CUDA(cudaGetDevice(&dev));
-  if (!mesh_next) {
-    if (dev >= 64 || !ready[0][dev]) {
-      PMGB_TRY(set_smem((const void *)rkd_tiles_kernel<false>, 0));
-      if (dev < 64) ready[0][dev] = true;
-    }
-    rkd_tiles_kernel<false><<<tile_grid(keys), TILE_THREADS, 0, s>>>(
-        f3, cs, nx, ny, nz, pos, pos_out, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts,
-        sc.rank, stats, map, use_tma, nullptr, 0, pmap, 0);
-    PMGB_LAUNCHED("rkd_tiles_kernel");
-    return PMGB_OK;
+  const int variant = (mesh_next ? 1 : 0) + (pot ? 2 : 0);
+  const void *fn = variant == 0   ? (const void *)rkd_tiles_kernel<false, false>
+                   : variant == 1 ? (const void *)rkd_tiles_kernel<true, false>
+                   : variant == 2 ? (const void *)rkd_tiles_kernel<false, true>
+                                  : (const void *)rkd_tiles_kernel<true, true>;
+  const size_t dsmem = mesh_next ? RKDP_SMEM : 0;
+  if (dev >= 64 || !ready[variant][dev]) {
+    PMGB_TRY(set_smem(fn, dsmem));
+    if (dev < 64) ready[variant][dev] = true;
   }
-  const int64_t ncell = (int64_t)nx * ny * nz;
-  PMGB_CUDA(cudaMemsetAsync(mesh_next, 0, ncell * sizeof(float), s));
-  const bool aligned = nz % 4 == 0 && reinterpret_cast<uintptr_t>(mesh_next) % 16 == 0;
   int use_ptma = 0;
-  if (aligned && nz >= NBZ && ny >= NB && nx >= NB) {
-    // 3-D map of the density mesh, box 16 x 11 x 11 (the paint box)
-    const uint64_t dims[3] = {(uint64_t)nz, (uint64_t)ny, (uint64_t)nx};
-    const uint64_t strides[2] = {(uint64_t)nz * 4, (uint64_t)ny * nz * 4};
-    const uint32_t box[3] = {NBZ, NB, 1};  // one x-plane of the paint box
-    use_ptma = make_tensor_map(&pmap, mesh_next, 3, dims, strides, box) == PMGB_OK ? 1 : 0;
-    clear_error();
+  bool aligned = false;
+  if (mesh_next) {
+    const int64_t ncell = (int64_t)nx * ny * nz;
+    PMGB_CUDA(cudaMemsetAsync(mesh_next, 0, ncell * sizeof(float), s));
+    aligned = nz % 4 == 0 && reinterpret_cast<uintptr_t>(mesh_next) % 16 == 0;
+    if (aligned && nz >= NBZ && ny >= NB && nx >= NB) {
+      // 3-D map of the density mesh, box 12 x 9 x 1 (one x-plane of the paint box)
+      const uint64_t dims[3] = {(uint64_t)nz, (uint64_t)ny, (uint64_t)nx};
+      const uint64_t strides[2] = {(uint64_t)nz * 4, (uint64_t)ny * nz * 4};
+      const uint32_t box[3] = {NBZ, NB, 1};
+      use_ptma = make_tensor_map(&pmap, mesh_next, 3, dims, strides, box) == PMGB_OK ? 1 : 0;
+      clear_error();
+    }
   }
-  if (dev >= 64 || !ready[1][dev]) {
-    PMGB_TRY(set_smem((const void *)rkd_tiles_kernel<true>, RKDP_SMEM));
-    if (dev < 64) ready[1][dev] = true;
+#define RKD_ARGS                                                                             \
+  f3, cs, nx, ny, nz, pos, pos_out, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts, \
+      sc.rank, stats, map, use_tma, mesh_next, aligned ? 1 : 0, pmap, use_ptma
+  const unsigned grid = tile_grid(keys);
+  switch (variant) {
+    case 0: rkd_tiles_kernel<false, false><<<grid, TILE_THREADS, dsmem, s>>>(RKD_ARGS); break;
+    case 1: rkd_tiles_kernel<true, false><<<grid, TILE_THREADS, dsmem, s>>>(RKD_ARGS); break;
+    case 2: rkd_tiles_kernel<false, true><<<grid, TILE_THREADS, dsmem, s>>>(RKD_ARGS); break;
+    default: rkd_tiles_kernel<true, true><<<grid, TILE_THREADS, dsmem, s>>>(RKD_ARGS); break;
   }
-  rkd_tiles_kernel<true><<<tile_grid(keys), TILE_THREADS, RKDP_SMEM, s>>>(
-      f3, cs, nx, ny, nz, pos, pos_out, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts,
-      sc.rank, stats, map, use_tma, mesh_next, aligned ? 1 : 0, pmap, use_ptma);
-  PMGB_LAUNCHED("rkd_tiles_kernel<paint>");
+#undef RKD_ARGS
+  PMGB_LAUNCHED("rkd_tiles_kernel");
   return PMGB_OK;
 }
 
@@ -1258,8 +1376,20 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, flo
   unsigned *I[2] = {id_a, id_b};
   Aux *aux;
   PMGB_TRY(aux_stream(&aux));
+  // Forces from the potential where the spectral pipeline serves the mesh:
+  // one inverse transform instead of three, the order-1 gradient taken by
+  // the gather as the equivalent real-space stencil (f3 then holds the
+  // potential).
+  const bool pot = spectral_enabled() && spectral_supported(nx, ny, nz) && nz % 4 == 0 &&
+                   reinterpret_cast<uintptr_t>(mesh) % 16 == 0 &&
+                   reinterpret_cast<uintptr_t>(f3) % 16 == 0;
+  const float scale = 1.0f / (float)((int64_t)nx * ny * nz);
+  auto forces = [&]() -> int {
+    if (pot) return spectral_potential(mesh, dk, f3, nx, ny, nz, r_split, scale, s);
+    return mesh_forces(mesh, nx, ny, nz, r_split, dk, fk, f3, s);
+  };
   PMGB_TRY(paint_sorted(mesh, nx, ny, nz, pos_a, np, sort_ws, sort_bytes, stats, s));
-  PMGB_TRY(mesh_forces(mesh, nx, ny, nz, r_split, dk, fk, f3, s));
+  PMGB_TRY(forces());
   for (int i = 0; i < n_steps; ++i) {
     const int a = i & 1, b = a ^ 1;
     // the gather of step i needs step i-1's sort (positions in tile order,
@@ -1267,7 +1397,7 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, flo
     if (i > 0) PMGB_CUDA(cudaStreamWaitEvent(s, aux->sorted, 0));
     PMGB_TRY(rkd_sorted(f3, (int64_t)nx * ny * nz, nx, ny, nz, P[a], drifted, V[a], np, kick[i],
                         drift[i], sort_ws, sort_bytes, stats, s,
-                        i + 1 < n_steps ? mesh : nullptr));
+                        i + 1 < n_steps ? mesh : nullptr, pot));
     // the sort of step i (on the second stream) and the forces of step i+1
     // (from the density the gather just painted) are independent: they
     // touch disjoint buffers and overlap
@@ -1276,7 +1406,7 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, flo
     PMGB_TRY(tile_scatter(drifted, V[a], I[a], np, nx, ny, nz, P[b], V[b], I[b], nullptr,
                           sort_ws, sort_bytes, aux->s2));
     PMGB_CUDA(cudaEventRecord(aux->sorted, aux->s2));
-    if (i + 1 < n_steps) PMGB_TRY(mesh_forces(mesh, nx, ny, nz, r_split, dk, fk, f3, s));
+    if (i + 1 < n_steps) PMGB_TRY(forces());
   }
   // join: everything of the run is ordered before later work on s
   PMGB_CUDA(cudaStreamWaitEvent(s, aux->sorted, 0));

@@ -414,7 +414,7 @@ plane_c2r_kernel(const float2 *__restrict__ in, float *__restrict__ out, PlaneGe
 
 // ---- x pass -------------------------------------------------------------------
 
-enum XMode { X_FORWARD = 0, X_INVERSE = 1, X_FORCES = 2, X_FORCES_ADJ = 3 };
+enum XMode { X_FORWARD = 0, X_INVERSE = 1, X_FORCES = 2, X_FORCES_ADJ = 3, X_POTENTIAL = 4 };
 
 struct XGeom {
   int nx, ny, lgx, nzh, pitch, chunks;
@@ -493,6 +493,29 @@ xpass_kernel(const float2 *in, float2 *out, XGeom g, const float2 *__restrict__ 
       const int kx = i / XW, w = i % XW;
       out[gidx(kx, w)] = b0[dif_pos(kx, g.lgx) * XW + w];
     }
+    return;
+  }
+  if (MODE == X_POTENTIAL) {
+    // pot = (delta * invlaplace) * longrange * scale, inverse x transform
+    const AxisEntry Y = t.y[ky];
+    for (int i = tid; i < n; i += XPASS_THREADS) {
+      const int p = i / XW, w = i % XW, kz = kz0 + w;
+      float2 pv = make_float2(0.f, 0.f);
+      if (kz < g.nzh) {
+        Elem el;
+        el.X = t.x[dif_freq(p, g.lgx)];
+        el.Y = Y;
+        el.Z = t.z[kz];
+        const float inv = inv_laplace(el, fd), L = long_range(el, r2);
+        const float2 d = b0[i];
+        pv = make_float2(__fmul_rn(__fmul_rn(d.x, inv), L) * scale,
+                         __fmul_rn(__fmul_rn(d.y, inv), L) * scale);
+      }
+      b1[i] = pv;
+    }
+    __syncthreads();
+    fft_inverse<true>(b1, g.lgx, XW, 1, XW, twx, g.lgx, tid, XPASS_THREADS);
+    for (int i = tid; i < n; i += XPASS_THREADS) out[gidx(i / XW, i % XW)] = b1[i];
     return;
   }
   // X_FORCES
@@ -694,7 +717,7 @@ xpass_reg_kernel(const float2 *in, float2 *out, XGeom g, const float2 *__restric
   const int ky = blockIdx.x / g.chunks, kz0 = (blockIdx.x - ky * g.chunks) * XW;
   const int kz = kz0 + w;
   xload_twiddles<LG>(tw, twx, tid, T * XW);
-  if (MODE == X_FORCES || MODE == X_FORCES_ADJ) {
+  if (MODE == X_FORCES || MODE == X_FORCES_ADJ || MODE == X_POTENTIAL) {
     for (int i = tid; i < N; i += T * XW) {
       const AxisEntry X = t.x[i];
       xk[i] = make_float2(fd ? X.fdk2 : X.k2, order ? X.g1 : X.g0);
@@ -704,7 +727,7 @@ xpass_reg_kernel(const float2 *in, float2 *out, XGeom g, const float2 *__restric
   auto gidx = [&](int x) -> int64_t { return ((int64_t)x * g.ny + ky) * g.pitch + kz; };
   int flip = 0;
   float2 v[8];
-  if (MODE == X_FORWARD || MODE == X_FORCES) {
+  if (MODE == X_FORWARD || MODE == X_FORCES || MODE == X_POTENTIAL) {
 #pragma unroll
     for (int m = 0; m < 8; ++m) v[m] = in[gidx(b + T * m)];
     xforward<LG>(v, b, w, tw, buf0, buf1, flip);
@@ -739,6 +762,22 @@ xpass_reg_kernel(const float2 *in, float2 *out, XGeom g, const float2 *__restric
       L = expf(-k2 * r2);
     }
   };
+  if (MODE == X_POTENTIAL) {
+    // pot = (delta * invlaplace) * longrange * scale, one inverse transform
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
+      const int kx = xfreq<LG>(xpos<LG, NS - 1>(b, m));
+      float inv, L;
+      kfactor(kx, inv, L);
+      v[m] = live ? make_float2(__fmul_rn(__fmul_rn(v[m].x, inv), L) * scale,
+                                __fmul_rn(__fmul_rn(v[m].y, inv), L) * scale)
+                  : make_float2(0.f, 0.f);
+    }
+    xinverse<LG>(v, b, w, tw, buf0, buf1, flip);
+#pragma unroll
+    for (int m = 0; m < 8; ++m) out[gidx(b + T * m)] = v[m];
+    return;
+  }
   if (MODE == X_FORCES) {
     // pot = (delta * invlaplace) * longrange.  F_c = -(i g_c) pot: the x
     // component needs its own inverse x transform; g_y and g_z are constant
@@ -920,7 +959,8 @@ int xpass(const float2 *in, float2 *out, int nx, int ny, int nz, int pitch, int6
   const float2 *twx;
   PMGB_TRY(twiddles(nx, &twx));
   Tables t{nullptr, nullptr, nullptr};
-  if (MODE == X_FORCES || MODE == X_FORCES_ADJ) PMGB_TRY(tables(nx, ny, nz, &t));
+  if (MODE == X_FORCES || MODE == X_FORCES_ADJ || MODE == X_POTENTIAL)
+    PMGB_TRY(tables(nx, ny, nz, &t));
   const float r2 = r_split * r_split;
   switch (g.lgx) {
     case 6: return xpass_reg<6, MODE>(in, out, g, twx, t, r2, order, fd, scale, s);
@@ -1013,6 +1053,23 @@ int spectral_forces(const float *mesh, void *spec, void *fspec, float *f3, int n
   PMGB_TRY(planes_r2c(mesh, d, nx, ny, nz, pitch, s));
   PMGB_TRY(xpass<X_FORCES>(d, f, nx, ny, nz, pitch, cs, cs, r_split, order, fd, scale, s));
   PMGB_TRY(planes_c2r(f, f3, 3 * nx, ny, nz, pitch, s));
+  return PMGB_OK;
+}
+
+// mesh -> spec -> the potential pot = IFFT(delta_k * invlaplace * longrange
+// * scale) as a real mesh [nx][ny][nz]: the forces' pipeline with one
+// inverse transform instead of three (the order-1 gradient is then the
+// real-space stencil whose transfer function it is).  The x pass runs in
+// place on spec.
+int spectral_potential(const float *mesh, void *spec, float *pot, int nx, int ny, int nz,
+                       float r_split, float scale, cudaStream_t s) {
+  PMGB_TRY(check_spectral(nx, ny, nz));
+  const int pitch = spectral_pitch(nz);
+  const int64_t cs = (int64_t)nx * ny * pitch;
+  float2 *d = static_cast<float2 *>(spec);
+  PMGB_TRY(planes_r2c(mesh, d, nx, ny, nz, pitch, s));
+  PMGB_TRY(xpass<X_POTENTIAL>(d, d, nx, ny, nz, pitch, cs, cs, r_split, 1, 0, scale, s));
+  PMGB_TRY(planes_c2r(d, pot, nx, ny, nz, pitch, s));
   return PMGB_OK;
 }
 
