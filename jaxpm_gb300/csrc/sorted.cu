@@ -454,16 +454,11 @@ __device__ __forceinline__ bool pot_interior(int ox, int oy, int oz, int nx, int
          oz + PBZ - 4 <= nz;
 }
 
-// -(i g(w)) applied to the potential along `axis` at box entry q (stride st
-// between neighbours along the axis): the force component.
-__device__ __forceinline__ float stencil_force(const float *p, int q, int st) {
-  const float t1 = p[q + st] - p[q - st];
-  const float t2 = p[q + 2 * st] - p[q - 2 * st];
-  return (t2 - 8.0f * t1) * (1.0f / 12.0f);
-}
-
-// The same at mesh cell (ix, iy, iz) from the potential in global memory
-// (wrapped neighbours), for particles found outside their tile.
+// -(i g(w)) applied to the potential along `axis` at mesh cell (ix, iy, iz),
+// from the potential in global memory (wrapped neighbours): the force
+// component, (t2 - 8 t1) / 12 with t1 = p[+1] - p[-1], t2 = p[+2] - p[-2]
+// (the gather's box path computes the same expression), for particles found
+// outside their tile.
 __device__ __forceinline__ float stencil_force_global(const float *__restrict__ pot, int ix,
                                                       int iy, int iz, int axis, int nx, int ny,
                                                       int nz) {
@@ -624,12 +619,43 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
       }
       if (POT) {
         // the tile's force box from the potential box (box cell (a, b, c) is
-        // potential entry (a + 2, b + 2, c + 4))
-        for (int q = tid; q < 3 * TB * TB * TB; q += TILE_THREADS) {
-          const int c = q % TB, r = q / TB, b = r % TB, r2 = r / TB, a = r2 % TB, comp = r2 / TB;
-          const int pq = ((a + 2) * PBY + b + 2) * PBZ + c + 4;
-          const int st = comp == 0 ? PBY * PBZ : (comp == 1 ? PBZ : 1);
-          ff[((comp * TB + a) * TB + b) * TBZ + c] = stencil_force(box, pq, st);
+        // potential entry (a + 2, b + 2, c + 4)), four z cells per item with
+        // 16-byte shared loads: rows of 16 potentials, c0 = 0, 4, 8 (cells
+        // 9..11 are the rows' padding; their neighbours may read the next
+        // row, which stays inside the buffer)
+        for (int q = tid; q < TB * TB * 3; q += TILE_THREADS) {
+          const int c0 = 4 * (q % 3), r = q / 3, b = r % TB, a = r / TB;
+          const float *row = box + ((a + 2) * PBY + b + 2) * PBZ + c0;
+          const float4 z0 = *reinterpret_cast<const float4 *>(row);
+          const float4 zc = *reinterpret_cast<const float4 *>(row + 4);
+          const float4 z2 = *reinterpret_cast<const float4 *>(row + 8);
+          const float zz[12] = {z0.x, z0.y, z0.z, z0.w, zc.x, zc.y, zc.z, zc.w,
+                                z2.x, z2.y, z2.z, z2.w};
+          auto nb = [&](int off) { return *reinterpret_cast<const float4 *>(row + 4 + off); };
+          const float4 xm2 = nb(-2 * PBY * PBZ), xm1 = nb(-PBY * PBZ), xp1 = nb(PBY * PBZ),
+                       xp2 = nb(2 * PBY * PBZ);
+          const float4 ym2 = nb(-2 * PBZ), ym1 = nb(-PBZ), yp1 = nb(PBZ), yp2 = nb(2 * PBZ);
+          auto f = [](float m2, float m1, float p1, float p2) {
+            const float t1 = p1 - m1, t2 = p2 - m2;
+            return (t2 - 8.0f * t1) * (1.0f / 12.0f);
+          };
+          float4 fx, fy, fz;
+          fx.x = f(xm2.x, xm1.x, xp1.x, xp2.x);
+          fx.y = f(xm2.y, xm1.y, xp1.y, xp2.y);
+          fx.z = f(xm2.z, xm1.z, xp1.z, xp2.z);
+          fx.w = f(xm2.w, xm1.w, xp1.w, xp2.w);
+          fy.x = f(ym2.x, ym1.x, yp1.x, yp2.x);
+          fy.y = f(ym2.y, ym1.y, yp1.y, yp2.y);
+          fy.z = f(ym2.z, ym1.z, yp1.z, yp2.z);
+          fy.w = f(ym2.w, ym1.w, yp1.w, yp2.w);
+          fz.x = f(zz[2], zz[3], zz[5], zz[6]);
+          fz.y = f(zz[3], zz[4], zz[6], zz[7]);
+          fz.z = f(zz[4], zz[5], zz[7], zz[8]);
+          fz.w = f(zz[5], zz[6], zz[8], zz[9]);
+          const int o = (a * TB + b) * TBZ + c0;
+          *reinterpret_cast<float4 *>(ff + o) = fx;
+          *reinterpret_cast<float4 *>(ff + TBOX + o) = fy;
+          *reinterpret_cast<float4 *>(ff + 2 * TBOX + o) = fz;
         }
         __syncthreads();
         box = ff;
