@@ -229,6 +229,10 @@ def run_gb300(args):
     P = lambda name: _lib.ptr(buf[name])  # noqa: E731
     det_bytes = ncell * 8 if mode == _lib.PAINT_DETERMINISTIC else 0
 
+    # the sorted run loop takes the forces from the potential where the
+    # spectral pipeline serves the mesh (pmgb_fpm_run_sorted_f32); the phase
+    # pass issues the same kernels
+    use_pot = engine == "sorted" and fft_path != 0
     if engine == "sorted":
         eng = simulate.SortedFastPM((n,) * 3, cosmo, 0.1, 1.0, K, device=dev)
         kick, drift = eng.kick, eng.drift
@@ -273,11 +277,21 @@ def run_gb300(args):
             _lib.call("pmgb_cic_paint_f32", P("mesh"), nx, ny, nz, _lib.ptr(px), Np, None, 1.0,
                       mode, 0, P("det"), det_bytes, s)
         rec(1)
-        # density -> three force meshes (fused FFT pipeline, or cuFFT)
-        _lib.call("pmgb_mesh_forces_f32", P("mesh"), P("f3"), nx, ny, nz, 0.0, P("mfws"),
-                  mf_bytes, s)
+        if use_pot:
+            # density -> potential (the run loop's one inverse transform)
+            _lib.call("pmgb_mesh_potential_f32", P("mesh"), P("f3"), nx, ny, nz, 0.0, P("mfws"),
+                      mf_bytes, s)
+        else:
+            # density -> three force meshes (fused FFT pipeline, or cuFFT)
+            _lib.call("pmgb_mesh_forces_f32", P("mesh"), P("f3"), nx, ny, nz, 0.0, P("mfws"),
+                      mf_bytes, s)
         rec(2)
-        if engine == "sorted":
+        if use_pot:  # gather (forces from the potential) + kick + drift + next paint
+            _lib.call("pmgb_read_potential_kick_drift_paint_binned_f32", P("f3"), nx, ny, nz,
+                      _lib.ptr(px), _lib.ptr(pv), Np, float(kick[i]), float(drift[i]),
+                      P("mesh") if i + 1 < K else None, _lib.ptr(eng.sort_ws), eng.sort_bytes,
+                      _lib.ptr(eng.stats_buf), s)
+        elif engine == "sorted":
             if i + 1 < K:  # gather + kick + drift + paint of the next density
                 _lib.call("pmgb_read3_kick_drift_paint_binned_f32", P("f3"), ncell, nx, ny, nz,
                           _lib.ptr(px), _lib.ptr(pv), Np, float(kick[i]), float(drift[i]),
@@ -364,6 +378,8 @@ def run_gb300(args):
                                      f"2LPT a=0.1, {K} steps to a=1",
                          "particles": Np, "mesh": [n, n, n], "box_mpc_h": n * BOX_PER_CELL,
                          "engine": engine, "fft": ["cufft", "fused", "own"][fft_path],
+                         "forces": ("potential, order-1 gradient as a stencil in the gather"
+                                    if use_pot else "three force meshes"),
                          "paint_mode": {0: "atomic", 1: "binned",
                                                           2: "deterministic"}[mode],
                          "parallelism": "replicas" if world > 1 else "single",
@@ -382,7 +398,12 @@ def run_gb300(args):
     # 12 force + 24 read + 24 write, + 4 for the sorted loop's paint of the
     # next density (its paint phase runs once per run, so it has no per-step
     # roofline)
-    if engine == "sorted":
+    if use_pot:
+        # the potential pipeline: plane R2C 4 + 4, x pass 4 + 4, plane C2R
+        # 4 + 4; the gather reads the potential (4) instead of three force
+        # meshes (12)
+        alg = {"forces": 24.0, "read_kick_drift": 56.0}
+    elif engine == "sorted":
         alg = {"forces": 48.0, "read_kick_drift": 64.0}
     else:
         alg = {"paint": 16.0, "forces": 48.0, "read_kick_drift": 60.0}

@@ -219,6 +219,16 @@ int pmgb_mesh_forces_f32(const float *mesh, float *force3, int nx, int ny,
                          size_t workspace_bytes, pmgb_stream_t stream);
 
 /* Adjoint: g_mesh = sum_i (ifft3d K_i fft3d)^T g_force3[i]. */
+/* The potential of the run loop, pot = IFFT(delta_k * invlaplace *
+ * longrange) (pm.py:49-53) as a real mesh [nx][ny][nz], through the spectral
+ * pipeline (PMGB_ERR_UNSUPPORTED outside its shapes).  The forces of
+ * pmgb_mesh_forces_f32 are its order-1 gradient, the stencil
+ * (8 (p[+1] - p[-1]) - (p[+2] - p[-2])) / 12 per axis, negated.  Workspace:
+ * pmgb_mesh_forces_workspace_size. */
+int pmgb_mesh_potential_f32(const float *mesh, float *pot, int nx, int ny,
+                            int nz, float r_split, void *workspace,
+                            size_t workspace_bytes, pmgb_stream_t stream);
+
 int pmgb_mesh_forces_vjp_f32(const float *g_force3, float *g_mesh, int nx,
                              int ny, int nz, float r_split, void *workspace,
                              size_t workspace_bytes, pmgb_stream_t stream);
@@ -437,6 +447,19 @@ int pmgb_fpm_step_sorted_f32(const float *pos, float *vel, const uint32_t *id,
  * drift are HOST arrays of n_steps coefficients.  The state ping-pongs
  * between the a and b buffers: after the call it is in a when n_steps is
  * even, in b when odd. */
+/* pmgb_read3_kick_drift_paint_binned_f32 with the forces derived from the
+ * potential mesh (pmgb_mesh_potential_f32) in each tile's shared-memory box:
+ * the gather of the run loop.  mesh_next may be NULL (no paint). */
+int pmgb_read_potential_kick_drift_paint_binned_f32(const float *pot, int nx,
+                                                    int ny, int nz, float *pos,
+                                                    float *vel, int64_t np,
+                                                    float kick, float drift,
+                                                    float *mesh_next,
+                                                    void *sort_workspace,
+                                                    size_t sort_workspace_bytes,
+                                                    uint32_t *stats,
+                                                    pmgb_stream_t stream);
+
 int pmgb_fpm_run_sorted_f32(float *pos_a, float *vel_a, uint32_t *id_a,
                             float *pos_b, float *vel_b, uint32_t *id_b,
                             int64_t np, int nx, int ny, int nz, int n_steps,

@@ -59,6 +59,10 @@ SIGNATURES = {
     "pmgb_mesh_forces_workspace_size": (c_size_t, [c_int, c_int, c_int]),
     "pmgb_mesh_forces_f32": (c_int, [P, P, c_int, c_int, c_int, c_float, P, c_size_t, P]),
     "pmgb_mesh_forces_vjp_f32": (c_int, [P, P, c_int, c_int, c_int, c_float, P, c_size_t, P]),
+    "pmgb_mesh_potential_f32": (c_int, [P, P, c_int, c_int, c_int, c_float, P, c_size_t, P]),
+    "pmgb_read_potential_kick_drift_paint_binned_f32": (c_int, [P, c_int, c_int, c_int, P, P,
+                                                                c_int64, c_float, c_float, P, P,
+                                                                c_size_t, P, P]),
     "pmgb_kspace_forces_f32": (c_int, [P, P, c_int64, c_int, c_int, c_int, c_float, c_int, c_int,
                                        c_float, P]),
     "pmgb_kspace_forces_vjp_f32": (c_int, [P, c_int64, P, c_int, c_int, c_int, c_float, c_int,

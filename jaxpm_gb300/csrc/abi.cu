@@ -269,6 +269,17 @@ int pmgb_mesh_forces_f32(const float *mesh, float *force3, int nx, int ny, int n
   return mesh_forces_ws(mesh, force3, nx, ny, nz, r_split, workspace, workspace_bytes, stream);
 }
 
+int pmgb_mesh_potential_f32(const float *mesh, float *pot, int nx, int ny, int nz,
+                            float r_split, void *workspace, size_t workspace_bytes,
+                            pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NEED(mesh);
+  NEED(pot);
+  PMGB_REQUIRE(r_split >= 0.0f, "r_split must be non-negative");
+  return mesh_potential_ws(mesh, pot, nx, ny, nz, r_split, workspace, workspace_bytes, stream);
+}
+
 int pmgb_mesh_forces_vjp_f32(const float *g_force3, float *g_mesh, int nx, int ny, int nz,
                              float r_split, void *workspace, size_t workspace_bytes,
                              pmgb_stream_t stream) {
@@ -521,6 +532,28 @@ int pmgb_read3_kick_drift_paint_binned_f32(const float *force3, int64_t comp_str
   PMGB_REQUIRE(mesh_next != force3, "mesh_next must not alias the force meshes");
   return rkd_sorted(force3, comp_stride, nx, ny, nz, pos, pos, vel, np, kick, drift,
                     sort_workspace, sort_workspace_bytes, stats, stream, mesh_next);
+}
+
+int pmgb_read_potential_kick_drift_paint_binned_f32(const float *pot, int nx, int ny, int nz,
+                                                    float *pos, float *vel, int64_t np,
+                                                    float kick, float drift, float *mesh_next,
+                                                    void *sort_workspace,
+                                                    size_t sort_workspace_bytes, uint32_t *stats,
+                                                    pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  if (np == 0) {
+    if (mesh_next)
+      PMGB_CUDA(cudaMemsetAsync(mesh_next, 0, (size_t)nx * ny * nz * sizeof(float), stream));
+    return PMGB_OK;
+  }
+  NEED(pot);
+  NEED(pos);
+  NEED(vel);
+  NEED(sort_workspace);
+  PMGB_REQUIRE(mesh_next != pot, "mesh_next must not alias the potential");
+  return rkd_sorted(pot, (int64_t)nx * ny * nz, nx, ny, nz, pos, pos, vel, np, kick, drift,
+                    sort_workspace, sort_workspace_bytes, stats, stream, mesh_next, true);
 }
 
 int pmgb_fpm_run_sorted_f32(float *pos_a, float *vel_a, uint32_t *id_a, float *pos_b,

@@ -159,6 +159,9 @@ int force_meshes_sorted(const float *pos, int64_t np, int nx, int ny, int nz,
 size_t mesh_forces_workspace_size(int nx, int ny, int nz);
 int mesh_forces_ws(const float *mesh, float *f3, int nx, int ny, int nz,
                    float r_split, void *ws, size_t bytes, cudaStream_t s);
+// density mesh -> the potential mesh of the run loop (spectral pipeline only)
+int mesh_potential_ws(const float *mesh, float *pot, int nx, int ny, int nz, float r_split,
+                      void *ws, size_t bytes, cudaStream_t s);
 int mesh_forces_vjp_ws(const float *g3, float *rbar, int nx, int ny, int nz,
                        float r_split, void *ws, size_t bytes, cudaStream_t s);
 // step.cu: the three force-mesh cotangents g3 -> the density cotangent

@@ -246,6 +246,18 @@ int mesh_forces_ws(const float *mesh, float *f3, int nx, int ny, int nz, float r
   return mesh_forces(mesh, nx, ny, nz, r_split, dk, fk, f3, s);
 }
 
+int mesh_potential_ws(const float *mesh, float *pot, int nx, int ny, int nz, float r_split,
+                      void *ws, size_t bytes, cudaStream_t s) {
+  void *dk, *fk;
+  PMGB_TRY(mesh_ws(ws, bytes, nx, ny, nz, &dk, &fk));
+  if (!spectral_supported(nx, ny, nz))
+    return fail(PMGB_ERR_UNSUPPORTED,
+                "the potential pipeline needs power-of-two nx in [8,1024], ny in [64,512], "
+                "nz in [16,512]");
+  return spectral_potential(mesh, dk, pot, nx, ny, nz, r_split,
+                            1.0f / (float)((int64_t)nx * ny * nz), s);
+}
+
 int mesh_forces_vjp_ws(const float *g3, float *rbar, int nx, int ny, int nz, float r_split,
                        void *ws, size_t bytes, cudaStream_t s) {
   void *dk, *fk;
