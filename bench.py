@@ -286,13 +286,13 @@ def run_gb300(args):
             _lib.call("pmgb_mesh_forces_f32", P("mesh"), P("f3"), nx, ny, nz, 0.0, P("mfws"),
                       mf_bytes, s)
         rec(2)
-        if use_pot:  # gather (forces from the potential) + kick + drift + next paint
-            _lib.call("pmgb_read_potential_kick_drift_paint_binned_f32", P("f3"), nx, ny, nz,
-                      _lib.ptr(px), _lib.ptr(pv), Np, float(kick[i]), float(drift[i]),
-                      P("mesh") if i + 1 < K else None, _lib.ptr(eng.sort_ws), eng.sort_bytes,
-                      _lib.ptr(eng.stats_buf), s)
-        elif engine == "sorted":
-            if i + 1 < K:  # gather + kick + drift + paint of the next density
+        if engine == "sorted":
+            if use_pot:  # gather (forces from the potential) + kick + drift + next paint
+                _lib.call("pmgb_read_potential_kick_drift_paint_binned_f32", P("f3"), nx, ny,
+                          nz, _lib.ptr(px), _lib.ptr(pv), Np, float(kick[i]), float(drift[i]),
+                          P("mesh") if i + 1 < K else None, _lib.ptr(eng.sort_ws),
+                          eng.sort_bytes, _lib.ptr(eng.stats_buf), s)
+            elif i + 1 < K:  # gather + kick + drift + paint of the next density
                 _lib.call("pmgb_read3_kick_drift_paint_binned_f32", P("f3"), ncell, nx, ny, nz,
                           _lib.ptr(px), _lib.ptr(pv), Np, float(kick[i]), float(drift[i]),
                           P("mesh"), _lib.ptr(eng.sort_ws), eng.sort_bytes,
