@@ -589,7 +589,23 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
           tma_load_4d(fb[buf ^ 1], &tmap, nxt.oz, nxt.oy, nxt.ox, 0, &bar[buf ^ 1]);
       }
     }
+    float px[RKD_ILP], py[RKD_ILP], pz[RKD_ILP], pu[RKD_ILP], pv[RKD_ILP], pw[RKD_ILP];
+    auto load_chunk = [&](unsigned p0) {
+#pragma unroll
+      for (int j = 0; j < RKD_ILP; ++j) {
+        const unsigned p = p0 + tid + j * TILE_THREADS;
+        if (p < cur.end) {
+          px[j] = pos[3 * (int64_t)p];
+          py[j] = pos[3 * (int64_t)p + 1];
+          pz[j] = pos[3 * (int64_t)p + 2];
+          pu[j] = vel[3 * (int64_t)p];
+          pv[j] = vel[3 * (int64_t)p + 1];
+          pw[j] = vel[3 * (int64_t)p + 2];
+        }
+      }
+    };
     if (cur.beg != cur.end) {
+      load_chunk(cur.beg);  // in flight during the box wait (and the force box)
       float *box = fb[buf];
       if (cur.tma) {
         const bool ok = mbar_wait(&bar[buf], buf ? phase1 : phase0);
@@ -663,19 +679,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
       // every lane of a warp runs the same iterations (ballot / match inside);
       // each thread loads RKD_ILP particles before computing any of them
       for (unsigned p0 = cur.beg; p0 < cur.end; p0 += TILE_THREADS * RKD_ILP) {
-       float px[RKD_ILP], py[RKD_ILP], pz[RKD_ILP], pu[RKD_ILP], pv[RKD_ILP], pw[RKD_ILP];
-#pragma unroll
-       for (int j = 0; j < RKD_ILP; ++j) {
-         const unsigned p = p0 + tid + j * TILE_THREADS;
-         if (p < cur.end) {
-           px[j] = pos[3 * (int64_t)p];
-           py[j] = pos[3 * (int64_t)p + 1];
-           pz[j] = pos[3 * (int64_t)p + 2];
-           pu[j] = vel[3 * (int64_t)p];
-           pv[j] = vel[3 * (int64_t)p + 1];
-           pw[j] = vel[3 * (int64_t)p + 2];
-         }
-       }
+       if (p0 != cur.beg) load_chunk(p0);
 #pragma unroll
        for (int j = 0; j < RKD_ILP; ++j) {
         const unsigned p = p0 + tid + j * TILE_THREADS;
