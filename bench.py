@@ -436,7 +436,8 @@ def run_gb300(args):
         a0 = torch.cuda.Event(enable_timing=True)
         a1 = torch.cuda.Event(enable_timing=True)
         a0.record(stream)
-        eng.vjp(x0, v0, gx, gv, store=store)
+        with nvtx("adjoint"):
+            eng.vjp(x0, v0, gx, gv, store=store)
         a1.record(stream)
         torch.cuda.synchronize(dev)
         ams = max_over_ranks(a0.elapsed_time(a1), world)
@@ -623,7 +624,8 @@ def run_batched(args):
         a0 = torch.cuda.Event(enable_timing=True)
         a1 = torch.cuda.Event(enable_timing=True)
         a0.record(stream)
-        eng.vjp(x0, v0, gx, gv, store=store)
+        with nvtx("adjoint"):
+            eng.vjp(x0, v0, gx, gv, store=store)
         a1.record(stream)
         torch.cuda.synchronize(dev)
         ams = max_over_ranks(a0.elapsed_time(a1), world)

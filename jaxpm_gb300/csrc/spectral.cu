@@ -1044,12 +1044,191 @@ int spectral_c2r(void *in, float *out, int nx, int ny, int nz, int batch, cudaSt
   return PMGB_OK;
 }
 
+// ---- real-space order-1 gradient -------------------------------------------
+//
+// The order-1 gradient multiplier i g(w), g(w) = (8 sin w - sin 2w)/6
+// (jaxpm/kernels.py:41-66), is the transfer function of the stencil
+// D p = (8 (p[+1] - p[-1]) - (p[+2] - p[-2])) / 12 along each axis; D is
+// antisymmetric (D^T = -D).  One thread per cell, z fastest: the twelve
+// neighbours come through L1 / L2 (each potential value is read by 13
+// threads), one potential read and three force writes per cell from DRAM.
+
+__device__ __forceinline__ float d_stencil(float m2, float m1, float p1, float p2) {
+  const float t1 = p1 - m1, t2 = p2 - m2;
+  return (8.0f * t1 - t2) * (1.0f / 12.0f);
+}
+
+// f3[c] = -D_c pot: the forces of the potential (spectral_forces' result).
+__global__ void __launch_bounds__(256)
+stencil_forces_kernel(const float *__restrict__ pot, float *__restrict__ f3, int nx, int ny,
+                      int nz) {
+  const int64_t n = (int64_t)nx * ny * nz;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int z = (int)(e % nz);
+    const int64_t r = e / nz;
+    const int y = (int)(r % ny), x = (int)(r / ny);
+    auto at = [&](int xx, int yy, int zz) {
+      return __ldg(pot + ((int64_t)xx * ny + yy) * nz + zz);
+    };
+    const int xm1 = x == 0 ? nx - 1 : x - 1, xm2 = x < 2 ? x - 2 + nx : x - 2;
+    const int xp1 = x + 1 == nx ? 0 : x + 1, xp2 = x + 2 >= nx ? x + 2 - nx : x + 2;
+    const int ym1 = y == 0 ? ny - 1 : y - 1, ym2 = y < 2 ? y - 2 + ny : y - 2;
+    const int yp1 = y + 1 == ny ? 0 : y + 1, yp2 = y + 2 >= ny ? y + 2 - ny : y + 2;
+    const int zm1 = z == 0 ? nz - 1 : z - 1, zm2 = z < 2 ? z - 2 + nz : z - 2;
+    const int zp1 = z + 1 == nz ? 0 : z + 1, zp2 = z + 2 >= nz ? z + 2 - nz : z + 2;
+    f3[e] = -d_stencil(at(xm2, y, z), at(xm1, y, z), at(xp1, y, z), at(xp2, y, z));
+    f3[n + e] = -d_stencil(at(x, ym2, z), at(x, ym1, z), at(x, yp1, z), at(x, yp2, z));
+    f3[2 * n + e] = -d_stencil(at(x, y, zm2), at(x, y, zm1), at(x, y, zp1), at(x, y, zp2));
+  }
+}
+
+// out = sum_c D_c g3[c]: the potential cotangent of force-mesh cotangents
+// (the transpose of stencil_forces_kernel, -D_c^T = D_c).
+__global__ void __launch_bounds__(256)
+stencil_adjoint_kernel(const float *__restrict__ g3, float *__restrict__ out, int nx, int ny,
+                       int nz) {
+  const int64_t n = (int64_t)nx * ny * nz;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int z = (int)(e % nz);
+    const int64_t r = e / nz;
+    const int y = (int)(r % ny), x = (int)(r / ny);
+    auto at = [&](int c, int xx, int yy, int zz) {
+      return __ldg(g3 + c * n + ((int64_t)xx * ny + yy) * nz + zz);
+    };
+    const int xm1 = x == 0 ? nx - 1 : x - 1, xm2 = x < 2 ? x - 2 + nx : x - 2;
+    const int xp1 = x + 1 == nx ? 0 : x + 1, xp2 = x + 2 >= nx ? x + 2 - nx : x + 2;
+    const int ym1 = y == 0 ? ny - 1 : y - 1, ym2 = y < 2 ? y - 2 + ny : y - 2;
+    const int yp1 = y + 1 == ny ? 0 : y + 1, yp2 = y + 2 >= ny ? y + 2 - ny : y + 2;
+    const int zm1 = z == 0 ? nz - 1 : z - 1, zm2 = z < 2 ? z - 2 + nz : z - 2;
+    const int zp1 = z + 1 == nz ? 0 : z + 1, zp2 = z + 2 >= nz ? z + 2 - nz : z + 2;
+    out[e] = d_stencil(at(0, xm2, y, z), at(0, xm1, y, z), at(0, xp1, y, z), at(0, xp2, y, z)) +
+             d_stencil(at(1, x, ym2, z), at(1, x, ym1, z), at(1, x, yp1, z), at(1, x, yp2, z)) +
+             d_stencil(at(2, x, y, zm2), at(2, x, y, zm1), at(2, x, y, zp1), at(2, x, y, zp2));
+  }
+}
+
+// Tiled forms of the two stencils: a CTA takes a 32 (z) x 8 (y) tile and
+// marches along ST_XCH planes of x, keeping each thread's column along x in a
+// register window (the x stencil) and staging the current plane (with the
+// halo its y and z stencils need) in shared memory, so each input value
+// comes from DRAM about once.  Needs nz % 32 == 0, ny % 8 == 0, nx % ST_XCH == 0.
+constexpr int ST_TZ = 32, ST_TY = 8, ST_XCH = 32;
+
+__device__ __forceinline__ int wrap_lo_hi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+__global__ void __launch_bounds__(256)
+stencil_forces_tiled_kernel(const float *__restrict__ pot, float *__restrict__ f3, int nx, int ny,
+                            int nz) {
+  __shared__ float pl[ST_TY + 4][ST_TZ + 4];
+  const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * ST_TZ + tz;
+  const int zb = blockIdx.x * ST_TZ, yb = blockIdx.y * ST_TY, x0 = blockIdx.z * ST_XCH;
+  const int64_t plane = (int64_t)ny * nz, n = plane * nx;
+  const int64_t col = (int64_t)(yb + ty) * nz + zb + tz;
+  float w0 = __ldg(pot + wrap_lo_hi(x0 - 2, nx) * plane + col);
+  float w1 = __ldg(pot + wrap_lo_hi(x0 - 1, nx) * plane + col);
+  float w2 = __ldg(pot + (int64_t)x0 * plane + col);
+  float w3 = __ldg(pot + wrap_lo_hi(x0 + 1, nx) * plane + col);
+  for (int x = x0; x < x0 + ST_XCH; ++x) {
+    const float w4 = __ldg(pot + wrap_lo_hi(x + 2, nx) * plane + col);
+    const float *P = pot + (int64_t)x * plane;
+    for (int q = tid; q < (ST_TY + 4) * (ST_TZ + 4); q += ST_TZ * ST_TY) {
+      const int r = q / (ST_TZ + 4), c = q - r * (ST_TZ + 4);
+      pl[r][c] = __ldg(P + (int64_t)wrap_lo_hi(yb + r - 2, ny) * nz + wrap_lo_hi(zb + c - 2, nz));
+    }
+    __syncthreads();
+    const int64_t e = (int64_t)x * plane + col;
+    f3[e] = -d_stencil(w0, w1, w3, w4);
+    f3[n + e] = -d_stencil(pl[ty][tz + 2], pl[ty + 1][tz + 2], pl[ty + 3][tz + 2],
+                           pl[ty + 4][tz + 2]);
+    f3[2 * n + e] = -d_stencil(pl[ty + 2][tz], pl[ty + 2][tz + 1], pl[ty + 2][tz + 3],
+                               pl[ty + 2][tz + 4]);
+    __syncthreads();
+    w0 = w1;
+    w1 = w2;
+    w2 = w3;
+    w3 = w4;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+stencil_adjoint_tiled_kernel(const float *__restrict__ g3, float *__restrict__ out, int nx,
+                             int ny, int nz) {
+  __shared__ float gy[ST_TY + 4][ST_TZ];
+  __shared__ float gz[ST_TY][ST_TZ + 4];
+  const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * ST_TZ + tz;
+  const int zb = blockIdx.x * ST_TZ, yb = blockIdx.y * ST_TY, x0 = blockIdx.z * ST_XCH;
+  const int64_t plane = (int64_t)ny * nz, n = plane * nx;
+  const int64_t col = (int64_t)(yb + ty) * nz + zb + tz;
+  float w0 = __ldg(g3 + wrap_lo_hi(x0 - 2, nx) * plane + col);
+  float w1 = __ldg(g3 + wrap_lo_hi(x0 - 1, nx) * plane + col);
+  float w3 = __ldg(g3 + wrap_lo_hi(x0 + 1, nx) * plane + col);
+  for (int x = x0; x < x0 + ST_XCH; ++x) {
+    const float w4 = __ldg(g3 + wrap_lo_hi(x + 2, nx) * plane + col);
+    const float *Py = g3 + n + (int64_t)x * plane, *Pz = g3 + 2 * n + (int64_t)x * plane;
+    for (int q = tid; q < (ST_TY + 4) * ST_TZ; q += ST_TZ * ST_TY) {
+      const int r = q / ST_TZ, c = q - r * ST_TZ;
+      gy[r][c] = __ldg(Py + (int64_t)wrap_lo_hi(yb + r - 2, ny) * nz + zb + c);
+    }
+    for (int q = tid; q < ST_TY * (ST_TZ + 4); q += ST_TZ * ST_TY) {
+      const int r = q / (ST_TZ + 4), c = q - r * (ST_TZ + 4);
+      gz[r][c] = __ldg(Pz + (int64_t)(yb + r) * nz + wrap_lo_hi(zb + c - 2, nz));
+    }
+    __syncthreads();
+    out[(int64_t)x * plane + col] =
+        d_stencil(w0, w1, w3, w4) +
+        d_stencil(gy[ty][tz], gy[ty + 1][tz], gy[ty + 3][tz], gy[ty + 4][tz]) +
+        d_stencil(gz[ty][tz], gz[ty][tz + 1], gz[ty][tz + 3], gz[ty][tz + 4]);
+    __syncthreads();
+    w0 = w1;
+    w1 = __ldg(g3 + (int64_t)x * plane + col);
+    w3 = w4;
+  }
+}
+
+static bool stencil_tiled(int nx, int ny, int nz) {
+  return nz % ST_TZ == 0 && ny % ST_TY == 0 && nx % ST_XCH == 0;
+}
+
+static int stencil_forces(const float *pot, float *f3, int nx, int ny, int nz, cudaStream_t s) {
+  if (stencil_tiled(nx, ny, nz)) {
+    stencil_forces_tiled_kernel<<<dim3(nz / ST_TZ, ny / ST_TY, nx / ST_XCH), dim3(ST_TZ, ST_TY), 0,
+                                  s>>>(pot, f3, nx, ny, nz);
+    PMGB_LAUNCHED("stencil_forces_tiled_kernel");
+    return PMGB_OK;
+  }
+  stencil_forces_kernel<<<grid_for((int64_t)nx * ny * nz, 256), 256, 0, s>>>(pot, f3, nx, ny, nz);
+  PMGB_LAUNCHED("stencil_forces_kernel");
+  return PMGB_OK;
+}
+
+static int stencil_adjoint(const float *g3, float *out, int nx, int ny, int nz, cudaStream_t s) {
+  if (stencil_tiled(nx, ny, nz)) {
+    stencil_adjoint_tiled_kernel<<<dim3(nz / ST_TZ, ny / ST_TY, nx / ST_XCH),
+                                   dim3(ST_TZ, ST_TY), 0, s>>>(g3, out, nx, ny, nz);
+    PMGB_LAUNCHED("stencil_adjoint_tiled_kernel");
+    return PMGB_OK;
+  }
+  stencil_adjoint_kernel<<<grid_for((int64_t)nx * ny * nz, 256), 256, 0, s>>>(g3, out, nx, ny,
+                                                                             nz);
+  PMGB_LAUNCHED("stencil_adjoint_kernel");
+  return PMGB_OK;
+}
+
 int spectral_forces(const float *mesh, void *spec, void *fspec, float *f3, int nx, int ny,
                     int nz, float r_split, int order, int fd, float scale, cudaStream_t s) {
   PMGB_TRY(check_spectral(nx, ny, nz));
   const int pitch = spectral_pitch(nz);
   const int64_t cs = (int64_t)nx * ny * pitch;
   float2 *d = static_cast<float2 *>(spec), *f = static_cast<float2 *>(fspec);
+  if (order == 1 && fd == 0) {
+    // one inverse transform of the potential (into fspec's memory), then
+    // the order-1 gradient as its real-space stencil
+    float *pot = reinterpret_cast<float *>(f);
+    PMGB_TRY(spectral_potential(mesh, d, pot, nx, ny, nz, r_split, scale, s));
+    return stencil_forces(pot, f3, nx, ny, nz, s);
+  }
   PMGB_TRY(planes_r2c(mesh, d, nx, ny, nz, pitch, s));
   PMGB_TRY(xpass<X_FORCES>(d, f, nx, ny, nz, pitch, cs, cs, r_split, order, fd, scale, s));
   PMGB_TRY(planes_c2r(f, f3, 3 * nx, ny, nz, pitch, s));
@@ -1080,6 +1259,13 @@ int spectral_forces_vjp(const float *g3, void *spec3, void *dspec, float *rbar, 
   const int pitch = spectral_pitch(nz);
   const int64_t cs = (int64_t)nx * ny * pitch;
   float2 *a = static_cast<float2 *>(spec3), *d = static_cast<float2 *>(dspec);
+  if (order == 1 && fd == 0) {
+    // the potential cotangent sum_c D_c g_c in real space (into spec3's
+    // memory), then the symmetric k-space multiply of the potential
+    float *pbar = reinterpret_cast<float *>(a);
+    PMGB_TRY(stencil_adjoint(g3, pbar, nx, ny, nz, s));
+    return spectral_potential(pbar, d, rbar, nx, ny, nz, r_split, scale, s);
+  }
   PMGB_TRY(planes_r2c(g3, a, 3 * nx, ny, nz, pitch, s));
   PMGB_TRY(xpass<X_FORCES_ADJ>(a, d, nx, ny, nz, pitch, cs, cs, r_split, order, fd, scale, s));
   PMGB_TRY(planes_c2r(d, rbar, nx, ny, nz, pitch, s));
