@@ -9,9 +9,9 @@
 // appearance in the table, the simulations of a group in table order.  A
 // group's meshes and spectra are contiguous with a uniform stride, so one
 // batched cuFFT plan transforms the whole group:
-//   mesh pool  [group][sim][nx][ny][nz]           f32  (density; adjoint: rho_bar)
+//   mesh pool  [group][sim][nx][ny][nz]           f32  (density, then potential;
+//                                                       adjoint: potential cotangent, rho_bar)
 //   dk pool    [group][sim][nx][ny][nz/2+1]       c64
-//   fk pool    [group][sim][3][nx][ny][nz/2+1]    c64
 //   f3 pool    [group][sim][3][nx][ny][nz]        f32  (force meshes)
 //   g3 pool    [group][sim][3][nx][ny][nz]        f32  (adjoint: force-mesh cotangents)
 // Particles are the concatenation, in table order, of every simulation's
@@ -22,10 +22,12 @@
 // particle per thread: block b belongs to the simulation whose first block
 // is the largest not above b (binary search of the device descriptor
 // table), so a block never straddles two simulations and reads its own mesh
-// shape, pool offsets and kick/drift coefficients.  The k-space multiply is
-// one launch over all groups' spectra; the FFTs are one batched cuFFT
-// execution per group and direction, with plans made when the workspace is
-// initialised (so that a step can be captured in a CUDA graph).
+// shape, pool offsets and kick/drift coefficients.  The forces come from the
+// potentials: one batched cuFFT R2C per group, one k-space launch over all
+// groups' spectra (the potential multiply, in place), one batched C2R per
+// group, and the order-1 gradient as its real-space stencil (one launch per
+// group); plans are made when the workspace is initialised (so that a step
+// can be captured in a CUDA graph).
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -63,7 +65,7 @@ struct Plan {
   std::vector<BatchSim> sims;
   std::vector<Group> groups;
   int64_t np = 0, cells = 0, specs = 0, blocks = 0;
-  size_t o_desc = 0, o_mesh = 0, o_dk = 0, o_fk = 0, o_f3 = 0, o_g3 = 0, total = 0;
+  size_t o_desc = 0, o_mesh = 0, o_dk = 0, o_f3 = 0, o_g3 = 0, total = 0;
   uint64_t key = 0;
 };
 
@@ -145,7 +147,6 @@ int make_plan(const pmgb_sim *t, int n, Plan *P) {
   P->o_desc = o; o = al256(o + (size_t)n * sizeof(BatchSim));
   P->o_mesh = o; o = al256(o + (size_t)P->cells * 4);
   P->o_dk = o;   o = al256(o + (size_t)P->specs * 8);
-  P->o_fk = o;   o = al256(o + (size_t)P->specs * 3 * 8);
   P->o_f3 = o;   o = al256(o + (size_t)P->cells * 3 * 4);
   P->o_g3 = o;   o = al256(o + (size_t)P->cells * 3 * 4);
   P->total = o;
@@ -423,9 +424,10 @@ __device__ __forceinline__ Elem kelement(const KGroup &g, uint32_t el) {
   return E;
 }
 
-// dk [sim][half] -> fk [sim][3][half] for every simulation of the groups.
+// dk [sim][half] *= invlaplace * longrange * scale, in place: the spectra of
+// the potentials (the forces are their order-1 stencil gradients).
 __global__ void __launch_bounds__(256)
-batch_forces_kernel(const float2 *__restrict__ dk, float2 *__restrict__ fk, KGroups G, float r2) {
+batch_potential_kernel(float2 *__restrict__ dk, KGroups G, float r2) {
   for (int64_t e = G.begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < G.end;
        e += (int64_t)gridDim.x * blockDim.x) {
     const KGroup &g = G.g[kgroup_of(G, e)];
@@ -433,33 +435,18 @@ batch_forces_kernel(const float2 *__restrict__ dk, float2 *__restrict__ fk, KGro
     if (local >= g.count) continue;  // padding between groups
     const int64_t inst = local / g.total;
     const uint32_t el = (uint32_t)(local - inst * g.total);
-    float2 f[3];
-    force_modes(kelement(g, el), dk[e], r2, 1, 0, g.scale, f);
-    float2 *o = fk + 3 * g.start + inst * 3 * (int64_t)g.total + el;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) o[c * (int64_t)g.total] = f[c];
+    const Elem E = kelement(g, el);
+    const float inv = inv_laplace(E, 0), L = long_range(E, r2);
+    const float2 d = dk[e];
+    dk[e] = make_float2(__fmul_rn(__fmul_rn(d.x, inv), L) * g.scale,
+                        __fmul_rn(__fmul_rn(d.y, inv), L) * g.scale);
   }
 }
 
-// Adjoint: gfk [sim][3][half] -> gdk [sim][half].
-__global__ void __launch_bounds__(256)
-batch_forces_vjp_kernel(const float2 *__restrict__ gfk, float2 *__restrict__ gdk, KGroups G,
-                        float r2) {
-  for (int64_t e = G.begin + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < G.end;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const KGroup &g = G.g[kgroup_of(G, e)];
-    const int64_t local = e - g.start;
-    if (local >= g.count) continue;  // padding between groups
-    const int64_t inst = local / g.total;
-    const uint32_t el = (uint32_t)(local - inst * g.total);
-    const float2 *v3 = gfk + 3 * g.start + inst * 3 * (int64_t)g.total + el;
-    const float2 v[3] = {v3[0], v3[g.total], v3[2 * (int64_t)g.total]};
-    gdk[e] = force_modes_adjoint(kelement(g, el), v, r2, 1, 0, g.scale);
-  }
-}
-
-int kspace_batched(const Plan &P, const float2 *in, float2 *out, float r_split, bool adjoint,
-                   cudaStream_t s) {
+// The potentials' spectra for every group, in place (one launch per
+// MAX_KGROUPS groups).  The multiply is symmetric, so the adjoint is the
+// same operation.
+int kspace_potential_batched(const Plan &P, float2 *dk, float r_split, cudaStream_t s) {
   const size_t ng = P.groups.size();
   for (size_t g0 = 0; g0 < ng; g0 += MAX_KGROUPS) {
     KGroups G;
@@ -479,39 +466,45 @@ int kspace_batched(const Plan &P, const float2 *in, float2 *out, float r_split, 
     G.begin = G.g[0].start;
     const Group &last = P.groups[g0 + G.count - 1];
     G.end = last.spec + (int64_t)last.n * last.nx * last.ny * (last.nz / 2 + 1);
-    const unsigned grid = grid_for(G.end - G.begin, 256);
-    if (adjoint) {
-      batch_forces_vjp_kernel<<<grid, 256, 0, s>>>(in, out, G, r_split * r_split);
-      PMGB_LAUNCHED("batch_forces_vjp_kernel");
-    } else {
-      batch_forces_kernel<<<grid, 256, 0, s>>>(in, out, G, r_split * r_split);
-      PMGB_LAUNCHED("batch_forces_kernel");
-    }
+    batch_potential_kernel<<<grid_for(G.end - G.begin, 256), 256, 0, s>>>(dk, G,
+                                                                          r_split * r_split);
+    PMGB_LAUNCHED("batch_potential_kernel");
   }
   return PMGB_OK;
 }
 
-// density pool -> f3 pool: R2C per group, one k-space launch, C2R per group.
+// density pool -> f3 pool through the potentials: R2C per group, one
+// k-space launch (in place), C2R per group into the mesh pool (the density
+// is no longer needed), then the order-1 gradient as a real-space stencil
+// per group (jaxpm/kernels.py:41-66: the multiplier i g(w) is the transfer
+// function of the stencil), one inverse transform per simulation instead of
+// three.
 int batch_mesh_forces(const Plan &P, void *ws, float r_split, cudaStream_t s) {
   float *mesh = BW(float, P.o_mesh);
-  float2 *dk = BW(float2, P.o_dk), *fk = BW(float2, P.o_fk);
+  float2 *dk = BW(float2, P.o_dk);
   float *f3 = BW(float, P.o_f3);
   for (const Group &g : P.groups)
     PMGB_TRY(fft_r2c(mesh + g.mesh, dk + g.spec, g.nx, g.ny, g.nz, g.n, s));
-  PMGB_TRY(kspace_batched(P, dk, fk, r_split, false, s));
-  for (const Group &g : P.groups)
-    PMGB_TRY(fft_c2r(fk + 3 * g.spec, f3 + 3 * g.mesh, g.nx, g.ny, g.nz, 3 * g.n, s));
+  PMGB_TRY(kspace_potential_batched(P, dk, r_split, s));
+  for (const Group &g : P.groups) {
+    PMGB_TRY(fft_c2r(dk + g.spec, mesh + g.mesh, g.nx, g.ny, g.nz, g.n, s));
+    PMGB_TRY(stencil_forces(mesh + g.mesh, f3 + 3 * g.mesh, g.nx, g.ny, g.nz, g.n, s));
+  }
   return PMGB_OK;
 }
 
-// g3 pool -> rho_bar in the mesh pool (adjoint of batch_mesh_forces).
+// g3 pool -> rho_bar in the mesh pool (adjoint of batch_mesh_forces): the
+// potential cotangents sum_c D_c g_c by the stencil, then the symmetric
+// k-space multiply between one R2C and one C2R per group.
 int batch_mesh_forces_vjp(const Plan &P, void *ws, float r_split, cudaStream_t s) {
   float *rbar = BW(float, P.o_mesh);
-  float2 *dk = BW(float2, P.o_dk), *fk = BW(float2, P.o_fk);
+  float2 *dk = BW(float2, P.o_dk);
   float *g3 = BW(float, P.o_g3);
-  for (const Group &g : P.groups)
-    PMGB_TRY(fft_r2c(g3 + 3 * g.mesh, fk + 3 * g.spec, g.nx, g.ny, g.nz, 3 * g.n, s));
-  PMGB_TRY(kspace_batched(P, fk, dk, r_split, true, s));
+  for (const Group &g : P.groups) {
+    PMGB_TRY(stencil_adjoint(g3 + 3 * g.mesh, rbar + g.mesh, g.nx, g.ny, g.nz, g.n, s));
+    PMGB_TRY(fft_r2c(rbar + g.mesh, dk + g.spec, g.nx, g.ny, g.nz, g.n, s));
+  }
+  PMGB_TRY(kspace_potential_batched(P, dk, r_split, s));
   for (const Group &g : P.groups)
     PMGB_TRY(fft_c2r(dk + g.spec, rbar + g.mesh, g.nx, g.ny, g.nz, g.n, s));
   return PMGB_OK;
@@ -557,8 +550,6 @@ int batch_init(const pmgb_sim *t, int n, void *ws, size_t bytes, cudaStream_t s)
   // steps launch work only
   for (const Group &g : P.groups) {
     PMGB_TRY(fft_prepare(g.nx, g.ny, g.nz, g.n, 1));
-    PMGB_TRY(fft_prepare(g.nx, g.ny, g.nz, 3 * g.n, 0));
-    PMGB_TRY(fft_prepare(g.nx, g.ny, g.nz, 3 * g.n, 1));
     PMGB_TRY(fft_prepare(g.nx, g.ny, g.nz, g.n, 0));
     Tables tb;
     PMGB_TRY(tables(g.nx, g.ny, g.nz, &tb));

@@ -197,6 +197,13 @@ int spectral_c2r(void *in, float *out, int nx, int ny, int nz, int batch,
 int spectral_forces(const float *mesh, void *spec, void *fspec, float *f3,
                     int nx, int ny, int nz, float r_split, int order, int fd,
                     float scale, cudaStream_t s);
+// The order-1 gradient as a real-space stencil over `batch` meshes:
+// f3 [b][3][nx][ny][nz] = -D pot [b][nx][ny][nz], and its transpose
+// out [b] = sum_c D_c g3 [b][c].
+int stencil_forces(const float *pot, float *f3, int nx, int ny, int nz, int batch,
+                   cudaStream_t s);
+int stencil_adjoint(const float *g3, float *out, int nx, int ny, int nz, int batch,
+                    cudaStream_t s);
 // mesh -> spec -> pot [nx][ny][nz]: the potential whose order-1 stencil
 // gradient gives the forces of spectral_forces (order 1, fd 0).
 int spectral_potential(const float *mesh, void *spec, float *pot, int nx, int ny, int nz,

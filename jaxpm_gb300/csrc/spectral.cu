@@ -1123,8 +1123,11 @@ stencil_forces_tiled_kernel(const float *__restrict__ pot, float *__restrict__ f
                             int nz) {
   __shared__ float pl[ST_TY + 4][ST_TZ + 4];
   const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * ST_TZ + tz;
-  const int zb = blockIdx.x * ST_TZ, yb = blockIdx.y * ST_TY, x0 = blockIdx.z * ST_XCH;
+  const int xch = nx / ST_XCH, b = blockIdx.z / xch;
+  const int zb = blockIdx.x * ST_TZ, yb = blockIdx.y * ST_TY, x0 = (blockIdx.z - b * xch) * ST_XCH;
   const int64_t plane = (int64_t)ny * nz, n = plane * nx;
+  pot += b * n;  // batch entry b: [b][nx][ny][nz] in, [b][3][nx][ny][nz] out
+  f3 += 3 * b * n;
   const int64_t col = (int64_t)(yb + ty) * nz + zb + tz;
   float w0 = __ldg(pot + wrap_lo_hi(x0 - 2, nx) * plane + col);
   float w1 = __ldg(pot + wrap_lo_hi(x0 - 1, nx) * plane + col);
@@ -1158,8 +1161,11 @@ stencil_adjoint_tiled_kernel(const float *__restrict__ g3, float *__restrict__ o
   __shared__ float gy[ST_TY + 4][ST_TZ];
   __shared__ float gz[ST_TY][ST_TZ + 4];
   const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * ST_TZ + tz;
-  const int zb = blockIdx.x * ST_TZ, yb = blockIdx.y * ST_TY, x0 = blockIdx.z * ST_XCH;
+  const int xch = nx / ST_XCH, b = blockIdx.z / xch;
+  const int zb = blockIdx.x * ST_TZ, yb = blockIdx.y * ST_TY, x0 = (blockIdx.z - b * xch) * ST_XCH;
   const int64_t plane = (int64_t)ny * nz, n = plane * nx;
+  g3 += 3 * b * n;  // batch entry b: [b][3][nx][ny][nz] in, [b][nx][ny][nz] out
+  out += b * n;
   const int64_t col = (int64_t)(yb + ty) * nz + zb + tz;
   float w0 = __ldg(g3 + wrap_lo_hi(x0 - 2, nx) * plane + col);
   float w1 = __ldg(g3 + wrap_lo_hi(x0 - 1, nx) * plane + col);
@@ -1187,32 +1193,42 @@ stencil_adjoint_tiled_kernel(const float *__restrict__ g3, float *__restrict__ o
   }
 }
 
-static bool stencil_tiled(int nx, int ny, int nz) {
-  return nz % ST_TZ == 0 && ny % ST_TY == 0 && nx % ST_XCH == 0;
+static bool stencil_tiled(int nx, int ny, int nz, int batch) {
+  return nz % ST_TZ == 0 && ny % ST_TY == 0 && nx % ST_XCH == 0 &&
+         (int64_t)batch * (nx / ST_XCH) <= 65535;
 }
 
-static int stencil_forces(const float *pot, float *f3, int nx, int ny, int nz, cudaStream_t s) {
-  if (stencil_tiled(nx, ny, nz)) {
-    stencil_forces_tiled_kernel<<<dim3(nz / ST_TZ, ny / ST_TY, nx / ST_XCH), dim3(ST_TZ, ST_TY), 0,
-                                  s>>>(pot, f3, nx, ny, nz);
+int stencil_forces(const float *pot, float *f3, int nx, int ny, int nz, int batch,
+                   cudaStream_t s) {
+  const int64_t n = (int64_t)nx * ny * nz;
+  if (stencil_tiled(nx, ny, nz, batch)) {
+    stencil_forces_tiled_kernel<<<dim3(nz / ST_TZ, ny / ST_TY, batch * (nx / ST_XCH)),
+                                  dim3(ST_TZ, ST_TY), 0, s>>>(pot, f3, nx, ny, nz);
     PMGB_LAUNCHED("stencil_forces_tiled_kernel");
     return PMGB_OK;
   }
-  stencil_forces_kernel<<<grid_for((int64_t)nx * ny * nz, 256), 256, 0, s>>>(pot, f3, nx, ny, nz);
-  PMGB_LAUNCHED("stencil_forces_kernel");
+  for (int b = 0; b < batch; ++b) {
+    stencil_forces_kernel<<<grid_for(n, 256), 256, 0, s>>>(pot + b * n, f3 + 3 * b * n, nx, ny,
+                                                            nz);
+    PMGB_LAUNCHED("stencil_forces_kernel");
+  }
   return PMGB_OK;
 }
 
-static int stencil_adjoint(const float *g3, float *out, int nx, int ny, int nz, cudaStream_t s) {
-  if (stencil_tiled(nx, ny, nz)) {
-    stencil_adjoint_tiled_kernel<<<dim3(nz / ST_TZ, ny / ST_TY, nx / ST_XCH),
+int stencil_adjoint(const float *g3, float *out, int nx, int ny, int nz, int batch,
+                    cudaStream_t s) {
+  const int64_t n = (int64_t)nx * ny * nz;
+  if (stencil_tiled(nx, ny, nz, batch)) {
+    stencil_adjoint_tiled_kernel<<<dim3(nz / ST_TZ, ny / ST_TY, batch * (nx / ST_XCH)),
                                    dim3(ST_TZ, ST_TY), 0, s>>>(g3, out, nx, ny, nz);
     PMGB_LAUNCHED("stencil_adjoint_tiled_kernel");
     return PMGB_OK;
   }
-  stencil_adjoint_kernel<<<grid_for((int64_t)nx * ny * nz, 256), 256, 0, s>>>(g3, out, nx, ny,
-                                                                             nz);
-  PMGB_LAUNCHED("stencil_adjoint_kernel");
+  for (int b = 0; b < batch; ++b) {
+    stencil_adjoint_kernel<<<grid_for(n, 256), 256, 0, s>>>(g3 + 3 * b * n, out + b * n, nx, ny,
+                                                             nz);
+    PMGB_LAUNCHED("stencil_adjoint_kernel");
+  }
   return PMGB_OK;
 }
 
@@ -1227,7 +1243,7 @@ int spectral_forces(const float *mesh, void *spec, void *fspec, float *f3, int n
     // the order-1 gradient as its real-space stencil
     float *pot = reinterpret_cast<float *>(f);
     PMGB_TRY(spectral_potential(mesh, d, pot, nx, ny, nz, r_split, scale, s));
-    return stencil_forces(pot, f3, nx, ny, nz, s);
+    return stencil_forces(pot, f3, nx, ny, nz, 1, s);
   }
   PMGB_TRY(planes_r2c(mesh, d, nx, ny, nz, pitch, s));
   PMGB_TRY(xpass<X_FORCES>(d, f, nx, ny, nz, pitch, cs, cs, r_split, order, fd, scale, s));
@@ -1263,7 +1279,7 @@ int spectral_forces_vjp(const float *g3, void *spec3, void *dspec, float *rbar, 
     // the potential cotangent sum_c D_c g_c in real space (into spec3's
     // memory), then the symmetric k-space multiply of the potential
     float *pbar = reinterpret_cast<float *>(a);
-    PMGB_TRY(stencil_adjoint(g3, pbar, nx, ny, nz, s));
+    PMGB_TRY(stencil_adjoint(g3, pbar, nx, ny, nz, 1, s));
     return spectral_potential(pbar, d, rbar, nx, ny, nz, r_split, scale, s);
   }
   PMGB_TRY(planes_r2c(g3, a, 3 * nx, ny, nz, pitch, s));

@@ -85,9 +85,9 @@ def test_batched_table_queries(lib):
     t = _lib.sim_table(shapes, [int(np.prod(s)) for s in shapes])
     nbytes = lib.pmgb_batch_workspace_size(t, len(shapes))
     cells = sum(int(np.prod(s)) for s in shapes)
-    # density + 3 force meshes + 3 cotangent meshes (f32) and 1 + 3 half spectra (c64)
-    assert nbytes >= cells * 4 * 7 + cells * 8 * 4 // 2
-    assert nbytes < cells * 4 * 7 + cells * 8 * 4 * 2
+    # density + 3 force meshes + 3 cotangent meshes (f32) and one half spectrum (c64)
+    assert nbytes >= cells * 4 * 7 + cells * 8 // 2
+    assert nbytes < cells * 4 * 7 + cells * 8 * 2
     np_total, cells_total = ctypes.c_int64(), ctypes.c_int64()
     _lib.call("pmgb_batch_counts", t, len(shapes), ctypes.byref(np_total),
               ctypes.byref(cells_total))
