@@ -460,6 +460,28 @@ int pmgb_read_potential_kick_drift_paint_binned_f32(const float *pot, int nx,
                                                     uint32_t *stats,
                                                     pmgb_stream_t stream);
 
+/* The forward run of the reverse sweep, recording what each step's
+ * pmgb_fpm_step_sorted_vjp_f32 needs, as one call with the run loop's
+ * fusions (each later density painted by the previous gather, the sort
+ * overlapped with the next forces).  xs: [n_steps][np][3], xs[0] holds the
+ * initial positions in tile order (ranges in sort_workspace); step i writes
+ * the positions it ends with into xs[i+1] (the last step into pos_out), its
+ * force meshes into force3s[i] ([n_steps][3][nx][ny][nz]), the re-sort map
+ * into dests[i] ([n_steps][np]) and the tile ranges it started from into
+ * offsets[i] ([n_steps][keys+1]).  Velocities and ids ping-pong between the
+ * a and b buffers (final state in b when n_steps is odd); kick and drift are
+ * HOST arrays of n_steps coefficients. */
+int pmgb_fpm_run_sorted_record_f32(float *xs, float *vel_a, uint32_t *id_a,
+                                   float *vel_b, uint32_t *id_b, float *pos_out,
+                                   int64_t np, int nx, int ny, int nz,
+                                   int n_steps, const float *kick,
+                                   const float *drift, float r_split,
+                                   void *workspace, size_t workspace_bytes,
+                                   void *sort_workspace,
+                                   size_t sort_workspace_bytes, float *force3s,
+                                   uint32_t *dests, uint32_t *offsets,
+                                   uint32_t *stats, pmgb_stream_t stream);
+
 int pmgb_fpm_run_sorted_f32(float *pos_a, float *vel_a, uint32_t *id_a,
                             float *pos_b, float *vel_b, uint32_t *id_b,
                             int64_t np, int nx, int ny, int nz, int n_steps,

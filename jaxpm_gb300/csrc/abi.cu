@@ -556,6 +556,35 @@ int pmgb_read_potential_kick_drift_paint_binned_f32(const float *pot, int nx, in
                     sort_workspace, sort_workspace_bytes, stats, stream, mesh_next, true);
 }
 
+int pmgb_fpm_run_sorted_record_f32(float *xs, float *vel_a, uint32_t *id_a, float *vel_b,
+                                   uint32_t *id_b, float *pos_out, int64_t np, int nx, int ny,
+                                   int nz, int n_steps, const float *kick, const float *drift,
+                                   float r_split, void *workspace, size_t workspace_bytes,
+                                   void *sort_workspace, size_t sort_workspace_bytes,
+                                   float *force3s, uint32_t *dests, uint32_t *offsets,
+                                   uint32_t *stats, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  PMGB_REQUIRE(n_steps >= 0, "n_steps is negative");
+  PMGB_REQUIRE(r_split >= 0.0f, "r_split must be non-negative");
+  if (n_steps == 0) return PMGB_OK;
+  NEED(xs);
+  NEED(vel_a);
+  NEED(id_a);
+  NEED(vel_b);
+  NEED(id_b);
+  NEED(pos_out);
+  NEED(kick);
+  NEED(drift);
+  NEED(sort_workspace);
+  NEED(force3s);
+  NEED(dests);
+  NEED(offsets);
+  return fpm_run_sorted_record(xs, vel_a, id_a, vel_b, id_b, pos_out, np, nx, ny, nz, n_steps,
+                               kick, drift, r_split, workspace, workspace_bytes, sort_workspace,
+                               sort_workspace_bytes, force3s, dests, offsets, stats, stream);
+}
+
 int pmgb_fpm_run_sorted_f32(float *pos_a, float *vel_a, uint32_t *id_a, float *pos_b,
                             float *vel_b, uint32_t *id_b, int64_t np, int nx, int ny, int nz,
                             int n_steps, const float *kick, const float *drift, float r_split,

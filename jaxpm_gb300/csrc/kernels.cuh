@@ -112,6 +112,13 @@ int permute3(const float *in, const unsigned *id, int64_t np, float *out,
 int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos,
                  int64_t np, void *sort_ws, size_t sort_bytes, unsigned *stats,
                  cudaStream_t s);
+// the recording forward of the reverse sweep as one run (see sorted.cu)
+int fpm_run_sorted_record(float *xs, float *vel_a, unsigned *id_a, float *vel_b, unsigned *id_b,
+                          float *pos_out, int64_t np, int nx, int ny, int nz, int n_steps,
+                          const float *kick, const float *drift, float r_split, void *mesh_ws,
+                          size_t mesh_bytes, void *sort_ws, size_t sort_bytes, float *f3s,
+                          unsigned *dests, unsigned *offs, unsigned *stats, cudaStream_t s);
+
 int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz,
                const float *pos, float *pos_out, float *vel, int64_t np,
                float kick, float drift, void *sort_ws, size_t sort_bytes,

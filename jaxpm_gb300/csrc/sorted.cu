@@ -1443,6 +1443,62 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, flo
   return PMGB_OK;
 }
 
+// The recording forward of the reverse sweep as one run: per step i the
+// positions it starts from are xs + i*3np (tile order i; xs[0] given), its
+// force meshes are computed into f3s + i*3ncell, the tile ranges are copied
+// to offs + i*(keys+1) and the re-sort map to dests + i*np.  Like
+// fpm_run_sorted, every density after the first is painted by the previous
+// step's gather and the sort overlaps the next step's forces.  The final
+// state goes to (pos_out, vel_b, id_b) if n_steps is odd, else to
+// (pos_out, vel_a, id_a); vel_a / id_a hold the initial velocities / ids.
+int fpm_run_sorted_record(float *xs, float *vel_a, unsigned *id_a, float *vel_b, unsigned *id_b,
+                          float *pos_out, int64_t np, int nx, int ny, int nz, int n_steps,
+                          const float *kick, const float *drift, float r_split, void *mesh_ws,
+                          size_t mesh_bytes, void *sort_ws, size_t sort_bytes, float *f3s,
+                          unsigned *dests, unsigned *offs, unsigned *stats, cudaStream_t s) {
+  PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
+  float *mesh, *f3, *g3;
+  void *dk, *fk;
+  unsigned *work;
+  PMGB_TRY(pm_workspace_regions(mesh_ws, mesh_bytes, nx, ny, nz, np, &mesh, &dk, &fk, &f3, &g3,
+                                &work));
+  (void)f3;
+  (void)g3;
+  (void)work;
+  float *drifted = pm_workspace_particles(mesh_ws, mesh_bytes, nx, ny, nz, np);
+  if (!drifted) return PMGB_ERR_WORKSPACE;
+  if (n_steps <= 0) return PMGB_OK;
+  const int64_t ncell = (int64_t)nx * ny * nz, keys = tile_key_count(nx, ny, nz);
+  float *V[2] = {vel_a, vel_b};
+  unsigned *I[2] = {id_a, id_b};
+  Aux *aux;
+  PMGB_TRY(aux_stream(&aux));
+  PMGB_TRY(paint_sorted(mesh, nx, ny, nz, xs, np, sort_ws, sort_bytes, stats, s));
+  PMGB_TRY(mesh_forces(mesh, nx, ny, nz, r_split, dk, fk, f3s, s));
+  for (int i = 0; i < n_steps; ++i) {
+    const int a = i & 1, b = a ^ 1;
+    float *x = xs + 3 * np * (int64_t)i;
+    float *xn = i + 1 < n_steps ? x + 3 * np : pos_out;
+    if (i > 0) PMGB_CUDA(cudaStreamWaitEvent(s, aux->sorted, 0));
+    PMGB_CUDA(cudaMemcpyAsync(offs + (keys + 1) * (int64_t)i,
+                              tile_offsets(sort_ws, nx, ny, nz, np),
+                              (keys + 1) * sizeof(unsigned), cudaMemcpyDeviceToDevice, s));
+    PMGB_TRY(rkd_sorted(f3s + 3 * ncell * (int64_t)i, ncell, nx, ny, nz, x, drifted, V[a], np,
+                        kick[i], drift[i], sort_ws, sort_bytes, stats, s,
+                        i + 1 < n_steps ? mesh : nullptr));
+    PMGB_CUDA(cudaEventRecord(aux->gathered, s));
+    PMGB_CUDA(cudaStreamWaitEvent(aux->s2, aux->gathered, 0));
+    PMGB_TRY(tile_scatter(drifted, V[a], I[a], np, nx, ny, nz, xn, V[b], I[b],
+                          dests + np * (int64_t)i, sort_ws, sort_bytes, aux->s2));
+    PMGB_CUDA(cudaEventRecord(aux->sorted, aux->s2));
+    if (i + 1 < n_steps)
+      PMGB_TRY(mesh_forces(mesh, nx, ny, nz, r_split, dk, fk, f3s + 3 * ncell * (int64_t)(i + 1),
+                           s));
+  }
+  PMGB_CUDA(cudaStreamWaitEvent(s, aux->sorted, 0));
+  return PMGB_OK;
+}
+
 // ---------------------------------------------------------------------------
 // Adjoint of the sorted step.
 //

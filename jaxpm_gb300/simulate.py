@@ -251,10 +251,20 @@ class SortedFastPM:
         self.load(pos, vel)
         ids0 = self.ids[self.cur].clone()
         if n:
+            # the recording forward as one run (pmgb_fpm_run_sorted_record_f32)
             xs[0].copy_(self.pos[self.cur])
-        for i in range(n):
-            out = xs[i + 1] if i + 1 < n else None
-            self.step(i, pos_in=xs[i], pos_out=out, record=(f3s[i], dests[i], offs[i]))
+            a, b = self.cur, 1 - self.cur
+            last = a if n % 2 == 0 else b
+            kick = np.ascontiguousarray(self.kick[:n], dtype=np.float32)
+            drift = np.ascontiguousarray(self.drift[:n], dtype=np.float32)
+            fp = ctypes.POINTER(ctypes.c_float)
+            _lib.call("pmgb_fpm_run_sorted_record_f32", _lib.ptr(xs), _lib.ptr(self.vel[a]),
+                      _lib.ptr(self.ids[a]), _lib.ptr(self.vel[b]), _lib.ptr(self.ids[b]),
+                      _lib.ptr(self.pos[last]), self.n, nx, ny, nz, n, kick.ctypes.data_as(fp),
+                      drift.ctypes.data_as(fp), self.r_split, _lib.ptr(self.ws), self.ws_bytes,
+                      _lib.ptr(self.sort_ws), self.sort_bytes, _lib.ptr(f3s), _lib.ptr(dests),
+                      _lib.ptr(offs), _lib.ptr(self.stats_buf), _lib.stream())
+            self.cur = last
         final = self.state()
         if not hasattr(self, "_adj"):
             e = lambda: torch.empty((self.n, 3), dtype=torch.float32, device=self.ws.device)  # noqa
