@@ -546,10 +546,12 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
                  unsigned *__restrict__ counts, unsigned *__restrict__ rank,
                  unsigned *__restrict__ stats, const __grid_constant__ CUtensorMap tmap,
                  int use_tma, float *__restrict__ mesh_next, int pvec,
-                 const __grid_constant__ CUtensorMap pmap, int use_ptma) {
+                 const __grid_constant__ CUtensorMap pmap, int use_ptma,
+                 unsigned *__restrict__ work) {
   __shared__ __align__(128) float fb[2][FBOX_STRIDE];
   __shared__ __align__(16) float ff[POT ? FBOX : 4];  // POT: the tile's force box
   __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t s_grab[2];  // the tile after next, as grabbed by thread 0
   extern __shared__ __align__(128) unsigned pbox[];  // PAINT: 2 x NBOX_WORDS
   constexpr uint32_t BOX_BYTES = POT ? PBOX_BYTES : FBOX_BYTES;
   const int tid = threadIdx.x;
@@ -562,9 +564,14 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
   __syncthreads();
   int pbuf = 0;
   uint32_t phase0 = 0u, phase1 = 0u;  // parity of the next completion of bar[0] / bar[1]
-  const uint32_t stride = gridDim.x;
+  // Dynamic tile schedule (the particle count per tile varies widely once
+  // structure forms): each CTA starts on tiles blockIdx.x and gridDim.x +
+  // blockIdx.x, and thread 0 takes every later tile from the counter *work
+  // (zero at launch) two tiles ahead, so the atomic's latency hides behind a
+  // tile's work.  Every key is processed exactly once.
   uint32_t key = blockIdx.x;
   if (key >= nkeys) return;
+  uint32_t knext = gridDim.x + blockIdx.x;
   TileInfo cur = tile_info(offsets, key, nx, ny, nz, use_tma, POT);
   if (cur.tma && tid == 0) {
     mbar_expect_tx(&bar[0], BOX_BYTES);
@@ -572,10 +579,11 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
     else tma_load_4d(fb[0], &tmap, cur.oz, cur.oy, cur.ox, 0, &bar[0]);
   }
   int buf = 0;
-  for (; key < nkeys; key += stride) {
+  while (key < nkeys) {
+    uint32_t kgrab = 0xffffffffu;  // thread 0: the tile after next
+    if (tid == 0 && knext < nkeys) kgrab = 2u * gridDim.x + atomicAdd(work, 1u);
     // prefetch the next tile's box into the other buffer (freed by the
     // barrier at the end of the previous iteration)
-    const uint32_t knext = key + stride;
     TileInfo nxt;
     nxt.tma = false;
     if (knext < nkeys) {
@@ -676,6 +684,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
         __syncthreads();
         box = ff;
       }
+      if (tid == 0) s_grab[buf] = kgrab;  // returned by now; frees its register
       // every lane of a warp runs the same iterations (ballot / match inside);
       // each thread loads RKD_ILP particles before computing any of them
       for (unsigned p0 = cur.beg; p0 < cur.end; p0 += TILE_THREADS * RKD_ILP) {
@@ -770,8 +779,11 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
         if (counts) count_home(counts, k, key, valid);
        }
       }
+    } else if (tid == 0) {
+      s_grab[buf] = kgrab;
     }
     __syncthreads();  // buffer `buf` is free for the prefetch two tiles ahead
+    const uint32_t kafter = s_grab[buf];  // rewritten two iterations later, after a barrier
     if (PAINT && cur.beg != cur.end) {
       // flush the paint box, each warp its x-planes (w and w + 8): fixed
       // point -> float in place, one TMA reduce-add per plane into the mesh
@@ -837,6 +849,8 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
       pbuf ^= 1;
     }
     cur = nxt;
+    key = knext;
+    knext = kafter;
     buf ^= 1;
   }
   if (PAINT && use_ptma && (tid & 31) == 0) bulk_wait_all();  // reductions done before exit
@@ -1255,7 +1269,9 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float 
   }
   CUtensorMap pmap;
   memset(&pmap, 0, sizeof(pmap));
-  static bool ready[4][64] = {{false}};
+  // per variant and device: shared-memory opt-in done, and the resident CTAs
+  // per SM (the grid of the dynamic tile schedule)
+  static int resident[4][64] = {{0}};
   int dev = 0;
   PMGB_CUDA(cudaGetDevice(&dev));
   const int variant = (mesh_next ? 1 : 0) + (pot ? 2 : 0);
@@ -1264,9 +1280,12 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float 
                    : variant == 2 ? (const void *)rkd_tiles_kernel<false, true>
                                   : (const void *)rkd_tiles_kernel<true, true>;
   const size_t dsmem = mesh_next ? RKDP_SMEM : 0;
-  if (dev >= 64 || !ready[variant][dev]) {
+  int per_sm = dev < 64 ? resident[variant][dev] : 0;
+  if (per_sm == 0) {
     PMGB_TRY(set_smem(fn, dsmem));
-    if (dev < 64) ready[variant][dev] = true;
+    PMGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, TILE_THREADS, dsmem));
+    per_sm = std::max(per_sm, 1);
+    if (dev < 64) resident[variant][dev] = per_sm;
   }
   int use_ptma = 0;
   bool aligned = false;
@@ -1283,10 +1302,13 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float 
       clear_error();
     }
   }
+  // the tile counter of the dynamic schedule (the word after the painter's)
+  unsigned *work = sc.work + 1;
+  PMGB_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
 #define RKD_ARGS                                                                             \
   f3, cs, nx, ny, nz, pos, pos_out, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts, \
-      sc.rank, stats, map, use_tma, mesh_next, aligned ? 1 : 0, pmap, use_ptma
-  const unsigned grid = tile_grid(keys);
+      sc.rank, stats, map, use_tma, mesh_next, aligned ? 1 : 0, pmap, use_ptma, work
+  const unsigned grid = (unsigned)std::min<int64_t>(keys, (int64_t)sm_count() * per_sm);
   switch (variant) {
     case 0: rkd_tiles_kernel<false, false><<<grid, TILE_THREADS, dsmem, s>>>(RKD_ARGS); break;
     case 1: rkd_tiles_kernel<true, false><<<grid, TILE_THREADS, dsmem, s>>>(RKD_ARGS); break;
