@@ -1159,6 +1159,25 @@ static unsigned tile_grid(int64_t keys) {
   return (unsigned)std::min<int64_t>(keys, (int64_t)sm_count() * 8);
 }
 
+// The scatter's grid: one wave of resident CTAs (every CTA strides over the
+// same number of 1024-particle chunks, so a partial last wave would leave
+// SMs idle for a third of the kernel).
+static int scatter_grid(int64_t np, unsigned *grid) {
+  static int resident[64] = {0};
+  int dev = 0;
+  PMGB_CUDA(cudaGetDevice(&dev));
+  int per_sm = dev < 64 ? resident[dev] : 0;
+  if (per_sm == 0) {
+    PMGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)scatter_kernel,
+                                                            256, 0));
+    per_sm = std::max(per_sm, 1);
+    if (dev < 64) resident[dev] = per_sm;
+  }
+  const int64_t chunks = (np + 256 * SCATTER_ILP - 1) / (256 * SCATTER_ILP);
+  *grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(chunks, (int64_t)sm_count() * per_sm));
+  return PMGB_OK;
+}
+
 int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np, int nx, int ny,
               int nz, float *pos2, float *vel2, unsigned *id2, void *ws, size_t bytes,
               cudaStream_t s) {
@@ -1172,9 +1191,10 @@ int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np
   }
   PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
   if (np > 0) {
-    scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
-                                                      sc.offsets, nullptr, pos2, vel2, id2,
-                                                      nullptr);
+    unsigned grid = 1;
+    PMGB_TRY(scatter_grid(np, &grid));
+    scatter_kernel<<<grid, 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz, sc.offsets,
+                                        nullptr, pos2, vel2, id2, nullptr);
     PMGB_LAUNCHED("scatter_kernel");
   }
   return PMGB_OK;
@@ -1333,9 +1353,10 @@ int tile_scatter(const float *pos, const float *vel, const unsigned *id, int64_t
   // the counts become the per-tile slot cursors of the scatter
   PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
   if (np > 0) {
-    scatter_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, vel, id, nullptr, np, nx, ny, nz,
-                                                      sc.offsets, sc.counts, pos2, vel2, id2,
-                                                      dest);
+    unsigned grid = 1;
+    PMGB_TRY(scatter_grid(np, &grid));
+    scatter_kernel<<<grid, 256, 0, s>>>(pos, vel, id, nullptr, np, nx, ny, nz, sc.offsets,
+                                        sc.counts, pos2, vel2, id2, dest);
     PMGB_LAUNCHED("scatter_kernel");
   }
   return PMGB_OK;
@@ -1687,10 +1708,12 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
                         float *__restrict__ gv_out, float kick, float drift,
                         const unsigned *__restrict__ offsets, uint32_t nkeys,
                         unsigned *__restrict__ stats, const __grid_constant__ CUtensorMap fmap,
-                        const __grid_constant__ CUtensorMap rmap, int use_tma) {
+                        const __grid_constant__ CUtensorMap rmap, int use_tma,
+                        unsigned *__restrict__ work) {
   __shared__ __align__(128) float fb[2][FBOX_STRIDE];
   __shared__ __align__(128) float rb[2][RBOX_STRIDE];
   __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t s_grab[2];
   const int tid = threadIdx.x;
   if (tid == 0) {
     mbar_init(&bar[0], 1);
@@ -1699,9 +1722,12 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
   }
   __syncthreads();
   uint32_t phase0 = 0u, phase1 = 0u;
-  const uint32_t stride = gridDim.x;
+  // dynamic tile schedule, as in rkd_tiles_kernel: tiles blockIdx.x and
+  // gridDim.x + blockIdx.x, then thread 0 takes each later one from *work two
+  // tiles ahead
   uint32_t key = blockIdx.x;
   if (key >= nkeys) return;
+  uint32_t knext = gridDim.x + blockIdx.x;
   TileInfo cur = tile_info(offsets, key, nx, ny, nz, use_tma);
   if (cur.tma && tid == 0) {
     mbar_expect_tx(&bar[0], FBOX_BYTES + RBOX_BYTES);
@@ -1709,8 +1735,9 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
     tma_load_3d(rb[0], &rmap, cur.oz, cur.oy, cur.ox, &bar[0]);
   }
   int buf = 0;
-  for (; key < nkeys; key += stride) {
-    const uint32_t knext = key + stride;
+  while (key < nkeys) {
+    uint32_t kgrab = 0xffffffffu;
+    if (tid == 0 && knext < nkeys) kgrab = 2u * gridDim.x + atomicAdd(work, 1u);
     TileInfo nxt;
     nxt.tma = false;
     if (knext < nkeys) {
@@ -1744,6 +1771,7 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
         }
         __syncthreads();
       }
+      if (tid == 0) s_grab[buf] = kgrab;
       for (unsigned p = cur.beg + tid; p < cur.end; p += TILE_THREADS) {
         float g[3], u[3], w[3];
         adj_cotangent(gx, gv, dest, p, kick, drift, g, u, w);
@@ -1783,9 +1811,14 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
         gv_out[3 * (int64_t)p + 1] = u[1];
         gv_out[3 * (int64_t)p + 2] = u[2];
       }
+    } else if (tid == 0) {
+      s_grab[buf] = kgrab;
     }
     __syncthreads();
+    const uint32_t kafter = s_grab[buf];  // rewritten two iterations later, after a barrier
     cur = nxt;
+    key = knext;
+    knext = kafter;
     buf ^= 1;
   }
 }
@@ -1849,9 +1882,19 @@ int fpm_step_sorted_vjp(const float *pos, const float *force3, const unsigned *d
   // 2. rho_bar = sum_c A_c^T (painted component c)
   PMGB_TRY(mesh_forces_vjp(g3, nx, ny, nz, r_split, dk, fk, mesh, s));
   // 3. gather of both position terms and the cotangent update
-  adj_gather_tiles_kernel<<<tile_grid(keys), TILE_THREADS, 0, s>>>(
+  static int resident[64] = {0};
+  int per_sm = dev < 64 ? resident[dev] : 0;
+  if (per_sm == 0) {
+    PMGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, (const void *)adj_gather_tiles_kernel, TILE_THREADS, 0));
+    per_sm = std::max(per_sm, 1);
+    if (dev < 64) resident[dev] = per_sm;
+  }
+  PMGB_CUDA(cudaMemsetAsync(work + 1, 0, sizeof(unsigned), s));
+  adj_gather_tiles_kernel<<<(unsigned)std::min<int64_t>(keys, (int64_t)sm_count() * per_sm),
+                            TILE_THREADS, 0, s>>>(
       force3, ncell, mesh, nx, ny, nz, pos, dest, gx_in, gv_in, gx_out, gv_out, kick, drift,
-      offsets, (uint32_t)keys, stats, fmap, rmap, use_tma);
+      offsets, (uint32_t)keys, stats, fmap, rmap, use_tma, work + 1);
   PMGB_LAUNCHED("adj_gather_tiles_kernel");
   return PMGB_OK;
 }
