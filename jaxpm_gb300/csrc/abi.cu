@@ -4,6 +4,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 
 #include "common.cuh"
 #include "kernels.cuh"
@@ -37,6 +38,28 @@ int sm_count() {
   if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
     n = 148;
   g_sm[dev] = n;
+  return n;
+}
+
+int resident_ctas(const void *kernel, int threads, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void *, int, int, size_t>, int> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return sm_count();
+  const auto key = std::make_tuple(kernel, dev, threads, smem);
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+  }
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const int n = per_sm * sm_count();
+  std::lock_guard<std::mutex> lk(mu);
+  cache[key] = n;
   return n;
 }
 

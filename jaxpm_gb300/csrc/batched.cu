@@ -466,8 +466,8 @@ int kspace_potential_batched(const Plan &P, float2 *dk, float r_split, cudaStrea
     G.begin = G.g[0].start;
     const Group &last = P.groups[g0 + G.count - 1];
     G.end = last.spec + (int64_t)last.n * last.nx * last.ny * (last.nz / 2 + 1);
-    batch_potential_kernel<<<grid_for(G.end - G.begin, 256), 256, 0, s>>>(dk, G,
-                                                                          r_split * r_split);
+    batch_potential_kernel<<<wave_grid(batch_potential_kernel, G.end - G.begin, 256), 256, 0, s>>>(
+        dk, G, r_split * r_split);
     PMGB_LAUNCHED("batch_potential_kernel");
   }
   return PMGB_OK;

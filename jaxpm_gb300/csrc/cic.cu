@@ -324,20 +324,20 @@ int paint(float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
     auto *acc = static_cast<unsigned long long *>(ws);
     PMGB_CUDA(cudaMemsetAsync(acc, 0, need, s));
     if (np > 0) {
-      paint_fixed_kernel<<<grid_for(np, 256), 256, 0, s>>>(acc, nx, ny, nz, pos, np,
-                                                            weights, wscale);
+      paint_fixed_kernel<<<wave_grid(paint_fixed_kernel, np, 256), 256, 0, s>>>(
+          acc, nx, ny, nz, pos, np, weights, wscale);
       PMGB_LAUNCHED("paint_fixed_kernel");
     }
-    fixed_to_float_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(mesh, acc, ncell, accumulate);
+    fixed_to_float_kernel<<<wave_grid(fixed_to_float_kernel, ncell, 256), 256, 0, s>>>(
+        mesh, acc, ncell, accumulate);
     PMGB_LAUNCHED("fixed_to_float_kernel");
     return PMGB_OK;
   }
   if (!accumulate) PMGB_CUDA(cudaMemsetAsync(mesh, 0, ncell * sizeof(float), s));
   if (np == 0) return PMGB_OK;
   if (mode == PMGB_PAINT_ATOMIC) {
-    paint_atomic_kernel<<<grid_for(np, 256), 256, 0, s>>>(mesh, nx, ny, nz, pos, np,
-                                                           weights, wscale,
-                                                           zpair_vec_ok(mesh, nz));
+    paint_atomic_kernel<<<wave_grid(paint_atomic_kernel, np, 256), 256, 0, s>>>(
+        mesh, nx, ny, nz, pos, np, weights, wscale, zpair_vec_ok(mesh, nz));
     PMGB_LAUNCHED("paint_atomic_kernel");
     return PMGB_OK;
   }
@@ -355,11 +355,12 @@ int paint_fixed_into(unsigned long long *acc, float *mesh, int nx, int ny, int n
   const int64_t ncell = (int64_t)nx * ny * nz;
   PMGB_CUDA(cudaMemsetAsync(acc, 0, ncell * sizeof(unsigned long long), s));
   if (np > 0) {
-    paint_fixed_kernel<<<grid_for(np, 256), 256, 0, s>>>(acc, nx, ny, nz, pos, np, weights,
-                                                          wscale);
+    paint_fixed_kernel<<<wave_grid(paint_fixed_kernel, np, 256), 256, 0, s>>>(
+        acc, nx, ny, nz, pos, np, weights, wscale);
     PMGB_LAUNCHED("paint_fixed_kernel");
   }
-  fixed_to_float_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(mesh, acc, ncell, accumulate);
+  fixed_to_float_kernel<<<wave_grid(fixed_to_float_kernel, ncell, 256), 256, 0, s>>>(
+      mesh, acc, ncell, accumulate);
   PMGB_LAUNCHED("fixed_to_float_kernel");
   return PMGB_OK;
 }
@@ -367,7 +368,7 @@ int paint_fixed_into(unsigned long long *acc, float *mesh, int nx, int ny, int n
 int read(const float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
          float *out, cudaStream_t s) {
   if (np == 0) return PMGB_OK;
-  read_kernel<<<grid_for(np, 256), 256, 0, s>>>(mesh, nx, ny, nz, pos, np, out);
+  read_kernel<<<wave_grid(read_kernel, np, 256), 256, 0, s>>>(mesh, nx, ny, nz, pos, np, out);
   PMGB_LAUNCHED("read_kernel");
   return PMGB_OK;
 }
@@ -375,7 +376,8 @@ int read(const float *mesh, int nx, int ny, int nz, const float *pos, int64_t np
 int read3(const float *mesh3, int64_t cs, int nx, int ny, int nz, const float *pos,
           int64_t np, float *out, cudaStream_t s) {
   if (np == 0) return PMGB_OK;
-  read3_kernel<<<grid_for(np, 256), 256, 0, s>>>(mesh3, cs, nx, ny, nz, pos, np, out);
+  read3_kernel<<<wave_grid(read3_kernel, np, 256), 256, 0, s>>>(
+      mesh3, cs, nx, ny, nz, pos, np, out);
   PMGB_LAUNCHED("read3_kernel");
   return PMGB_OK;
 }
@@ -383,7 +385,7 @@ int read3(const float *mesh3, int64_t cs, int nx, int ny, int nz, const float *p
 int cic_weights(const float *pos, int64_t np, int nx, int ny, int nz, int32_t *idx,
                 float *w, cudaStream_t s) {
   if (np == 0) return PMGB_OK;
-  weights_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, np, nx, ny, nz, idx, w);
+  weights_kernel<<<wave_grid(weights_kernel, np, 256), 256, 0, s>>>(pos, np, nx, ny, nz, idx, w);
   PMGB_LAUNCHED("weights_kernel");
   return PMGB_OK;
 }
@@ -392,8 +394,8 @@ int paint_vjp(const float *g_mesh, int nx, int ny, int nz, const float *pos, int
               const float *weights, float wscale, float *g_pos, float *g_w,
               cudaStream_t s) {
   if (np == 0 || (!g_pos && !g_w)) return PMGB_OK;
-  paint_vjp_kernel<<<grid_for(np, 256), 256, 0, s>>>(g_mesh, nx, ny, nz, pos, np, weights,
-                                                      wscale, g_pos, g_w);
+  paint_vjp_kernel<<<wave_grid(paint_vjp_kernel, np, 256), 256, 0, s>>>(
+      g_mesh, nx, ny, nz, pos, np, weights, wscale, g_pos, g_w);
   PMGB_LAUNCHED("paint_vjp_kernel");
   return PMGB_OK;
 }
@@ -402,14 +404,13 @@ int read_vjp(const float *mesh, int nx, int ny, int nz, const float *pos, int64_
              const float *g_out, float *g_mesh, float *g_pos, cudaStream_t s) {
   if (np == 0) return PMGB_OK;
   if (g_mesh) {
-    paint_atomic_kernel<<<grid_for(np, 256), 256, 0, s>>>(g_mesh, nx, ny, nz, pos, np,
-                                                           g_out, 1.0f,
-                                                           zpair_vec_ok(g_mesh, nz));
+    paint_atomic_kernel<<<wave_grid(paint_atomic_kernel, np, 256), 256, 0, s>>>(
+        g_mesh, nx, ny, nz, pos, np, g_out, 1.0f, zpair_vec_ok(g_mesh, nz));
     PMGB_LAUNCHED("paint_atomic_kernel");
   }
   if (g_pos) {
-    read_vjp_pos_kernel<<<grid_for(np, 256), 256, 0, s>>>(mesh, nx, ny, nz, pos, np,
-                                                           g_out, g_pos);
+    read_vjp_pos_kernel<<<wave_grid(read_vjp_pos_kernel, np, 256), 256, 0, s>>>(
+        mesh, nx, ny, nz, pos, np, g_out, g_pos);
     PMGB_LAUNCHED("read_vjp_pos_kernel");
   }
   return PMGB_OK;
@@ -419,7 +420,8 @@ int paint_dx(float *mesh, int nx, int ny, int nz, const float *disp, const float
              float wscale, int accumulate, cudaStream_t s) {
   const int64_t n = (int64_t)nx * ny * nz;
   if (!accumulate) PMGB_CUDA(cudaMemsetAsync(mesh, 0, n * sizeof(float), s));
-  paint_dx_kernel<<<grid_for(n, 256), 256, 0, s>>>(mesh, nx, ny, nz, disp, weights, wscale);
+  paint_dx_kernel<<<wave_grid(paint_dx_kernel, n, 256), 256, 0, s>>>(
+      mesh, nx, ny, nz, disp, weights, wscale);
   PMGB_LAUNCHED("paint_dx_kernel");
   return PMGB_OK;
 }
@@ -427,7 +429,7 @@ int paint_dx(float *mesh, int nx, int ny, int nz, const float *disp, const float
 int read_dx(const float *mesh, int nx, int ny, int nz, const float *disp, float *out,
             cudaStream_t s) {
   const int64_t n = (int64_t)nx * ny * nz;
-  read_dx_kernel<<<grid_for(n, 256), 256, 0, s>>>(mesh, nx, ny, nz, disp, out);
+  read_dx_kernel<<<wave_grid(read_dx_kernel, n, 256), 256, 0, s>>>(mesh, nx, ny, nz, disp, out);
   PMGB_LAUNCHED("read_dx_kernel");
   return PMGB_OK;
 }
@@ -435,7 +437,7 @@ int read_dx(const float *mesh, int nx, int ny, int nz, const float *disp, float 
 int enmesh(const float *disp, int nx, int ny, int nz, int32_t *idx, float *w,
            cudaStream_t s) {
   const int64_t n = (int64_t)nx * ny * nz;
-  enmesh_kernel<<<grid_for(n, 256), 256, 0, s>>>(disp, nx, ny, nz, idx, w);
+  enmesh_kernel<<<wave_grid(enmesh_kernel, n, 256), 256, 0, s>>>(disp, nx, ny, nz, idx, w);
   PMGB_LAUNCHED("enmesh_kernel");
   return PMGB_OK;
 }

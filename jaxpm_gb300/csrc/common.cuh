@@ -65,6 +65,23 @@ inline unsigned grid_for(int64_t n, int threads, int per_sm = 8) {
   return (unsigned)(need < cap ? need : cap);
 }
 
+// CTAs of `kernel` resident on the whole device at once (its occupancy at
+// `threads` per block and `smem` dynamic shared bytes, times the SM count),
+// cached per kernel and device.
+int resident_ctas(const void *kernel, int threads, size_t smem);
+
+// Grid of a grid-stride loop over n items whose chunks all cost about the
+// same: at most one wave of the kernel's resident CTAs.  A fixed cap of
+// 8 CTAs per SM leaves a partial last wave (SMs idle for part of the kernel)
+// whenever the kernel's registers allow fewer than 8 per SM.
+template <typename K>
+inline unsigned wave_grid(K *kernel, int64_t n, int threads, size_t smem = 0) {
+  int64_t need = (n + threads - 1) / threads;
+  const int64_t cap = resident_ctas(reinterpret_cast<const void *>(kernel), threads, smem);
+  if (need < 1) need = 1;
+  return (unsigned)(need < cap ? need : cap);
+}
+
 // ---------------------------------------------------------------------------
 // CIC arithmetic, absolute mode (reference: jaxpm/painting.py:21-37).
 // Every operation is rounded separately (no FMA contraction) so that the

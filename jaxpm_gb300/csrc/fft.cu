@@ -155,7 +155,7 @@ int fft_planes_c2r(void *in, float *out, int nplanes, int ny, int nz, int pitch,
 
 int scale_inplace(float *x, int64_t n, float scale, cudaStream_t s) {
   if (n == 0) return PMGB_OK;
-  scale_kernel<<<grid_for(n, 256), 256, 0, s>>>(x, n, scale);
+  scale_kernel<<<wave_grid(scale_kernel, n, 256), 256, 0, s>>>(x, n, scale);
   PMGB_LAUNCHED("scale_kernel");
   return PMGB_OK;
 }

@@ -164,7 +164,7 @@ int kspace_forces(const void *dk, void *fk, int64_t cs, int nx, int ny, int nz, 
   uint32_t total, nzh;
   PMGB_TRY(geometry(nx, ny, nz, &total, &nzh));
   PMGB_TRY(tables(nx, ny, nz, &t));
-  forces_kernel<<<grid_for(total, 256), 256, 0, s>>>(
+  forces_kernel<<<wave_grid(forces_kernel, total, 256), 256, 0, s>>>(
       static_cast<const float2 *>(dk), static_cast<float2 *>(fk), cs, t, ny, nzh, total,
       r_split * r_split, order, fd, scale);
   PMGB_LAUNCHED("forces_kernel");
@@ -177,7 +177,7 @@ int kspace_forces_vjp(const void *gfk, int64_t cs, void *gdk, int nx, int ny, in
   uint32_t total, nzh;
   PMGB_TRY(geometry(nx, ny, nz, &total, &nzh));
   PMGB_TRY(tables(nx, ny, nz, &t));
-  forces_vjp_kernel<<<grid_for(total, 256), 256, 0, s>>>(
+  forces_vjp_kernel<<<wave_grid(forces_vjp_kernel, total, 256), 256, 0, s>>>(
       static_cast<const float2 *>(gfk), cs, static_cast<float2 *>(gdk), t, ny, nzh, total,
       r_split * r_split, order, fd, scale);
   PMGB_LAUNCHED("forces_vjp_kernel");
@@ -189,8 +189,8 @@ int kspace_invlaplace(void *spec, int nx, int ny, int nz, int fd, float scale, c
   uint32_t total, nzh;
   PMGB_TRY(geometry(nx, ny, nz, &total, &nzh));
   PMGB_TRY(tables(nx, ny, nz, &t));
-  invlaplace_kernel<<<grid_for(total, 256), 256, 0, s>>>(static_cast<float2 *>(spec), t, ny,
-                                                          nzh, total, fd, scale);
+  invlaplace_kernel<<<wave_grid(invlaplace_kernel, total, 256), 256, 0, s>>>(
+      static_cast<float2 *>(spec), t, ny, nzh, total, fd, scale);
   PMGB_LAUNCHED("invlaplace_kernel");
   return PMGB_OK;
 }
@@ -200,8 +200,8 @@ int kspace_longrange(void *spec, int nx, int ny, int nz, float r_split, cudaStre
   uint32_t total, nzh;
   PMGB_TRY(geometry(nx, ny, nz, &total, &nzh));
   PMGB_TRY(tables(nx, ny, nz, &t));
-  longrange_kernel<<<grid_for(total, 256), 256, 0, s>>>(static_cast<float2 *>(spec), t, ny,
-                                                         nzh, total, r_split * r_split);
+  longrange_kernel<<<wave_grid(longrange_kernel, total, 256), 256, 0, s>>>(
+      static_cast<float2 *>(spec), t, ny, nzh, total, r_split * r_split);
   PMGB_LAUNCHED("longrange_kernel");
   return PMGB_OK;
 }
@@ -212,9 +212,8 @@ int kspace_gradient(const void *in, void *out, int nx, int ny, int nz, int dir, 
   uint32_t total, nzh;
   PMGB_TRY(geometry(nx, ny, nz, &total, &nzh));
   PMGB_TRY(tables(nx, ny, nz, &t));
-  gradient_kernel<<<grid_for(total, 256), 256, 0, s>>>(static_cast<const float2 *>(in),
-                                                        static_cast<float2 *>(out), t, ny, nzh,
-                                                        total, dir, order);
+  gradient_kernel<<<wave_grid(gradient_kernel, total, 256), 256, 0, s>>>(
+      static_cast<const float2 *>(in), static_cast<float2 *>(out), t, ny, nzh, total, dir, order);
   PMGB_LAUNCHED("gradient_kernel");
   return PMGB_OK;
 }

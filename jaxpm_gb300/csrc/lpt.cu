@@ -173,8 +173,8 @@ int linear_field_colour(void *spec, int nx, int ny, int nz, float bx, float by, 
                         const float *tk, const float *tp, int nt, float scale, cudaStream_t s) {
   const int64_t total = (int64_t)nx * ny * (nz / 2 + 1);
   float norm = (float)((double)nx * ny * nz / ((double)bx * by * bz));
-  colour_kernel<<<grid_for(total, 256), 256, 0, s>>>(static_cast<float2 *>(spec), nx, ny, nz,
-                                                      bx, by, bz, tk, tp, nt, norm, scale);
+  colour_kernel<<<wave_grid(colour_kernel, total, 256), 256, 0, s>>>(
+      static_cast<float2 *>(spec), nx, ny, nz, bx, by, bz, tk, tp, nt, norm, scale);
   PMGB_LAUNCHED("colour_kernel");
   return PMGB_OK;
 }
@@ -195,11 +195,11 @@ int lpt2_source(const void *dk, float *delta2, int nx, int ny, int nz, void *ws,
   const int64_t nhalf = (int64_t)nx * ny * (nz / 2 + 1);
   float2 *spec = static_cast<float2 *>(ws);
   float *shear = reinterpret_cast<float *>(static_cast<char *>(ws) + align256(6 * nhalf * 8));
-  shear_kernel<<<grid_for(nhalf, 256), 256, 0, s>>>(static_cast<const float2 *>(dk), spec, nhalf,
-                                                     nx, ny, nz, 1.0f / (float)ncell);
+  shear_kernel<<<wave_grid(shear_kernel, nhalf, 256), 256, 0, s>>>(
+      static_cast<const float2 *>(dk), spec, nhalf, nx, ny, nz, 1.0f / (float)ncell);
   PMGB_LAUNCHED("shear_kernel");
   PMGB_TRY(fft_c2r(spec, shear, nx, ny, nz, 6, s));
-  source_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(shear, ncell, delta2, ncell);
+  source_kernel<<<wave_grid(source_kernel, ncell, 256), 256, 0, s>>>(shear, ncell, delta2, ncell);
   PMGB_LAUNCHED("source_kernel");
   return PMGB_OK;
 }
@@ -219,13 +219,16 @@ int lpt2_source_vjp(const float *ic, const float *g, float *g_ic, int nx, int ny
   // meshes' region, which holds one spectrum and is overwritten next)
   float2 *dk = reinterpret_cast<float2 *>(shear);
   PMGB_TRY(fft_r2c(ic, dk, nx, ny, nz, 1, s));
-  shear_kernel<<<grid_for(nhalf, 256), 256, 0, s>>>(dk, spec, nhalf, nx, ny, nz, scale);
+  shear_kernel<<<wave_grid(shear_kernel, nhalf, 256), 256, 0, s>>>(
+      dk, spec, nhalf, nx, ny, nz, scale);
   PMGB_LAUNCHED("shear_kernel");
   PMGB_TRY(fft_c2r(spec, shear, nx, ny, nz, 6, s));
-  source_vjp_kernel<<<grid_for(ncell, 256), 256, 0, s>>>(shear, ncell, g, ncell);
+  source_vjp_kernel<<<wave_grid(source_vjp_kernel, ncell, 256), 256, 0, s>>>(
+      shear, ncell, g, ncell);
   PMGB_LAUNCHED("source_vjp_kernel");
   PMGB_TRY(fft_r2c(shear, spec, nx, ny, nz, 6, s));
-  shear_vjp_kernel<<<grid_for(nhalf, 256), 256, 0, s>>>(spec, nhalf, nx, ny, nz, scale);
+  shear_vjp_kernel<<<wave_grid(shear_vjp_kernel, nhalf, 256), 256, 0, s>>>(
+      spec, nhalf, nx, ny, nz, scale);
   PMGB_LAUNCHED("shear_vjp_kernel");
   return fft_c2r(spec, g_ic, nx, ny, nz, 1, s);
 }
@@ -233,7 +236,7 @@ int lpt2_source_vjp(const float *ic, const float *g, float *g_ic, int nx, int ny
 int lpt_combine(const float *a, const float *b, int64_t n, float ca, float cb, float *out,
                 cudaStream_t s) {
   if (n == 0) return PMGB_OK;
-  combine_kernel<<<grid_for(n, 256), 256, 0, s>>>(a, b, n, ca, cb, out);
+  combine_kernel<<<wave_grid(combine_kernel, n, 256), 256, 0, s>>>(a, b, n, ca, cb, out);
   PMGB_LAUNCHED("combine_kernel");
   return PMGB_OK;
 }

@@ -1109,7 +1109,7 @@ int exclusive_scan(const unsigned *in, unsigned *out, int64_t n, unsigned *sums,
   if (nb > 1) {
     scan_sums_kernel<<<1, SCAN_THREADS, 0, s>>>(sums, (int)nb);
     PMGB_LAUNCHED("scan_sums_kernel");
-    scan_add_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, n, sums, grand_total);
+    scan_add_kernel<<<wave_grid(scan_add_kernel, n, 256), 256, 0, s>>>(out, n, sums, grand_total);
     PMGB_LAUNCHED("scan_add_kernel");
   }
   return PMGB_OK;
@@ -1162,20 +1162,8 @@ static unsigned tile_grid(int64_t keys) {
 // The scatter's grid: one wave of resident CTAs (every CTA strides over the
 // same number of 1024-particle chunks, so a partial last wave would leave
 // SMs idle for a third of the kernel).
-static int scatter_grid(int64_t np, unsigned *grid) {
-  static int resident[64] = {0};
-  int dev = 0;
-  PMGB_CUDA(cudaGetDevice(&dev));
-  int per_sm = dev < 64 ? resident[dev] : 0;
-  if (per_sm == 0) {
-    PMGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void *)scatter_kernel,
-                                                            256, 0));
-    per_sm = std::max(per_sm, 1);
-    if (dev < 64) resident[dev] = per_sm;
-  }
-  const int64_t chunks = (np + 256 * SCATTER_ILP - 1) / (256 * SCATTER_ILP);
-  *grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(chunks, (int64_t)sm_count() * per_sm));
-  return PMGB_OK;
+static unsigned scatter_grid(int64_t np) {
+  return wave_grid(scatter_kernel, (np + SCATTER_ILP - 1) / SCATTER_ILP, 256);
 }
 
 int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np, int nx, int ny,
@@ -1186,15 +1174,15 @@ int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np
   SortScratch sc = sort_scratch(ws, nx, ny, nz, np);
   PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
   if (np > 0) {
-    tile_rank_kernel<<<grid_for(np, 256), 256, 0, s>>>(pos, np, nx, ny, nz, sc.counts, sc.rank);
+    tile_rank_kernel<<<wave_grid(tile_rank_kernel, np, 256), 256, 0, s>>>(
+        pos, np, nx, ny, nz, sc.counts, sc.rank);
     PMGB_LAUNCHED("tile_rank_kernel");
   }
   PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
   if (np > 0) {
-    unsigned grid = 1;
-    PMGB_TRY(scatter_grid(np, &grid));
-    scatter_kernel<<<grid, 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz, sc.offsets,
-                                        nullptr, pos2, vel2, id2, nullptr);
+    scatter_kernel<<<scatter_grid(np), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
+                                                    sc.offsets, nullptr, pos2, vel2, id2,
+                                                    nullptr);
     PMGB_LAUNCHED("scatter_kernel");
   }
   return PMGB_OK;
@@ -1202,14 +1190,14 @@ int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np
 
 int unpermute3(const float *in, const unsigned *id, int64_t np, float *out, cudaStream_t s) {
   if (np == 0) return PMGB_OK;
-  unpermute3_kernel<<<grid_for(np, 256), 256, 0, s>>>(in, id, np, out);
+  unpermute3_kernel<<<wave_grid(unpermute3_kernel, np, 256), 256, 0, s>>>(in, id, np, out);
   PMGB_LAUNCHED("unpermute3_kernel");
   return PMGB_OK;
 }
 
 int permute3(const float *in, const unsigned *id, int64_t np, float *out, cudaStream_t s) {
   if (np == 0) return PMGB_OK;
-  permute3_kernel<<<grid_for(np, 256), 256, 0, s>>>(in, id, np, out);
+  permute3_kernel<<<wave_grid(permute3_kernel, np, 256), 256, 0, s>>>(in, id, np, out);
   PMGB_LAUNCHED("permute3_kernel");
   return PMGB_OK;
 }
@@ -1353,10 +1341,9 @@ int tile_scatter(const float *pos, const float *vel, const unsigned *id, int64_t
   // the counts become the per-tile slot cursors of the scatter
   PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
   if (np > 0) {
-    unsigned grid = 1;
-    PMGB_TRY(scatter_grid(np, &grid));
-    scatter_kernel<<<grid, 256, 0, s>>>(pos, vel, id, nullptr, np, nx, ny, nz, sc.offsets,
-                                        sc.counts, pos2, vel2, id2, dest);
+    scatter_kernel<<<scatter_grid(np), 256, 0, s>>>(pos, vel, id, nullptr, np, nx, ny, nz,
+                                                    sc.offsets, sc.counts, pos2, vel2, id2,
+                                                    dest);
     PMGB_LAUNCHED("scatter_kernel");
   }
   return PMGB_OK;

@@ -1208,8 +1208,8 @@ int stencil_forces(const float *pot, float *f3, int nx, int ny, int nz, int batc
     return PMGB_OK;
   }
   for (int b = 0; b < batch; ++b) {
-    stencil_forces_kernel<<<grid_for(n, 256), 256, 0, s>>>(pot + b * n, f3 + 3 * b * n, nx, ny,
-                                                            nz);
+    stencil_forces_kernel<<<wave_grid(stencil_forces_kernel, n, 256), 256, 0, s>>>(
+        pot + b * n, f3 + 3 * b * n, nx, ny, nz);
     PMGB_LAUNCHED("stencil_forces_kernel");
   }
   return PMGB_OK;
@@ -1225,8 +1225,8 @@ int stencil_adjoint(const float *g3, float *out, int nx, int ny, int nz, int bat
     return PMGB_OK;
   }
   for (int b = 0; b < batch; ++b) {
-    stencil_adjoint_kernel<<<grid_for(n, 256), 256, 0, s>>>(g3 + 3 * b * n, out + b * n, nx, ny,
-                                                             nz);
+    stencil_adjoint_kernel<<<wave_grid(stencil_adjoint_kernel, n, 256), 256, 0, s>>>(
+        g3 + 3 * b * n, out + b * n, nx, ny, nz);
     PMGB_LAUNCHED("stencil_adjoint_kernel");
   }
   return PMGB_OK;

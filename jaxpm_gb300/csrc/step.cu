@@ -320,8 +320,8 @@ int read3_kick_drift(const float *f3, int64_t cs, int nx, int ny, int nz, float 
                      float *vel, int64_t np, float kick, float drift, float *fout,
                      cudaStream_t s) {
   if (np == 0) return PMGB_OK;
-  read3_kick_drift_kernel<<<grid_for(np, 256), 256, 0, s>>>(f3, cs, nx, ny, nz, pos, vel, np,
-                                                             kick, drift, fout);
+  read3_kick_drift_kernel<<<wave_grid(read3_kick_drift_kernel, np, 256), 256, 0, s>>>(
+      f3, cs, nx, ny, nz, pos, vel, np, kick, drift, fout);
   PMGB_LAUNCHED("read3_kick_drift_kernel");
   return PMGB_OK;
 }
@@ -338,14 +338,14 @@ int fpm_step(float *pos, float *vel, int64_t np, int nx, int ny, int nz, float k
 
 int kick(float *vel, const float *forces, int64_t np, float k, cudaStream_t s) {
   if (np == 0) return PMGB_OK;
-  axpy3_kernel<<<grid_for(3 * np, 256), 256, 0, s>>>(vel, forces, 3 * np, k);
+  axpy3_kernel<<<wave_grid(axpy3_kernel, 3 * np, 256), 256, 0, s>>>(vel, forces, 3 * np, k);
   PMGB_LAUNCHED("kick(axpy3_kernel)");
   return PMGB_OK;
 }
 
 int drift(float *pos, const float *vel, int64_t np, float d, cudaStream_t s) {
   if (np == 0) return PMGB_OK;
-  axpy3_kernel<<<grid_for(3 * np, 256), 256, 0, s>>>(pos, vel, 3 * np, d);
+  axpy3_kernel<<<wave_grid(axpy3_kernel, 3 * np, 256), 256, 0, s>>>(pos, vel, 3 * np, d);
   PMGB_LAUNCHED("drift(axpy3_kernel)");
   return PMGB_OK;
 }
@@ -371,8 +371,8 @@ int fpm_step_plain(float *pos, float *vel, int64_t np, int nx, int ny, int nz, f
   }
   if (np > 0) {
     for (int d = 0; d < 3; ++d) {
-      read_strided_kernel<<<grid_for(np, 256), 256, 0, s>>>(f3 + d * ncell, nx, ny, nz, pos, np,
-                                                             forces + d, 3);
+      read_strided_kernel<<<wave_grid(read_strided_kernel, np, 256), 256, 0, s>>>(
+          f3 + d * ncell, nx, ny, nz, pos, np, forces + d, 3);
       PMGB_LAUNCHED("read_strided_kernel");
     }
   }
@@ -391,14 +391,15 @@ int pm_forces_vjp(const float *pos, int64_t np, int nx, int ny, int nz, float r_
   float *g3 = WS(float, L.g3);
   PMGB_CUDA(cudaMemsetAsync(g3, 0, 3 * ncell * sizeof(float), s));
   if (np > 0) {
-    paint3_kernel<<<grid_for(np, 256), 256, 0, s>>>(g3, ncell, nx, ny, nz, pos, np, g);
+    paint3_kernel<<<wave_grid(paint3_kernel, np, 256), 256, 0, s>>>(
+        g3, ncell, nx, ny, nz, pos, np, g);
     PMGB_LAUNCHED("paint3_kernel");
   }
   float *rbar = WS(float, L.mesh);
   PMGB_TRY(mesh_forces_vjp(g3, nx, ny, nz, r_split, WS(void, L.dk), WS(void, L.fk), rbar, s));
   if (np > 0) {
-    forces_vjp_gather_kernel<<<grid_for(np, 256), 256, 0, s>>>(WS(float, L.f3), ncell, rbar, nx,
-                                                                ny, nz, pos, np, g, gpos);
+    forces_vjp_gather_kernel<<<wave_grid(forces_vjp_gather_kernel, np, 256), 256, 0, s>>>(
+        WS(float, L.f3), ncell, rbar, nx, ny, nz, pos, np, g, gpos);
     PMGB_LAUNCHED("forces_vjp_gather_kernel");
   }
   return PMGB_OK;
