@@ -336,7 +336,11 @@ int paint(float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
   if (!accumulate) PMGB_CUDA(cudaMemsetAsync(mesh, 0, ncell * sizeof(float), s));
   if (np == 0) return PMGB_OK;
   if (mode == PMGB_PAINT_ATOMIC) {
-    paint_atomic_kernel<<<wave_grid(paint_atomic_kernel, np, 256), 256, 0, s>>>(
+    // 8 CTAs per SM requested rather than one wave of the 6 resident: the
+    // atomics-bound paint runs faster with the extra CTAs queued (16.7M
+    // particles on 256^3: 0.41 against 0.44 ms uniform, 0.44 against 0.46 ms
+    // clustered)
+    paint_atomic_kernel<<<grid_for(np, 256), 256, 0, s>>>(
         mesh, nx, ny, nz, pos, np, weights, wscale, zpair_vec_ok(mesh, nz));
     PMGB_LAUNCHED("paint_atomic_kernel");
     return PMGB_OK;
@@ -404,7 +408,7 @@ int read_vjp(const float *mesh, int nx, int ny, int nz, const float *pos, int64_
              const float *g_out, float *g_mesh, float *g_pos, cudaStream_t s) {
   if (np == 0) return PMGB_OK;
   if (g_mesh) {
-    paint_atomic_kernel<<<wave_grid(paint_atomic_kernel, np, 256), 256, 0, s>>>(
+    paint_atomic_kernel<<<grid_for(np, 256), 256, 0, s>>>(
         g_mesh, nx, ny, nz, pos, np, g_out, 1.0f, zpair_vec_ok(g_mesh, nz));
     PMGB_LAUNCHED("paint_atomic_kernel");
   }
