@@ -191,7 +191,7 @@ def profile_traffic():
 
 def run_gb300(args):
     import torch
-    from jaxpm_gb300 import _lib, cosmology, painting, simulate
+    from jaxpm_gb300 import _lib, cosmology, painting, simulate, utils
 
     rank, world, local = dist_env()
     if world > 1:
@@ -363,6 +363,9 @@ def run_gb300(args):
     rho = painting.paint(torch.zeros((n,) * 3, device=dev), current_positions(),
                          mode="deterministic")
     mass_err = abs(rho.double().sum().item() - Np) / Np
+    # P(k) of the final density (GPU R2C + binned |delta_k|^2), compared below
+    # with the one-kernel-per-op path's run from the same initial state
+    _, pk_run = utils.power_spectrum(rho)
     del rho
     # own kernels launched in the timed region, counted by the library
     # (cuFFT's kernels are not counted)
@@ -463,6 +466,17 @@ def run_gb300(args):
         pms = max_over_ranks(b0.elapsed_time(b1), world)
         result["plain_gpu"] = {"value": world * Np * K / (pms / 1e3), "unit": "particle-steps/s",
                                "ms_per_step": pms / K, "fused_speedup": pms / ms_max}
+        # parity of the timed path at full size: its final P(k) against the
+        # one-kernel-per-op path (atomic paint, three force meshes through
+        # cuFFT, separate gather / kick / drift) run from the same state
+        rho_p = painting.paint(torch.zeros((n,) * 3, device=dev), xp, mode="deterministic")
+        _, pk_plain = utils.power_spectrum(rho_p)
+        del rho_p
+        rel = np.abs(pk_run / pk_plain - 1.0)
+        rel = rel[np.isfinite(rel)]
+        result["plain_gpu"]["pk_vs_timed_run"] = {
+            "max_rel_dev_per_bin": float(rel.max()), "bins": int(rel.size),
+            "tolerance": 1e-3, "within": bool(rel.max() < 1e-3)}
         del plain, xp, vp
 
     # end to end through the C ABI with host buffers: every step copies
