@@ -482,6 +482,26 @@ int pmgb_fpm_run_sorted_record_f32(float *xs, float *vel_a, uint32_t *id_a,
                                    uint32_t *dests, uint32_t *offsets,
                                    uint32_t *stats, pmgb_stream_t stream);
 
+/* The same recording run keeping each step's potential instead of its three
+ * force meshes: potentials[i] ([n_steps][nx][ny][nz]) is step i's
+ * potential, from which that step's gather (and its reverse step,
+ * pmgb_fpm_step_sorted_vjp_pot_f32) derive the forces with the order-1
+ * gradient stencil, as pmgb_fpm_run_sorted_f32 does.  A third of the
+ * recorded mesh bytes.  PMGB_ERR_UNSUPPORTED outside the potential
+ * pipeline's shapes (pmgb_fft3_supported). */
+int pmgb_fpm_run_sorted_record_pot_f32(float *xs, float *vel_a, uint32_t *id_a,
+                                       float *vel_b, uint32_t *id_b,
+                                       float *pos_out, int64_t np, int nx,
+                                       int ny, int nz, int n_steps,
+                                       const float *kick, const float *drift,
+                                       float r_split, void *workspace,
+                                       size_t workspace_bytes,
+                                       void *sort_workspace,
+                                       size_t sort_workspace_bytes,
+                                       float *potentials, uint32_t *dests,
+                                       uint32_t *offsets, uint32_t *stats,
+                                       pmgb_stream_t stream);
+
 int pmgb_fpm_run_sorted_f32(float *pos_a, float *vel_a, uint32_t *id_a,
                             float *pos_b, float *vel_b, uint32_t *id_b,
                             int64_t np, int nx, int ny, int nz, int n_steps,
@@ -518,6 +538,21 @@ int pmgb_fpm_step_sorted_vjp_f32(const float *pos, const float *force3,
                                  float kick, float drift, float r_split,
                                  void *workspace, size_t workspace_bytes,
                                  uint32_t *stats, pmgb_stream_t stream);
+
+/* pmgb_fpm_step_sorted_vjp_f32 for a step recorded by
+ * pmgb_fpm_run_sorted_record_pot_f32: `potential` is the potential the step
+ * took its forces from; the reverse gather derives each tile's forces from
+ * a TMA-staged potential box. */
+int pmgb_fpm_step_sorted_vjp_pot_f32(const float *pos, const float *potential,
+                                     const uint32_t *dest,
+                                     const uint32_t *tile_offsets,
+                                     const float *g_pos_in,
+                                     const float *g_vel_in, float *g_pos_out,
+                                     float *g_vel_out, int64_t np, int nx,
+                                     int ny, int nz, float kick, float drift,
+                                     float r_split, void *workspace,
+                                     size_t workspace_bytes, uint32_t *stats,
+                                     pmgb_stream_t stream);
 
 /* ---- initial conditions (jaxpm/pm.py:61-144) ----------------------------- */
 

@@ -109,9 +109,15 @@ SIGNATURES = {
     "pmgb_fpm_run_sorted_record_f32": (c_int, [P, P, P, P, P, P, c_int64, c_int, c_int, c_int,
                                                c_int, P, P, c_float, P, c_size_t, P, c_size_t, P,
                                                P, P, P, P]),
+    "pmgb_fpm_run_sorted_record_pot_f32": (c_int, [P, P, P, P, P, P, c_int64, c_int, c_int,
+                                                   c_int, c_int, P, P, c_float, P, c_size_t, P,
+                                                   c_size_t, P, P, P, P, P]),
     "pmgb_tile_key_count": (c_int64, [c_int, c_int, c_int]),
     "pmgb_fpm_step_sorted_vjp_f32": (c_int, [P, P, P, P, P, P, P, P, c_int64, c_int, c_int, c_int,
                                              c_float, c_float, c_float, P, c_size_t, P, P]),
+    "pmgb_fpm_step_sorted_vjp_pot_f32": (c_int, [P, P, P, P, P, P, P, P, c_int64, c_int, c_int,
+                                                 c_int, c_float, c_float, c_float, P, c_size_t, P,
+                                                 P]),
     "pmgb_power_spectrum_f32": (c_int, [P, c_int, c_int, c_int, ctypes.c_double, ctypes.c_double,
                                         ctypes.c_double, P, c_int, P, P, P, P]),
     "pmgb_lpt2_source_vjp_f32": (c_int, [P, P, P, c_int, c_int, c_int, P, c_size_t, P]),

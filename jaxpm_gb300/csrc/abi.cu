@@ -579,14 +579,12 @@ int pmgb_read_potential_kick_drift_paint_binned_f32(const float *pot, int nx, in
                     sort_workspace, sort_workspace_bytes, stats, stream, mesh_next, true);
 }
 
-int pmgb_fpm_run_sorted_record_f32(float *xs, float *vel_a, uint32_t *id_a, float *vel_b,
-                                   uint32_t *id_b, float *pos_out, int64_t np, int nx, int ny,
-                                   int nz, int n_steps, const float *kick, const float *drift,
-                                   float r_split, void *workspace, size_t workspace_bytes,
-                                   void *sort_workspace, size_t sort_workspace_bytes,
-                                   float *force3s, uint32_t *dests, uint32_t *offsets,
-                                   uint32_t *stats, pmgb_stream_t stream) {
-  BEGIN();
+static int run_sorted_record(float *xs, float *vel_a, uint32_t *id_a, float *vel_b,
+                             uint32_t *id_b, float *pos_out, int64_t np, int nx, int ny, int nz,
+                             int n_steps, const float *kick, const float *drift, float r_split,
+                             void *workspace, size_t workspace_bytes, void *sort_workspace,
+                             size_t sort_workspace_bytes, float *force3s, uint32_t *dests,
+                             uint32_t *offsets, uint32_t *stats, pmgb_stream_t stream, bool pot) {
   PMGB_TRY(check_sortable(nx, ny, nz, np));
   PMGB_REQUIRE(n_steps >= 0, "n_steps is negative");
   PMGB_REQUIRE(r_split >= 0.0f, "r_split must be non-negative");
@@ -605,7 +603,34 @@ int pmgb_fpm_run_sorted_record_f32(float *xs, float *vel_a, uint32_t *id_a, floa
   NEED(offsets);
   return fpm_run_sorted_record(xs, vel_a, id_a, vel_b, id_b, pos_out, np, nx, ny, nz, n_steps,
                                kick, drift, r_split, workspace, workspace_bytes, sort_workspace,
-                               sort_workspace_bytes, force3s, dests, offsets, stats, stream);
+                               sort_workspace_bytes, force3s, dests, offsets, stats, stream, pot);
+}
+
+int pmgb_fpm_run_sorted_record_f32(float *xs, float *vel_a, uint32_t *id_a, float *vel_b,
+                                   uint32_t *id_b, float *pos_out, int64_t np, int nx, int ny,
+                                   int nz, int n_steps, const float *kick, const float *drift,
+                                   float r_split, void *workspace, size_t workspace_bytes,
+                                   void *sort_workspace, size_t sort_workspace_bytes,
+                                   float *force3s, uint32_t *dests, uint32_t *offsets,
+                                   uint32_t *stats, pmgb_stream_t stream) {
+  BEGIN();
+  return run_sorted_record(xs, vel_a, id_a, vel_b, id_b, pos_out, np, nx, ny, nz, n_steps, kick,
+                           drift, r_split, workspace, workspace_bytes, sort_workspace,
+                           sort_workspace_bytes, force3s, dests, offsets, stats, stream, false);
+}
+
+int pmgb_fpm_run_sorted_record_pot_f32(float *xs, float *vel_a, uint32_t *id_a, float *vel_b,
+                                       uint32_t *id_b, float *pos_out, int64_t np, int nx,
+                                       int ny, int nz, int n_steps, const float *kick,
+                                       const float *drift, float r_split, void *workspace,
+                                       size_t workspace_bytes, void *sort_workspace,
+                                       size_t sort_workspace_bytes, float *potentials,
+                                       uint32_t *dests, uint32_t *offsets, uint32_t *stats,
+                                       pmgb_stream_t stream) {
+  BEGIN();
+  return run_sorted_record(xs, vel_a, id_a, vel_b, id_b, pos_out, np, nx, ny, nz, n_steps, kick,
+                           drift, r_split, workspace, workspace_bytes, sort_workspace,
+                           sort_workspace_bytes, potentials, dests, offsets, stats, stream, true);
 }
 
 int pmgb_fpm_run_sorted_f32(float *pos_a, float *vel_a, uint32_t *id_a, float *pos_b,
@@ -694,13 +719,12 @@ int64_t pmgb_tile_key_count(int nx, int ny, int nz) {
   return tile_key_count(nx, ny, nz);
 }
 
-int pmgb_fpm_step_sorted_vjp_f32(const float *pos, const float *force3, const uint32_t *dest,
-                                 const uint32_t *tile_offsets, const float *g_pos_in,
-                                 const float *g_vel_in, float *g_pos_out, float *g_vel_out,
-                                 int64_t np, int nx, int ny, int nz, float kick, float drift,
-                                 float r_split, void *workspace, size_t workspace_bytes,
-                                 uint32_t *stats, pmgb_stream_t stream) {
-  BEGIN();
+static int step_sorted_vjp(const float *pos, const float *force3, const uint32_t *dest,
+                           const uint32_t *tile_offsets, const float *g_pos_in,
+                           const float *g_vel_in, float *g_pos_out, float *g_vel_out, int64_t np,
+                           int nx, int ny, int nz, float kick, float drift, float r_split,
+                           void *workspace, size_t workspace_bytes, uint32_t *stats,
+                           pmgb_stream_t stream, bool pot) {
   PMGB_TRY(check_sortable(nx, ny, nz, np));
   NEED(force3);
   NEED(tile_offsets);
@@ -715,7 +739,32 @@ int pmgb_fpm_step_sorted_vjp_f32(const float *pos, const float *force3, const ui
   }
   return fpm_step_sorted_vjp(pos, force3, dest, tile_offsets, g_pos_in, g_vel_in, g_pos_out,
                              g_vel_out, np, nx, ny, nz, kick, drift, r_split, workspace,
-                             workspace_bytes, stats, stream);
+                             workspace_bytes, stats, stream, pot);
+}
+
+int pmgb_fpm_step_sorted_vjp_f32(const float *pos, const float *force3, const uint32_t *dest,
+                                 const uint32_t *tile_offsets, const float *g_pos_in,
+                                 const float *g_vel_in, float *g_pos_out, float *g_vel_out,
+                                 int64_t np, int nx, int ny, int nz, float kick, float drift,
+                                 float r_split, void *workspace, size_t workspace_bytes,
+                                 uint32_t *stats, pmgb_stream_t stream) {
+  BEGIN();
+  return step_sorted_vjp(pos, force3, dest, tile_offsets, g_pos_in, g_vel_in, g_pos_out,
+                         g_vel_out, np, nx, ny, nz, kick, drift, r_split, workspace,
+                         workspace_bytes, stats, stream, false);
+}
+
+int pmgb_fpm_step_sorted_vjp_pot_f32(const float *pos, const float *potential,
+                                     const uint32_t *dest, const uint32_t *tile_offsets,
+                                     const float *g_pos_in, const float *g_vel_in,
+                                     float *g_pos_out, float *g_vel_out, int64_t np, int nx,
+                                     int ny, int nz, float kick, float drift, float r_split,
+                                     void *workspace, size_t workspace_bytes, uint32_t *stats,
+                                     pmgb_stream_t stream) {
+  BEGIN();
+  return step_sorted_vjp(pos, potential, dest, tile_offsets, g_pos_in, g_vel_in, g_pos_out,
+                         g_vel_out, np, nx, ny, nz, kick, drift, r_split, workspace,
+                         workspace_bytes, stats, stream, true);
 }
 
 int pmgb_linear_field_colour_f32(void *spec, int nx, int ny, int nz, float box_x, float box_y,

@@ -117,7 +117,8 @@ int fpm_run_sorted_record(float *xs, float *vel_a, unsigned *id_a, float *vel_b,
                           float *pos_out, int64_t np, int nx, int ny, int nz, int n_steps,
                           const float *kick, const float *drift, float r_split, void *mesh_ws,
                           size_t mesh_bytes, void *sort_ws, size_t sort_bytes, float *f3s,
-                          unsigned *dests, unsigned *offs, unsigned *stats, cudaStream_t s);
+                          unsigned *dests, unsigned *offs, unsigned *stats, cudaStream_t s,
+                          bool pot = false);
 
 int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz,
                const float *pos, float *pos_out, float *vel, int64_t np,
@@ -153,7 +154,8 @@ int fpm_step_sorted_vjp(const float *pos, const float *force3,
                         const float *gx_in, const float *gv_in, float *gx_out,
                         float *gv_out, int64_t np, int nx, int ny, int nz,
                         float kick, float drift, float r_split, void *mesh_ws,
-                        size_t mesh_bytes, unsigned *stats, cudaStream_t s);
+                        size_t mesh_bytes, unsigned *stats, cudaStream_t s,
+                        bool pot = false);
 // step.cu: paint of tile-sorted particles -> R2C -> k-space -> C2R inside the
 // composite workspace; *f3 receives the three force meshes (f3_out when it
 // is given, else the workspace's region).

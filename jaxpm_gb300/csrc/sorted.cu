@@ -496,6 +496,52 @@ __device__ __noinline__ void pot_gather_global(const float *__restrict__ pot, Ax
   a[2] = a2;
 }
 
+// The tile's force box (three components [c][x][y][z(12)], TBOX apart) from
+// its potential box `pbox` (PBX x PBY x PBZ, force-box cell (a, b, c) is
+// potential entry (a + 2, b + 2, c + 4)): -(i g(w)) of the order-1 gradient
+// kernel (8 sin w - sin 2w)/6 of jaxpm/kernels.py:41-66 as the stencil
+// (t2 - 8 t1) / 12, t1 = p[+1] - p[-1], t2 = p[+2] - p[-2], four z cells per
+// item with 16-byte shared loads: rows of 16 potentials, c0 = 0, 4, 8 (cells
+// 9..11 are the rows' padding; their neighbours may read the next row,
+// which stays inside the buffer).  The caller synchronises afterwards.
+__device__ __forceinline__ void force_box_from_potential(const float *__restrict__ box,
+                                                         float *__restrict__ ff, int tid) {
+  for (int q = tid; q < TB * TB * 3; q += TILE_THREADS) {
+    const int c0 = 4 * (q % 3), r = q / 3, b = r % TB, a = r / TB;
+    const float *row = box + ((a + 2) * PBY + b + 2) * PBZ + c0;
+    const float4 z0 = *reinterpret_cast<const float4 *>(row);
+    const float4 zc = *reinterpret_cast<const float4 *>(row + 4);
+    const float4 z2 = *reinterpret_cast<const float4 *>(row + 8);
+    const float zz[12] = {z0.x, z0.y, z0.z, z0.w, zc.x, zc.y, zc.z, zc.w,
+                          z2.x, z2.y, z2.z, z2.w};
+    auto nb = [&](int off) { return *reinterpret_cast<const float4 *>(row + 4 + off); };
+    const float4 xm2 = nb(-2 * PBY * PBZ), xm1 = nb(-PBY * PBZ), xp1 = nb(PBY * PBZ),
+                 xp2 = nb(2 * PBY * PBZ);
+    const float4 ym2 = nb(-2 * PBZ), ym1 = nb(-PBZ), yp1 = nb(PBZ), yp2 = nb(2 * PBZ);
+    auto f = [](float m2, float m1, float p1, float p2) {
+      const float t1 = p1 - m1, t2 = p2 - m2;
+      return (t2 - 8.0f * t1) * (1.0f / 12.0f);
+    };
+    float4 fx, fy, fz;
+    fx.x = f(xm2.x, xm1.x, xp1.x, xp2.x);
+    fx.y = f(xm2.y, xm1.y, xp1.y, xp2.y);
+    fx.z = f(xm2.z, xm1.z, xp1.z, xp2.z);
+    fx.w = f(xm2.w, xm1.w, xp1.w, xp2.w);
+    fy.x = f(ym2.x, ym1.x, yp1.x, yp2.x);
+    fy.y = f(ym2.y, ym1.y, yp1.y, yp2.y);
+    fy.z = f(ym2.z, ym1.z, yp1.z, yp2.z);
+    fy.w = f(ym2.w, ym1.w, yp1.w, yp2.w);
+    fz.x = f(zz[2], zz[3], zz[5], zz[6]);
+    fz.y = f(zz[3], zz[4], zz[6], zz[7]);
+    fz.z = f(zz[4], zz[5], zz[7], zz[8]);
+    fz.w = f(zz[5], zz[6], zz[8], zz[9]);
+    const int o = (a * TB + b) * TBZ + c0;
+    *reinterpret_cast<float4 *>(ff + o) = fx;
+    *reinterpret_cast<float4 *>(ff + TBOX + o) = fy;
+    *reinterpret_cast<float4 *>(ff + 2 * TBOX + o) = fz;
+  }
+}
+
 struct TileInfo {
   unsigned beg, end;
   int ox, oy, oz;
@@ -667,45 +713,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
         __syncthreads();
       }
       if (POT) {
-        // the tile's force box from the potential box (box cell (a, b, c) is
-        // potential entry (a + 2, b + 2, c + 4)), four z cells per item with
-        // 16-byte shared loads: rows of 16 potentials, c0 = 0, 4, 8 (cells
-        // 9..11 are the rows' padding; their neighbours may read the next
-        // row, which stays inside the buffer)
-        for (int q = tid; q < TB * TB * 3; q += TILE_THREADS) {
-          const int c0 = 4 * (q % 3), r = q / 3, b = r % TB, a = r / TB;
-          const float *row = box + ((a + 2) * PBY + b + 2) * PBZ + c0;
-          const float4 z0 = *reinterpret_cast<const float4 *>(row);
-          const float4 zc = *reinterpret_cast<const float4 *>(row + 4);
-          const float4 z2 = *reinterpret_cast<const float4 *>(row + 8);
-          const float zz[12] = {z0.x, z0.y, z0.z, z0.w, zc.x, zc.y, zc.z, zc.w,
-                                z2.x, z2.y, z2.z, z2.w};
-          auto nb = [&](int off) { return *reinterpret_cast<const float4 *>(row + 4 + off); };
-          const float4 xm2 = nb(-2 * PBY * PBZ), xm1 = nb(-PBY * PBZ), xp1 = nb(PBY * PBZ),
-                       xp2 = nb(2 * PBY * PBZ);
-          const float4 ym2 = nb(-2 * PBZ), ym1 = nb(-PBZ), yp1 = nb(PBZ), yp2 = nb(2 * PBZ);
-          auto f = [](float m2, float m1, float p1, float p2) {
-            const float t1 = p1 - m1, t2 = p2 - m2;
-            return (t2 - 8.0f * t1) * (1.0f / 12.0f);
-          };
-          float4 fx, fy, fz;
-          fx.x = f(xm2.x, xm1.x, xp1.x, xp2.x);
-          fx.y = f(xm2.y, xm1.y, xp1.y, xp2.y);
-          fx.z = f(xm2.z, xm1.z, xp1.z, xp2.z);
-          fx.w = f(xm2.w, xm1.w, xp1.w, xp2.w);
-          fy.x = f(ym2.x, ym1.x, yp1.x, yp2.x);
-          fy.y = f(ym2.y, ym1.y, yp1.y, yp2.y);
-          fy.z = f(ym2.z, ym1.z, yp1.z, yp2.z);
-          fy.w = f(ym2.w, ym1.w, yp1.w, yp2.w);
-          fz.x = f(zz[2], zz[3], zz[5], zz[6]);
-          fz.y = f(zz[3], zz[4], zz[6], zz[7]);
-          fz.z = f(zz[4], zz[5], zz[7], zz[8]);
-          fz.w = f(zz[5], zz[6], zz[8], zz[9]);
-          const int o = (a * TB + b) * TBZ + c0;
-          *reinterpret_cast<float4 *>(ff + o) = fx;
-          *reinterpret_cast<float4 *>(ff + TBOX + o) = fy;
-          *reinterpret_cast<float4 *>(ff + 2 * TBOX + o) = fz;
-        }
+        force_box_from_potential(box, ff, tid);
         __syncthreads();
         box = ff;
       }
@@ -1501,17 +1509,24 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, flo
 
 // The recording forward of the reverse sweep as one run: per step i the
 // positions it starts from are xs + i*3np (tile order i; xs[0] given), its
-// force meshes are computed into f3s + i*3ncell, the tile ranges are copied
-// to offs + i*(keys+1) and the re-sort map to dests + i*np.  Like
-// fpm_run_sorted, every density after the first is painted by the previous
-// step's gather and the sort overlaps the next step's forces.  The final
-// state goes to (pos_out, vel_b, id_b) if n_steps is odd, else to
-// (pos_out, vel_a, id_a); vel_a / id_a hold the initial velocities / ids.
+// force meshes are computed into f3s + i*3ncell (with `pot`: its potential
+// into f3s + i*ncell, the gather deriving the forces as in fpm_run_sorted),
+// the tile ranges are copied to offs + i*(keys+1) and the re-sort map to
+// dests + i*np.  Like fpm_run_sorted, every density after the first is
+// painted by the previous step's gather and the sort overlaps the next
+// step's forces.  The final state goes to (pos_out, vel_b, id_b) if n_steps
+// is odd, else to (pos_out, vel_a, id_a); vel_a / id_a hold the initial
+// velocities / ids.
 int fpm_run_sorted_record(float *xs, float *vel_a, unsigned *id_a, float *vel_b, unsigned *id_b,
                           float *pos_out, int64_t np, int nx, int ny, int nz, int n_steps,
                           const float *kick, const float *drift, float r_split, void *mesh_ws,
                           size_t mesh_bytes, void *sort_ws, size_t sort_bytes, float *f3s,
-                          unsigned *dests, unsigned *offs, unsigned *stats, cudaStream_t s) {
+                          unsigned *dests, unsigned *offs, unsigned *stats, cudaStream_t s,
+                          bool pot) {
+  if (pot && !spectral_supported(nx, ny, nz))
+    return fail(PMGB_ERR_UNSUPPORTED,
+                "recording the potential needs the potential pipeline's mesh shapes "
+                "(power-of-two nx in [8,1024], ny in [64,512], nz in [16,512])");
   PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
   float *mesh, *f3, *g3;
   void *dk, *fk;
@@ -1529,8 +1544,16 @@ int fpm_run_sorted_record(float *xs, float *vel_a, unsigned *id_a, float *vel_b,
   unsigned *I[2] = {id_a, id_b};
   Aux *aux;
   PMGB_TRY(aux_stream(&aux));
+  // step i's forces: three meshes at f3s + i*3ncell, or the potential at
+  // f3s + i*ncell
+  const int64_t per = pot ? ncell : 3 * ncell;
+  const float scale = 1.0f / (float)ncell;
+  auto forces = [&](int i) -> int {
+    if (pot) return spectral_potential(mesh, dk, f3s + per * i, nx, ny, nz, r_split, scale, s);
+    return mesh_forces(mesh, nx, ny, nz, r_split, dk, fk, f3s + per * i, s);
+  };
   PMGB_TRY(paint_sorted(mesh, nx, ny, nz, xs, np, sort_ws, sort_bytes, stats, s));
-  PMGB_TRY(mesh_forces(mesh, nx, ny, nz, r_split, dk, fk, f3s, s));
+  PMGB_TRY(forces(0));
   for (int i = 0; i < n_steps; ++i) {
     const int a = i & 1, b = a ^ 1;
     float *x = xs + 3 * np * (int64_t)i;
@@ -1539,17 +1562,15 @@ int fpm_run_sorted_record(float *xs, float *vel_a, unsigned *id_a, float *vel_b,
     PMGB_CUDA(cudaMemcpyAsync(offs + (keys + 1) * (int64_t)i,
                               tile_offsets(sort_ws, nx, ny, nz, np),
                               (keys + 1) * sizeof(unsigned), cudaMemcpyDeviceToDevice, s));
-    PMGB_TRY(rkd_sorted(f3s + 3 * ncell * (int64_t)i, ncell, nx, ny, nz, x, drifted, V[a], np,
-                        kick[i], drift[i], sort_ws, sort_bytes, stats, s,
-                        i + 1 < n_steps ? mesh : nullptr));
+    PMGB_TRY(rkd_sorted(f3s + per * i, ncell, nx, ny, nz, x, drifted, V[a], np, kick[i],
+                        drift[i], sort_ws, sort_bytes, stats, s,
+                        i + 1 < n_steps ? mesh : nullptr, pot));
     PMGB_CUDA(cudaEventRecord(aux->gathered, s));
     PMGB_CUDA(cudaStreamWaitEvent(aux->s2, aux->gathered, 0));
     PMGB_TRY(tile_scatter(drifted, V[a], I[a], np, nx, ny, nz, xn, V[b], I[b],
                           dests + np * (int64_t)i, sort_ws, sort_bytes, aux->s2));
     PMGB_CUDA(cudaEventRecord(aux->sorted, aux->s2));
-    if (i + 1 < n_steps)
-      PMGB_TRY(mesh_forces(mesh, nx, ny, nz, r_split, dk, fk, f3s + 3 * ncell * (int64_t)(i + 1),
-                           s));
+    if (i + 1 < n_steps) PMGB_TRY(forces(i + 1));
   }
   PMGB_CUDA(cudaStreamWaitEvent(s, aux->sorted, 0));
   return PMGB_OK;
@@ -1713,6 +1734,11 @@ adj_paint3_tiles_kernel(float *__restrict__ g3, int64_t cs, int nx, int ny, int 
 constexpr int RBOX_STRIDE = (TBOX + 31) / 32 * 32;
 constexpr uint32_t RBOX_BYTES = TBOX * sizeof(float);
 
+// POT: f3 is the potential the step's forces came from (cs unused, fmap its
+// 3-D map with the 16 x 13 x 13 box of the forward gather) and each tile's
+// force box is computed from the staged potential box, as in
+// rkd_tiles_kernel<., true>.
+template <bool POT>
 __global__ void __launch_bounds__(TILE_THREADS)
 adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *__restrict__ rbar,
                         int nx, int ny, int nz, const float *__restrict__ pos,
@@ -1725,9 +1751,17 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
                         unsigned *__restrict__ work) {
   __shared__ __align__(128) float fb[2][FBOX_STRIDE];
   __shared__ __align__(128) float rb[2][RBOX_STRIDE];
+  __shared__ __align__(16) float ff[POT ? FBOX : 4];  // POT: the tile's force box
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ uint32_t s_grab[2];
+  constexpr uint32_t BOX_BYTES = (POT ? PBOX_BYTES : FBOX_BYTES) + RBOX_BYTES;
   const int tid = threadIdx.x;
+  // the tile's boxes by TMA, completing on `b`
+  auto issue = [&](float *fdst, float *rdst, const TileInfo &t, uint64_t *b) {
+    if (POT) tma_load_3d(fdst, &fmap, t.oz - 4, t.oy - 2, t.ox - 2, b);
+    else tma_load_4d(fdst, &fmap, t.oz, t.oy, t.ox, 0, b);
+    tma_load_3d(rdst, &rmap, t.oz, t.oy, t.ox, b);
+  };
   if (tid == 0) {
     mbar_init(&bar[0], 1);
     mbar_init(&bar[1], 1);
@@ -1741,11 +1775,10 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
   const TileSchedule sched(nkeys, 0);  // no global atomics: dynamic
   uint32_t knext = gridDim.x + blockIdx.x;  // tiles 0 and 1 are static
   uint32_t it = 0;                          // index of the current tile
-  TileInfo cur = tile_info(offsets, key, nx, ny, nz, use_tma);
+  TileInfo cur = tile_info(offsets, key, nx, ny, nz, use_tma, POT);
   if (cur.tma && tid == 0) {
-    mbar_expect_tx(&bar[0], FBOX_BYTES + RBOX_BYTES);
-    tma_load_4d(fb[0], &fmap, cur.oz, cur.oy, cur.ox, 0, &bar[0]);
-    tma_load_3d(rb[0], &rmap, cur.oz, cur.oy, cur.ox, &bar[0]);
+    mbar_expect_tx(&bar[0], BOX_BYTES);
+    issue(fb[0], rb[0], cur, &bar[0]);
   }
   int buf = 0;
   while (key < nkeys) {
@@ -1754,12 +1787,11 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
     TileInfo nxt;
     nxt.tma = false;
     if (knext < nkeys) {
-      nxt = tile_info(offsets, knext, nx, ny, nz, use_tma);
+      nxt = tile_info(offsets, knext, nx, ny, nz, use_tma, POT);
       if (nxt.tma && tid == 0) {
         fence_async_shared();
-        mbar_expect_tx(&bar[buf ^ 1], FBOX_BYTES + RBOX_BYTES);
-        tma_load_4d(fb[buf ^ 1], &fmap, nxt.oz, nxt.oy, nxt.ox, 0, &bar[buf ^ 1]);
-        tma_load_3d(rb[buf ^ 1], &rmap, nxt.oz, nxt.oy, nxt.ox, &bar[buf ^ 1]);
+        mbar_expect_tx(&bar[buf ^ 1], BOX_BYTES);
+        issue(fb[buf ^ 1], rb[buf ^ 1], nxt, &bar[buf ^ 1]);
       }
     }
     if (cur.beg != cur.end) {
@@ -1773,6 +1805,20 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
           return;
         }
         if (buf) phase1 ^= 1u; else phase0 ^= 1u;
+      } else if (POT) {
+        for (int q = tid; q < PBOX; q += TILE_THREADS) {
+          const int zc = q % PBZ, r = q / PBZ, yc = r % PBY, xc = r / PBY;
+          box[q] = __ldg(f3 + cell_index(wrap_index(cur.ox - 2 + xc, nx),
+                                         wrap_index(cur.oy - 2 + yc, ny),
+                                         wrap_index(cur.oz - 4 + zc, nz), ny, nz));
+        }
+        for (int q = tid; q < TB * TB * TB; q += TILE_THREADS) {
+          const int c = q % TB, r = q / TB, b = r % TB, a = r / TB;
+          rbox[(a * TB + b) * TBZ + c] =
+              __ldg(rbar + cell_index(wrap_index(cur.ox + a, nx), wrap_index(cur.oy + b, ny),
+                                      wrap_index(cur.oz + c, nz), ny, nz));
+        }
+        __syncthreads();
       } else {
         for (int q = tid; q < 4 * TB * TB * TB; q += TILE_THREADS) {
           const int c = q % TB, r = q / TB, b = r % TB, r2 = r / TB, a = r2 % TB, comp = r2 / TB;
@@ -1783,6 +1829,11 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
           else rbox[li] = __ldg(rbar + cell);
         }
         __syncthreads();
+      }
+      if (POT) {
+        force_box_from_potential(box, ff, tid);
+        __syncthreads();
+        box = ff;
       }
       if (tid == 0) s_grab[buf] = kgrab;
       for (unsigned p = cur.beg + tid; p < cur.end; p += TILE_THREADS) {
@@ -1807,6 +1858,13 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
           if (in) {
             const int q = ((lx + conn_x(n)) * TB + ly + conn_y(n)) * TBZ + lz + conn_z(n);
             v = rbox[q] + w[0] * box[q] + w[1] * box[TBOX + q] + w[2] * box[2 * TBOX + q];
+          } else if (POT) {
+            const int ix = conn_x(n) ? ax.i1 : ax.i0, iy = conn_y(n) ? ay.i1 : ay.i0,
+                      iz = conn_z(n) ? az.i1 : az.i0;
+            v = __ldg(rbar + cell_index(ix, iy, iz, ny, nz)) +
+                w[0] * stencil_force_global(f3, ix, iy, iz, 0, nx, ny, nz) +
+                w[1] * stencil_force_global(f3, ix, iy, iz, 1, nx, ny, nz) +
+                w[2] * stencil_force_global(f3, ix, iy, iz, 2, nx, ny, nz);
           } else {
             const int64_t c = cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
                                          conn_z(n) ? az.i1 : az.i0, ny, nz);
@@ -1839,14 +1897,16 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
 
 // One reverse step of the sorted loop (see the block comment above).
 // pos: the positions the step started from (order i); force3: the force
-// meshes the step used; dest: where each particle went (order i -> i+1;
-// NULL = identity); offsets: the tile ranges of order i (nkeys + 1
-// entries); (gx_in, gv_in) in order i+1 -> (gx_out, gv_out) in order i.
+// meshes the step used, or with `pot` the potential they were derived from
+// (the order-1 stencil, as in the run loop); dest: where each particle went
+// (order i -> i+1; NULL = identity); offsets: the tile ranges of order i
+// (nkeys + 1 entries); (gx_in, gv_in) in order i+1 -> (gx_out, gv_out) in
+// order i.
 int fpm_step_sorted_vjp(const float *pos, const float *force3, const unsigned *dest,
                         const unsigned *offsets, const float *gx_in, const float *gv_in,
                         float *gx_out, float *gv_out, int64_t np, int nx, int ny, int nz,
                         float kick, float drift, float r_split, void *mesh_ws, size_t mesh_bytes,
-                        unsigned *stats, cudaStream_t s) {
+                        unsigned *stats, cudaStream_t s, bool pot) {
   float *mesh, *f3w, *g3;
   void *dk, *fk;
   unsigned *work;
@@ -1867,15 +1927,20 @@ int fpm_step_sorted_vjp(const float *pos, const float *force3, const unsigned *d
   const uint32_t box4[4] = {TBZ, TB, TB, 3};
   const uint64_t dims3[3] = {(uint64_t)nz, (uint64_t)ny, (uint64_t)nx};
   const uint32_t box3[3] = {TBZ, TB, TB};
+  const uint32_t pbox3[3] = {PBZ, PBY, PBX};
   CUtensorMap gmap, fmap, rmap;
   memset(&gmap, 0, sizeof(gmap));
   memset(&fmap, 0, sizeof(fmap));
   memset(&rmap, 0, sizeof(rmap));
-  int use_tma = 0;
+  int use_tma = 0, use_gtma = 0;  // the paint's map; the gather's two maps
   if (aligned) {
-    use_tma = make_tensor_map(&gmap, g3, 4, dims4, strides4, box4) == PMGB_OK &&
-              make_tensor_map(&fmap, force3, 4, dims4, strides4, box4) == PMGB_OK &&
-              make_tensor_map(&rmap, mesh, 3, dims3, strides4, box3) == PMGB_OK;
+    use_tma = make_tensor_map(&gmap, g3, 4, dims4, strides4, box4) == PMGB_OK;
+    if (pot)
+      use_gtma = nz >= PBZ && ny >= PBY && nx >= PBX &&
+                 make_tensor_map(&fmap, force3, 3, dims3, strides4, pbox3) == PMGB_OK;
+    else
+      use_gtma = make_tensor_map(&fmap, force3, 4, dims4, strides4, box4) == PMGB_OK;
+    use_gtma = use_gtma && make_tensor_map(&rmap, mesh, 3, dims3, strides4, box3) == PMGB_OK;
     clear_error();
   }
   static bool ready[64] = {false};
@@ -1896,19 +1961,19 @@ int fpm_step_sorted_vjp(const float *pos, const float *force3, const unsigned *d
   // 2. rho_bar = sum_c A_c^T (painted component c)
   PMGB_TRY(mesh_forces_vjp(g3, nx, ny, nz, r_split, dk, fk, mesh, s));
   // 3. gather of both position terms and the cotangent update
-  static int resident[64] = {0};
-  int per_sm = dev < 64 ? resident[dev] : 0;
-  if (per_sm == 0) {
-    PMGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, (const void *)adj_gather_tiles_kernel, TILE_THREADS, 0));
-    per_sm = std::max(per_sm, 1);
-    if (dev < 64) resident[dev] = per_sm;
-  }
+  const void *gfn = pot ? (const void *)adj_gather_tiles_kernel<true>
+                        : (const void *)adj_gather_tiles_kernel<false>;
+  const unsigned ggrid =
+      (unsigned)std::min<int64_t>(keys, (int64_t)resident_ctas(gfn, TILE_THREADS, 0));
   PMGB_CUDA(cudaMemsetAsync(work + 1, 0, sizeof(unsigned), s));
-  adj_gather_tiles_kernel<<<(unsigned)std::min<int64_t>(keys, (int64_t)sm_count() * per_sm),
-                            TILE_THREADS, 0, s>>>(
-      force3, ncell, mesh, nx, ny, nz, pos, dest, gx_in, gv_in, gx_out, gv_out, kick, drift,
-      offsets, (uint32_t)keys, stats, fmap, rmap, use_tma, work + 1);
+#define ADJ_GATHER_ARGS                                                                     \
+  force3, ncell, mesh, nx, ny, nz, pos, dest, gx_in, gv_in, gx_out, gv_out, kick, drift, \
+      offsets, (uint32_t)keys, stats, fmap, rmap, use_gtma, work + 1
+  if (pot)
+    adj_gather_tiles_kernel<true><<<ggrid, TILE_THREADS, 0, s>>>(ADJ_GATHER_ARGS);
+  else
+    adj_gather_tiles_kernel<false><<<ggrid, TILE_THREADS, 0, s>>>(ADJ_GATHER_ARGS);
+#undef ADJ_GATHER_ARGS
   PMGB_LAUNCHED("adj_gather_tiles_kernel");
   return PMGB_OK;
 }

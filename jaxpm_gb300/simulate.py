@@ -219,15 +219,26 @@ class SortedFastPM:
         c = self.stats_buf.cpu().tolist()
         return {"paint": c[0], "gather": c[1], "tma_wait_timeout": c[2]}
 
-    def alloc_store(self):
+    def alloc_store(self, potential=None):
         """Buffers of what the forward run records for the reverse sweep:
-        ``(positions [n,Np,3], force meshes [n,3,nx,ny,nz], dest [n,Np],
-        tile ranges [n,keys+1])``."""
+        ``(positions [n,Np,3], meshes, dest [n,Np], tile ranges [n,keys+1])``
+        with ``meshes`` each step's three force meshes ``[n,3,nx,ny,nz]``
+        or, with ``potential``, its potential ``[n,nx,ny,nz]`` (a third of
+        the mesh bytes; the reverse gather then derives each tile's forces
+        from the potential, 0.8 ms per step slower at 512^3).  The default
+        (None) records force meshes unless they would not fit in the free
+        device memory and the potential pipeline serves the mesh shape."""
         n, dev = self.n_steps, self.ws.device
         nx, ny, nz = self.mesh_shape
-        keys = _lib.load().pmgb_tile_key_count(nx, ny, nz)
+        lib = _lib.load()
+        if potential is None:
+            free = torch.cuda.mem_get_info(dev)[0]
+            f3_bytes = 4 * n * (3 * self.n + 3 * nx * ny * nz + self.n)
+            potential = f3_bytes > 0.9 * free and bool(lib.pmgb_fft3_supported(nx, ny, nz))
+        keys = lib.pmgb_tile_key_count(nx, ny, nz)
+        meshes = (n, nx, ny, nz) if potential else (n, 3, nx, ny, nz)
         return (torch.empty((n, self.n, 3), dtype=torch.float32, device=dev),
-                torch.empty((n, 3, nx, ny, nz), dtype=torch.float32, device=dev),
+                torch.empty(meshes, dtype=torch.float32, device=dev),
                 torch.empty((n, self.n), dtype=torch.int32, device=dev),
                 torch.empty((n, keys + 1), dtype=torch.int32, device=dev))
 
@@ -236,9 +247,10 @@ class SortedFastPM:
         sweep; returns the final state and the cotangents of the initial
         state, all in the caller's order.
 
-        Each forward step records the positions it starts from, its force
-        meshes, where each particle moved in the re-sort and the tile ranges
-        (``store`` from ``alloc_store()``, or allocated here).  The reverse
+        Each forward step records the positions it starts from, its
+        potential (or its force meshes, by the store's layout), where each
+        particle moved in the re-sort and the tile ranges (``store`` from
+        ``alloc_store()``, or allocated here).  The reverse
         sweep then runs in tile order throughout: the cotangents are put in
         the final tile order once, each ``pmgb_fpm_step_sorted_vjp_f32``
         pulls them one re-sort back, and the result is returned to the
@@ -248,6 +260,9 @@ class SortedFastPM:
         if store is None:
             store = self.alloc_store()
         xs, f3s, dests, offs = store
+        pot = f3s.dim() == 4  # [n, nx, ny, nz]: the potentials
+        record = "pmgb_fpm_run_sorted_record_pot_f32" if pot else "pmgb_fpm_run_sorted_record_f32"
+        reverse = "pmgb_fpm_step_sorted_vjp_pot_f32" if pot else "pmgb_fpm_step_sorted_vjp_f32"
         self.load(pos, vel)
         ids0 = self.ids[self.cur].clone()
         if n:
@@ -258,7 +273,7 @@ class SortedFastPM:
             kick = np.ascontiguousarray(self.kick[:n], dtype=np.float32)
             drift = np.ascontiguousarray(self.drift[:n], dtype=np.float32)
             fp = ctypes.POINTER(ctypes.c_float)
-            _lib.call("pmgb_fpm_run_sorted_record_f32", _lib.ptr(xs), _lib.ptr(self.vel[a]),
+            _lib.call(record, _lib.ptr(xs), _lib.ptr(self.vel[a]),
                       _lib.ptr(self.ids[a]), _lib.ptr(self.vel[b]), _lib.ptr(self.ids[b]),
                       _lib.ptr(self.pos[last]), self.n, nx, ny, nz, n, kick.ctypes.data_as(fp),
                       drift.ctypes.data_as(fp), self.r_split, _lib.ptr(self.ws), self.ws_bytes,
@@ -277,7 +292,7 @@ class SortedFastPM:
         _lib.call("pmgb_permute3_f32", _lib.ptr(g_vel.contiguous()), _lib.ptr(idn), self.n,
                   _lib.ptr(gva), s)
         for i in reversed(range(n)):
-            _lib.call("pmgb_fpm_step_sorted_vjp_f32", _lib.ptr(xs[i]), _lib.ptr(f3s[i]),
+            _lib.call(reverse, _lib.ptr(xs[i]), _lib.ptr(f3s[i]),
                       _lib.ptr(dests[i]), _lib.ptr(offs[i]), _lib.ptr(gxa), _lib.ptr(gva),
                       _lib.ptr(gxb), _lib.ptr(gvb), self.n, nx, ny, nz, float(self.kick[i]),
                       float(self.drift[i]), self.r_split, _lib.ptr(self.ws), self.ws_bytes,

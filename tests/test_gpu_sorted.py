@@ -211,7 +211,7 @@ def test_sorted_reverse_step_identity_dest(cuda, lib):
     eng = simulate.SortedFastPM(shape, cosmology.Planck15(), 0.3, 1.0, 1, device=cuda)
     eng.load(x, v)
     xs = eng.pos[eng.cur].clone()
-    f3, dest, offs = [t[0] for t in eng.alloc_store()[1:]]
+    f3, dest, offs = [t[0] for t in eng.alloc_store(potential=False)[1:]]
     eng.step(0, record=(f3, dest, offs))
     gx = torch.randn((np_, 3), device=cuda)
     gv = torch.randn((np_, 3), device=cuda)
@@ -319,3 +319,35 @@ def test_run_loop_potential_path_matches_oracle(cuda, r_split):
     assert rel_l2(v.cpu().numpy() - v0, vr - v0) < 1e-5
     assert rel_l2(x.cpu().numpy() - x0, xr - x0) < 1e-5
     assert eng.stats["gather"] == 0 and eng.stats["tma_wait_timeout"] == 0
+
+
+@pytest.mark.parametrize("r_split", [0.0, 1.5])
+def test_sorted_adjoint_potential_recording(cuda, r_split):
+    """The reverse sweep recorded with each step's potential (the gather and
+    its reverse step derive the forces with the order-1 stencil) against the
+    same sweep recorded with three force meshes per step, and against the
+    lattice-order adjoint, on a 64^3 perturbed lattice over 3 steps."""
+    from jaxpm_gb300 import cosmology, simulate
+    n = 64
+    shape = (n,) * 3
+    rng = np.random.default_rng(21)
+    lat = cic.lattice(shape).reshape(-1, 3)
+    x0 = T((lat + rng.normal(0, 0.6, lat.shape)).astype(np.float32), cuda)
+    v0 = T(rng.normal(0, 0.3, lat.shape).astype(np.float32), cuda)
+    g = torch.Generator(device=cuda).manual_seed(8)
+    gx = torch.randn(x0.shape, device=cuda, generator=g)
+    gv = torch.randn(x0.shape, device=cuda, generator=g)
+    cosmo = cosmology.Planck15()
+    eng = simulate.SortedFastPM(shape, cosmo, 0.3, 1.0, 3, r_split=r_split, device=cuda)
+    store_p = eng.alloc_store(potential=True)
+    assert store_p[1].dim() == 4  # [n, nx, ny, nz]: one potential per step
+    (px, pv), (pgx, pgv) = eng.vjp(x0, v0, gx, gv, store=store_p)
+    (fx, fv), (fgx, fgv) = eng.vjp(x0, v0, gx, gv, store=eng.alloc_store(potential=False))
+    assert rel_l2(px.cpu(), fx.cpu()) < 1e-6
+    assert rel_l2(pgx.cpu(), fgx.cpu()) < 1e-5
+    assert rel_l2(pgv.cpu(), fgv.cpu()) < 1e-5
+    ref = simulate.FastPM(shape, cosmo, 0.3, 1.0, 3, r_split=r_split, device=cuda)
+    (_, _), (ax, av) = ref.vjp(x0, v0, gx, gv)
+    assert rel_l2(pgx.cpu(), ax.cpu()) < 1e-4
+    assert rel_l2(pgv.cpu(), av.cpu()) < 1e-4
+    assert eng.stats["tma_wait_timeout"] == 0
