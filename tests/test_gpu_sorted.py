@@ -351,3 +351,40 @@ def test_sorted_adjoint_potential_recording(cuda, r_split):
     assert rel_l2(pgx.cpu(), ax.cpu()) < 1e-4
     assert rel_l2(pgv.cpu(), av.cpu()) < 1e-4
     assert eng.stats["tma_wait_timeout"] == 0
+
+
+def test_tile_schedule_dynamic_tails_128(cuda):
+    """At 128^3 (4096 tiles) both gathers reach the dynamic part of their
+    tile schedule: the forward gather takes three quarters of the keys
+    statically and the rest from its counter, the reverse gather only its
+    first two tiles per CTA.  Two run-loop steps against the oracle's FastPM
+    steps (float64), and the reverse sweep against the lattice-order
+    adjoint."""
+    from jaxpm_gb300 import cosmology, simulate
+    shape = (128, 128, 128)
+    rng = np.random.default_rng(41)
+    lat = cic.lattice(shape).reshape(-1, 3)
+    x0 = (lat + rng.normal(0, 1.0, lat.shape)).astype(np.float32)
+    v0 = rng.normal(0, 0.3, lat.shape).astype(np.float32)
+    cosmo = cosmology.Planck15()
+    eng = simulate.SortedFastPM(shape, cosmo, 0.1, 1.0, 2, device=cuda)
+    eng.load(T(x0, cuda), T(v0, cuda))
+    eng.run()
+    x, v = eng.state()
+    xr, vr = x0.astype(np.float64), v0.astype(np.float64)
+    for i in range(2):
+        F = fo.pm_forces(xr, mesh_shape=shape, dtype=np.float64)
+        vr = vr + eng.kick[i] * F
+        xr = xr + eng.drift[i] * vr
+    assert rel_l2(v.cpu().numpy() - v0, vr - v0) < 1e-5
+    assert rel_l2(x.cpu().numpy() - x0, xr - x0) < 1e-5
+    assert eng.stats["gather"] == 0 and eng.stats["tma_wait_timeout"] == 0
+    g = torch.Generator(device=cuda).manual_seed(9)
+    gx = torch.randn(x.shape, device=cuda, generator=g)
+    gv = torch.randn(x.shape, device=cuda, generator=g)
+    (_, _), (bx, bv) = eng.vjp(T(x0, cuda), T(v0, cuda), gx, gv)
+    ref = simulate.FastPM(shape, cosmo, 0.1, 1.0, 2, device=cuda)
+    (_, _), (ax, av) = ref.vjp(T(x0, cuda), T(v0, cuda), gx, gv)
+    assert rel_l2(bx.cpu(), ax.cpu()) < 1e-4
+    assert rel_l2(bv.cpu(), av.cpu()) < 1e-4
+    assert eng.stats["tma_wait_timeout"] == 0
