@@ -482,59 +482,23 @@ def run_gb300(args):
             "tolerance": 1e-3, "within": bool(rel.max() < 1e-3)}
         del plain, xp, vp
 
-    # end to end through the C ABI with host buffers: every step copies
-    # positions and velocities (caller's order) from pinned host memory,
-    # sorts them by tile, runs pmgb_fpm_step_sorted_f32, returns them to the
-    # caller's order and copies them back.  The copies go in E2E_CHUNKS
-    # chunks on two copy streams: chunk c of step i+1's input starts up as
-    # soon as chunk c of step i's result has come down, so the device-to-host
-    # read and the next host-to-device copy share the link's two directions
+    # end to end with the state in pinned host memory (SortedFastPM.run_host):
+    # every step copies positions and velocities (caller's order) up, sorts
+    # them by tile, runs pmgb_fpm_step_sorted_f32, returns them to the
+    # caller's order and copies them back; the copies go in E2E_CHUNKS chunks
+    # on two copy streams, chunk c of step i+1's input going up as soon as
+    # chunk c of step i's result is down
     if "e2e" not in skip:
         hx = x0.cpu().pin_memory()
         hv = v0.cpu().pin_memory()
-        dx_, dv_ = torch.empty_like(x0), torch.empty_like(v0)
         E = eng if engine == "sorted" else simulate.SortedFastPM((n,) * 3, cosmo, 0.1, 1.0, K,
                                                                 device=dev)
-        up, down = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
-        bounds = np.linspace(0, Np, E2E_CHUNKS + 1).astype(np.int64)
-        chunks = [slice(int(a), int(b)) for a, b in zip(bounds[:-1], bounds[1:])]
-        came_down = [torch.cuda.Event() for _ in chunks]
-        went_up, computed = torch.cuda.Event(), torch.cuda.Event()
         torch.cuda.synchronize(dev)
         barrier(world)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        up.wait_stream(stream)
-        for i in range(K):
-            with torch.cuda.stream(up):
-                for c, sl in enumerate(chunks):
-                    if i > 0:
-                        up.wait_event(came_down[c])
-                    dx_[sl].copy_(hx[sl], non_blocking=True)
-                    dv_[sl].copy_(hv[sl], non_blocking=True)
-                went_up.record(up)
-            stream.wait_event(went_up)
-            _lib.call("pmgb_tile_sort_f32", _lib.ptr(dx_), _lib.ptr(dv_), None, Np, nx, ny, nz,
-                      _lib.ptr(E.pos[0]), _lib.ptr(E.vel[0]), _lib.ptr(E.ids[0]),
-                      _lib.ptr(E.sort_ws), E.sort_bytes, s)
-            _lib.call("pmgb_fpm_step_sorted_f32", _lib.ptr(E.pos[0]), _lib.ptr(E.vel[0]),
-                      _lib.ptr(E.ids[0]), _lib.ptr(E.pos[1]), _lib.ptr(E.vel[1]),
-                      _lib.ptr(E.ids[1]), Np, nx, ny, nz, float(E.kick[i]), float(E.drift[i]),
-                      0.0, _lib.ptr(E.ws), E.ws_bytes, _lib.ptr(E.sort_ws), E.sort_bytes, None,
-                      None, None, None, s)
-            _lib.call("pmgb_unpermute3_f32", _lib.ptr(E.pos[1]), _lib.ptr(E.ids[1]), Np,
-                      _lib.ptr(dx_), s)
-            _lib.call("pmgb_unpermute3_f32", _lib.ptr(E.vel[1]), _lib.ptr(E.ids[1]), Np,
-                      _lib.ptr(dv_), s)
-            computed.record(stream)
-            with torch.cuda.stream(down):
-                down.wait_event(computed)
-                for c, sl in enumerate(chunks):
-                    hx[sl].copy_(dx_[sl], non_blocking=True)
-                    hv[sl].copy_(dv_[sl], non_blocking=True)
-                    came_down[c].record(down)
-        stream.wait_stream(down)
+        E.run_host(hx, hv, steps=K, chunks=E2E_CHUNKS)
         e1.record(stream)
         torch.cuda.synchronize(dev)
         ems = max_over_ranks(e0.elapsed_time(e1), world)
@@ -549,8 +513,9 @@ def run_gb300(args):
         result["e2e"] = {"value": world * Np * K / (ems / 1e3), "unit": "particle-steps/s",
                          "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                          "ms_per_step": ems / K,
-                         "api": "pmgb_tile_sort_f32 + pmgb_fpm_step_sorted_f32 + "
-                                "pmgb_unpermute3_f32 (C ABI), pinned host buffers, copies in "
+                         "api": "SortedFastPM.run_host: pmgb_tile_sort_f32 + "
+                                "pmgb_fpm_step_sorted_f32 + pmgb_unpermute3_f32 (C ABI) per "
+                                "step, pinned host buffers, copies in "
                                 f"{E2E_CHUNKS} chunks on two copy streams (each result chunk "
                                 "back before the next step's copy of it goes up)",
                          "pk_vs_timed_run": {"max_rel_dev_per_bin": float(rel.max()),

@@ -202,6 +202,67 @@ class SortedFastPM:
     def ids_current(self):
         return self.ids[self.cur]
 
+    def run_host(self, hpos, hvel, steps=None, chunks=8):
+        """Steps a state that lives in pinned host memory: ``hpos``/``hvel``
+        ([Np, 3] float32, caller's order) are updated in place after each of
+        ``steps`` steps (default all), each step copying them up, sorting
+        them by tile (``pmgb_tile_sort_f32``), stepping
+        (``pmgb_fpm_step_sorted_f32``), returning them to the caller's order
+        (``pmgb_unpermute3_f32``) and copying them back.  The copies go in
+        ``chunks`` chunks on two copy streams: chunk c of the next step's
+        input goes up as soon as chunk c of this step's result is down, so
+        the read-back and the next upload share the host link's two
+        directions.  Returns when the last copy has been issued (ordered
+        before later work on the current stream)."""
+        if not (hpos.is_pinned() and hvel.is_pinned()):
+            raise ValueError("run_host needs pinned host tensors")
+        n = self.n_steps if steps is None else int(steps)
+        nx, ny, nz = self.mesh_shape
+        dev = self.ws.device
+        stream = torch.cuda.current_stream(dev)
+        s = _lib.stream(dev)
+        if not hasattr(self, "_host_bufs"):
+            f = dict(dtype=torch.float32, device=dev)
+            self._host_bufs = (torch.empty((self.n, 3), **f), torch.empty((self.n, 3), **f),
+                               torch.cuda.Stream(dev), torch.cuda.Stream(dev))
+        dx, dv, up, down = self._host_bufs
+        bounds = np.linspace(0, self.n, int(chunks) + 1).astype(np.int64)
+        parts = [slice(int(a), int(b)) for a, b in zip(bounds[:-1], bounds[1:])]
+        came_down = [torch.cuda.Event() for _ in parts]
+        went_up, computed = torch.cuda.Event(), torch.cuda.Event()
+        up.wait_stream(stream)
+        for i in range(n):
+            with torch.cuda.stream(up):
+                for c, sl in enumerate(parts):
+                    if i > 0:
+                        up.wait_event(came_down[c])
+                    dx[sl].copy_(hpos[sl], non_blocking=True)
+                    dv[sl].copy_(hvel[sl], non_blocking=True)
+                went_up.record(up)
+            stream.wait_event(went_up)
+            _lib.call("pmgb_tile_sort_f32", _lib.ptr(dx), _lib.ptr(dv), None, self.n, nx, ny, nz,
+                      _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]), _lib.ptr(self.ids[0]),
+                      _lib.ptr(self.sort_ws), self.sort_bytes, s)
+            _lib.call("pmgb_fpm_step_sorted_f32", _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]),
+                      _lib.ptr(self.ids[0]), _lib.ptr(self.pos[1]), _lib.ptr(self.vel[1]),
+                      _lib.ptr(self.ids[1]), self.n, nx, ny, nz, float(self.kick[i]),
+                      float(self.drift[i]), self.r_split, _lib.ptr(self.ws), self.ws_bytes,
+                      _lib.ptr(self.sort_ws), self.sort_bytes, None, None, None,
+                      _lib.ptr(self.stats_buf), s)
+            _lib.call("pmgb_unpermute3_f32", _lib.ptr(self.pos[1]), _lib.ptr(self.ids[1]),
+                      self.n, _lib.ptr(dx), s)
+            _lib.call("pmgb_unpermute3_f32", _lib.ptr(self.vel[1]), _lib.ptr(self.ids[1]),
+                      self.n, _lib.ptr(dv), s)
+            computed.record(stream)
+            with torch.cuda.stream(down):
+                down.wait_event(computed)
+                for c, sl in enumerate(parts):
+                    hpos[sl].copy_(dx[sl], non_blocking=True)
+                    hvel[sl].copy_(dv[sl], non_blocking=True)
+                    came_down[c].record(down)
+        stream.wait_stream(down)
+        self.cur = 1
+
     def state(self):
         """``(pos, vel)`` in the caller's order (new tensors)."""
         out_p = torch.empty_like(self.pos[self.cur])
