@@ -29,7 +29,7 @@ import time
 import numpy as np
 
 # chunks of the end-to-end leg's host copies (see the e2e leg)
-E2E_CHUNKS = 8
+E2E_CHUNKS = 16
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)

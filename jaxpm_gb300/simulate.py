@@ -202,7 +202,7 @@ class SortedFastPM:
     def ids_current(self):
         return self.ids[self.cur]
 
-    def run_host(self, hpos, hvel, steps=None, chunks=8):
+    def run_host(self, hpos, hvel, steps=None, chunks=16):
         """Steps a state that lives in pinned host memory: ``hpos``/``hvel``
         ([Np, 3] float32, caller's order) are updated in place after each of
         ``steps`` steps (default all), each step copying them up, sorting
