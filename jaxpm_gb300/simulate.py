@@ -261,7 +261,8 @@ class SortedFastPM:
                     hvel[sl].copy_(dv[sl], non_blocking=True)
                     came_down[c].record(down)
         stream.wait_stream(down)
-        self.cur = 1
+        if n > 0:
+            self.cur = 1  # the engine's buffers hold the last step's sorted state
 
     def state(self):
         """``(pos, vel)`` in the caller's order (new tensors)."""
