@@ -4,7 +4,7 @@ Workload: 512^3 particles on a 512^3 mesh (FP32 positions and
 velocities), box 512 Mpc/h, Planck15 cosmology, initial conditions from a
 seeded Gaussian random field (NumPy PCG64 white noise coloured by the
 Eisenstein-Hu linear power spectrum), 2LPT to a = 0.1, then K FastPM steps
-(K = --steps, 40 by default) linear in a up to a = 1.  One step is one
+(K = --steps, 20 by default) linear in a up to a = 1.  One step is one
 force evaluation (paint, R2C, fused k-space kernel, batched C2R) plus the
 fused gather + kick + drift over all particles.
 
@@ -46,7 +46,7 @@ def parse():
                          "of 64^3-128^3; paint: cic_paint/cic_read microbenchmarks; grad: "
                          "gradients w.r.t. noise and cosmology")
     ap.add_argument("--steps", type=int, default=None,
-                    help="timed steps (default 40; 20 for the batched workload)")
+                    help="timed steps (default 20)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--mesh", type=int, default=N_DEFAULT)
@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--skip", default="", help="comma list of legs to skip: "
                     "adjoint,plain,e2e,cpu,clocks")
     ap.add_argument("--phases-only", action="store_true")
+    ap.add_argument("--repeats", type=int, default=5,
+                    help="timed repetitions of each K-step run (the median is reported)")
     ap.add_argument("--fft", default=None, choices=["cufft", "fused", "own"],
                     help="FFT path of the force evaluation (library default if omitted)")
     return ap.parse_args()
@@ -335,29 +337,38 @@ def run_gb300(args):
         reset()
         torch.cuda.synchronize(dev)
 
+    R = max(1, args.repeats)
     clocks = ClockSampler(local) if "clocks" not in skip else None
     if clocks:
         clocks.start()
         time.sleep(0.3)
-    barrier(world)
-    torch.cuda.synchronize(dev)
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
-    launches0 = lib.pmgb_launch_count()
-    t0.record(stream)
-    with nvtx("timed"):
-        if engine == "sorted":
-            eng.run()  # pmgb_fpm_run_sorted_f32: the K steps in one call
-        else:
-            for i in range(K):
-                step_phased(i, events[i])
-    t1.record(stream)
-    launches = lib.pmgb_launch_count() - launches0
-    torch.cuda.synchronize(dev)
-    barrier(world)
+
+    def timed_run():
+        """One timed K-step run from the initial state: (ms, own launches)."""
+        reset()
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        torch.cuda.synchronize(dev)
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        launches0 = lib.pmgb_launch_count()
+        t0.record(stream)
+        with nvtx("timed"):
+            if engine == "sorted":
+                eng.run()  # pmgb_fpm_run_sorted_f32: the K steps in one call
+            else:
+                for i in range(K):
+                    step_phased(i, events[i])
+        t1.record(stream)
+        launches = lib.pmgb_launch_count() - launches0
+        torch.cuda.synchronize(dev)
+        barrier(world)
+        return max_over_ranks(t0.elapsed_time(t1), world), launches
+
+    runs = [timed_run() for _ in range(R)]
     clk = clocks.stop() if clocks else None
-    ms = t0.elapsed_time(t1)
-    ms_max = max_over_ranks(ms, world)
+    run_ms = [r[0] for r in runs]
+    ms_max = float(np.median(run_ms))
     value = world * Np * K / (ms_max / 1e3)
     phase_ms = {name: float(np.mean([events[i][j].elapsed_time(events[i][j + 1])
                                      for i in range(K)])) for j, name in enumerate(phase_names)}
@@ -366,13 +377,13 @@ def run_gb300(args):
     rho = painting.paint(torch.zeros((n,) * 3, device=dev), current_positions(),
                          mode="deterministic")
     mass_err = abs(rho.double().sum().item() - Np) / Np
-    # P(k) of the final density (GPU R2C + binned |delta_k|^2), compared below
-    # with the one-kernel-per-op path's run from the same initial state
-    _, pk_run = utils.power_spectrum(rho)
+    # P(k) of the final density (GPU R2C + binned |delta_k|^2): against the
+    # oracle's run of the same workload (below) and the one-kernel-per-op path
+    _, pk_run = utils.power_spectrum(rho, box_shape=[n * BOX_PER_CELL] * 3)
     del rho
-    # own kernels launched in the timed region, counted by the library
-    # (cuFFT's kernels are not counted)
-    gpu_launches = int(launches)
+    # own kernels launched in one timed run, counted by the library (cuFFT's
+    # kernels are not counted)
+    gpu_launches = int(runs[-1][1])
 
     result = {"metric": "particle-steps/s (FastPM PM step, 512^3 particles on 512^3 mesh)",
               "value": value, "unit": "particle-steps/s", "n_gpus": world, "steps": K,
@@ -391,10 +402,19 @@ def run_gb300(args):
                          "parallelism": "replicas" if world > 1 else "single",
                          "l2": "inputs larger than L2 (positions+velocities 3.2 GB, "
                                "meshes 0.54 GB each)"},
+              "repeats": {"n": R, "ms_per_step": [m / K for m in run_ms],
+                          "median_ms_per_step": ms_max / K,
+                          "spread": (max(run_ms) - min(run_ms)) / ms_max,
+                          "note": "value is the median of the repeated K-step runs, each "
+                                  "from the same initial state"},
               "phases_ms": phase_ms, "mass_rel_err": mass_err,
               "gpu_launches": gpu_launches}
     if engine == "sorted":
         result["particles_outside_tile"] = eng.stats
+        if eng.stats.get("tma_wait_timeout"):
+            raise RuntimeError("a TMA wait of the gather timed out: the run is invalid")
+    result["parity"] = parity_vs_oracle(n, K, pk_run, eng.state() if engine == "sorted"
+                                        else (x, v))
 
     # roofline of the dominant own kernel
     peak, peak_kind = peaks()
@@ -427,6 +447,25 @@ def run_gb300(args):
         print(json.dumps(result))
         return
 
+    def repeated(fn, reps):
+        """Median and spread of `reps` timed calls of fn (CUDA events on the
+        stream, max over ranks); fn(prepare=True) runs untimed first."""
+        out = []
+        for _ in range(reps):
+            fn(True)
+            torch.cuda.synchronize(dev)
+            barrier(world)
+            a0 = torch.cuda.Event(enable_timing=True)
+            a1 = torch.cuda.Event(enable_timing=True)
+            a0.record(stream)
+            fn(False)
+            a1.record(stream)
+            torch.cuda.synchronize(dev)
+            out.append(max_over_ranks(a0.elapsed_time(a1), world))
+        med = float(np.median(out))
+        return med, {"n": reps, "ms_per_step": [m / K for m in out],
+                     "spread": (max(out) - min(out)) / med}
+
     # forward + adjoint (hand-written adjoint; positions stored before every
     # step, and for the sorted loop also its force meshes and re-sort map)
     if "adjoint" not in skip:
@@ -437,19 +476,15 @@ def run_gb300(args):
         else:
             store = torch.empty((K, Np, 3), dtype=torch.float32, device=dev)
         eng.vjp(x0, v0, gx, gv, store=store)  # warm-up (plans, buffers)
-        torch.cuda.synchronize(dev)
-        barrier(world)
-        a0 = torch.cuda.Event(enable_timing=True)
-        a1 = torch.cuda.Event(enable_timing=True)
-        a0.record(stream)
-        with nvtx("adjoint"):
-            eng.vjp(x0, v0, gx, gv, store=store)
-        a1.record(stream)
-        torch.cuda.synchronize(dev)
-        ams = max_over_ranks(a0.elapsed_time(a1), world)
+
+        def adj(prepare):
+            if not prepare:
+                with nvtx("adjoint"):
+                    eng.vjp(x0, v0, gx, gv, store=store)
+        ams, rep = repeated(adj, R)
         result["fwd_adjoint"] = {"value": world * Np * K / (ams / 1e3),
                                  "unit": "particle-steps/s", "ms_per_step": ams / K,
-                                 "cost_vs_forward": ams / ms_max}
+                                 "cost_vs_forward": ams / ms_max, "repeats": rep}
         del store
 
     # one-kernel-per-op GPU form
@@ -457,29 +492,28 @@ def run_gb300(args):
         plain = simulate.FastPM((n,) * 3, cosmo, 0.1, 1.0, K, plain=True, device=dev)
         xp, vp = x0.clone(), v0.clone()
         plain.step(xp, vp, 0)
-        xp.copy_(x0)
-        vp.copy_(v0)
-        torch.cuda.synchronize(dev)
-        b0 = torch.cuda.Event(enable_timing=True)
-        b1 = torch.cuda.Event(enable_timing=True)
-        b0.record(stream)
-        plain.run(xp, vp)
-        b1.record(stream)
-        torch.cuda.synchronize(dev)
-        pms = max_over_ranks(b0.elapsed_time(b1), world)
+
+        def plain_run(prepare):
+            if prepare:
+                xp.copy_(x0)
+                vp.copy_(v0)
+            else:
+                plain.run(xp, vp)
+        pms, rep = repeated(plain_run, R)
         result["plain_gpu"] = {"value": world * Np * K / (pms / 1e3), "unit": "particle-steps/s",
-                               "ms_per_step": pms / K, "fused_speedup": pms / ms_max}
-        # parity of the timed path at full size: its final P(k) against the
+                               "ms_per_step": pms / K, "fused_speedup": pms / ms_max,
+                               "repeats": rep}
+        # the two GPU forms from the same state: final P(k) of the
         # one-kernel-per-op path (atomic paint, three force meshes through
-        # cuFFT, separate gather / kick / drift) run from the same state
+        # cuFFT, separate gather / kick / drift) against the timed run's
         rho_p = painting.paint(torch.zeros((n,) * 3, device=dev), xp, mode="deterministic")
-        _, pk_plain = utils.power_spectrum(rho_p)
+        _, pk_plain = utils.power_spectrum(rho_p, box_shape=[n * BOX_PER_CELL] * 3)
         del rho_p
         rel = np.abs(pk_run / pk_plain - 1.0)
         rel = rel[np.isfinite(rel)]
         result["plain_gpu"]["pk_vs_timed_run"] = {
-            "max_rel_dev_per_bin": float(rel.max()), "bins": int(rel.size),
-            "tolerance": 1e-3, "within": bool(rel.max() < 1e-3)}
+            "max_rel_dev_per_bin": float(rel.max()), "bins": int(rel.size)}
+        result["plain_gpu"]["parity"] = parity_vs_oracle(n, K, pk_plain, None)
         del plain, xp, vp
 
     # end to end with the state in pinned host memory (SortedFastPM.run_host):
@@ -493,26 +527,25 @@ def run_gb300(args):
         hv = v0.cpu().pin_memory()
         E = eng if engine == "sorted" else simulate.SortedFastPM((n,) * 3, cosmo, 0.1, 1.0, K,
                                                                 device=dev)
-        torch.cuda.synchronize(dev)
-        barrier(world)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        E.run_host(hx, hv, steps=K, chunks=E2E_CHUNKS)
-        e1.record(stream)
-        torch.cuda.synchronize(dev)
-        ems = max_over_ranks(e0.elapsed_time(e1), world)
+
+        def e2e(prepare):
+            if prepare:  # the caller's state back to the initial one (untimed)
+                hx.copy_(x0.cpu())
+                hv.copy_(v0.cpu())
+            else:
+                E.run_host(hx, hv, steps=K, chunks=E2E_CHUNKS)
+        ems, rep = repeated(e2e, R)
         nbytes = 2 * Np * 12
         # the state that came back: its P(k) against the timed run's
         rho_e = painting.paint(torch.zeros((n,) * 3, device=dev), hx.to(dev),
                                mode="deterministic")
-        _, pk_e2e = utils.power_spectrum(rho_e)
+        _, pk_e2e = utils.power_spectrum(rho_e, box_shape=[n * BOX_PER_CELL] * 3)
         del rho_e
         rel = np.abs(pk_e2e / pk_run - 1.0)
         rel = rel[np.isfinite(rel)]
         result["e2e"] = {"value": world * Np * K / (ems / 1e3), "unit": "particle-steps/s",
                          "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
-                         "ms_per_step": ems / K,
+                         "ms_per_step": ems / K, "repeats": rep,
                          "api": "SortedFastPM.run_host: pmgb_tile_sort_f32 + "
                                 "pmgb_fpm_step_sorted_f32 + pmgb_unpermute3_f32 (C ABI) per "
                                 "step, pinned host buffers, copies in "
@@ -520,6 +553,21 @@ def run_gb300(args):
                                 "back before the next step's copy of it goes up)",
                          "pk_vs_timed_run": {"max_rel_dev_per_bin": float(rel.max()),
                                              "bins": int(rel.size)}}
+        del hx, hv
+
+    # paint / read microbenchmarks (16.7M uniform and clustered particles on
+    # 256^3) and the paint-only case: the timed run's a=1 particles on 1024^3
+    if "paint" not in skip and rank == 0 and n == 512:
+        big = None
+        if "1024" not in skip:
+            reset()
+            eng.run()
+            big = (eng.state()[0] * 2.0).contiguous()  # cell units of the 1024^3 mesh
+        torch.cuda.empty_cache()
+        suite, _ = paint_read_suite(dev, max(W, 3), max(R, 5), big, skip)
+        del big
+        torch.cuda.empty_cache()
+        result["paint_read"] = suite
 
     if clk is not None:
         result["clocks"] = clk
@@ -531,6 +579,40 @@ def run_gb300(args):
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def parity_vs_oracle(n, K, pk, state):
+    """The final density's P(k) (and, with ``state`` = (pos, vel) in the
+    caller's order, a fixed sample of particles) against the oracle's
+    float32 and float64 runs of the same workload (``tests/golden/
+    large_<n>_<K>.npz``, made by ``tests/golden/make_large_golden.py``),
+    when a fixture exists for this mesh and step count."""
+    path = os.path.join(ROOT, "tests", "golden", f"large_{n}_{K}.npz")
+    if not os.path.exists(path):
+        return {"fixture": None, "note": f"no oracle fixture for {n}^3 and {K} steps"}
+    d = np.load(path)
+    out = {"fixture": os.path.relpath(path, ROOT), "tolerance_per_bin": 1e-3}
+    for tag in ("32", "64"):
+        rel = np.abs(pk / d[f"pk1_{tag}"] - 1.0)
+        out[f"pk_vs_oracle_f{tag}"] = {"max_rel_dev_per_bin": float(rel.max()),
+                                       "bins": int(rel.size)}
+    out["oracle_f32_vs_f64"] = float(np.abs(d["pk1_32"] / d["pk1_64"] - 1.0).max())
+    out["within"] = bool(out["pk_vs_oracle_f32"]["max_rel_dev_per_bin"] < 1e-3)
+    if state is not None:
+        import torch
+        idx = torch.from_numpy(d["sample"]).to(state[0].device)
+        x = state[0][idx].double().cpu().numpy()
+        v = state[1][idx].double().cpu().numpy()
+        i = d["sample"].astype(np.int64)
+        lat = np.stack([i // (n * n), (i // n) % n, i % n], -1)
+        for tag in ("32", "64"):
+            dx = x - d[f"x1_{tag}"]
+            dx -= n * np.round(dx / n)
+            out[f"displacement_vs_oracle_f{tag}"] = float(
+                np.linalg.norm(dx) / np.linalg.norm(d[f"x1_{tag}"] - lat))
+            out[f"velocity_vs_oracle_f{tag}"] = float(
+                np.linalg.norm(v - d[f"v1_{tag}"]) / np.linalg.norm(d[f"v1_{tag}"]))
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -728,27 +810,25 @@ def cpu_batched_sample(ns, ocs, s8s, K):
 # ---------------------------------------------------------------------------
 # paint / read microbenchmarks
 # ---------------------------------------------------------------------------
-def run_paint(args):
+def paint_read_suite(dev, W, K, big=None, skip=()):
+    """The cic_paint / cic_read microbenchmarks on 16,777,216 particles on a
+    256^3 mesh: (i) uniform U[0,256)^3 positions (PCG64 seed 1) and (ii) the
+    a = 1 positions of the 256^3 run (2LPT to a = 0.1, 20 steps), in the
+    caller's (lattice) order; each painter (atomic, binned, sort + box) and
+    the one- and three-component reads, median of K launches after W
+    warm-up launches, with the fraction of the measured HBM peak.  With
+    ``big`` (positions in cell units of a 1024^3 mesh) also the paint-only
+    case on 1024^3.  Returns ``(results, launches)``."""
     import torch
-    from jaxpm_gb300 import _lib, painting, simulate, cosmology
+    from jaxpm_gb300 import _lib, cosmology, simulate
 
-    rank, world, local = dist_env()
-    if rank != 0:
-        return
-    dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
-    skip = set(filter(None, args.skip.split(",")))
-    K, W = max(args.steps, 5), max(args.warmup, 3)
     lib = _lib.load()
     stream = torch.cuda.current_stream(dev)
     s = _lib.stream(dev)
-    peak, peak_kind = peaks()
+    peak, _ = peaks()
     n = 256
     Np = n**3
     cosmo = cosmology.Planck15()
-
-    # (i) uniform U[0,256)^3, PCG64 seed 1; (ii) the a=1 positions of the
-    # 256^3 run (2LPT to a=0.1, 20 steps), in the caller's (lattice) order
     uni = torch.from_numpy(np.random.Generator(np.random.PCG64(1)).uniform(
         0.0, n, (Np, 3)).astype(np.float32)).to(dev)
     x0, v0 = initial_state(n, cosmo, dev)
@@ -773,7 +853,7 @@ def run_paint(args):
             torch.cuda.synchronize(dev)
             ts.append(a.elapsed_time(b))
         if tag is not None:
-            launches[tag] = lib.pmgb_launch_count() - l0
+            launches[tag] = (lib.pmgb_launch_count() - l0) // K
         return float(np.median(ts))
 
     def paint_ops(pos, shape, tag):
@@ -803,16 +883,18 @@ def run_paint(args):
         out = {}
         for name, fn in ops.items():
             with nvtx(f"paint_{tag}_{name}"):
-                ms = timed(fn, (shape, pos.data_ptr(), name))
+                ms = timed(fn, f"paint_{tag}_{name}")
             total = float(mesh.double().sum())
             out[name] = {"ms": ms, "particles_per_s": npart / (ms / 1e3),
                          "achieved_gbs": alg / (ms / 1e3) / 1e9,
                          "frac": alg / (ms / 1e3) / 1e9 / peak,
                          "mass_rel_err": abs(total - npart) / npart}
         del mesh, sws, spos, sid
+        best = max(out, key=lambda k: out[k]["particles_per_s"])
+        out["best"] = best
         return out
 
-    def read_ops(pos, shape):
+    def read_ops(pos, shape, tag):
         nx, ny, nz = shape
         npart = pos.shape[0]
         g = torch.Generator(device=dev).manual_seed(3)
@@ -821,15 +903,19 @@ def run_paint(args):
         out3 = torch.empty((npart, 3), dtype=torch.float32, device=dev)
         ncell = nx * ny * nz
         res = {}
-        ms = timed(lambda: _lib.call("pmgb_cic_read_f32", _lib.ptr(mesh3), nx, ny, nz,
-                                     _lib.ptr(pos), npart, _lib.ptr(out1), s))
-        alg = 20.0 * npart
+        with nvtx(f"read_{tag}"):
+            ms = timed(lambda: _lib.call("pmgb_cic_read_f32", _lib.ptr(mesh3), nx, ny, nz,
+                                         _lib.ptr(pos), npart, _lib.ptr(out1), s),
+                       f"read_{tag}")
+        alg = 16.0 * npart + 4.0 * ncell  # positions + output + the mesh once
         res["read"] = {"ms": ms, "particles_per_s": npart / (ms / 1e3),
                        "achieved_gbs": alg / (ms / 1e3) / 1e9,
                        "frac": alg / (ms / 1e3) / 1e9 / peak}
-        ms = timed(lambda: _lib.call("pmgb_cic_read3_f32", _lib.ptr(mesh3), ncell, nx, ny, nz,
-                                     _lib.ptr(pos), npart, _lib.ptr(out3), s))
-        alg = 36.0 * npart
+        with nvtx(f"read3_{tag}"):
+            ms = timed(lambda: _lib.call("pmgb_cic_read3_f32", _lib.ptr(mesh3), ncell, nx, ny,
+                                         nz, _lib.ptr(pos), npart, _lib.ptr(out3), s),
+                       f"read3_{tag}")
+        alg = 24.0 * npart + 12.0 * ncell
         res["read3"] = {"ms": ms, "particles_per_s": npart / (ms / 1e3),
                         "achieved_gbs": alg / (ms / 1e3) / 1e9,
                         "frac": alg / (ms / 1e3) / 1e9 / peak}
@@ -839,11 +925,35 @@ def run_paint(args):
     results = {}
     for dname, pos in [("uniform", uni), ("clustered_a1", clustered)]:
         results[dname] = {"paint": paint_ops(pos, (n,) * 3, dname),
-                          "read": read_ops(pos, (n,) * 3)}
-    del uni
+                          "read": read_ops(pos, (n,) * 3, dname)}
+    del uni, clustered
+    if big is not None and "1024" not in skip:
+        torch.cuda.empty_cache()
+        results["paint_only_1024"] = paint_ops(big, (1024,) * 3, "1024")
+        torch.cuda.empty_cache()
+    results["accounting"] = ("paint 12 B/particle read + 4 B/cell written; read 12 B/particle "
+                             "positions + 4 B/particle out + the mesh once; read3 12 + 12 B/"
+                             "particle + three meshes once; fractions of the measured "
+                             "HBM copy bandwidth")
+    return results, launches
 
-    # paint-only: the 512^3 run's a=1 particles on a 1024^3 mesh
+
+def run_paint(args):
+    import torch
+    from jaxpm_gb300 import cosmology, simulate
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    skip = set(filter(None, args.skip.split(",")))
+    K, W = max(args.steps, 5), max(args.warmup, 3)
+    peak, peak_kind = peaks()
+    big = None
     if "1024" not in skip:
+        # paint-only: the 512^3 run's a=1 particles on a 1024^3 mesh
+        cosmo = cosmology.Planck15()
         x5, v5 = initial_state(512, cosmo, dev)
         sim = simulate.SortedFastPM((512,) * 3, cosmo, 0.1, 1.0, 40, device=dev)
         sim.load(x5, v5)
@@ -852,12 +962,10 @@ def run_paint(args):
         big = (sim.state()[0] * 2.0).contiguous()  # cell units of the 1024^3 mesh
         del sim
         torch.cuda.empty_cache()
-        results["paint_only_1024"] = paint_ops(big, (1024,) * 3, "1024")
-        del big
-        torch.cuda.empty_cache()
-
+    results, launches = paint_read_suite(dev, W, K, big, skip)
+    del big
     head = results["clustered_a1"]["paint"]
-    best = max(head, key=lambda k: head[k]["particles_per_s"])
+    best = head["best"]
     result = {"metric": "particles/s (cic_paint, 16.7M clustered a=1 particles on 256^3 mesh)",
               "value": head[best]["particles_per_s"], "unit": "particles/s", "n_gpus": 1,
               "steps": K, "warmup": W, "ms_per_step": head[best]["ms"],
@@ -876,7 +984,7 @@ def run_paint(args):
                            "achieved": head[best]["achieved_gbs"], "peak": peak, "unit": "GB/s",
                            "frac": head[best]["frac"], "peak_kind": peak_kind,
                            "algorithmic_bytes_per_particle": 16.0, "traffic": None},
-              "gpu_launches": int(launches[((n,) * 3, clustered.data_ptr(), best)])}
+              "gpu_launches": int(launches[f"paint_clustered_a1_{best}"])}
     print(json.dumps(result))
 
 
@@ -1019,20 +1127,33 @@ def oracle_state(n, seed=0):
     return cosmo, lat + dx, p
 
 
+def oracle_threads():
+    """Host threads the oracle's step uses: its C paint/read (OpenMP) and
+    scipy.fft (all workers)."""
+    from oracle import native
+    return max(native.threads(), host_threads()) if native.lib() is not None else \
+        host_threads()
+
+
+def oracle_kind():
+    from oracle import native
+    return ("C paint/read (OpenMP) + scipy.fft" if native.lib() is not None
+            else "NumPy paint/read + scipy.fft")
+
+
 def cpu_baseline_sample(cosmo_unused=None, n=256):
     """One oracle FastPM step (paint, C2C FFTs, k-space, three reads, kick,
     drift) on a 256^3 sub-problem, timed on the host cores."""
     from oracle import nbody as onb
     cosmo, x, v = oracle_state(n)
-    kc, dc = onb.fpm_coefficients(cosmo, 0.1, 1.0, 40)
+    kc, dc = onb.fpm_coefficients(cosmo, 0.1, 1.0, 20)
     t = time.perf_counter()
     onb.fpm_step(x, v, (n,) * 3, kc[0], dc[0])
     dt = time.perf_counter() - t
-    return {"value": n**3 / dt, "unit": "particle-steps/s", "cores": host_threads(),
+    return {"value": n**3 / dt, "unit": "particle-steps/s", "cores": oracle_threads(),
             "kind": "port",
-            "sample": f"one FastPM step of the NumPy oracle on {n}^3 particles/{n}^3 mesh "
-                      f"({dt:.1f} s; FFTs on all host threads via scipy.fft, scatter/gather "
-                      "single-threaded NumPy)"}
+            "sample": f"one FastPM step of the oracle on a {n}^3-particle/{n}^3-mesh sub-problem "
+                      f"of the workload ({dt:.1f} s; {oracle_kind()}, all host threads)"}
 
 
 def run_reference(args):
@@ -1045,13 +1166,13 @@ def run_reference(args):
         return run_reference_paint(args)
     if args.workload == "grad":
         return run_reference_grad(args)
-    n_sample = 128
+    n_sample = 256
     K, W = args.steps, args.warmup
     from oracle import nbody as onb
     cosmo, x0, v0 = oracle_state(n_sample)
     kc, dc = onb.fpm_coefficients(cosmo, 0.1, 1.0, K)
     x, v = x0, v0
-    for i in range(W):
+    for i in range(min(W, 2)):  # warm-up bounded: a CPU step takes seconds
         x, v = onb.fpm_step(x, v, (n_sample,) * 3, kc[i % K], dc[i % K])
     x, v = x0, v0
     t = time.perf_counter()
@@ -1065,13 +1186,17 @@ def run_reference(args):
            "ms_per_step": dt / K * 1e3, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "impl": "reference",
            "data": "synthetic: seeded Gaussian random field, 2LPT to a=0.1",
-           "config": {"workload": f"FastPM {n}^3 particles on {n}^3 mesh, box {n} Mpc/h, "
-                                  f"2LPT a=0.1, {K} steps to a=1"},
-           "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": host_threads(),
-                            "kind": "port",
-                            "sample": f"each timed step is one FastPM step of the NumPy oracle "
-                                      f"(the reference's algorithm restated; JAX is not "
-                                      f"installed) on a {n_sample}^3 sub-problem"},
+           "config": {"workload": f"FastPM {n_sample}^3 particles on {n_sample}^3 mesh, box "
+                                  f"{n_sample} Mpc/h, 2LPT a=0.1, {K} steps to a=1: a bounded "
+                                  f"sample of the {n}^3 workload (the same per-particle work "
+                                  f"at 1/{(n // n_sample)**3} of the particles)",
+                      "particles": n_sample**3, "mesh": [n_sample] * 3,
+                      "sample_of": f"{n}^3 particles on {n}^3 mesh, box {n} Mpc/h"},
+           "cpu_baseline": {"value": value, "unit": "particle-steps/s",
+                            "cores": oracle_threads(), "kind": "port",
+                            "sample": f"each timed step is one FastPM step of the oracle "
+                                      f"(the reference's algorithm restated: {oracle_kind()}; "
+                                      f"JAX is not installed) on the {n_sample}^3 sample"},
            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -1180,7 +1305,7 @@ def main():
     args = parse()
     args.steps_given = args.steps is not None
     if args.steps is None:
-        args.steps = 20 if args.workload == "batched" else 40
+        args.steps = 20
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":

@@ -52,7 +52,11 @@ enum pmgb_paint_mode {
                              coalesced flush; global atomics when a chunk's box
                              does not fit                                   */
   PMGB_PAINT_DETERMINISTIC = 2 /* fixed-point 64-bit integer accumulation:
-                             bit-identical results run to run             */
+                             bit-identical results run to run.  Signed 32.32
+                             fixed point: each contribution is rounded to a
+                             multiple of 2^-32, and a cell's sum must stay
+                             below 2^31 in magnitude (larger sums wrap
+                             silently)                                    */
 };
 
 /* ---- library ----------------------------------------------------------- */
@@ -92,10 +96,15 @@ int pmgb_cic_paint_f32(float *mesh, int nx, int ny, int nz, const float *pos,
  * cudaMalloc while another runtime's pool owns the device memory.  The
  * fixed-point scratch (8 bytes per cell) is a static device array inside
  * libpmgb, so meshes are limited to 128^3 = 2097152 cells (larger ones are
- * rejected with PMGB_ERR_INVALID_ARGUMENT); every GPU that loads the
- * library holds those 16 MiB until the process exits.  The first call on a
- * device looks the array's address up (cudaGetSymbolAddress) and caches
- * it: make that first call before any stream capture.  The scratch is
+ * rejected with PMGB_ERR_INVALID_ARGUMENT).  A CUDA context takes those
+ * 16 MiB when it first uses this code (lazy module loading, the default
+ * since CUDA 12.2: the first call), or when it is created under
+ * CUDA_MODULE_LOADING=EAGER, and holds them until it is destroyed.  The
+ * first call in a context (the device's primary context, or the caller's
+ * own current context) looks the array's address up with
+ * cudaGetSymbolAddress and caches it under the context's unique id: make
+ * that first call before any stream capture.  Same fixed-point range as
+ * PMGB_PAINT_DETERMINISTIC (|cell sum| < 2^31, resolution 2^-32).  The scratch is
  * cleared by every call, but all calls share it: calls that overlap on the
  * GPU (different streams, or different host threads on one device) race
  * and must be serialised by the caller. */
@@ -351,6 +360,25 @@ int pmgb_unpermute3_f32(const float *in, const uint32_t *id, int64_t np,
 /* out[p] = in[id[p]] for [np][3] arrays (caller's order -> tile order). */
 int pmgb_permute3_f32(const float *in, const uint32_t *id, int64_t np,
                       float *out, pmgb_stream_t stream);
+
+/* Failure check of the tile-staged kernels: waits for `stream`, reads the
+ * three counters a tile kernel kept in `stats` and returns
+ * PMGB_ERR_CUDA if [2] is set, i.e. a wait on a TMA transfer reached its
+ * spin limit and the kernel abandoned its work (the results of every call
+ * since the counters were zeroed are then invalid); PMGB_OK otherwise, and
+ * for stats == NULL.  No counterpart in the reference: JAX raises on its own
+ * errors; here a device-side failure is reported through these counters
+ * instead of a trap, which would take down the context.  The Python engine
+ * calls it after every run, reverse sweep and host-state run. */
+int pmgb_check_stats(const uint32_t *stats, pmgb_stream_t stream);
+
+/* Test of the bounded wait behind that check: one CTA arms an mbarrier for
+ * 16 bytes, issues no copy and waits for at most spin_limit polls (1 to
+ * 2^20); *status (a device word) becomes 1 when the wait ran out, 0 if it
+ * completed.  Nothing is in flight, so the kernel ends at once and the
+ * context stays usable.  No counterpart in the reference. */
+int pmgb_test_wait_timeout(uint32_t spin_limit, uint32_t *status,
+                           pmgb_stream_t stream);
 
 /* Paint of tile-sorted particles (the sorted loop's paint; mesh overwritten):
  * one CTA per tile accumulates the tile plus a one-cell halo in shared

@@ -40,6 +40,8 @@ SIGNATURES = {
                                    P, c_size_t, P]),
     "pmgb_cic_paint_deterministic_noalloc_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P,
                                                          c_float, c_int, P]),
+    "pmgb_check_stats": (c_int, [P, P]),
+    "pmgb_test_wait_timeout": (c_int, [ctypes.c_uint32, P, P]),
     "pmgb_cic_read_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P, P]),
     "pmgb_cic_read3_f32": (c_int, [P, c_int64, c_int, c_int, c_int, P, c_int64, P, P]),
     "pmgb_cic_weights_f32": (c_int, [P, c_int64, c_int, c_int, c_int, P, P, P]),

@@ -8,6 +8,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "tma.cuh"
 
 namespace pmgb {
 
@@ -658,6 +659,19 @@ int pmgb_fpm_run_sorted_f32(float *pos_a, float *vel_a, uint32_t *id_a, float *p
   return fpm_run_sorted(pos_a, vel_a, id_a, pos_b, vel_b, id_b, np, nx, ny, nz, n_steps, kick,
                         drift, r_split, workspace, workspace_bytes, sort_workspace,
                         sort_workspace_bytes, stats, stream);
+}
+
+int pmgb_check_stats(const uint32_t *stats, pmgb_stream_t stream) {
+  BEGIN();
+  return check_wait_stats(stats, stream);
+}
+
+int pmgb_test_wait_timeout(uint32_t spin_limit, uint32_t *status, pmgb_stream_t stream) {
+  BEGIN();
+  NEED(status);
+  PMGB_REQUIRE(spin_limit >= 1 && spin_limit <= (1u << 20),
+               "spin_limit must lie in [1, 2^20]");
+  return test_wait_timeout(spin_limit, status, stream);
 }
 
 int pmgb_cic_paint_sorted_f32(float *mesh, int nx, int ny, int nz, const float *pos,

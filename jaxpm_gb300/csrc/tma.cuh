@@ -41,11 +41,11 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                : "memory");
 }
 
-// Waits for phase `parity` of the barrier to complete; returns false if the
-// spin limit was reached first.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Waits for phase `parity` of the barrier to complete; returns false if
+// `limit` polls went by first.
+__device__ __forceinline__ bool mbar_wait_limit(uint64_t *bar, uint32_t parity, uint32_t limit) {
   const uint32_t a = smem_addr(bar);
-  for (uint32_t i = 0; i < MBAR_SPIN_LIMIT; ++i) {
+  for (uint32_t i = 0; i < limit; ++i) {
     uint32_t done;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
@@ -57,6 +57,21 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
   }
   return false;
 }
+
+// The same with the library's spin limit.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  return mbar_wait_limit(bar, parity, MBAR_SPIN_LIMIT);
+}
+
+// Host side: PMGB_OK, or PMGB_ERR_CUDA when the counters a tile kernel kept
+// (stats[2]) show that one of its mbarrier waits reached its spin limit.
+// Waits for `stream` (the counters are read back).
+int check_wait_stats(const uint32_t *stats, cudaStream_t stream);
+
+// Host side: launches a one-CTA kernel that arms an mbarrier for 16 bytes,
+// issues no copy and waits with a limit of `limit` polls; *status_dev (a
+// device word) becomes 1 if the wait ran out, 0 if it completed.
+int test_wait_timeout(uint32_t limit, uint32_t *status_dev, cudaStream_t stream);
 
 // 4-D tiled load of the tensor-map box at (c0, c1, c2, c3) into shared
 // memory, completing on `bar`.

@@ -172,10 +172,20 @@ class SortedFastPM:
                   _lib.ptr(dest), _lib.ptr(offs), _lib.ptr(self.stats_buf), s)
         self.cur = b
 
-    def run(self, steps=None, start=0, stream=None):
+    def check(self, stream=None):
+        """Raises ``PmgbError`` if a wait on a TMA transfer in one of the tile
+        kernels reached its spin limit since the counters were zeroed (the
+        kernel then abandoned its work, so the state is invalid):
+        ``pmgb_check_stats``, which waits for the stream."""
+        s = _lib.stream(self.ws.device) if stream is None else stream
+        _lib.call("pmgb_check_stats", _lib.ptr(self.stats_buf), s)
+
+    def run(self, steps=None, start=0, stream=None, check=True):
         """Runs steps ``start .. start+steps-1`` (default: all remaining) with
         one ``pmgb_fpm_run_sorted_f32`` call: each step's gather also paints
-        the next step's density."""
+        the next step's density.  With ``check`` (default) it then waits for
+        the run and raises if a kernel reported a failed wait (``check()``);
+        ``check=False`` returns at once (call ``check()`` later)."""
         n = (self.n_steps - start) if steps is None else int(steps)
         if n <= 0:
             return
@@ -191,6 +201,8 @@ class SortedFastPM:
                   drift.ctypes.data_as(fp), self.r_split, _lib.ptr(self.ws), self.ws_bytes,
                   _lib.ptr(self.sort_ws), self.sort_bytes, _lib.ptr(self.stats_buf), s)
         self.cur = a if n % 2 == 0 else b
+        if check:
+            self.check(s)
 
     @property
     def positions(self):
@@ -202,21 +214,29 @@ class SortedFastPM:
     def ids_current(self):
         return self.ids[self.cur]
 
-    def run_host(self, hpos, hvel, steps=None, chunks=16):
+    def run_host(self, hpos, hvel, steps=None, chunks=16, start=0, check=True):
         """Steps a state that lives in pinned host memory: ``hpos``/``hvel``
         ([Np, 3] float32, caller's order) are updated in place after each of
-        ``steps`` steps (default all), each step copying them up, sorting
+        steps ``start .. start+steps-1`` (default: all remaining; a range
+        past the engine's steps raises before any work is queued), each
+        step copying them up, sorting
         them by tile (``pmgb_tile_sort_f32``), stepping
         (``pmgb_fpm_step_sorted_f32``), returning them to the caller's order
         (``pmgb_unpermute3_f32``) and copying them back.  The copies go in
         ``chunks`` chunks on two copy streams: chunk c of the next step's
         input goes up as soon as chunk c of this step's result is down, so
         the read-back and the next upload share the host link's two
-        directions.  Returns when the last copy has been issued (ordered
-        before later work on the current stream)."""
+        directions.  With ``check`` (default) it waits for the steps and
+        raises if a kernel reported a failed wait; otherwise it returns when
+        the last copy has been issued (ordered before later work on the
+        current stream)."""
         if not (hpos.is_pinned() and hvel.is_pinned()):
             raise ValueError("run_host needs pinned host tensors")
-        n = self.n_steps if steps is None else int(steps)
+        start = int(start)
+        n = (self.n_steps - start) if steps is None else int(steps)
+        if start < 0 or n < 0 or start + n > self.n_steps:
+            raise ValueError(f"steps {start}..{start + n - 1} outside the engine's "
+                             f"{self.n_steps} steps")
         nx, ny, nz = self.mesh_shape
         dev = self.ws.device
         stream = torch.cuda.current_stream(dev)
@@ -245,9 +265,9 @@ class SortedFastPM:
                       _lib.ptr(self.sort_ws), self.sort_bytes, s)
             _lib.call("pmgb_fpm_step_sorted_f32", _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]),
                       _lib.ptr(self.ids[0]), _lib.ptr(self.pos[1]), _lib.ptr(self.vel[1]),
-                      _lib.ptr(self.ids[1]), self.n, nx, ny, nz, float(self.kick[i]),
-                      float(self.drift[i]), self.r_split, _lib.ptr(self.ws), self.ws_bytes,
-                      _lib.ptr(self.sort_ws), self.sort_bytes, None, None, None,
+                      _lib.ptr(self.ids[1]), self.n, nx, ny, nz, float(self.kick[start + i]),
+                      float(self.drift[start + i]), self.r_split, _lib.ptr(self.ws),
+                      self.ws_bytes, _lib.ptr(self.sort_ws), self.sort_bytes, None, None, None,
                       _lib.ptr(self.stats_buf), s)
             _lib.call("pmgb_unpermute3_f32", _lib.ptr(self.pos[1]), _lib.ptr(self.ids[1]),
                       self.n, _lib.ptr(dx), s)
@@ -263,6 +283,8 @@ class SortedFastPM:
         stream.wait_stream(down)
         if n > 0:
             self.cur = 1  # the engine's buffers hold the last step's sorted state
+        if check:
+            self.check(s)
 
     def state(self):
         """``(pos, vel)`` in the caller's order (new tensors)."""
@@ -304,10 +326,11 @@ class SortedFastPM:
                 torch.empty((n, self.n), dtype=torch.int32, device=dev),
                 torch.empty((n, keys + 1), dtype=torch.int32, device=dev))
 
-    def vjp(self, pos, vel, g_pos, g_vel, store=None):
+    def vjp(self, pos, vel, g_pos, g_vel, store=None, check=True):
         """Forward run from ``(pos, vel)`` (caller's order) then the reverse
         sweep; returns the final state and the cotangents of the initial
-        state, all in the caller's order.
+        state, all in the caller's order.  With ``check`` (default) it waits
+        for the sweep and raises if a kernel reported a failed wait.
 
         Each forward step records the positions it starts from, its
         potential (or its force meshes, by the store's layout), where each
@@ -363,6 +386,8 @@ class SortedFastPM:
         gx, gv = torch.empty_like(gxa), torch.empty_like(gva)
         _lib.call("pmgb_unpermute3_f32", _lib.ptr(gxa), _lib.ptr(ids0), self.n, _lib.ptr(gx), s)
         _lib.call("pmgb_unpermute3_f32", _lib.ptr(gva), _lib.ptr(ids0), self.n, _lib.ptr(gv), s)
+        if check:
+            self.check(s)
         return final, (gx, gv)
 
 

@@ -8,8 +8,28 @@ Absolute mode follows ``jaxpm/painting.py:15-45`` (paint) and
 Every floating-point step is written in the reference's order and in the
 requested dtype, so that float32 indices and per-neighbour weights can be
 compared bit for bit with the CUDA kernels.
+
+``cic_paint`` and ``cic_read`` hand absolute-mode work to the C statement of
+the same arithmetic (``oracle/ccic.c`` via ``oracle/native.py``) when it is
+built and ``NATIVE`` is true; ``tests/test_oracle.py`` holds the two
+statements equal.
 """
 import numpy as np
+
+from . import native
+
+# use the C statement of paint/read when it can be built (same arithmetic)
+NATIVE = True
+
+
+def _c(dtype):
+    """The C oracle and its function suffix for ``dtype``, or None."""
+    if not NATIVE or dtype not in (np.float32, np.float64):
+        return None
+    h = native.lib()
+    if h is None:
+        return None
+    return h, ("f32" if dtype == np.float32 else "f64")
 
 # Neighbour order of absolute mode, ``jaxpm/painting.py:24-25``.
 CONNECTION_ABS = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1],
@@ -52,6 +72,18 @@ def cic_paint(grid_mesh, positions, weight=1.0, dtype=np.float32):
     """
     grid_mesh = np.asarray(grid_mesh, dtype=dtype)
     shape = grid_mesh.shape
+    c = _c(dtype)
+    if c is not None:
+        h, sfx = c
+        pos = np.ascontiguousarray(np.asarray(positions, dtype=dtype).reshape(-1, 3))
+        acc = np.zeros(int(np.prod(shape)), np.float64)
+        scalar = np.isscalar(weight) or np.ndim(weight) == 0
+        wts = None if scalar else np.ascontiguousarray(
+            np.broadcast_to(np.asarray(weight, dtype=dtype).reshape(-1), (len(pos),)))
+        getattr(h, f"oc_paint_{sfx}")(acc.ctypes.data, *shape, pos.ctypes.data, len(pos),
+                                      None if wts is None else wts.ctypes.data,
+                                      float(weight) if scalar else 0.0)
+        return (grid_mesh.astype(np.float64) + acc.reshape(shape)).astype(dtype)
     idx, w = cic_weights(positions, shape, dtype)
     if np.isscalar(weight) or np.ndim(weight) == 0:
         w = np.asarray(weight, dtype=dtype) * w
@@ -68,6 +100,15 @@ def cic_read(grid_mesh, positions, dtype=np.float32):
     weighted neighbour values, output shaped ``positions.shape[:-1]``."""
     grid_mesh = np.asarray(grid_mesh, dtype=dtype)
     positions = np.asarray(positions, dtype=dtype)
+    c = _c(dtype)
+    if c is not None:
+        h, sfx = c
+        pos = np.ascontiguousarray(positions.reshape(-1, 3))
+        mesh = np.ascontiguousarray(grid_mesh)
+        out = np.empty(len(pos), dtype)
+        getattr(h, f"oc_read_{sfx}")(mesh.ctypes.data, *mesh.shape, pos.ctypes.data, len(pos),
+                                     out.ctypes.data)
+        return out.reshape(positions.shape[:-1])
     idx, w = cic_weights(positions, grid_mesh.shape, dtype)
     vals = grid_mesh[idx[..., 0], idx[..., 1], idx[..., 2]]
     out = vals[:, 0] * w[:, 0]

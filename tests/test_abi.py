@@ -125,3 +125,19 @@ def test_npy_header_is_read_by_numpy(lib, shape, descr):
     got_shape, fortran, dtype = np.lib.format.read_array_header_1_0(f)
     assert got_shape == tuple(shape) and not fortran and dtype == np.dtype(descr)
     assert f.tell() == n
+
+
+def test_failure_check_entry_points_validate_on_the_host(lib):
+    """pmgb_check_stats with no counters is a no-op; the wait-timeout probe
+    rejects an out-of-range limit and a NULL status before any launch."""
+    from jaxpm_gb300 import _lib
+    assert _lib.call("pmgb_check_stats", None, None) == 0
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_test_wait_timeout", 0, ctypes.c_void_p(16), None)
+    assert e.value.status == 1 and "spin_limit" in str(e.value)
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_test_wait_timeout", 1 << 21, ctypes.c_void_p(16), None)
+    assert "spin_limit" in str(e.value)
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_test_wait_timeout", 100, None, None)
+    assert "status is NULL" in str(e.value)

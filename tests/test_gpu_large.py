@@ -1,0 +1,113 @@
+"""Parity at full size: the 256^3 single-simulation configuration (2LPT to
+a = 0.1, 20 FastPM steps to a = 1, box 256 Mpc/h) against the oracle's own
+run of it (``tests/golden/large_256_20.npz``, made by
+``tests/golden/make_large_golden.py`` in float32 and float64 from the same
+PCG64 white noise).
+
+The bars: the final density's P(k) within 1e-3 per k-bin of the float32
+oracle (``jaxpm/utils.py:14-128`` binning; the reference's own N-body bar is
+an MSRE of 1e-3, ``tests/test_against_fpm.py:119-123``), and the sampled
+particles' a = 1 displacements within 1e-3 relative L2 of the oracle's.
+Each result's distance to the float64 oracle run is checked too, at 1e-4
+(the float32 oracle itself is 1.3e-6 from it in P(k) and 3e-6 in the
+displacements at this size)."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import GOLDEN, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+PATH = os.path.join(GOLDEN, "large_256_20.npz")
+
+
+def gpu_initial_state(n, box, seed, dev):
+    from jaxpm_gb300 import cosmology, distributed, pm
+    cosmo = cosmology.Planck15()
+    ic = pm.linear_field((n,) * 3, [box] * 3, pm.pk_table(cosmo), seed=seed, device=dev)
+    lat = distributed.uniform_particles((n,) * 3, device=dev).reshape(-1, 3)
+    with torch.no_grad():
+        dx, p, _ = pm.lpt(cosmo, ic, lat, a=0.1, order=2)
+    return cosmo, (lat + dx).contiguous(), p.contiguous()
+
+
+def pk_of(x, n, box):
+    from jaxpm_gb300 import painting, utils
+    rho = painting.paint(torch.zeros((n,) * 3, device=x.device), x, mode="deterministic")
+    return utils.power_spectrum(rho, box_shape=[box] * 3)
+
+
+def lattice_sample(n, idx):
+    i = np.asarray(idx, dtype=np.int64)
+    return np.stack([i // (n * n), (i // n) % n, i % n], -1).astype(np.float64)
+
+
+@pytest.fixture(scope="module")
+def c2(cuda):
+    if not os.path.exists(PATH):
+        pytest.fail(f"fixture missing: {PATH}")
+    d = dict(np.load(PATH))
+    from jaxpm_gb300 import simulate
+    n, box = int(d["n"]), float(d["box"])
+    cosmo, x0, v0 = gpu_initial_state(n, box, int(d["seed"]), cuda)
+    _, pk0 = pk_of(x0, n, box)
+    idx = torch.from_numpy(d["sample"]).to(cuda)
+    s0 = (x0[idx].cpu().numpy(), v0[idx].cpu().numpy())
+    eng = simulate.SortedFastPM((n,) * 3, cosmo, float(d["a0"]), float(d["a1"]), int(d["steps"]),
+                                device=cuda)
+    eng.load(x0, v0)
+    del x0, v0
+    eng.run()
+    x1, v1 = eng.state()
+    k, pk1 = pk_of(x1, n, box)
+    s1 = (x1[idx].cpu().numpy(), v1[idx].cpu().numpy())
+    stats = eng.stats
+    del eng, x1, v1
+    torch.cuda.empty_cache()
+    return d, k, pk0, pk1, s0, s1, stats
+
+
+def test_c2_coefficients_match_oracle(c2):
+    from jaxpm_gb300 import cosmology, ode
+    d = c2[0]
+    kick, drift = ode.fpm_coefficients(cosmology.Planck15(), float(d["a0"]), float(d["a1"]),
+                                       int(d["steps"]))
+    np.testing.assert_allclose(kick, d["kick"], rtol=1e-9)
+    np.testing.assert_allclose(drift, d["drift"], rtol=1e-9)
+
+
+def test_c2_initial_state_matches_oracle(c2):
+    d, k, pk0, _, (x0, v0), _, _ = c2
+    n = int(d["n"])
+    np.testing.assert_allclose(k, d["k"], rtol=1e-6)
+    assert np.max(np.abs(pk0 / d["pk0_32"] - 1)) < 1e-4
+    lat = lattice_sample(n, d["sample"])
+    assert rel_l2(x0 - lat, d["x0_32"] - lat) < 1e-5
+    assert rel_l2(v0, d["v0_32"]) < 1e-5
+
+
+def test_c2_final_pk_within_1e3_of_oracle(c2):
+    d, _, _, pk1, _, _, stats = c2
+    dev32 = np.abs(pk1 / d["pk1_32"] - 1)
+    assert dev32.max() < 1e-3, f"max per-bin deviation {dev32.max():.2e}"
+    dev64 = np.abs(pk1 / d["pk1_64"] - 1).max()
+    assert dev64 < 1e-4, f"max per-bin deviation from the float64 run {dev64:.2e}"
+    assert stats["tma_wait_timeout"] == 0
+
+
+def test_c2_final_particles_match_oracle(c2):
+    d, _, _, _, _, (x1, v1), _ = c2
+    n = int(d["n"])
+    lat = lattice_sample(n, d["sample"])
+    # displacements, unwrapped to the nearest periodic image of the oracle's
+    dx = x1 - d["x1_32"]
+    dx -= n * np.round(dx / n)
+    err = np.linalg.norm(dx) / np.linalg.norm(d["x1_32"] - lat)
+    assert err < 1e-3, f"displacement rel L2 {err:.2e}"
+    assert rel_l2(v1, d["v1_32"]) < 1e-3
+    err64 = x1 - d["x1_64"]
+    err64 -= n * np.round(err64 / n)
+    assert np.linalg.norm(err64) / np.linalg.norm(d["x1_64"] - lat) < 1e-4

@@ -211,3 +211,59 @@ def test_oracle_step_adjoint_matches_float64_finite_difference():
     fd_v = (loss(x0, v0 + eps * d) - loss(x0, v0 - eps * d)) / (2 * eps)
     assert abs(fd_x - (gx * d).sum()) < 1e-6 * abs(fd_x)
     assert abs(fd_v - (gv * d).sum()) < 1e-6 * abs(fd_v)
+
+
+# --- the C statement of paint/read against the NumPy statement --------------
+
+@pytest.mark.parametrize("shape", [(8, 8, 8), (8, 6, 10), (32, 32, 32)])
+def test_c_oracle_matches_numpy_oracle(shape):
+    from oracle import native
+    if native.lib() is None:
+        pytest.skip("no C compiler for the C oracle")
+    rng = np.random.default_rng(5)
+    n = np.array(shape)
+    for dtype in (np.float32, np.float64):
+        pos = (rng.uniform(-2, 3, (20000, 3)) * n).astype(dtype)
+        pos[:5] = [[0, 0, 0], [n[0], 0, n[2]], [-1e-4, -1e-4, -1e-4], [n[0] - 1e-4, 1, 2],
+                   [0.5, 0.5, 0.5]]
+        mesh = rng.standard_normal(shape).astype(dtype)
+        wts = rng.uniform(0.5, 1.5, len(pos)).astype(dtype)
+        out = {}
+        for use_c in (True, False):
+            cic.NATIVE = use_c
+            try:
+                out[use_c] = (cic.cic_read(mesh, pos, dtype),
+                              cic.cic_paint(np.zeros(shape), pos, weight=wts, dtype=dtype),
+                              cic.cic_paint(np.zeros(shape), pos, weight=0.7, dtype=dtype))
+            finally:
+                cic.NATIVE = True
+        # reads: the same float operations in the same order, bit for bit
+        assert np.array_equal(out[True][0], out[False][0])
+        for a, b in zip(out[True][1:], out[False][1:]):
+            if dtype == np.float32:  # float64 sums cast to float32: identical
+                assert np.array_equal(a, b)
+            else:  # float64: only the order of the float64 additions differs
+                assert np.allclose(a, b, rtol=1e-13, atol=1e-13)
+
+
+def test_large_fixtures_are_self_consistent(golden):
+    """The full-size oracle fixtures: float32 and float64 runs of the same
+    initial conditions agree (P(k) to 1e-5 per bin at a = 0.1 and a = 1), and
+    the sample's lattice points sit where the particles started."""
+    import os
+    from conftest import GOLDEN
+    import glob
+    paths = sorted(glob.glob(os.path.join(GOLDEN, "large_*_*.npz")))
+    assert paths, "no full-size oracle fixture"
+    for path in paths:
+        n, steps = (int(v) for v in os.path.basename(path)[6:-4].split("_"))
+        d = golden(os.path.basename(path))
+        assert int(d["n"]) == n and int(d["steps"]) == steps
+        for key in ("pk0", "pk1"):
+            assert np.max(np.abs(d[f"{key}_32"] / d[f"{key}_64"] - 1)) < 1e-5
+        i = d["sample"].astype(np.int64)
+        lat = np.stack([i // (n * n), (i // n) % n, i % n], -1)
+        assert np.max(np.abs(d["x0_64"] - lat)) < 0.1 * n  # 2LPT displacements are small
+        kc, dc = nb.fpm_coefficients(cm.Cosmology(), 0.1, 1.0, steps)
+        np.testing.assert_allclose(d["kick"], kc, rtol=1e-12)
+        np.testing.assert_allclose(d["drift"], dc, rtol=1e-12)
