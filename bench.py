@@ -230,7 +230,11 @@ def run_gb300(args):
            "mfws": torch.empty(mf_bytes, dtype=torch.uint8, device=dev),
            "f3": torch.empty(3 * ncell, dtype=torch.float32, device=dev),
            "det": torch.empty(ncell * 8 if mode == _lib.PAINT_DETERMINISTIC else 1,
-                              dtype=torch.uint8, device=dev)}
+                              dtype=torch.uint8, device=dev),
+           "perm": torch.empty((2, Np if engine == "sorted" else 1), dtype=torch.int32,
+                               device=dev)}
+    perms = buf["perm"]
+    perm_cur = [0]
     P = lambda name: _lib.ptr(buf[name])  # noqa: E731
     det_bytes = ncell * 8 if mode == _lib.PAINT_DETERMINISTIC else 0
 
@@ -254,9 +258,11 @@ def run_gb300(args):
     # (pmgb_read3_kick_drift_paint_binned_f32), so only the first step of a
     # run has a paint phase
     density_ready = [False]
+    permuted = [False]  # the engine's particles are read through buf["perm"]
 
     def reset():
         density_ready[0] = False
+        permuted[0] = False
         if engine == "sorted":
             eng.load(x0, v0)
         else:
@@ -291,13 +297,42 @@ def run_gb300(args):
             _lib.call("pmgb_mesh_forces_f32", P("mesh"), P("f3"), nx, ny, nz, 0.0, P("mfws"),
                       mf_bytes, s)
         rec(2)
-        if engine == "sorted":
-            if use_pot:  # gather (forces from the potential) + kick + drift + next paint
-                _lib.call("pmgb_read_potential_kick_drift_paint_binned_f32", P("f3"), nx, ny,
-                          nz, _lib.ptr(px), _lib.ptr(pv), Np, float(kick[i]), float(drift[i]),
-                          P("mesh") if i + 1 < K else None, _lib.ptr(eng.sort_ws),
-                          eng.sort_bytes, _lib.ptr(eng.stats_buf), s)
-            elif i + 1 < K:  # gather + kick + drift + paint of the next density
+        if engine == "sorted" and use_pot:
+            # the run loop's permuted gather: slot p is read from index perm[p]
+            # (in place, without perm, on the first step after a sort) and
+            # written to index p of the other buffer, with its new tile key
+            last = i + 1 == K
+            out = a if not permuted[0] else b
+            pc = perm_cur[0]
+            _lib.call("pmgb_read_potential_kick_drift_paint_perm_f32", P("f3"), nx, ny, nz,
+                      _lib.ptr(px), _lib.ptr(pv), _lib.ptr(perms[pc]) if permuted[0] else None,
+                      _lib.ptr(eng.pos[out]), _lib.ptr(eng.vel[out]), Np, float(kick[i]),
+                      float(drift[i]), None if last else P("mesh"), _lib.ptr(eng.sort_ws),
+                      eng.sort_bytes, _lib.ptr(eng.stats_buf), s)
+            density_ready[0] = not last
+            rec(3)
+            if last:  # the ids follow the gather, then the run's one full sort
+                if permuted[0]:
+                    _lib.call("pmgb_gather_u32", _lib.ptr(eng.ids[a]), _lib.ptr(perms[pc]), Np,
+                              _lib.ptr(eng.ids[out]), s)
+                _lib.call("pmgb_tile_scatter_f32", _lib.ptr(eng.pos[out]),
+                          _lib.ptr(eng.vel[out]), _lib.ptr(eng.ids[out]), Np, nx, ny, nz,
+                          _lib.ptr(eng.pos[1 - out]), _lib.ptr(eng.vel[1 - out]),
+                          _lib.ptr(eng.ids[1 - out]), None, _lib.ptr(eng.sort_ws),
+                          eng.sort_bytes, s)
+                eng.cur = 1 - out
+                permuted[0] = False
+            else:  # the re-sort of the permutation (the ids follow it)
+                _lib.call("pmgb_tile_resort_index", Np, nx, ny, nz,
+                          _lib.ptr(perms[pc]) if permuted[0] else None, _lib.ptr(perms[1 - pc]),
+                          _lib.ptr(eng.ids[a]), _lib.ptr(eng.ids[out]), _lib.ptr(eng.sort_ws),
+                          eng.sort_bytes, s)
+                perm_cur[0] = 1 - pc
+                eng.cur = out
+                permuted[0] = True
+            rec(4)
+        elif engine == "sorted":
+            if i + 1 < K:  # gather + kick + drift + paint of the next density
                 _lib.call("pmgb_read3_kick_drift_paint_binned_f32", P("f3"), ncell, nx, ny, nz,
                           _lib.ptr(px), _lib.ptr(pv), Np, float(kick[i]), float(drift[i]),
                           P("mesh"), _lib.ptr(eng.sort_ws), eng.sort_bytes,

@@ -470,7 +470,11 @@ int pmgb_fpm_step_sorted_f32(const float *pos, float *vel, const uint32_t *id,
  * pmgb_fpm_step_sorted_f32, except that the density of every step after the
  * first is painted by the previous step's gather
  * (pmgb_read3_kick_drift_paint_binned_f32), so each step reads the
- * particles once.  The sort_workspace must hold the tile ranges of
+ * particles once, and that between steps the particles are not moved: each
+ * gather reads its tiles' particles through a permutation and writes them
+ * in the order it read them, so the re-sort only rebuilds the permutation
+ * (8 bytes per particle); one full sort after the last step leaves the
+ * state in tile order.  The sort_workspace must hold the tile ranges of
  * (pos_a, ...) (as left by pmgb_tile_sort_f32 or a previous step).  kick and
  * drift are HOST arrays of n_steps coefficients.  The state ping-pongs
  * between the a and b buffers: after the call it is in a when n_steps is
@@ -487,6 +491,41 @@ int pmgb_read_potential_kick_drift_paint_binned_f32(const float *pot, int nx,
                                                     size_t sort_workspace_bytes,
                                                     uint32_t *stats,
                                                     pmgb_stream_t stream);
+
+/* The run loop's gather in its permuted form: slot p of the tile ranges in
+ * sort_workspace is the particle at index perm[p] of (pos, vel) (perm NULL:
+ * index p), gathered from the potential as
+ * pmgb_read_potential_kick_drift_paint_binned_f32 does, and written to index
+ * p of (pos_out, vel_out); its new tile key goes to the sort workspace for
+ * pmgb_tile_resort_index.  With perm the outputs are other buffers than the
+ * inputs; without it they may be the inputs (an in-place update).  The
+ * particles then never move between steps: only the permutation is
+ * re-sorted, and the ids follow it there.  No counterpart of its own in the
+ * reference: it is the reference's cic_read x3 + kick + drift + next
+ * cic_paint (pm.py:54-56, ode.py:20-58, painting.py:15-45) in the order the
+ * particles already lie. */
+int pmgb_read_potential_kick_drift_paint_perm_f32(
+    const float *pot, int nx, int ny, int nz, const float *pos, const float *vel,
+    const uint32_t *perm, float *pos_out, float *vel_out, int64_t np, float kick,
+    float drift, float *mesh_next, void *sort_workspace,
+    size_t sort_workspace_bytes, uint32_t *stats, pmgb_stream_t stream);
+
+/* The permuted loop's re-sort: the exclusive scan of the tile counts left by
+ * the last permuted gather, then perm_new[d] = p for every slot p, d the
+ * slot it claims in its new tile (from the keys the gather wrote).  With
+ * perm_old (the permutation that gather read through) the ids follow:
+ * id_out[p] = id_in[perm_old[p]].  8 bytes of traffic per particle (20
+ * with the ids) instead of moving (pos, vel, id). */
+int pmgb_tile_resort_index(int64_t np, int nx, int ny, int nz,
+                           const uint32_t *perm_old, uint32_t *perm_new,
+                           const uint32_t *id_in, uint32_t *id_out,
+                           void *sort_workspace, size_t sort_workspace_bytes,
+                           pmgb_stream_t stream);
+
+/* out[p] = in[idx[p]] for np 32-bit words (the ids after a permuted
+ * gather, before the run's final full sort). */
+int pmgb_gather_u32(const uint32_t *in, const uint32_t *idx, int64_t np,
+                    uint32_t *out, pmgb_stream_t stream);
 
 /* The forward run of the reverse sweep, recording what each step's
  * pmgb_fpm_step_sorted_vjp_f32 needs, as one call with the run loop's

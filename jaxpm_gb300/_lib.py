@@ -41,6 +41,12 @@ SIGNATURES = {
     "pmgb_cic_paint_deterministic_noalloc_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P,
                                                          c_float, c_int, P]),
     "pmgb_check_stats": (c_int, [P, P]),
+    "pmgb_read_potential_kick_drift_paint_perm_f32": (c_int, [P, c_int, c_int, c_int, P, P, P, P,
+                                                              P, c_int64, c_float, c_float, P, P,
+                                                              c_size_t, P, P]),
+    "pmgb_tile_resort_index": (c_int, [c_int64, c_int, c_int, c_int, P, P, P, P, P, c_size_t,
+                                       P]),
+    "pmgb_gather_u32": (c_int, [P, P, c_int64, P, P]),
     "pmgb_test_wait_timeout": (c_int, [ctypes.c_uint32, P, P]),
     "pmgb_cic_read_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P, P]),
     "pmgb_cic_read3_f32": (c_int, [P, c_int64, c_int, c_int, c_int, P, c_int64, P, P]),

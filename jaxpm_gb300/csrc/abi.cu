@@ -580,6 +580,72 @@ int pmgb_read_potential_kick_drift_paint_binned_f32(const float *pot, int nx, in
                     sort_workspace, sort_workspace_bytes, stats, stream, mesh_next, true);
 }
 
+int pmgb_read_potential_kick_drift_paint_perm_f32(
+    const float *pot, int nx, int ny, int nz, const float *pos, const float *vel,
+    const uint32_t *perm, float *pos_out, float *vel_out, int64_t np, float kick, float drift,
+    float *mesh_next, void *sort_workspace, size_t sort_workspace_bytes, uint32_t *stats,
+    pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  if (np == 0) {
+    if (mesh_next)
+      PMGB_CUDA(cudaMemsetAsync(mesh_next, 0, (size_t)nx * ny * nz * sizeof(float), stream));
+    return PMGB_OK;
+  }
+  NEED(pot);
+  NEED(pos);
+  NEED(vel);
+  NEED(pos_out);
+  NEED(vel_out);
+  NEED(sort_workspace);
+  PMGB_REQUIRE(mesh_next != pot, "mesh_next must not alias the potential");
+  if (perm)
+    PMGB_REQUIRE(pos_out != pos && vel_out != vel,
+                 "with a permutation the outputs must not alias the inputs");
+  else
+    PMGB_REQUIRE((pos_out == pos) == (vel_out == vel),
+                 "without a permutation the outputs alias both inputs or neither");
+  PMGB_TRY(check_sort_workspace(sort_workspace, sort_workspace_bytes, nx, ny, nz, np));
+  PermIO io;
+  io.perm = perm;
+  io.vel_out = vel_out;
+  io.key_out = tile_key_scratch(sort_workspace, nx, ny, nz, np);
+  return rkd_sorted(pot, (int64_t)nx * ny * nz, nx, ny, nz, pos, pos_out,
+                    const_cast<float *>(vel), np, kick, drift, sort_workspace,
+                    sort_workspace_bytes, stats, stream, mesh_next, true, io);
+}
+
+int pmgb_tile_resort_index(int64_t np, int nx, int ny, int nz, const uint32_t *perm_old,
+                           uint32_t *perm_new, const uint32_t *id_in, uint32_t *id_out,
+                           void *sort_workspace, size_t sort_workspace_bytes,
+                           pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  NEED(sort_workspace);
+  if (np > 0) NEED(perm_new);
+  if (np > 0 && perm_old) {
+    NEED(id_in);
+    NEED(id_out);
+    PMGB_REQUIRE(perm_old != perm_new && id_in != id_out,
+                 "perm_old/perm_new and id_in/id_out must be distinct buffers");
+  }
+  return index_resort(np, nx, ny, nz, perm_old, perm_new, perm_old ? id_in : nullptr,
+                      perm_old ? id_out : nullptr, sort_workspace, sort_workspace_bytes,
+                      stream);
+}
+
+int pmgb_gather_u32(const uint32_t *in, const uint32_t *idx, int64_t np, uint32_t *out,
+                    pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_REQUIRE(np >= 0, "np is negative");
+  if (np == 0) return PMGB_OK;
+  NEED(in);
+  NEED(idx);
+  NEED(out);
+  PMGB_REQUIRE(in != out, "in and out must be distinct buffers");
+  return gather_u32(in, idx, np, out, stream);
+}
+
 static int run_sorted_record(float *xs, float *vel_a, uint32_t *id_a, float *vel_b,
                              uint32_t *id_b, float *pos_out, int64_t np, int nx, int ny, int nz,
                              int n_steps, const float *kick, const float *drift, float r_split,

@@ -120,11 +120,23 @@ int fpm_run_sorted_record(float *xs, float *vel_a, unsigned *id_a, float *vel_b,
                           unsigned *dests, unsigned *offs, unsigned *stats, cudaStream_t s,
                           bool pot = false);
 
+// The gather's permuted mode (the run loop): particle slot p of the tile
+// ranges is read from index perm[p] of (pos, vel) and written, with its new
+// tile key, to slot p of (pos_out, vel_out, key_out), so the arrays never
+// need moving between steps; only perm is re-sorted (and the ids follow in
+// the re-sort).  perm == nullptr reads slot p itself (the arrays are in tile
+// order).
+struct PermIO {
+  const unsigned *perm = nullptr;
+  float *vel_out = nullptr;  // nullptr: the velocities are updated in place
+  unsigned *key_out = nullptr;  // nullptr: keys are not written
+};
+
 int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz,
                const float *pos, float *pos_out, float *vel, int64_t np,
                float kick, float drift, void *sort_ws, size_t sort_bytes,
                unsigned *stats, cudaStream_t s, float *mesh_next = nullptr,
-               bool pot = false);
+               bool pot = false, const PermIO &io = PermIO());
 // n_steps sorted steps with the paint of each next density fused into the
 // gather; the state ping-pongs between the a and b buffers (in a after an
 // even number of steps).  kick/drift: host arrays of n_steps.
@@ -138,6 +150,18 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b,
 // spectra (dk, fk) by the selected FFT path.
 int mesh_forces(const float *mesh, int nx, int ny, int nz, float r_split,
                 void *dk, void *fk, float *f3, cudaStream_t s);
+unsigned *tile_key_scratch(void *sort_ws, int nx, int ny, int nz, int64_t np);
+int check_sort_workspace(void *ws, size_t bytes, int nx, int ny, int nz, int64_t np);
+// scan of the tile counts, then perm from the keys in the rank array (the
+// permuted run loop's re-sort)
+// (perm_new[d] = p for the slot d particle p claims); with perm_old, also
+// id_out[p] = id_in[perm_old[p]] (the ids follow the permuted gather)
+int index_resort(int64_t np, int nx, int ny, int nz, const unsigned *perm_old,
+                 unsigned *perm_new, const unsigned *id_in, unsigned *id_out, void *sort_ws,
+                 size_t sort_bytes, cudaStream_t s);
+// out[p] = in[idx[p]] for np 32-bit words
+int gather_u32(const unsigned *in, const unsigned *idx, int64_t np, unsigned *out,
+               cudaStream_t s);
 int tile_scatter(const float *pos, const float *vel, const unsigned *id,
                  int64_t np, int nx, int ny, int nz, float *pos2, float *vel2,
                  unsigned *id2, unsigned *dest, void *sort_ws, size_t sort_bytes,

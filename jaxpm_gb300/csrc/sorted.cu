@@ -613,13 +613,13 @@ __device__ __forceinline__ void zero_words(unsigned *p, int words, int tid) {
 template <bool PAINT, bool POT = false>
 __global__ void __launch_bounds__(TILE_THREADS, 4)
 rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int nz,
-                 const float *pos, float *pos_out, float *__restrict__ vel,
+                 const float *pos, float *pos_out, float *vel,
                  const unsigned *__restrict__ offsets, uint32_t nkeys, float kick, float drift,
                  unsigned *__restrict__ counts, unsigned *__restrict__ rank,
                  unsigned *__restrict__ stats, const __grid_constant__ CUtensorMap tmap,
                  int use_tma, float *__restrict__ mesh_next, int pvec,
                  const __grid_constant__ CUtensorMap pmap, int use_ptma,
-                 unsigned *__restrict__ work) {
+                 unsigned *__restrict__ work, const PermIO io) {
   __shared__ __align__(128) float fb[2][FBOX_STRIDE];
   __shared__ __align__(16) float ff[POT ? FBOX : 4];  // POT: the tile's force box
   __shared__ __align__(8) uint64_t bar[2];
@@ -649,6 +649,17 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
     if (POT) tma_load_3d(fb[0], &tmap, cur.oz - 4, cur.oy - 2, cur.ox - 2, &bar[0]);
     else tma_load_4d(fb[0], &tmap, cur.oz, cur.oy, cur.ox, 0, &bar[0]);
   }
+  // permuted mode: the indices of a tile's first chunk are loaded one tile
+  // ahead, so that its particle loads do not wait on them
+  unsigned qpre[RKD_ILP];
+  auto prefetch_perm = [&](const TileInfo &t) {
+#pragma unroll
+    for (int j = 0; j < RKD_ILP; ++j) {
+      const unsigned p = t.beg + tid + j * TILE_THREADS;
+      qpre[j] = (io.perm && p < t.end) ? __ldg(io.perm + p) : p;
+    }
+  };
+  prefetch_perm(cur);
   int buf = 0;
   while (key < nkeys) {
     uint32_t kgrab = 0xffffffffu;  // thread 0: the tile after next
@@ -674,17 +685,22 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
       for (int j = 0; j < RKD_ILP; ++j) {
         const unsigned p = p0 + tid + j * TILE_THREADS;
         if (p < cur.end) {
-          px[j] = pos[3 * (int64_t)p];
-          py[j] = pos[3 * (int64_t)p + 1];
-          pz[j] = pos[3 * (int64_t)p + 2];
-          pu[j] = vel[3 * (int64_t)p];
-          pv[j] = vel[3 * (int64_t)p + 1];
-          pw[j] = vel[3 * (int64_t)p + 2];
+          // slot p's particle: at index perm[p] in the permuted mode
+          const int64_t q = p0 == cur.beg ? (int64_t)qpre[j]
+                            : io.perm    ? (int64_t)__ldg(io.perm + p)
+                                         : (int64_t)p;
+          px[j] = pos[3 * q];
+          py[j] = pos[3 * q + 1];
+          pz[j] = pos[3 * q + 2];
+          pu[j] = vel[3 * q];
+          pv[j] = vel[3 * q + 1];
+          pw[j] = vel[3 * q + 2];
         }
       }
     };
     if (cur.beg != cur.end) {
       load_chunk(cur.beg);  // in flight during the box wait (and the force box)
+      if (knext < nkeys) prefetch_perm(nxt);
       float *box = fb[buf];
       if (cur.tma) {
         const bool ok = mbar_wait(&bar[buf], buf ? phase1 : phase0);
@@ -766,9 +782,10 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
             }
           }
           const float vx = v0 + kick * a0, vy = v1 + kick * a1, vz = v2 + kick * a2;
-          vel[3 * (int64_t)p] = vx;
-          vel[3 * (int64_t)p + 1] = vy;
-          vel[3 * (int64_t)p + 2] = vz;
+          float *vo = io.vel_out ? io.vel_out : vel;
+          vo[3 * (int64_t)p] = vx;
+          vo[3 * (int64_t)p + 1] = vy;
+          vo[3 * (int64_t)p + 2] = vz;
           const float xn = x + drift * vx, yn = y + drift * vy, zn = z + drift * vz;
           pos_out[3 * (int64_t)p] = xn;
           pos_out[3 * (int64_t)p + 1] = yn;
@@ -810,10 +827,12 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
           }
         }
         if (counts) count_home(counts, k, key, valid);
+        if (io.key_out && valid) io.key_out[p] = k;
        }
       }
-    } else if (tid == 0) {
-      s_grab[buf] = kgrab;
+    } else {
+      if (knext < nkeys) prefetch_perm(nxt);
+      if (tid == 0) s_grab[buf] = kgrab;
     }
     __syncthreads();  // buffer `buf` is free for the prefetch two tiles ahead
     const uint32_t kafter = s_grab[buf];  // rewritten two iterations later, after a barrier
@@ -911,13 +930,80 @@ tile_rank_kernel(const float *__restrict__ pos, int64_t np, int nx, int ny, int 
 // in flight together.
 constexpr int SCATTER_ILP = 4;
 
+// Slot claims of ILP particles per thread (particle b0 + threadIdx.x +
+// j * blockDim.x has tile key k[j]): r[j] becomes its slot in the tile,
+// taken from the per-tile `cursor`.  Warp-aggregated: lanes whose key equals
+// the first valid lane's (most of a warp, since neighbouring particles
+// share their tile) take consecutive slots from one atomic, the others
+// claim one each; all ILP atomics are in flight before any result is used.
+// Every lane of the warp must call it (votes and shuffles).
+template <int ILP>
+__device__ __forceinline__ void claim_slots(const uint32_t (&k)[ILP], int64_t b0, int64_t np,
+                                            unsigned *__restrict__ cursor, unsigned (&r)[ILP]) {
+  const int lane = threadIdx.x & 31;
+  unsigned same[ILP], base[ILP];
+  uint32_t lead[ILP];
+#pragma unroll
+  for (int j = 0; j < ILP; ++j) {
+    const bool valid = b0 + threadIdx.x + j * (int64_t)blockDim.x < np;
+    const unsigned act = __ballot_sync(0xffffffffu, valid);
+    lead[j] = __shfl_sync(0xffffffffu, k[j], act ? __ffs(act) - 1 : 0);
+    same[j] = __ballot_sync(0xffffffffu, valid && k[j] == lead[j]);
+    base[j] = 0;
+    if (same[j] && lane == __ffs(same[j]) - 1)
+      base[j] = atomicAdd(cursor + lead[j], (unsigned)__popc(same[j]));
+    r[j] = (valid && k[j] != lead[j]) ? atomicAdd(cursor + k[j], 1u) : 0u;
+  }
+#pragma unroll
+  for (int j = 0; j < ILP; ++j) {
+    const unsigned b = __shfl_sync(0xffffffffu, base[j], same[j] ? __ffs(same[j]) - 1 : 0);
+    if ((same[j] >> lane) & 1u) r[j] = b + __popc(same[j] & ((1u << lane) - 1u));
+  }
+}
+
+// The permuted run loop's re-sort: the particle in slot p (the order its
+// step started from) has the new tile key[p]; it claims a slot d of that
+// tile's new range, and perm_new[d] = p tells the next gather where to read
+// it.  With perm_old the ids follow the gather, which read slot p's particle
+// from index perm_old[p]: id_out[p] = id_in[perm_old[p]].  8 bytes per
+// particle (20 with the ids) instead of moving the particles themselves.
+constexpr int ISCATTER_ILP = 8;
+__global__ void __launch_bounds__(256)
+index_scatter_kernel(const unsigned *__restrict__ key, int64_t np,
+                     const unsigned *__restrict__ offsets, unsigned *__restrict__ cursor,
+                     unsigned *__restrict__ perm_new, const unsigned *__restrict__ perm_old,
+                     const unsigned *__restrict__ id_in, unsigned *__restrict__ id_out) {
+  const int64_t span = (int64_t)blockDim.x * ISCATTER_ILP;
+  for (int64_t b0 = blockIdx.x * span; b0 < np; b0 += gridDim.x * span) {
+    uint32_t k[ISCATTER_ILP];
+    unsigned r[ISCATTER_ILP];
+#pragma unroll
+    for (int j = 0; j < ISCATTER_ILP; ++j) {
+      const int64_t p = b0 + threadIdx.x + j * (int64_t)blockDim.x;
+      k[j] = p < np ? __ldg(key + p) : 0u;
+      if (perm_old && p < np) id_out[p] = __ldg(id_in + __ldg(perm_old + p));
+    }
+    claim_slots<ISCATTER_ILP>(k, b0, np, cursor, r);
+#pragma unroll
+    for (int j = 0; j < ISCATTER_ILP; ++j) {
+      const int64_t p = b0 + threadIdx.x + j * (int64_t)blockDim.x;
+      if (p < np) perm_new[__ldg(offsets + k[j]) + r[j]] = (unsigned)p;
+    }
+  }
+}
+
+__global__ void gather_u32_kernel(const unsigned *__restrict__ in,
+                                  const unsigned *__restrict__ idx, int64_t np,
+                                  unsigned *__restrict__ out) {
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+       p += (int64_t)gridDim.x * blockDim.x)
+    out[p] = __ldg(in + __ldg(idx + p));
+}
+
 // Moves particle p to offsets[key] + its rank in the tile: rank[p] when the
 // ranks were recorded (the first sort), else a slot claimed from `cursor`
-// (the zeroed tile counters) here, so the gather only counts.  A claim is
-// warp-aggregated: lanes whose key equals the first valid lane's (most of a
-// warp, since neighbouring particles share their tile) take consecutive
-// slots from one atomic, the others claim one each.  The loop is
-// warp-uniform (the claims vote across the warp).
+// (the zeroed tile counters) here (claim_slots), so the gather only counts.
+// The loop is warp-uniform (the claims vote across the warp).
 __global__ void __launch_bounds__(256, 3)
 scatter_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
                const unsigned *__restrict__ id, const unsigned *__restrict__ rank, int64_t np,
@@ -951,29 +1037,7 @@ scatter_kernel(const float *__restrict__ pos, const float *__restrict__ vel,
       const int64_t p = b0 + threadIdx.x + j * (int64_t)blockDim.x;
       k[j] = p < np ? tile_key(x[j], y[j], z[j], nx, ny, nz) : 0u;
     }
-    if (!rank) {
-      // slot claims (see claim_slot), all SCATTER_ILP atomics in flight
-      // before any result is used
-      const int lane = threadIdx.x & 31;
-      unsigned same[SCATTER_ILP], base[SCATTER_ILP];
-      uint32_t lead[SCATTER_ILP];
-#pragma unroll
-      for (int j = 0; j < SCATTER_ILP; ++j) {
-        const bool valid = b0 + threadIdx.x + j * (int64_t)blockDim.x < np;
-        const unsigned act = __ballot_sync(0xffffffffu, valid);
-        lead[j] = __shfl_sync(0xffffffffu, k[j], act ? __ffs(act) - 1 : 0);
-        same[j] = __ballot_sync(0xffffffffu, valid && k[j] == lead[j]);
-        base[j] = 0;
-        if (same[j] && lane == __ffs(same[j]) - 1)
-          base[j] = atomicAdd(cursor + lead[j], (unsigned)__popc(same[j]));
-        r[j] = (valid && k[j] != lead[j]) ? atomicAdd(cursor + k[j], 1u) : 0u;
-      }
-#pragma unroll
-      for (int j = 0; j < SCATTER_ILP; ++j) {
-        const unsigned b = __shfl_sync(0xffffffffu, base[j], same[j] ? __ffs(same[j]) - 1 : 0);
-        if ((same[j] >> lane) & 1u) r[j] = b + __popc(same[j] & ((1u << lane) - 1u));
-      }
-    }
+    if (!rank) claim_slots<SCATTER_ILP>(k, b0, np, cursor, r);
 #pragma unroll
     for (int j = 0; j < SCATTER_ILP; ++j) {
       const int64_t p = b0 + threadIdx.x + j * (int64_t)blockDim.x;
@@ -1282,7 +1346,8 @@ int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos, int64_t 
 // potential mesh from which the gather derives them.
 int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float *pos,
                float *pos_out, float *vel, int64_t np, float kick, float drift, void *sort_ws,
-               size_t sort_bytes, unsigned *stats, cudaStream_t s, float *mesh_next, bool pot) {
+               size_t sort_bytes, unsigned *stats, cudaStream_t s, float *mesh_next, bool pot,
+               const PermIO &io) {
   PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
   const int64_t keys = tile_key_count(nx, ny, nz);
   SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
@@ -1349,7 +1414,7 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float 
   PMGB_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
 #define RKD_ARGS                                                                             \
   f3, cs, nx, ny, nz, pos, pos_out, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts, \
-      sc.rank, stats, map, use_tma, mesh_next, aligned ? 1 : 0, pmap, use_ptma, work
+      sc.rank, stats, map, use_tma, mesh_next, aligned ? 1 : 0, pmap, use_ptma, work, io
   const unsigned grid = (unsigned)std::min<int64_t>(keys, (int64_t)sm_count() * per_sm);
   switch (variant) {
     case 0: rkd_tiles_kernel<false, false><<<grid, TILE_THREADS, dsmem, s>>>(RKD_ARGS); break;
@@ -1381,6 +1446,45 @@ int tile_scatter(const float *pos, const float *vel, const unsigned *id, int64_t
     PMGB_LAUNCHED("scatter_kernel");
   }
   return PMGB_OK;
+}
+
+// The permuted loop's re-sort: scan of the tile counts the gather left,
+// then perm (where each new slot's particle is) from the keys the gather
+// wrote (the sort workspace's rank array).
+int index_resort(int64_t np, int nx, int ny, int nz, const unsigned *perm_old,
+                 unsigned *perm_new, const unsigned *id_in, unsigned *id_out, void *sort_ws,
+                 size_t sort_bytes, cudaStream_t s) {
+  PMGB_TRY(check_sort_ws(sort_ws, sort_bytes, nx, ny, nz, np));
+  const int64_t keys = tile_key_count(nx, ny, nz);
+  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
+  PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
+  PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
+  if (np > 0) {
+    index_scatter_kernel<<<wave_grid(index_scatter_kernel,
+                                     (np + ISCATTER_ILP - 1) / ISCATTER_ILP, 256),
+                           256, 0, s>>>(sc.rank, np, sc.offsets, sc.counts, perm_new, perm_old,
+                                        id_in, id_out);
+    PMGB_LAUNCHED("index_scatter_kernel");
+  }
+  return PMGB_OK;
+}
+
+int gather_u32(const unsigned *in, const unsigned *idx, int64_t np, unsigned *out,
+               cudaStream_t s) {
+  if (np == 0) return PMGB_OK;
+  gather_u32_kernel<<<wave_grid(gather_u32_kernel, np, 256), 256, 0, s>>>(in, idx, np, out);
+  PMGB_LAUNCHED("gather_u32_kernel");
+  return PMGB_OK;
+}
+
+// The per-particle key array of the sort workspace (the permuted gather's
+// new tile keys).
+unsigned *tile_key_scratch(void *sort_ws, int nx, int ny, int nz, int64_t np) {
+  return sort_scratch(sort_ws, nx, ny, nz, np).rank;
+}
+
+int check_sort_workspace(void *ws, size_t bytes, int nx, int ny, int nz, int64_t np) {
+  return check_sort_ws(ws, bytes, nx, ny, nz, np);
 }
 
 // The tile ranges (nkeys + 1 offsets) of the current order.
@@ -1482,41 +1586,63 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, flo
     if (pot) return spectral_potential(mesh, dk, f3, nx, ny, nz, r_split, scale, s);
     return mesh_forces(mesh, nx, ny, nz, r_split, dk, fk, f3, s);
   };
+  // The particles stay where the gather writes them: step i's gather reads
+  // slot p of the tile ranges from index perm[p] of buffer `cur` and writes
+  // it to index p of the other buffer (step 0, whose input is already in
+  // tile order, updates buffer a in place), with its new tile key; the
+  // re-sort between steps then only rebuilds perm (index_resort, 8 bytes
+  // per particle instead of 56), and one full scatter after the last gather
+  // puts the state in tile order.  perm lives in the workspace's particle
+  // region, the keys in the sort workspace's rank array.
+  // two permutations in turn (the re-sort reads the one the gather used)
+  unsigned *perm[2] = {reinterpret_cast<unsigned *>(drifted),
+                       reinterpret_cast<unsigned *>(drifted) + np};
+  SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
   PMGB_TRY(paint_sorted(mesh, nx, ny, nz, pos_a, np, sort_ws, sort_bytes, stats, s));
   PMGB_TRY(forces());
+  int cur = 0, pc = 0;  // buffer holding the state; perm[pc] its permutation
   for (int i = 0; i < n_steps; ++i) {
-    const int a = i & 1, b = a ^ 1;
-    // the gather of step i needs step i-1's sort (positions in tile order,
-    // tile offsets) and step i's forces (issued on s)
+    const bool last = i + 1 == n_steps;
+    const int out = i == 0 ? cur : cur ^ 1;
+    // the gather of step i needs step i-1's re-sort (perm, tile offsets) and
+    // step i's forces (issued on s)
     if (i > 0) PMGB_CUDA(cudaStreamWaitEvent(s, aux->sorted, 0));
-    PMGB_TRY(rkd_sorted(f3, (int64_t)nx * ny * nz, nx, ny, nz, P[a], drifted, V[a], np, kick[i],
-                        drift[i], sort_ws, sort_bytes, stats, s,
-                        i + 1 < n_steps ? mesh : nullptr, pot));
-    // the sort of step i (on the second stream) and the forces of step i+1
-    // (from the density the gather just painted) are independent: they
+    PermIO io;
+    io.perm = i == 0 ? nullptr : perm[pc];
+    io.vel_out = V[out];
+    io.key_out = sc.rank;
+    PMGB_TRY(rkd_sorted(f3, (int64_t)nx * ny * nz, nx, ny, nz, P[cur], P[out], V[cur], np,
+                        kick[i], drift[i], sort_ws, sort_bytes, stats, s,
+                        last ? nullptr : mesh, pot, io));
+    // the re-sort of step i (on the second stream) and the forces of step
+    // i+1 (from the density the gather just painted) are independent: they
     // touch disjoint buffers and overlap
     PMGB_CUDA(cudaEventRecord(aux->gathered, s));
     PMGB_CUDA(cudaStreamWaitEvent(aux->s2, aux->gathered, 0));
-    PMGB_TRY(tile_scatter(drifted, V[a], I[a], np, nx, ny, nz, P[b], V[b], I[b], nullptr,
-                          sort_ws, sort_bytes, aux->s2));
+    if (!last) {
+      // ids follow the gather (from the order it read), perm is rebuilt
+      PMGB_TRY(index_resort(np, nx, ny, nz, i == 0 ? nullptr : perm[pc], perm[pc ^ 1],
+                            I[cur], I[out], sort_ws, sort_bytes, aux->s2));
+      pc ^= 1;
+      cur = out;
+    } else {
+      if (i > 0) PMGB_TRY(gather_u32(I[cur], perm[pc], np, I[out], aux->s2));
+      cur = out;
+      PMGB_TRY(tile_scatter(P[cur], V[cur], I[cur], np, nx, ny, nz, P[cur ^ 1], V[cur ^ 1],
+                            I[cur ^ 1], nullptr, sort_ws, sort_bytes, aux->s2));
+      cur ^= 1;
+    }
     PMGB_CUDA(cudaEventRecord(aux->sorted, aux->s2));
-    if (i + 1 < n_steps) PMGB_TRY(forces());
+    if (!last) PMGB_TRY(forces());
   }
+  // the state ends in buffer n_steps & 1 (one buffer change per step: none
+  // in step 0, one in each later gather, one in the final scatter)
+  (void)cur;
   // join: everything of the run is ordered before later work on s
   PMGB_CUDA(cudaStreamWaitEvent(s, aux->sorted, 0));
   return PMGB_OK;
 }
 
-// The recording forward of the reverse sweep as one run: per step i the
-// positions it starts from are xs + i*3np (tile order i; xs[0] given), its
-// force meshes are computed into f3s + i*3ncell (with `pot`: its potential
-// into f3s + i*ncell, the gather deriving the forces as in fpm_run_sorted),
-// the tile ranges are copied to offs + i*(keys+1) and the re-sort map to
-// dests + i*np.  Like fpm_run_sorted, every density after the first is
-// painted by the previous step's gather and the sort overlaps the next
-// step's forces.  The final state goes to (pos_out, vel_b, id_b) if n_steps
-// is odd, else to (pos_out, vel_a, id_a); vel_a / id_a hold the initial
-// velocities / ids.
 int fpm_run_sorted_record(float *xs, float *vel_a, unsigned *id_a, float *vel_b, unsigned *id_b,
                           float *pos_out, int64_t np, int nx, int ny, int nz, int n_steps,
                           const float *kick, const float *drift, float r_split, void *mesh_ws,

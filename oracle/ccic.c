@@ -75,6 +75,38 @@ static inline int64_t fmod_i32(int32_t a, int32_t n) {
     }                                                                                \
   }                                                                                  \
                                                                                      \
+  /* out[i] = sum_j mesh[idx_j] * grad W_j(pos_i): the position gradient of    \
+     the interpolated field (d(1 - |u|)/du = -1 for u >= 0, +1 below, the    \
+     rule JAX applies to abs; floor has a zero derivative) */                \
+  void oc_grad_##SUFFIX(const T *mesh, int nx, int ny, int nz, const T *pos,         \
+                        int64_t np, T *out) {                                        \
+    _Pragma("omp parallel for schedule(static)")                                     \
+    for (int64_t i = 0; i < np; ++i) {                                               \
+      const T *p = pos + 3 * i;                                                      \
+      T f[3] = {FLOOR(p[0]), FLOOR(p[1]), FLOOR(p[2])};                              \
+      const int32_t n[3] = {nx, ny, nz};                                             \
+      T g0 = 0, g1 = 0, g2 = 0;                                                      \
+      for (int j = 0; j < 8; ++j) {                                                  \
+        T k[3], dk[3];                                                               \
+        int64_t c[3];                                                                \
+        for (int d = 0; d < 3; ++d) {                                                \
+          T nc = f[d] + (T)CONN[j][d];                                               \
+          T u = p[d] - nc;                                                           \
+          k[d] = (T)1 - FABS(u);                                                     \
+          dk[d] = u >= 0 ? (T)-1 : (T)1;                                             \
+          c[d] = fmod_i32((int32_t)nc, n[d]);                                        \
+        }                                                                            \
+        T m = mesh[(c[0] * ny + c[1]) * nz + c[2]];                                  \
+        g0 += ((m * dk[0]) * k[1]) * k[2];                                           \
+        g1 += ((m * k[0]) * dk[1]) * k[2];                                           \
+        g2 += ((m * k[0]) * k[1]) * dk[2];                                           \
+      }                                                                              \
+      out[3 * i] = g0;                                                               \
+      out[3 * i + 1] = g1;                                                           \
+      out[3 * i + 2] = g2;                                                           \
+    }                                                                                \
+  }                                                                                  \
+                                                                                     \
   void oc_weights_##SUFFIX(const T *pos, int64_t np, int nx, int ny, int nz,         \
                            int64_t *idx, T *w) {                                     \
     _Pragma("omp parallel for schedule(static)")                                     \

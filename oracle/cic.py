@@ -131,6 +131,29 @@ def _dkernel(pos, dtype):
     return k, dk
 
 
+def cic_grad(grid_mesh, positions, dtype=np.float64):
+    """``sum_j mesh[idx_j] * grad W_j(x)`` per particle ``[Np, 3]``: the
+    position gradient of the interpolated field, with the derivative of each
+    axis factor times the other two (``_dkernel``).  The C statement when it
+    is built, else NumPy."""
+    grid_mesh = np.ascontiguousarray(np.asarray(grid_mesh, dtype=dtype))
+    pos = np.ascontiguousarray(np.asarray(positions, dtype=dtype).reshape(-1, 3))
+    c = _c(dtype)
+    if c is not None:
+        h, sfx = c
+        out = np.empty((len(pos), 3), dtype)
+        getattr(h, f"oc_grad_{sfx}")(grid_mesh.ctypes.data, *grid_mesh.shape, pos.ctypes.data,
+                                     len(pos), out.ctypes.data)
+        return out
+    idx, _ = cic_weights(pos, grid_mesh.shape, dtype)
+    k, dk = _dkernel(pos.reshape(-1, 1, 3), dtype)
+    m = grid_mesh[idx[..., 0], idx[..., 1], idx[..., 2]]
+    gx = (m * dk[..., 0] * k[..., 1] * k[..., 2]).sum(-1)
+    gy = (m * k[..., 0] * dk[..., 1] * k[..., 2]).sum(-1)
+    gz = (m * k[..., 0] * k[..., 1] * dk[..., 2]).sum(-1)
+    return np.stack([gx, gy, gz], -1)
+
+
 def cic_paint_vjp(positions, mesh_shape, g_mesh, weight=1.0, dtype=np.float64):
     """Vector-Jacobian product of ``cic_paint`` w.r.t. positions and weight.
 
@@ -140,6 +163,11 @@ def cic_paint_vjp(positions, mesh_shape, g_mesh, weight=1.0, dtype=np.float64):
     """
     pos = np.asarray(positions, dtype=dtype).reshape(-1, 1, 3)
     g_mesh = np.asarray(g_mesh, dtype=dtype)
+    if _c(dtype) is not None:
+        wt = (np.asarray(weight, dtype=dtype).reshape(-1, 1)
+              if np.ndim(weight) else np.asarray(weight, dtype=dtype))
+        gpos = cic_grad(g_mesh, pos, dtype) * wt
+        return gpos, cic_read(g_mesh, pos.reshape(-1, 3), dtype)
     idx, _ = cic_weights(pos.reshape(-1, 3), mesh_shape, dtype)
     k, dk = _dkernel(pos, dtype)
     g = g_mesh[idx[..., 0], idx[..., 1], idx[..., 2]]
@@ -164,6 +192,8 @@ def cic_read_vjp(grid_mesh, positions, g_out, dtype=np.float64):
     g_out = np.asarray(g_out, dtype=dtype).reshape(-1)
     g_mesh = cic_paint(np.zeros(grid_mesh.shape, dtype), pos.reshape(-1, 3),
                        weight=g_out, dtype=dtype)
+    if _c(dtype) is not None:
+        return g_mesh, cic_grad(grid_mesh, pos, dtype) * g_out[:, None]
     idx, _ = cic_weights(pos.reshape(-1, 3), grid_mesh.shape, dtype)
     k, dk = _dkernel(pos, dtype)
     m = grid_mesh[idx[..., 0], idx[..., 1], idx[..., 2]]

@@ -46,6 +46,9 @@ def _declare(lib):
         f = getattr(lib, f"oc_paint_{sfx}")
         f.argtypes = [P, I, I, I, P, L, P, real]
         f.restype = None
+        f = getattr(lib, f"oc_grad_{sfx}")
+        f.argtypes = [P, I, I, I, P, L, P]
+        f.restype = None
         f = getattr(lib, f"oc_weights_{sfx}")
         f.argtypes = [P, L, I, I, I, P, P]
         f.restype = None

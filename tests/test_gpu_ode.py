@@ -70,8 +70,9 @@ def test_make_diffrax_ode_stacks_the_state(state):
     from jaxpm_gb300 import cosmology, ode
     _, _, x, v = state
     cosmo = cosmology.Planck15()
-    f = ode.make_ode_fn((N,) * 3)
-    g = ode.make_diffrax_ode((N,) * 3)
+    # deterministic paint: the two calls' forces are then identical bit for bit
+    f = ode.make_ode_fn((N,) * 3, paint_mode="deterministic")
+    g = ode.make_diffrax_ode((N,) * 3, paint_mode="deterministic")
     y = torch.stack([x, v])
     out = g(0.4, y, cosmo)
     dpos, dvel = f((x, v), 0.4, cosmo)

@@ -1,0 +1,130 @@
+"""The batched and differentiable configurations at their configured sizes,
+against the oracle per simulation.
+
+* Batched: simulations of 64^3, 96^3 and 128^3 particles on meshes of the
+  same size (box 2N Mpc/h, own cosmology and seed each, 2LPT initial
+  conditions), one launch per phase for all of them; each simulation's
+  final state against the oracle's float64 FastPM steps with that
+  simulation's own coefficients, and the batched reverse sweep against the
+  oracle's (``oracle/nbody.py:fpm_run_vjp``) on the smaller two.
+* Differentiable: the sorted engine's reverse sweep at 128^3 and the
+  checkpointed autograd steps at 64^3, from 2LPT initial conditions, against
+  the float64 oracle's reverse sweep (the transpose ``jax.grad`` takes
+  through ``jaxpm/ode.py:13-82``).
+
+Bars: 1e-5 relative L2 for forward states (the force parity bar), 1e-4 for
+cotangents (float32 against float64 through the CIC kernel's kinks)."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+from oracle import fourier as fo, nbody as onb
+
+pytestmark = pytest.mark.gpu
+
+
+def _cosmos(n, seed):
+    from jaxpm_gb300 import cosmology
+    rng = np.random.default_rng(seed)
+    return [cosmology.Planck15(Omega_c=float(rng.uniform(0.2, 0.35)),
+                               sigma8=float(rng.uniform(0.6, 1.0))) for _ in range(n)]
+
+
+def _oracle_steps(x, v, shape, kick, drift):
+    x, v = x.astype(np.float64), v.astype(np.float64)
+    for k, d in zip(kick, drift):
+        v = v + k * fo.pm_forces(x, mesh_shape=shape, dtype=np.float64)
+        x = x + d * v
+    return x, v
+
+
+@pytest.fixture(scope="module")
+def batch(cuda):
+    from jaxpm_gb300 import batched
+    ns = [64, 96, 128]
+    shapes = [(n,) * 3 for n in ns]
+    cs = _cosmos(len(ns), seed=12)
+    x, v = batched.initial_conditions(shapes, [[2.0 * n] * 3 for n in ns], cs, [21, 22, 23],
+                                      device=cuda)
+    b = batched.BatchedFastPM(shapes, cs, 0.1, 1.0, 2, device=cuda)
+    return b, shapes, x, v
+
+
+def test_batched_configured_sizes_match_oracle(batch):
+    b, shapes, x0, v0 = batch
+    x, v = x0.clone(), v0.clone()
+    b.run(x, v)
+    torch.cuda.synchronize()
+    kick, drift = b.kick.double().cpu().numpy(), b.drift.double().cpu().numpy()
+    for s, shape in enumerate(shapes):
+        xs0, vs0 = b.split(x0)[s].cpu().numpy(), b.split(v0)[s].cpu().numpy()
+        xr, vr = _oracle_steps(xs0, vs0, shape, kick[:, s], drift[:, s])
+        assert rel_l2(b.split(x)[s].cpu().numpy() - xs0, xr - xs0) < 1e-5, shape
+        assert rel_l2(b.split(v)[s].cpu().numpy(), vr) < 1e-5, shape
+
+
+def test_batched_configured_sizes_vjp_match_oracle(batch):
+    b, shapes, x0, v0 = batch
+    rng = np.random.default_rng(3)
+    gx = torch.from_numpy(rng.standard_normal(x0.shape).astype(np.float32)).to(x0.device)
+    gv = torch.from_numpy(rng.standard_normal(x0.shape).astype(np.float32)).to(x0.device)
+    _, (gxb, gvb) = b.vjp(x0, v0, gx, gv)
+    kick, drift = b.kick.double().cpu().numpy(), b.drift.double().cpu().numpy()
+    for s, shape in enumerate(shapes[:2]):
+        _, (gxr, gvr) = onb.fpm_run_vjp(b.split(x0)[s].cpu().numpy(), b.split(v0)[s].cpu().numpy(),
+                                        shape, kick[:, s], drift[:, s],
+                                        b.split(gx)[s].cpu().numpy(),
+                                        b.split(gv)[s].cpu().numpy())
+        assert rel_l2(b.split(gxb)[s].cpu(), gxr) < 1e-4, shape
+        assert rel_l2(b.split(gvb)[s].cpu(), gvr) < 1e-4, shape
+
+
+def _ic(n, box, seed, dev):
+    from jaxpm_gb300 import cosmology, distributed, pm
+    cosmo = cosmology.Planck15()
+    ic = pm.linear_field((n,) * 3, [box] * 3, pm.pk_table(cosmo), seed=seed, device=dev)
+    lat = distributed.uniform_particles((n,) * 3, device=dev).reshape(-1, 3)
+    with torch.no_grad():
+        dx, p, _ = pm.lpt(cosmo, ic, lat, a=0.1, order=2)
+    return cosmo, (lat + dx).contiguous(), p.contiguous()
+
+
+def test_sorted_vjp_128_matches_oracle(cuda):
+    from jaxpm_gb300 import simulate
+    n, steps = 128, 4
+    cosmo, x0, v0 = _ic(n, 256.0, 8, cuda)
+    g = torch.Generator(device=cuda).manual_seed(2)
+    gx = torch.randn(x0.shape, device=cuda, generator=g)
+    gv = torch.randn(x0.shape, device=cuda, generator=g)
+    eng = simulate.SortedFastPM((n,) * 3, cosmo, 0.1, 1.0, steps, device=cuda)
+    (xf, vf), (gx0, gv0) = eng.vjp(x0, v0, gx, gv)
+    (xr, vr), (gxr, gvr) = onb.fpm_run_vjp(x0.cpu().numpy(), v0.cpu().numpy(), (n,) * 3,
+                                           eng.kick, eng.drift, gx.cpu().numpy(),
+                                           gv.cpu().numpy())
+    xs = x0.cpu().numpy()
+    assert rel_l2(xf.cpu().numpy() - xs, xr - xs) < 1e-5
+    assert rel_l2(gx0.cpu(), gxr) < 1e-4
+    assert rel_l2(gv0.cpu(), gvr) < 1e-4
+
+
+def test_checkpointed_autograd_steps_64_match_oracle(cuda):
+    """simulate.nbody (torch autograd over the C-ABI step adjoints, a
+    checkpoint every 2 steps) at 64^3: the gradient of <gx, x_T> + <gv, v_T>
+    with respect to the initial state."""
+    from jaxpm_gb300 import simulate
+    n, steps = 64, 4
+    cosmo, x0, v0 = _ic(n, 128.0, 9, cuda)
+    g = torch.Generator(device=cuda).manual_seed(4)
+    gx = torch.randn(x0.shape, device=cuda, generator=g)
+    gv = torch.randn(x0.shape, device=cuda, generator=g)
+    x = x0.clone().requires_grad_(True)
+    v = v0.clone().requires_grad_(True)
+    xt, vt = simulate.nbody(x, v, cosmo, (n,) * 3, 0.1, 1.0, steps, checkpoint_every=2)
+    ((xt * gx).sum() + (vt * gv).sum()).backward()
+    from jaxpm_gb300 import ode
+    kick, drift = ode.fpm_coefficients(cosmo, 0.1, 1.0, steps)
+    _, (gxr, gvr) = onb.fpm_run_vjp(x0.cpu().numpy(), v0.cpu().numpy(), (n,) * 3, kick, drift,
+                                    gx.cpu().numpy(), gv.cpu().numpy())
+    assert rel_l2(x.grad.cpu(), gxr) < 1e-4
+    assert rel_l2(v.grad.cpu(), gvr) < 1e-4

@@ -295,6 +295,40 @@ def test_fused_run_matches_step_by_step(cuda, shape):
     assert a.stats["tma_wait_timeout"] == 0
 
 
+@pytest.mark.parametrize("split", [(1, 1), (2, 3), (3, 4)])
+def test_permuted_run_leaves_tile_order_and_chains(cuda, lib, split):
+    """The run loop moves only a permutation between steps and sorts the
+    particles once at the end: after run() they are in tile order (a sorted
+    paint finds no particle outside its tile), and runs of odd and even step
+    counts chained one after the other equal one run over all the steps."""
+    from jaxpm_gb300 import _lib, cosmology, simulate
+    shape = (32, 32, 32)
+    n1, n2 = split
+    rng = np.random.default_rng(5)
+    lat = cic.lattice(shape).reshape(-1, 3)
+    x0 = T((lat + rng.normal(0, 0.8, lat.shape)).astype(np.float32), cuda)
+    v0 = T(rng.normal(0, 0.5, lat.shape).astype(np.float32), cuda)
+    cosmo = cosmology.Planck15()
+    a = simulate.SortedFastPM(shape, cosmo, 0.1, 1.0, n1 + n2, device=cuda)
+    a.load(x0, v0)
+    a.run(steps=n1)
+    mesh = torch.empty(shape, device=cuda)
+    stats = torch.zeros(3, dtype=torch.int32, device=cuda)
+    _lib.call("pmgb_cic_paint_sorted_f32", _lib.ptr(mesh), *shape, _lib.ptr(a.positions),
+              a.n, _lib.ptr(a.sort_ws), a.sort_bytes, _lib.ptr(stats), _lib.stream())
+    torch.cuda.synchronize()
+    assert stats.tolist() == [0, 0, 0]
+    a.run(steps=n2, start=n1)
+    b = simulate.SortedFastPM(shape, cosmo, 0.1, 1.0, n1 + n2, device=cuda)
+    b.load(x0, v0)
+    b.run()
+    (ax, av), (bx, bv) = a.state(), b.state()
+    assert rel_l2(ax.cpu() - x0.cpu(), bx.cpu() - x0.cpu()) < 1e-5
+    assert rel_l2(av.cpu(), bv.cpu()) < 1e-5
+    assert torch.equal(a.ids_current.sort().values, torch.arange(a.n, device=cuda,
+                                                                  dtype=torch.int32))
+
+
 @pytest.mark.parametrize("r_split", [0.0, 1.5])
 def test_run_loop_potential_path_matches_oracle(cuda, r_split):
     """At 64^3 the run loop takes the forces from the potential (one inverse
@@ -412,3 +446,63 @@ def test_run_host_matches_device_run(cuda):
     assert rel_l2(hv.numpy() - v0, v.cpu().numpy() - v0) < 1e-4
     with pytest.raises(ValueError):
         eng.run_host(torch.from_numpy(x0.copy()), torch.from_numpy(v0.copy()))
+
+
+def test_permuted_gather_abi_pieces_compose_to_the_run(cuda, lib):
+    """The run loop's pieces through the C ABI (pmgb_mesh_potential_f32,
+    pmgb_read_potential_kick_drift_paint_perm_f32, pmgb_tile_resort_index,
+    pmgb_gather_u32, pmgb_tile_scatter_f32), issued one by one as a caller
+    would, give the state of pmgb_fpm_run_sorted_f32 (64^3: the potential
+    pipeline's shapes)."""
+    from jaxpm_gb300 import _lib, cosmology, simulate
+    shape = (64, 64, 64)
+    nx, ny, nz = shape
+    K = 4
+    rng = np.random.default_rng(9)
+    lat = cic.lattice(shape).reshape(-1, 3)
+    x0 = T((lat + rng.normal(0, 0.8, lat.shape)).astype(np.float32), cuda)
+    v0 = T(rng.normal(0, 0.5, lat.shape).astype(np.float32), cuda)
+    cosmo = cosmology.Planck15()
+    ref = simulate.SortedFastPM(shape, cosmo, 0.1, 1.0, K, device=cuda)
+    ref.load(x0, v0)
+    ref.run()
+    e = simulate.SortedFastPM(shape, cosmo, 0.1, 1.0, K, device=cuda)
+    e.load(x0, v0)
+    n = e.n
+    s = _lib.stream()
+    mesh = torch.empty(shape, device=cuda)
+    pot = torch.empty(shape, device=cuda)
+    wsb = lib.pmgb_mesh_forces_workspace_size(nx, ny, nz)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=cuda)
+    perms = torch.empty((2, n), dtype=torch.int32, device=cuda)
+    P = _lib.ptr
+    _lib.call("pmgb_cic_paint_sorted_f32", P(mesh), nx, ny, nz, P(e.pos[0]), n, P(e.sort_ws),
+              e.sort_bytes, P(e.stats_buf), s)
+    cur, pc, permuted = 0, 0, False
+    for i in range(K):
+        _lib.call("pmgb_mesh_potential_f32", P(mesh), P(pot), nx, ny, nz, 0.0, P(ws), wsb, s)
+        last = i + 1 == K
+        out = cur if not permuted else 1 - cur
+        _lib.call("pmgb_read_potential_kick_drift_paint_perm_f32", P(pot), nx, ny, nz,
+                  P(e.pos[cur]), P(e.vel[cur]), P(perms[pc]) if permuted else None,
+                  P(e.pos[out]), P(e.vel[out]), n, float(e.kick[i]), float(e.drift[i]),
+                  None if last else P(mesh), P(e.sort_ws), e.sort_bytes, P(e.stats_buf), s)
+        if last:
+            if permuted:
+                _lib.call("pmgb_gather_u32", P(e.ids[cur]), P(perms[pc]), n, P(e.ids[out]), s)
+            _lib.call("pmgb_tile_scatter_f32", P(e.pos[out]), P(e.vel[out]), P(e.ids[out]), n,
+                      nx, ny, nz, P(e.pos[1 - out]), P(e.vel[1 - out]), P(e.ids[1 - out]),
+                      None, P(e.sort_ws), e.sort_bytes, s)
+            cur = 1 - out
+        else:
+            _lib.call("pmgb_tile_resort_index", n, nx, ny, nz,
+                      P(perms[pc]) if permuted else None, P(perms[1 - pc]), P(e.ids[cur]),
+                      P(e.ids[out]), P(e.sort_ws), e.sort_bytes, s)
+            pc, cur, permuted = 1 - pc, out, True
+    e.cur = cur
+    (ax, av), (bx, bv) = ref.state(), e.state()
+    assert rel_l2(bx.cpu() - x0.cpu(), ax.cpu() - x0.cpu()) < 1e-5
+    assert rel_l2(bv.cpu(), av.cpu()) < 1e-5
+    assert torch.equal(e.ids_current.sort().values, torch.arange(n, device=cuda,
+                                                                  dtype=torch.int32))
+    assert e.stats == {"paint": 0, "gather": 0, "tma_wait_timeout": 0}

@@ -237,6 +237,18 @@ def test_c_oracle_matches_numpy_oracle(shape):
                               cic.cic_paint(np.zeros(shape), pos, weight=0.7, dtype=dtype))
             finally:
                 cic.NATIVE = True
+        # the position gradients of the VJPs (float64 sums in another order)
+        g = rng.standard_normal(len(pos))
+        vjp = {}
+        for use_c in (True, False):
+            cic.NATIVE = use_c
+            try:
+                vjp[use_c] = (cic.cic_read_vjp(mesh, pos, g, np.float64)[1],
+                              cic.cic_paint_vjp(pos, shape, mesh, weight=g)[0])
+            finally:
+                cic.NATIVE = True
+        for a, b in zip(vjp[True], vjp[False]):
+            assert np.allclose(a, b, rtol=1e-12, atol=1e-12)
         # reads: the same float operations in the same order, bit for bit
         assert np.array_equal(out[True][0], out[False][0])
         for a, b in zip(out[True][1:], out[False][1:]):
