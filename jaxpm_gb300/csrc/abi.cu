@@ -609,7 +609,7 @@ int pmgb_read_potential_kick_drift_paint_perm_f32(
   PermIO io;
   io.perm = perm;
   io.vel_out = vel_out;
-  io.key_out = tile_key_scratch(sort_workspace, nx, ny, nz, np);
+  perm_scratch(sort_workspace, nx, ny, nz, np, &io);
   return rkd_sorted(pot, (int64_t)nx * ny * nz, nx, ny, nz, pos, pos_out,
                     const_cast<float *>(vel), np, kick, drift, sort_workspace,
                     sort_workspace_bytes, stats, stream, mesh_next, true, io);

@@ -129,7 +129,10 @@ int fpm_run_sorted_record(float *xs, float *vel_a, unsigned *id_a, float *vel_b,
 struct PermIO {
   const unsigned *perm = nullptr;
   float *vel_out = nullptr;  // nullptr: the velocities are updated in place
-  unsigned *key_out = nullptr;  // nullptr: keys are not written
+  // nullptr: keys are not written; else np pairs (new tile key, rank among
+  // the particles that stayed in their tile, ~0 for those that left)
+  unsigned *key_out = nullptr;
+  unsigned *stay_out = nullptr;  // with key_out: per tile, how many stayed
 };
 
 int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz,
@@ -150,7 +153,9 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b,
 // spectra (dk, fk) by the selected FFT path.
 int mesh_forces(const float *mesh, int nx, int ny, int nz, float r_split,
                 void *dk, void *fk, float *f3, cudaStream_t s);
-unsigned *tile_key_scratch(void *sort_ws, int nx, int ny, int nz, int64_t np);
+// the permuted gather's outputs in the sort workspace (keys, stayer ranks,
+// stayer counts)
+void perm_scratch(void *sort_ws, int nx, int ny, int nz, int64_t np, PermIO *io);
 int check_sort_workspace(void *ws, size_t bytes, int nx, int ny, int nz, int64_t np);
 // scan of the tile counts, then perm from the keys in the rank array (the
 // permuted run loop's re-sort)

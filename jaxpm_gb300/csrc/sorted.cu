@@ -98,6 +98,23 @@ __device__ __forceinline__ void count_home(unsigned *__restrict__ counts, uint32
   if (valid && key != home) atomicAdd(counts + key, 1u);
 }
 
+// count_home that also ranks the particles that stay in `home` with the
+// shared counter *stay (one warp-aggregated shared atomic): returns a
+// stayer's rank among the tile's stayers, ~0 for a particle that left.
+__device__ __forceinline__ unsigned count_home_rank(unsigned *__restrict__ counts, uint32_t key,
+                                                    uint32_t home, bool valid, unsigned *stay) {
+  const int lane = threadIdx.x & 31;
+  const unsigned sm = __ballot_sync(0xffffffffu, valid && key == home);
+  unsigned b = 0;
+  if (sm && lane == __ffs(sm) - 1) {
+    atomicAdd(counts + home, (unsigned)__popc(sm));
+    b = atomicAdd(stay, (unsigned)__popc(sm));
+  }
+  if (valid && key != home) atomicAdd(counts + key, 1u);
+  b = __shfl_sync(0xffffffffu, b, sm ? __ffs(sm) - 1 : 0);
+  return (sm >> lane) & 1u ? b + __popc(sm & ((1u << lane) - 1u)) : 0xffffffffu;
+}
+
 // Fixed-point scale of a paint box whose tile holds `count` (< 2^20)
 // particles: 2^s with s = min(24, clz(count)), so that count * 2^s < 2^32
 // (a cell receives at most one contribution, <= 2^s, per particle) and the
@@ -624,6 +641,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
   __shared__ __align__(16) float ff[POT ? FBOX : 4];  // POT: the tile's force box
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ uint32_t s_grab[2];  // the tile after next, as grabbed by thread 0
+  __shared__ unsigned s_stay;     // permuted mode: particles of the tile that stayed
   extern __shared__ __align__(128) unsigned pbox[];  // PAINT: 2 x NBOX_WORDS
   constexpr uint32_t BOX_BYTES = POT ? PBOX_BYTES : FBOX_BYTES;
   const int tid = threadIdx.x;
@@ -664,6 +682,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
   while (key < nkeys) {
     uint32_t kgrab = 0xffffffffu;  // thread 0: the tile after next
     if (tid == 0 && knext < nkeys) kgrab = sched.key(it + 2, work);
+    if (tid == 0) s_stay = 0u;  // read by this thread last, after the tile's barrier
     // prefetch the next tile's box into the other buffer (freed by the
     // barrier at the end of the previous iteration)
     TileInfo nxt;
@@ -826,8 +845,14 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
             }
           }
         }
-        if (counts) count_home(counts, k, key, valid);
-        if (io.key_out && valid) io.key_out[p] = k;
+        if (io.key_out) {
+          // the stayers' ranks in the tile come from one shared counter
+          // (warp-aggregated), so the re-sort places them without atomics
+          const unsigned r = count_home_rank(counts, k, key, valid, &s_stay);
+          if (valid) *reinterpret_cast<uint2 *>(io.key_out + 2 * (int64_t)p) = make_uint2(k, r);
+        } else if (counts) {
+          count_home(counts, k, key, valid);
+        }
        }
       }
     } else {
@@ -836,6 +861,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
     }
     __syncthreads();  // buffer `buf` is free for the prefetch two tiles ahead
     const uint32_t kafter = s_grab[buf];  // rewritten two iterations later, after a barrier
+    if (io.stay_out && tid == 0) io.stay_out[key] = s_stay;
     if (PAINT && cur.beg != cur.end) {
       // flush the paint box, each warp its x-planes (w and w + 8): fixed
       // point -> float in place, one TMA reduce-add per plane into the mesh
@@ -962,17 +988,21 @@ __device__ __forceinline__ void claim_slots(const uint32_t (&k)[ILP], int64_t b0
 }
 
 // The permuted run loop's re-sort: the particle in slot p (the order its
-// step started from) has the new tile key[p]; it claims a slot d of that
-// tile's new range, and perm_new[d] = p tells the next gather where to read
-// it.  With perm_old the ids follow the gather, which read slot p's particle
-// from index perm_old[p]: id_out[p] = id_in[perm_old[p]].  8 bytes per
-// particle (20 with the ids) instead of moving the particles themselves.
-constexpr int ISCATTER_ILP = 8;
+// step started from) has the new tile key and, if it stayed in its tile,
+// its rank among the tile's stayers (key_rank[p], from the gather).  A stayer's
+// new slot is offsets[key] + rank, with no atomics; a leaver (rank ~0)
+// claims the next slot after the stayers from cursor[key] (the stayer
+// count), warp-aggregated by key.  perm_new[d] = p tells the next gather
+// where slot d's particle is.  With perm_old the ids follow the gather,
+// which read slot p's particle from index perm_old[p]:
+// id_out[p] = id_in[perm_old[p]].
+constexpr int ISCATTER_ILP = 2;
 __global__ void __launch_bounds__(256)
-index_scatter_kernel(const unsigned *__restrict__ key, int64_t np,
-                     const unsigned *__restrict__ offsets, unsigned *__restrict__ cursor,
-                     unsigned *__restrict__ perm_new, const unsigned *__restrict__ perm_old,
-                     const unsigned *__restrict__ id_in, unsigned *__restrict__ id_out) {
+index_scatter_kernel(const uint2 *__restrict__ key_rank, int64_t np, const unsigned *__restrict__ offsets,
+                     unsigned *__restrict__ cursor, unsigned *__restrict__ perm_new,
+                     const unsigned *__restrict__ perm_old, const unsigned *__restrict__ id_in,
+                     unsigned *__restrict__ id_out) {
+  const int lane = threadIdx.x & 31;
   const int64_t span = (int64_t)blockDim.x * ISCATTER_ILP;
   for (int64_t b0 = blockIdx.x * span; b0 < np; b0 += gridDim.x * span) {
     uint32_t k[ISCATTER_ILP];
@@ -980,10 +1010,24 @@ index_scatter_kernel(const unsigned *__restrict__ key, int64_t np,
 #pragma unroll
     for (int j = 0; j < ISCATTER_ILP; ++j) {
       const int64_t p = b0 + threadIdx.x + j * (int64_t)blockDim.x;
-      k[j] = p < np ? __ldg(key + p) : 0u;
+      const uint2 kr = p < np ? __ldg(key_rank + p) : make_uint2(0u, 0u);
+      k[j] = kr.x;
+      r[j] = kr.y;
       if (perm_old && p < np) id_out[p] = __ldg(id_in + __ldg(perm_old + p));
     }
-    claim_slots<ISCATTER_ILP>(k, b0, np, cursor, r);
+#pragma unroll
+    for (int j = 0; j < ISCATTER_ILP; ++j) {
+      const bool leave = r[j] == 0xffffffffu;  // invalid lanes hold r = 0
+      const unsigned lm = __ballot_sync(0xffffffffu, leave);
+      if (leave) {
+        const unsigned peers = __match_any_sync(lm, k[j]);
+        const int leader = __ffs(peers) - 1;
+        unsigned base = 0;
+        if (lane == leader) base = atomicAdd(cursor + k[j], (unsigned)__popc(peers));
+        base = __shfl_sync(peers, base, leader);
+        r[j] = base + __popc(peers & ((1u << lane) - 1u));
+      }
+    }
 #pragma unroll
     for (int j = 0; j < ISCATTER_ILP; ++j) {
       const int64_t p = b0 + threadIdx.x + j * (int64_t)blockDim.x;
@@ -1214,16 +1258,22 @@ int exclusive_scan(const unsigned *in, unsigned *out, int64_t n, unsigned *sums,
 }
 
 // Scratch of the sort: tile counts (keys), tile offsets (keys + 1: the last
-// entry is the particle count), scan block sums, one rank per particle.
+// entry is the particle count), scan block sums, two words per particle
+// (a rank, or the permuted gather's key and stayer rank), the stayer counts
+// (keys).
 size_t sort_workspace_size(int nx, int ny, int nz, int64_t np) {
   const size_t keys = (size_t)tile_key_count(nx, ny, nz);
   auto a = [](size_t b) { return (b + 255) & ~(size_t)255; };
   return a(keys * 4) + a((keys + 1) * 4) + a(((keys + SCAN_BLOCK - 1) / SCAN_BLOCK) * 4) +
-         a((size_t)np * 4) + 256;
+         a((size_t)np * 8) + a(keys * 4) + 256;
 }
 
 struct SortScratch {
-  unsigned *counts, *offsets, *sums, *rank, *work;
+  // rank: ranks of the first sort (np words), or (from the permuted gather)
+  // np pairs of the new tile key and the particle's rank among those that
+  // stayed in their tile (~0 for the others); stay: per tile, how many
+  // stayed (the leavers' slot cursor of the re-sort)
+  unsigned *counts, *offsets, *sums, *rank, *stay, *work;
 };
 
 static SortScratch sort_scratch(void *ws, int nx, int ny, int nz, int64_t np) {
@@ -1237,8 +1287,10 @@ static SortScratch sort_scratch(void *ws, int nx, int ny, int nz, int64_t np) {
   c += a((keys + 1) * 4);
   sc.sums = reinterpret_cast<unsigned *>(c);
   c += a(((keys + SCAN_BLOCK - 1) / SCAN_BLOCK) * 4);
-  sc.rank = reinterpret_cast<unsigned *>(c);
-  c += a((size_t)np * 4);
+  sc.rank = reinterpret_cast<unsigned *>(c);  // np words, or np (key, rank) pairs
+  c += a((size_t)np * 8);
+  sc.stay = reinterpret_cast<unsigned *>(c);
+  c += a(keys * 4);
   sc.work = reinterpret_cast<unsigned *>(c);
   return sc;
 }
@@ -1458,12 +1510,11 @@ int index_resort(int64_t np, int nx, int ny, int nz, const unsigned *perm_old,
   const int64_t keys = tile_key_count(nx, ny, nz);
   SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
   PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
-  PMGB_CUDA(cudaMemsetAsync(sc.counts, 0, keys * 4, s));
   if (np > 0) {
     index_scatter_kernel<<<wave_grid(index_scatter_kernel,
                                      (np + ISCATTER_ILP - 1) / ISCATTER_ILP, 256),
-                           256, 0, s>>>(sc.rank, np, sc.offsets, sc.counts, perm_new, perm_old,
-                                        id_in, id_out);
+                           256, 0, s>>>(reinterpret_cast<const uint2 *>(sc.rank), np,
+                                        sc.offsets, sc.stay, perm_new, perm_old, id_in, id_out);
     PMGB_LAUNCHED("index_scatter_kernel");
   }
   return PMGB_OK;
@@ -1477,10 +1528,10 @@ int gather_u32(const unsigned *in, const unsigned *idx, int64_t np, unsigned *ou
   return PMGB_OK;
 }
 
-// The per-particle key array of the sort workspace (the permuted gather's
-// new tile keys).
-unsigned *tile_key_scratch(void *sort_ws, int nx, int ny, int nz, int64_t np) {
-  return sort_scratch(sort_ws, nx, ny, nz, np).rank;
+void perm_scratch(void *sort_ws, int nx, int ny, int nz, int64_t np, PermIO *io) {
+  const SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
+  io->key_out = sc.rank;  // np (key, stayer rank) pairs
+  io->stay_out = sc.stay;
 }
 
 int check_sort_workspace(void *ws, size_t bytes, int nx, int ny, int nz, int64_t np) {
@@ -1610,7 +1661,7 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, flo
     PermIO io;
     io.perm = i == 0 ? nullptr : perm[pc];
     io.vel_out = V[out];
-    io.key_out = sc.rank;
+    perm_scratch(sort_ws, nx, ny, nz, np, &io);
     PMGB_TRY(rkd_sorted(f3, (int64_t)nx * ny * nz, nx, ny, nz, P[cur], P[out], V[cur], np,
                         kick[i], drift[i], sort_ws, sort_bytes, stats, s,
                         last ? nullptr : mesh, pot, io));
