@@ -53,7 +53,7 @@ def parse():
     ap.add_argument("--engine", default="sorted", choices=["sorted", "lattice"])
     ap.add_argument("--paint-mode", default="atomic", help="painter of the lattice engine")
     ap.add_argument("--skip", default="", help="comma list of legs to skip: "
-                    "adjoint,plain,e2e,cpu,clocks")
+                    "adjoint,plain,e2e,cpu,clocks,paint,1024,tune")
     ap.add_argument("--phases-only", action="store_true")
     ap.add_argument("--repeats", type=int, default=5,
                     help="timed repetitions of each K-step run (the median is reported)")
@@ -359,6 +359,17 @@ def run_gb300(args):
         step_phased(i % K)
     reset()
     torch.cuda.synchronize(dev)
+    # launch configuration of the run loop, tuned on this workload (untimed;
+    # cached per mesh, particle count, step count and GPU)
+    tuning = None
+    if engine == "sorted" and "tune" not in skip:
+        from jaxpm_gb300 import autotune
+        choice, report = autotune.tune_run(eng, x0, v0, steps=K)
+        tuning = {"choice": choice, "ms_per_step_by_candidate": report,
+                  "default": autotune.DEFAULT}
+        reset()
+        torch.cuda.synchronize(dev)
+
     if engine == "sorted":
         eng.stats_buf.zero_()
         # the phase breakdown: the step's C-ABI calls one by one, with events
@@ -444,6 +455,9 @@ def run_gb300(args):
                                   "from the same initial state"},
               "phases_ms": phase_ms, "mass_rel_err": mass_err,
               "gpu_launches": gpu_launches}
+    if tuning is not None:
+        result["config"]["tuning"] = tuning["choice"]
+        result["autotune"] = tuning
     if engine == "sorted":
         result["particles_outside_tile"] = eng.stats
         if eng.stats.get("tma_wait_timeout"):

@@ -214,6 +214,23 @@ enum pmgb_fft_path { PMGB_FFT_CUFFT = 0, PMGB_FFT_FUSED = 1, PMGB_FFT_OWN = 2 };
 int pmgb_set_fft_path(int path);
 int pmgb_fft_path(void);
 
+/* Launch choices of the tile-sorted run loop (process-wide, read at every
+ * launch): the quarters of the tiles the gather deals to its CTAs
+ * statically before the rest go to whichever CTA asks first (0 to 4;
+ * default 3), and the CTAs per SM of the gather and of the re-sort (0, the
+ * default: as many as fit; otherwise at most that many).  Set by the
+ * autotuner (jaxpm_gb300/autotune.py), which times the candidates on the
+ * caller's own workload.  No counterpart in the reference: XLA picks the
+ * launch shapes of its scatter and gather (painting.py:43-44, :104-106). */
+typedef struct {
+  int gather_static_quarters;
+  int gather_ctas_per_sm;
+  int resort_ctas_per_sm;
+  int reserved[5];
+} pmgb_tuning;
+int pmgb_get_tuning(pmgb_tuning *out);
+int pmgb_set_tuning(const pmgb_tuning *in);
+
 /* ---- Fourier-space force kernel (jaxpm/pm.py:49-56) --------------------- */
 
 /* The spectral part of pm_forces on a real density mesh (pm.py:30-56 from

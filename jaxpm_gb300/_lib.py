@@ -63,6 +63,8 @@ SIGNATURES = {
     "pmgb_fft3_r2c_f32": (c_int, [P, P, c_int, c_int, c_int, c_int, P]),
     "pmgb_fft3_c2r_f32": (c_int, [P, P, c_int, c_int, c_int, c_int, P]),
     "pmgb_set_fft_path": (c_int, [c_int]),
+    "pmgb_get_tuning": (c_int, [P]),
+    "pmgb_set_tuning": (c_int, [P]),
     "pmgb_fft_path": (c_int, []),
     "pmgb_mesh_forces_workspace_size": (c_size_t, [c_int, c_int, c_int]),
     "pmgb_mesh_forces_f32": (c_int, [P, P, c_int, c_int, c_int, c_float, P, c_size_t, P]),
@@ -159,6 +161,30 @@ def sim_table(shapes, counts):
         arr[i].reserved = 0
         arr[i].np = int(n)
     return arr
+
+
+class Tuning(ctypes.Structure):
+    """``pmgb_tuning``: launch choices of the tile-sorted run loop."""
+    _fields_ = [("gather_static_quarters", ctypes.c_int32),
+                ("gather_ctas_per_sm", ctypes.c_int32),
+                ("resort_ctas_per_sm", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 5)]
+
+
+def get_tuning():
+    t = Tuning()
+    call("pmgb_get_tuning", ctypes.byref(t))
+    return {"gather_static_quarters": t.gather_static_quarters,
+            "gather_ctas_per_sm": t.gather_ctas_per_sm,
+            "resort_ctas_per_sm": t.resort_ctas_per_sm}
+
+
+def set_tuning(gather_static_quarters=3, gather_ctas_per_sm=0, resort_ctas_per_sm=0):
+    t = Tuning()
+    t.gather_static_quarters = int(gather_static_quarters)
+    t.gather_ctas_per_sm = int(gather_ctas_per_sm)
+    t.resort_ctas_per_sm = int(resort_ctas_per_sm)
+    call("pmgb_set_tuning", ctypes.byref(t))
 
 
 class PmgbError(RuntimeError):

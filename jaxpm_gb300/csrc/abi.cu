@@ -249,6 +249,34 @@ int pmgb_set_fft_path(int path) {
 
 int pmgb_fft_path(void) { return spectral_mode(); }
 
+int pmgb_get_tuning(pmgb_tuning *out) {
+  BEGIN();
+  NEED(out);
+  const Tuning t = tuning();
+  *out = pmgb_tuning{};
+  out->gather_static_quarters = t.gather_static_quarters;
+  out->gather_ctas_per_sm = t.gather_ctas_per_sm;
+  out->resort_ctas_per_sm = t.resort_ctas_per_sm;
+  return PMGB_OK;
+}
+
+int pmgb_set_tuning(const pmgb_tuning *in) {
+  BEGIN();
+  NEED(in);
+  PMGB_REQUIRE(in->gather_static_quarters >= 0 && in->gather_static_quarters <= 4,
+               "gather_static_quarters must lie in [0, 4]");
+  PMGB_REQUIRE(in->gather_ctas_per_sm >= 0 && in->gather_ctas_per_sm <= 32,
+               "gather_ctas_per_sm must lie in [0, 32]");
+  PMGB_REQUIRE(in->resort_ctas_per_sm >= 0 && in->resort_ctas_per_sm <= 32,
+               "resort_ctas_per_sm must lie in [0, 32]");
+  Tuning t;
+  t.gather_static_quarters = in->gather_static_quarters;
+  t.gather_ctas_per_sm = in->gather_ctas_per_sm;
+  t.resort_ctas_per_sm = in->resort_ctas_per_sm;
+  set_tuning(t);
+  return PMGB_OK;
+}
+
 int pmgb_fft3_r2c_f32(const float *in, void *out, int nx, int ny, int nz, int batch,
                       pmgb_stream_t stream) {
   BEGIN();

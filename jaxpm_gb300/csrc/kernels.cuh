@@ -135,6 +135,18 @@ struct PermIO {
   unsigned *stay_out = nullptr;  // with key_out: per tile, how many stayed
 };
 
+// Launch choices of the sorted loop that the autotuner sets (process-wide):
+// the quarters of the tiles the gather deals statically (the rest from a
+// counter), and the CTAs per SM of the gather and of the re-sort (0: as many
+// as fit).
+struct Tuning {
+  int gather_static_quarters = 3;
+  int gather_ctas_per_sm = 0;
+  int resort_ctas_per_sm = 0;
+};
+Tuning tuning();
+void set_tuning(const Tuning &t);
+
 int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz,
                const float *pos, float *pos_out, float *vel, int64_t np,
                float kick, float drift, void *sort_ws, size_t sort_bytes,

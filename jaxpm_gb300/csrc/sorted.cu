@@ -16,6 +16,7 @@
 // from its own unwrapped position; the box only changes where partial sums
 // are accumulated and where mesh values are read from.
 #include <map>
+#include <mutex>
 #include <algorithm>
 #include <cstring>
 
@@ -636,7 +637,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
                  unsigned *__restrict__ stats, const __grid_constant__ CUtensorMap tmap,
                  int use_tma, float *__restrict__ mesh_next, int pvec,
                  const __grid_constant__ CUtensorMap pmap, int use_ptma,
-                 unsigned *__restrict__ work, const PermIO io) {
+                 unsigned *__restrict__ work, const PermIO io, int quarters) {
   __shared__ __align__(128) float fb[2][FBOX_STRIDE];
   __shared__ __align__(16) float ff[POT ? FBOX : 4];  // POT: the tile's force box
   __shared__ __align__(8) uint64_t bar[2];
@@ -658,7 +659,7 @@ rkd_tiles_kernel(const float *__restrict__ f3, int64_t cs, int nx, int ny, int n
   // latency hides behind a tile's work.
   uint32_t key = blockIdx.x;
   if (key >= nkeys) return;
-  const TileSchedule sched(nkeys, 3);
+  const TileSchedule sched(nkeys, (uint32_t)quarters);
   uint32_t knext = gridDim.x + blockIdx.x;  // tiles 0 and 1 are static
   uint32_t it = 0;                          // index of the current tile
   TileInfo cur = tile_info(offsets, key, nx, ny, nz, use_tma, POT);
@@ -1218,6 +1219,21 @@ __global__ void scan_add_kernel(unsigned *__restrict__ out, int64_t n,
 // ---------------------------------------------------------------------------
 int64_t tile_key_count(int nx, int ny, int nz) { return (int64_t)1 << (3 * tile_bits(nx, ny, nz)); }
 
+namespace {
+std::mutex g_tune_mu;
+Tuning g_tune;
+}  // namespace
+
+Tuning tuning() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  return g_tune;
+}
+
+void set_tuning(const Tuning &t) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune = t;
+}
+
 static int set_smem(const void *fn, int bytes) {
   PMGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
   return PMGB_OK;
@@ -1466,8 +1482,11 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz, const float 
   PMGB_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
 #define RKD_ARGS                                                                             \
   f3, cs, nx, ny, nz, pos, pos_out, vel, sc.offsets, (uint32_t)keys, kick, drift, sc.counts, \
-      sc.rank, stats, map, use_tma, mesh_next, aligned ? 1 : 0, pmap, use_ptma, work, io
-  const unsigned grid = (unsigned)std::min<int64_t>(keys, (int64_t)sm_count() * per_sm);
+      sc.rank, stats, map, use_tma, mesh_next, aligned ? 1 : 0, pmap, use_ptma, work, io, \
+      tu.gather_static_quarters
+  const Tuning tu = tuning();
+  const int use_sm = tu.gather_ctas_per_sm > 0 ? std::min(per_sm, tu.gather_ctas_per_sm) : per_sm;
+  const unsigned grid = (unsigned)std::min<int64_t>(keys, (int64_t)sm_count() * use_sm);
   switch (variant) {
     case 0: rkd_tiles_kernel<false, false><<<grid, TILE_THREADS, dsmem, s>>>(RKD_ARGS); break;
     case 1: rkd_tiles_kernel<true, false><<<grid, TILE_THREADS, dsmem, s>>>(RKD_ARGS); break;
@@ -1511,9 +1530,11 @@ int index_resort(int64_t np, int nx, int ny, int nz, const unsigned *perm_old,
   SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
   PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
   if (np > 0) {
-    index_scatter_kernel<<<wave_grid(index_scatter_kernel,
-                                     (np + ISCATTER_ILP - 1) / ISCATTER_ILP, 256),
-                           256, 0, s>>>(reinterpret_cast<const uint2 *>(sc.rank), np,
+    unsigned grid = wave_grid(index_scatter_kernel, (np + ISCATTER_ILP - 1) / ISCATTER_ILP, 256);
+    const Tuning tu = tuning();
+    if (tu.resort_ctas_per_sm > 0)
+      grid = (unsigned)std::min<int64_t>(grid, (int64_t)sm_count() * tu.resort_ctas_per_sm);
+    index_scatter_kernel<<<grid, 256, 0, s>>>(reinterpret_cast<const uint2 *>(sc.rank), np,
                                         sc.offsets, sc.stay, perm_new, perm_old, id_in, id_out);
     PMGB_LAUNCHED("index_scatter_kernel");
   }
