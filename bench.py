@@ -567,8 +567,9 @@ def run_gb300(args):
 
     # end to end with the state in pinned host memory (SortedFastPM.run_host):
     # every step copies positions and velocities (caller's order) up, sorts
-    # them by tile, runs pmgb_fpm_step_sorted_f32, returns them to the
-    # caller's order and copies them back; the copies go in E2E_CHUNKS chunks
+    # them by tile, paints them, takes the potential, runs the gather that
+    # kicks and drifts them in place, returns them to the caller's order and
+    # copies them back; the copies go in E2E_CHUNKS chunks
     # on two copy streams, chunk c of step i+1's input going up as soon as
     # chunk c of step i's result is down
     if "e2e" not in skip:
@@ -596,7 +597,9 @@ def run_gb300(args):
                          "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                          "ms_per_step": ems / K, "repeats": rep,
                          "api": "SortedFastPM.run_host: pmgb_tile_sort_f32 + "
-                                "pmgb_fpm_step_sorted_f32 + pmgb_unpermute3_f32 (C ABI) per "
+                                "pmgb_cic_paint_sorted_f32 + pmgb_mesh_potential_f32 + "
+                                "pmgb_read_potential_kick_drift_paint_perm_f32 + "
+                                "pmgb_unpermute3_f32 (C ABI) per "
                                 "step, pinned host buffers, copies in "
                                 f"{E2E_CHUNKS} chunks on two copy streams (each result chunk "
                                 "back before the next step's copy of it goes up)",

@@ -222,7 +222,12 @@ class SortedFastPM:
         step copying them up, sorting
         them by tile (``pmgb_tile_sort_f32``), stepping
         (``pmgb_fpm_step_sorted_f32``), returning them to the caller's order
-        (``pmgb_unpermute3_f32``) and copying them back.  The copies go in
+        (``pmgb_unpermute3_f32``) and copying them back.  Where the potential
+        pipeline serves the mesh the step is the run loop's: sorted paint,
+        potential (``pmgb_mesh_potential_f32``), the gather deriving the
+        forces from it and updating the sorted state in place
+        (``pmgb_read_potential_kick_drift_paint_perm_f32``), then straight
+        back to the caller's order, with no second sort.  The copies go in
         ``chunks`` chunks on two copy streams: chunk c of the next step's
         input goes up as soon as chunk c of this step's result is down, so
         the read-back and the next upload share the host link's two
@@ -246,6 +251,14 @@ class SortedFastPM:
             self._host_bufs = (torch.empty((self.n, 3), **f), torch.empty((self.n, 3), **f),
                                torch.cuda.Stream(dev), torch.cuda.Stream(dev))
         dx, dv, up, down = self._host_bufs
+        lib = _lib.load()
+        pot_path = (bool(lib.pmgb_fft3_supported(nx, ny, nz)) and lib.pmgb_fft_path() != 0 and
+                    nz % 4 == 0)
+        if pot_path and not hasattr(self, "_pot_bufs"):
+            mb = lib.pmgb_mesh_forces_workspace_size(nx, ny, nz)
+            f = dict(dtype=torch.float32, device=dev)
+            self._pot_bufs = (torch.empty((nx, ny, nz), **f), torch.empty((nx, ny, nz), **f),
+                              torch.empty(mb, dtype=torch.uint8, device=dev), mb)
         bounds = np.linspace(0, self.n, int(chunks) + 1).astype(np.int64)
         parts = [slice(int(a), int(b)) for a, b in zip(bounds[:-1], bounds[1:])]
         came_down = [torch.cuda.Event() for _ in parts]
@@ -263,15 +276,31 @@ class SortedFastPM:
             _lib.call("pmgb_tile_sort_f32", _lib.ptr(dx), _lib.ptr(dv), None, self.n, nx, ny, nz,
                       _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]), _lib.ptr(self.ids[0]),
                       _lib.ptr(self.sort_ws), self.sort_bytes, s)
-            _lib.call("pmgb_fpm_step_sorted_f32", _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]),
-                      _lib.ptr(self.ids[0]), _lib.ptr(self.pos[1]), _lib.ptr(self.vel[1]),
-                      _lib.ptr(self.ids[1]), self.n, nx, ny, nz, float(self.kick[start + i]),
-                      float(self.drift[start + i]), self.r_split, _lib.ptr(self.ws),
-                      self.ws_bytes, _lib.ptr(self.sort_ws), self.sort_bytes, None, None, None,
-                      _lib.ptr(self.stats_buf), s)
-            _lib.call("pmgb_unpermute3_f32", _lib.ptr(self.pos[1]), _lib.ptr(self.ids[1]),
+            kick, drift = float(self.kick[start + i]), float(self.drift[start + i])
+            if pot_path:
+                mesh, pot, mws, mb = self._pot_bufs
+                _lib.call("pmgb_cic_paint_sorted_f32", _lib.ptr(mesh), nx, ny, nz,
+                          _lib.ptr(self.pos[0]), self.n, _lib.ptr(self.sort_ws), self.sort_bytes,
+                          _lib.ptr(self.stats_buf), s)
+                _lib.call("pmgb_mesh_potential_f32", _lib.ptr(mesh), _lib.ptr(pot), nx, ny, nz,
+                          self.r_split, _lib.ptr(mws), mb, s)
+                _lib.call("pmgb_read_potential_kick_drift_paint_perm_f32", _lib.ptr(pot), nx, ny,
+                          nz, _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]), None,
+                          _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]), self.n, kick, drift,
+                          None, _lib.ptr(self.sort_ws), self.sort_bytes,
+                          _lib.ptr(self.stats_buf), s)
+                out = 0
+            else:
+                _lib.call("pmgb_fpm_step_sorted_f32", _lib.ptr(self.pos[0]),
+                          _lib.ptr(self.vel[0]), _lib.ptr(self.ids[0]), _lib.ptr(self.pos[1]),
+                          _lib.ptr(self.vel[1]), _lib.ptr(self.ids[1]), self.n, nx, ny, nz, kick,
+                          drift, self.r_split, _lib.ptr(self.ws), self.ws_bytes,
+                          _lib.ptr(self.sort_ws), self.sort_bytes, None, None, None,
+                          _lib.ptr(self.stats_buf), s)
+                out = 1
+            _lib.call("pmgb_unpermute3_f32", _lib.ptr(self.pos[out]), _lib.ptr(self.ids[out]),
                       self.n, _lib.ptr(dx), s)
-            _lib.call("pmgb_unpermute3_f32", _lib.ptr(self.vel[1]), _lib.ptr(self.ids[1]),
+            _lib.call("pmgb_unpermute3_f32", _lib.ptr(self.vel[out]), _lib.ptr(self.ids[out]),
                       self.n, _lib.ptr(dv), s)
             computed.record(stream)
             with torch.cuda.stream(down):
@@ -282,7 +311,13 @@ class SortedFastPM:
                     came_down[c].record(down)
         stream.wait_stream(down)
         if n > 0:
-            self.cur = 1  # the engine's buffers hold the last step's sorted state
+            if pot_path:  # the engine's buffers: the last state, sorted by tile again
+                _lib.call("pmgb_tile_sort_f32", _lib.ptr(dx), _lib.ptr(dv), None, self.n, nx, ny,
+                          nz, _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]),
+                          _lib.ptr(self.ids[0]), _lib.ptr(self.sort_ws), self.sort_bytes, s)
+                self.cur = 0
+            else:
+                self.cur = 1  # the engine's buffers hold the last step's sorted state
         if check:
             self.check(s)
 

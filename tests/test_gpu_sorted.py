@@ -444,6 +444,18 @@ def test_run_host_matches_device_run(cuda):
     torch.cuda.synchronize(cuda)
     assert rel_l2(hx.numpy() - x0, x.cpu().numpy() - x0) < 1e-5
     assert rel_l2(hv.numpy() - v0, v.cpu().numpy() - v0) < 1e-4
+    # the engine holds the same final state, in tile order again
+    ex, ev = eng.state()
+    assert torch.equal(ex.cpu(), hx) and torch.equal(ev.cpu(), hv)
+    # two calls over the halves of the run (start=) equal one call
+    hx2 = torch.from_numpy(x0.copy()).pin_memory()
+    hv2 = torch.from_numpy(v0.copy()).pin_memory()
+    eng.run_host(hx2, hv2, steps=2)
+    eng.run_host(hx2, hv2, steps=2, start=2)
+    torch.cuda.synchronize(cuda)
+    assert rel_l2(hx2.numpy() - x0, hx.numpy() - x0) < 1e-5
+    with pytest.raises(ValueError):
+        eng.run_host(hx2, hv2, steps=3, start=2)
     with pytest.raises(ValueError):
         eng.run_host(torch.from_numpy(x0.copy()), torch.from_numpy(v0.copy()))
 
