@@ -475,9 +475,12 @@ def run_gb300(args):
     # roofline)
     if use_pot:
         # the potential pipeline: plane R2C 4 + 4, x pass 4 + 4, plane C2R
-        # 4 + 4; the gather reads the potential (4) instead of three force
-        # meshes (12)
-        alg = {"forces": 24.0, "read_kick_drift": 56.0}
+        # 4 + 4.  The run loop's permuted gather: the potential 4, positions
+        # and velocities 24 read through the permutation (4) and 24 written,
+        # the (new tile key, stayer rank) pair 8, the next density 4.  The
+        # re-sort: the pairs 8, the new permutation 4, the ids following the
+        # old one 4 + 4 + 4.
+        alg = {"forces": 24.0, "read_kick_drift": 68.0, "sort": 24.0}
     elif engine == "sorted":
         alg = {"forces": 48.0, "read_kick_drift": 64.0}
     else:
