@@ -569,12 +569,10 @@ def run_gb300(args):
         del plain, xp, vp
 
     # end to end with the state in pinned host memory (SortedFastPM.run_host):
-    # every step copies positions and velocities (caller's order) up, sorts
-    # them by tile, paints them, takes the potential, runs the gather that
-    # kicks and drifts them in place, returns them to the caller's order and
-    # copies them back; the copies go in E2E_CHUNKS chunks
-    # on two copy streams, chunk c of step i+1's input going up as soon as
-    # chunk c of step i's result is down
+    # every step copies positions and velocities (caller's order) up in
+    # E2E_CHUNKS pieces, paints each piece as it lands, evaluates the forces,
+    # gathers + kicks + drifts each piece and copies it back as soon as it is
+    # done; piece c of step i+1 goes up as soon as piece c of step i is down
     if "e2e" not in skip:
         hx = x0.cpu().pin_memory()
         hv = v0.cpu().pin_memory()
@@ -599,13 +597,13 @@ def run_gb300(args):
         result["e2e"] = {"value": world * Np * K / (ems / 1e3), "unit": "particle-steps/s",
                          "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": nbytes,
                          "ms_per_step": ems / K, "repeats": rep,
-                         "api": "SortedFastPM.run_host: pmgb_tile_sort_f32 + "
-                                "pmgb_cic_paint_sorted_f32 + pmgb_mesh_potential_f32 + "
-                                "pmgb_read_potential_kick_drift_paint_perm_f32 + "
-                                "pmgb_unpermute3_f32 (C ABI) per "
-                                "step, pinned host buffers, copies in "
-                                f"{E2E_CHUNKS} chunks on two copy streams (each result chunk "
-                                "back before the next step's copy of it goes up)",
+                         "api": "SortedFastPM.run_host: per step and piece "
+                                "pmgb_cic_paint_f32 (binned, accumulating) as the piece "
+                                "lands, pmgb_mesh_forces_f32, per piece "
+                                "pmgb_read3_kick_drift_f32 then its copy down (C ABI); "
+                                f"pinned host buffers, {E2E_CHUNKS} pieces on two copy "
+                                "streams, piece c of the next step up as soon as piece c "
+                                "of this one is down",
                          "pk_vs_timed_run": {"max_rel_dev_per_bin": float(rel.max()),
                                              "bins": int(rel.size)}}
         del hx, hv

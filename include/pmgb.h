@@ -378,6 +378,23 @@ int pmgb_unpermute3_f32(const float *in, const uint32_t *id, int64_t np,
 int pmgb_permute3_f32(const float *in, const uint32_t *id, int64_t np,
                       float *out, pmgb_stream_t stream);
 
+/* pmgb_tile_sort_f32 that also records dest[p], the slot particle p went
+ * to: out[p] = sorted[dest[p]] (pmgb_gather3_f32) returns a sorted array to
+ * the caller's order with coalesced writes, in any number of pieces. */
+int pmgb_tile_sort_dest_f32(const float *pos, const float *vel,
+                            const uint32_t *id, int64_t np, int nx, int ny,
+                            int nz, float *pos_out, float *vel_out,
+                            uint32_t *id_out, uint32_t *dest, void *workspace,
+                            size_t workspace_bytes, pmgb_stream_t stream);
+
+/* out[p] = in[idx[p]] for p < n, in an [n_in][3] array (entries of idx at
+ * or past n_in are skipped); out must not overlap in.  With idx = dest + a
+ * and out = caller_array + 3 a it fills rows a .. a+n-1 of the caller's
+ * order: the pieces a run returns to the host as each one is ready.  No
+ * counterpart in the reference (JAX arrays never leave their order). */
+int pmgb_gather3_f32(const float *in, int64_t n_in, const uint32_t *idx,
+                     int64_t n, float *out, pmgb_stream_t stream);
+
 /* Failure check of the tile-staged kernels: waits for `stream`, reads the
  * three counters a tile kernel kept in `stats` and returns
  * PMGB_ERR_CUDA if [2] is set, i.e. a wait on a TMA transfer reached its

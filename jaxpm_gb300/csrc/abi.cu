@@ -535,6 +535,37 @@ int pmgb_unpermute3_f32(const float *in, const uint32_t *id, int64_t np, float *
   return unpermute3(in, id, np, out, stream);
 }
 
+int pmgb_tile_sort_dest_f32(const float *pos, const float *vel, const uint32_t *id, int64_t np,
+                            int nx, int ny, int nz, float *pos_out, float *vel_out,
+                            uint32_t *id_out, uint32_t *dest, void *workspace,
+                            size_t workspace_bytes, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_sortable(nx, ny, nz, np));
+  if (np == 0) return PMGB_OK;
+  NEED(pos);
+  NEED(pos_out);
+  NEED(id_out);
+  NEED(dest);
+  PMGB_REQUIRE((vel == nullptr) == (vel_out == nullptr), "vel and vel_out must both be given");
+  PMGB_REQUIRE(pos != pos_out && (!vel || vel != vel_out) && (!id || id != id_out),
+               "the sort cannot run in place");
+  return tile_sort(pos, vel, id, np, nx, ny, nz, pos_out, vel_out, id_out, workspace,
+                   workspace_bytes, stream, dest);
+}
+
+int pmgb_gather3_f32(const float *in, int64_t n_in, const uint32_t *idx, int64_t n, float *out,
+                     pmgb_stream_t stream) {
+  BEGIN();
+  NONNEG(n_in);
+  NONNEG(n);
+  if (n == 0) return PMGB_OK;
+  NEED(in);
+  NEED(idx);
+  NEED(out);
+  PMGB_REQUIRE(out + 3 * n <= in || in + 3 * n_in <= out, "the gather cannot overlap its source");
+  return gather3(in, n_in, idx, n, out, stream);
+}
+
 int pmgb_permute3_f32(const float *in, const uint32_t *id, int64_t np, float *out,
                       pmgb_stream_t stream) {
   BEGIN();

@@ -102,13 +102,18 @@ int paint_box(float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
               const float *weights, float wscale, unsigned *stats, cudaStream_t s);
 int64_t tile_key_count(int nx, int ny, int nz);
 size_t sort_workspace_size(int nx, int ny, int nz, int64_t np);
+// dest (nullable): dest[p] = the slot particle p went to.
 int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np,
               int nx, int ny, int nz, float *pos2, float *vel2, unsigned *id2,
-              void *ws, size_t bytes, cudaStream_t s);
+              void *ws, size_t bytes, cudaStream_t s, unsigned *dest = nullptr);
 int unpermute3(const float *in, const unsigned *id, int64_t np, float *out,
                cudaStream_t s);
 int permute3(const float *in, const unsigned *id, int64_t np, float *out,
              cudaStream_t s);
+// out[p] = in[idx[p]] for p < n, idx into an [n_in][3] array (entries >= n_in
+// skipped).
+int gather3(const float *in, int64_t n_in, const unsigned *idx, int64_t n,
+            float *out, cudaStream_t s);
 int paint_sorted(float *mesh, int nx, int ny, int nz, const float *pos,
                  int64_t np, void *sort_ws, size_t sort_bytes, unsigned *stats,
                  cudaStream_t s);

@@ -1122,12 +1122,13 @@ __global__ void unpermute3_kernel(const float *__restrict__ in, const unsigned *
 }
 
 // out[p] = in[id[p]] for [np][3] arrays (caller's order -> tile order).
+// out[p] = in[id[p]] for p < np, id indexing an [n_in][3] array
 __global__ void permute3_kernel(const float *__restrict__ in, const unsigned *__restrict__ id,
-                                int64_t np, float *__restrict__ out) {
+                                int64_t np, float *__restrict__ out, int64_t n_in) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
        p += (int64_t)gridDim.x * blockDim.x) {
     int64_t s = __ldg(id + p);
-    if (s >= np) continue;  // not a permutation entry: skipped
+    if (s >= n_in) continue;  // not an entry of the source: skipped
     out[3 * p] = __ldg(in + 3 * s);
     out[3 * p + 1] = __ldg(in + 3 * s + 1);
     out[3 * p + 2] = __ldg(in + 3 * s + 2);
@@ -1334,7 +1335,7 @@ static unsigned scatter_grid(int64_t np) {
 
 int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np, int nx, int ny,
               int nz, float *pos2, float *vel2, unsigned *id2, void *ws, size_t bytes,
-              cudaStream_t s) {
+              cudaStream_t s, unsigned *dest) {
   PMGB_TRY(check_sort_ws(ws, bytes, nx, ny, nz, np));
   const int64_t keys = tile_key_count(nx, ny, nz);
   SortScratch sc = sort_scratch(ws, nx, ny, nz, np);
@@ -1347,8 +1348,7 @@ int tile_sort(const float *pos, const float *vel, const unsigned *id, int64_t np
   PMGB_TRY(exclusive_scan(sc.counts, sc.offsets, keys, sc.sums, (unsigned)np, s));
   if (np > 0) {
     scatter_kernel<<<scatter_grid(np), 256, 0, s>>>(pos, vel, id, sc.rank, np, nx, ny, nz,
-                                                    sc.offsets, nullptr, pos2, vel2, id2,
-                                                    nullptr);
+                                                    sc.offsets, nullptr, pos2, vel2, id2, dest);
     PMGB_LAUNCHED("scatter_kernel");
   }
   return PMGB_OK;
@@ -1363,7 +1363,15 @@ int unpermute3(const float *in, const unsigned *id, int64_t np, float *out, cuda
 
 int permute3(const float *in, const unsigned *id, int64_t np, float *out, cudaStream_t s) {
   if (np == 0) return PMGB_OK;
-  permute3_kernel<<<wave_grid(permute3_kernel, np, 256), 256, 0, s>>>(in, id, np, out);
+  permute3_kernel<<<wave_grid(permute3_kernel, np, 256), 256, 0, s>>>(in, id, np, out, np);
+  PMGB_LAUNCHED("permute3_kernel");
+  return PMGB_OK;
+}
+
+int gather3(const float *in, int64_t n_in, const unsigned *idx, int64_t n, float *out,
+            cudaStream_t s) {
+  if (n == 0) return PMGB_OK;
+  permute3_kernel<<<wave_grid(permute3_kernel, n, 256), 256, 0, s>>>(in, idx, n, out, n_in);
   PMGB_LAUNCHED("permute3_kernel");
   return PMGB_OK;
 }

@@ -214,27 +214,35 @@ class SortedFastPM:
     def ids_current(self):
         return self.ids[self.cur]
 
-    def run_host(self, hpos, hvel, steps=None, chunks=16, start=0, check=True):
+    def run_host(self, hpos, hvel, steps=None, chunks=16, start=0, check=True,
+                 paint_mode="binned"):
         """Steps a state that lives in pinned host memory: ``hpos``/``hvel``
         ([Np, 3] float32, caller's order) are updated in place after each of
         steps ``start .. start+steps-1`` (default: all remaining; a range
-        past the engine's steps raises before any work is queued), each
-        step copying them up, sorting
-        them by tile (``pmgb_tile_sort_f32``), stepping
-        (``pmgb_fpm_step_sorted_f32``), returning them to the caller's order
-        (``pmgb_unpermute3_f32``) and copying them back.  Where the potential
-        pipeline serves the mesh the step is the run loop's: sorted paint,
-        potential (``pmgb_mesh_potential_f32``), the gather deriving the
-        forces from it and updating the sorted state in place
-        (``pmgb_read_potential_kick_drift_paint_perm_f32``), then straight
-        back to the caller's order, with no second sort.  The copies go in
-        ``chunks`` chunks on two copy streams: chunk c of the next step's
-        input goes up as soon as chunk c of this step's result is down, so
-        the read-back and the next upload share the host link's two
-        directions.  With ``check`` (default) it waits for the steps and
-        raises if a kernel reported a failed wait; otherwise it returns when
-        the last copy has been issued (ordered before later work on the
-        current stream)."""
+        past the engine's steps raises before any work is queued); every
+        step copies them up, steps them and copies them back, in ``chunks``
+        pieces on two copy streams.
+
+        Where the potential pipeline serves the mesh the step is streamed
+        through the host link: each piece is painted
+        (``pmgb_cic_paint_f32``, ``paint_mode``, accumulating) as soon as it
+        has landed, the forces follow the last piece
+        (``pmgb_mesh_forces_f32``: the potential and its order-1 gradient
+        stencil), and each piece is gathered, kicked and drifted
+        (``pmgb_read3_kick_drift_f32``) and goes back down as soon as it is
+        done; piece c of the next step goes up as soon as piece c of this
+        one is down.  The link then carries both directions while the
+        pieces are painted and gathered, and only the force evaluation
+        leaves it idle.  Otherwise each step sorts the state by tile
+        (``pmgb_tile_sort_f32``), runs the composite step
+        (``pmgb_fpm_step_sorted_f32``) and returns it to the caller's order
+        (``pmgb_unpermute3_f32``) before copying it back.
+
+        After the call the engine holds the last state, sorted by tile.
+        With ``check`` (default) it waits for the steps and raises if a
+        kernel reported a failed wait; otherwise it returns when the last
+        copy has been issued (ordered before later work on the current
+        stream)."""
         if not (hpos.is_pinned() and hvel.is_pinned()):
             raise ValueError("run_host needs pinned host tensors")
         start = int(start)
@@ -242,6 +250,8 @@ class SortedFastPM:
         if start < 0 or n < 0 or start + n > self.n_steps:
             raise ValueError(f"steps {start}..{start + n - 1} outside the engine's "
                              f"{self.n_steps} steps")
+        if paint_mode not in ("atomic", "binned", "deterministic"):
+            raise ValueError(f"unknown paint_mode {paint_mode!r}")
         nx, ny, nz = self.mesh_shape
         dev = self.ws.device
         stream = torch.cuda.current_stream(dev)
@@ -252,72 +262,93 @@ class SortedFastPM:
                                torch.cuda.Stream(dev), torch.cuda.Stream(dev))
         dx, dv, up, down = self._host_bufs
         lib = _lib.load()
-        pot_path = (bool(lib.pmgb_fft3_supported(nx, ny, nz)) and lib.pmgb_fft_path() != 0 and
+        streamed = (bool(lib.pmgb_fft3_supported(nx, ny, nz)) and lib.pmgb_fft_path() != 0 and
                     nz % 4 == 0)
-        if pot_path and not hasattr(self, "_pot_bufs"):
-            mb = lib.pmgb_mesh_forces_workspace_size(nx, ny, nz)
-            f = dict(dtype=torch.float32, device=dev)
-            self._pot_bufs = (torch.empty((nx, ny, nz), **f), torch.empty((nx, ny, nz), **f),
-                              torch.empty(mb, dtype=torch.uint8, device=dev), mb)
         bounds = np.linspace(0, self.n, int(chunks) + 1).astype(np.int64)
         parts = [slice(int(a), int(b)) for a, b in zip(bounds[:-1], bounds[1:])]
         came_down = [torch.cuda.Event() for _ in parts]
-        went_up, computed = torch.cuda.Event(), torch.cuda.Event()
+        ready = [torch.cuda.Event() for _ in parts]
+        went_up = [torch.cuda.Event() for _ in parts]
         up.wait_stream(stream)
-        for i in range(n):
+
+        def upload(i, c, sl):
             with torch.cuda.stream(up):
+                if i > 0:
+                    up.wait_event(came_down[c])
+                dx[sl].copy_(hpos[sl], non_blocking=True)
+                dv[sl].copy_(hvel[sl], non_blocking=True)
+                went_up[c].record(up)
+
+        def download(c, sl):
+            with torch.cuda.stream(down):
+                down.wait_event(ready[c])
+                hpos[sl].copy_(dx[sl], non_blocking=True)
+                hvel[sl].copy_(dv[sl], non_blocking=True)
+                came_down[c].record(down)
+
+        if streamed:
+            from .painting import MODES
+            mode = MODES[paint_mode]
+            big = max(sl.stop - sl.start for sl in parts)
+            key = (paint_mode, big)
+            if getattr(self, "_stream_key", None) != key:
+                mb = lib.pmgb_mesh_forces_workspace_size(nx, ny, nz)
+                pb = max(int(lib.pmgb_cic_paint_workspace_size(nx, ny, nz, big, mode)), 1)
+                f = dict(dtype=torch.float32, device=dev)
+                self._stream_bufs = (torch.empty((nx, ny, nz), **f),
+                                     torch.empty((3, nx, ny, nz), **f),
+                                     torch.empty(mb, dtype=torch.uint8, device=dev), mb,
+                                     torch.empty(pb, dtype=torch.uint8, device=dev), pb)
+                self._stream_key = key
+            mesh, f3, mws, mb, pws, pb = self._stream_bufs
+            cs = nx * ny * nz
+            for i in range(n):
+                kick, drift = float(self.kick[start + i]), float(self.drift[start + i])
+                # the density, piece by piece as the pieces land
                 for c, sl in enumerate(parts):
-                    if i > 0:
-                        up.wait_event(came_down[c])
-                    dx[sl].copy_(hpos[sl], non_blocking=True)
-                    dv[sl].copy_(hvel[sl], non_blocking=True)
-                went_up.record(up)
-            stream.wait_event(went_up)
-            _lib.call("pmgb_tile_sort_f32", _lib.ptr(dx), _lib.ptr(dv), None, self.n, nx, ny, nz,
-                      _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]), _lib.ptr(self.ids[0]),
-                      _lib.ptr(self.sort_ws), self.sort_bytes, s)
-            kick, drift = float(self.kick[start + i]), float(self.drift[start + i])
-            if pot_path:
-                mesh, pot, mws, mb = self._pot_bufs
-                _lib.call("pmgb_cic_paint_sorted_f32", _lib.ptr(mesh), nx, ny, nz,
-                          _lib.ptr(self.pos[0]), self.n, _lib.ptr(self.sort_ws), self.sort_bytes,
-                          _lib.ptr(self.stats_buf), s)
-                _lib.call("pmgb_mesh_potential_f32", _lib.ptr(mesh), _lib.ptr(pot), nx, ny, nz,
+                    upload(i, c, sl)
+                    stream.wait_event(went_up[c])
+                    _lib.call("pmgb_cic_paint_f32", _lib.ptr(mesh), nx, ny, nz, _lib.ptr(dx[sl]),
+                              sl.stop - sl.start, None, 1.0, mode, 1 if c else 0, _lib.ptr(pws),
+                              pb, s)
+                _lib.call("pmgb_mesh_forces_f32", _lib.ptr(mesh), _lib.ptr(f3), nx, ny, nz,
                           self.r_split, _lib.ptr(mws), mb, s)
-                _lib.call("pmgb_read_potential_kick_drift_paint_perm_f32", _lib.ptr(pot), nx, ny,
-                          nz, _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]), None,
-                          _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]), self.n, kick, drift,
-                          None, _lib.ptr(self.sort_ws), self.sort_bytes,
-                          _lib.ptr(self.stats_buf), s)
-                out = 0
-            else:
+                # gather + kick + drift piece by piece, each piece down when done
+                for c, sl in enumerate(parts):
+                    _lib.call("pmgb_read3_kick_drift_f32", _lib.ptr(f3), cs, nx, ny, nz,
+                              _lib.ptr(dx[sl]), _lib.ptr(dv[sl]), sl.stop - sl.start, kick,
+                              drift, None, s)
+                    ready[c].record(stream)
+                    download(c, sl)
+        else:
+            for i in range(n):
+                kick, drift = float(self.kick[start + i]), float(self.drift[start + i])
+                for c, sl in enumerate(parts):
+                    upload(i, c, sl)
+                for ev in went_up:
+                    stream.wait_event(ev)
+                _lib.call("pmgb_tile_sort_f32", _lib.ptr(dx), _lib.ptr(dv), None, self.n, nx, ny,
+                          nz, _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]),
+                          _lib.ptr(self.ids[0]), _lib.ptr(self.sort_ws), self.sort_bytes, s)
                 _lib.call("pmgb_fpm_step_sorted_f32", _lib.ptr(self.pos[0]),
                           _lib.ptr(self.vel[0]), _lib.ptr(self.ids[0]), _lib.ptr(self.pos[1]),
                           _lib.ptr(self.vel[1]), _lib.ptr(self.ids[1]), self.n, nx, ny, nz, kick,
                           drift, self.r_split, _lib.ptr(self.ws), self.ws_bytes,
                           _lib.ptr(self.sort_ws), self.sort_bytes, None, None, None,
                           _lib.ptr(self.stats_buf), s)
-                out = 1
-            _lib.call("pmgb_unpermute3_f32", _lib.ptr(self.pos[out]), _lib.ptr(self.ids[out]),
-                      self.n, _lib.ptr(dx), s)
-            _lib.call("pmgb_unpermute3_f32", _lib.ptr(self.vel[out]), _lib.ptr(self.ids[out]),
-                      self.n, _lib.ptr(dv), s)
-            computed.record(stream)
-            with torch.cuda.stream(down):
-                down.wait_event(computed)
+                _lib.call("pmgb_unpermute3_f32", _lib.ptr(self.pos[1]), _lib.ptr(self.ids[1]),
+                          self.n, _lib.ptr(dx), s)
+                _lib.call("pmgb_unpermute3_f32", _lib.ptr(self.vel[1]), _lib.ptr(self.ids[1]),
+                          self.n, _lib.ptr(dv), s)
                 for c, sl in enumerate(parts):
-                    hpos[sl].copy_(dx[sl], non_blocking=True)
-                    hvel[sl].copy_(dv[sl], non_blocking=True)
-                    came_down[c].record(down)
+                    ready[c].record(stream)
+                    download(c, sl)
         stream.wait_stream(down)
-        if n > 0:
-            if pot_path:  # the engine's buffers: the last state, sorted by tile again
-                _lib.call("pmgb_tile_sort_f32", _lib.ptr(dx), _lib.ptr(dv), None, self.n, nx, ny,
-                          nz, _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]),
-                          _lib.ptr(self.ids[0]), _lib.ptr(self.sort_ws), self.sort_bytes, s)
-                self.cur = 0
-            else:
-                self.cur = 1  # the engine's buffers hold the last step's sorted state
+        if n > 0:  # the engine's buffers: the last state, sorted by tile
+            _lib.call("pmgb_tile_sort_f32", _lib.ptr(dx), _lib.ptr(dv), None, self.n, nx, ny, nz,
+                      _lib.ptr(self.pos[0]), _lib.ptr(self.vel[0]), _lib.ptr(self.ids[0]),
+                      _lib.ptr(self.sort_ws), self.sort_bytes, s)
+            self.cur = 0
         if check:
             self.check(s)
 

@@ -54,6 +54,47 @@ def test_tile_sort_is_a_sorting_permutation(cuda, lib, shape):
     assert torch.equal(fwd, p2)
 
 
+@pytest.mark.parametrize("shape", [(64, 64, 64), (48, 40, 72)])
+def test_tile_sort_dest_and_gather3_pieces(cuda, lib, shape):
+    """dest is the inverse of the sort's ids, and gather3 over the pieces of
+    dest returns the sorted arrays to the caller's order bit for bit; index
+    entries at or past n_in leave their rows untouched."""
+    from jaxpm_gb300 import _lib
+    n = int(np.prod(shape))
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(0, shape[0], (n, 3)).astype(np.float32)
+    vel = rng.standard_normal((n, 3)).astype(np.float32)
+    p, v = T(pos, cuda), T(vel, cuda)
+    p2, v2 = torch.empty_like(p), torch.empty_like(v)
+    ids = torch.empty(n, dtype=torch.int32, device=cuda)
+    dest = torch.empty(n, dtype=torch.int32, device=cuda)
+    wsb = lib.pmgb_tile_sort_workspace_size(*shape, n)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=cuda)
+    _lib.call("pmgb_tile_sort_dest_f32", _lib.ptr(p), _lib.ptr(v), None, n, *shape, _lib.ptr(p2),
+              _lib.ptr(v2), _lib.ptr(ids), _lib.ptr(dest), _lib.ptr(ws), wsb, _lib.stream())
+    i, d = ids.cpu().numpy(), dest.cpu().numpy()
+    assert np.array_equal(i[d], np.arange(n)) and np.array_equal(d[i], np.arange(n))
+    bounds = np.linspace(0, n, 8).astype(np.int64)
+    back_p, back_v = torch.full_like(p, -1.0), torch.full_like(v, -1.0)
+    for a, b in zip(bounds[:-1], bounds[1:]):
+        a, b = int(a), int(b)
+        _lib.call("pmgb_gather3_f32", _lib.ptr(p2), n, _lib.ptr(dest[a:b]), b - a,
+                  _lib.ptr(back_p[a:b]), _lib.stream())
+        _lib.call("pmgb_gather3_f32", _lib.ptr(v2), n, _lib.ptr(dest[a:b]), b - a,
+                  _lib.ptr(back_v[a:b]), _lib.stream())
+    assert torch.equal(back_p, p) and torch.equal(back_v, v)
+    # rows whose index is past the source are skipped
+    idx = torch.tensor([0, n, 1, 2 * n], dtype=torch.int32, device=cuda)
+    out = torch.full((4, 3), 7.0, device=cuda)
+    _lib.call("pmgb_gather3_f32", _lib.ptr(p2), n, _lib.ptr(idx), 4, _lib.ptr(out), _lib.stream())
+    o = out.cpu().numpy()
+    assert np.array_equal(o[0], pos[i[0]]) and np.array_equal(o[2], pos[i[1]])
+    assert np.all(o[1] == 7.0) and np.all(o[3] == 7.0)
+    with pytest.raises(Exception):
+        _lib.call("pmgb_gather3_f32", _lib.ptr(p2), n, _lib.ptr(dest), n, _lib.ptr(p2),
+                  _lib.stream())
+
+
 def sorted_state(cuda, lib, pos, vel, shape):
     """Tile-sorts (pos, vel); returns sorted tensors, ids and the sort
     workspace holding the ranges."""
@@ -424,12 +465,17 @@ def test_tile_schedule_dynamic_tails_128(cuda):
     assert eng.stats["tma_wait_timeout"] == 0
 
 
-def test_run_host_matches_device_run(cuda):
+@pytest.mark.parametrize("shape,paint_mode", [((64, 64, 64), "binned"),
+                                              ((64, 64, 64), "atomic"),
+                                              ((64, 64, 64), "deterministic"),
+                                              ((48, 40, 72), "binned")])
+def test_run_host_matches_device_run(cuda, shape, paint_mode):
     """SortedFastPM.run_host (state in pinned host memory, copies chunked and
     overlapped across steps) equals the device run loop from the same
-    state."""
+    state: the streamed schedule (pieces painted as they land, gathered and
+    sent back as they are done) on the potential pipeline's shapes, the
+    sorted composite step on the others."""
     from jaxpm_gb300 import cosmology, simulate
-    shape = (64, 64, 64)
     rng = np.random.default_rng(51)
     lat = cic.lattice(shape).reshape(-1, 3)
     x0 = (lat + rng.normal(0, 0.8, lat.shape)).astype(np.float32)
@@ -440,7 +486,7 @@ def test_run_host_matches_device_run(cuda):
     x, v = eng.state()
     hx = torch.from_numpy(x0.copy()).pin_memory()
     hv = torch.from_numpy(v0.copy()).pin_memory()
-    eng.run_host(hx, hv, chunks=5)
+    eng.run_host(hx, hv, chunks=5, paint_mode=paint_mode)
     torch.cuda.synchronize(cuda)
     assert rel_l2(hx.numpy() - x0, x.cpu().numpy() - x0) < 1e-5
     assert rel_l2(hv.numpy() - v0, v.cpu().numpy() - v0) < 1e-4
@@ -450,14 +496,16 @@ def test_run_host_matches_device_run(cuda):
     # two calls over the halves of the run (start=) equal one call
     hx2 = torch.from_numpy(x0.copy()).pin_memory()
     hv2 = torch.from_numpy(v0.copy()).pin_memory()
-    eng.run_host(hx2, hv2, steps=2)
-    eng.run_host(hx2, hv2, steps=2, start=2)
+    eng.run_host(hx2, hv2, steps=2, paint_mode=paint_mode)
+    eng.run_host(hx2, hv2, steps=2, start=2, paint_mode=paint_mode)
     torch.cuda.synchronize(cuda)
     assert rel_l2(hx2.numpy() - x0, hx.numpy() - x0) < 1e-5
     with pytest.raises(ValueError):
         eng.run_host(hx2, hv2, steps=3, start=2)
     with pytest.raises(ValueError):
         eng.run_host(torch.from_numpy(x0.copy()), torch.from_numpy(v0.copy()))
+    with pytest.raises(ValueError):
+        eng.run_host(hx2, hv2, steps=1, paint_mode="nearest")
 
 
 def test_permuted_gather_abi_pieces_compose_to_the_run(cuda, lib):
