@@ -42,6 +42,20 @@ int sm_count() {
   return n;
 }
 
+int64_t l2_bytes() {
+  static std::mutex mu;
+  static std::map<int, int64_t> cache;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = cache.find(dev);
+  if (it != cache.end()) return it->second;
+  int b = 0;
+  if (cudaDeviceGetAttribute(&b, cudaDevAttrL2CacheSize, dev) != cudaSuccess || b < 0) b = 0;
+  cache[dev] = b;
+  return b;
+}
+
 int resident_ctas(const void *kernel, int threads, size_t smem) {
   static std::mutex mu;
   static std::map<std::tuple<const void *, int, int, size_t>, int> cache;

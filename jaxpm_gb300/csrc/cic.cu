@@ -82,9 +82,10 @@ __global__ void fixed_to_float_kernel(float *__restrict__ mesh,
 // ---------------------------------------------------------------------------
 // Readers.
 // ---------------------------------------------------------------------------
+// out[p * ostride] = the CIC read of `mesh` at particle p.
 __global__ void __launch_bounds__(256)
 read_kernel(const float *__restrict__ mesh, int nx, int ny, int nz,
-            const float *__restrict__ pos, int64_t np, float *__restrict__ out) {
+            const float *__restrict__ pos, int64_t np, float *__restrict__ out, int ostride) {
   for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
        p += (int64_t)gridDim.x * blockDim.x) {
     float x, y, z;
@@ -98,7 +99,7 @@ read_kernel(const float *__restrict__ mesh, int nx, int ny, int nz,
       s += __ldg(mesh + cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
                                    conn_z(n) ? az.i1 : az.i0, ny, nz)) * w;
     }
-    out[p] = s;
+    out[p * ostride] = s;
   }
 }
 
@@ -372,14 +373,31 @@ int paint_fixed_into(unsigned long long *acc, float *mesh, int nx, int ny, int n
 int read(const float *mesh, int nx, int ny, int nz, const float *pos, int64_t np,
          float *out, cudaStream_t s) {
   if (np == 0) return PMGB_OK;
-  read_kernel<<<wave_grid(read_kernel, np, 256), 256, 0, s>>>(mesh, nx, ny, nz, pos, np, out);
+  read_kernel<<<wave_grid(read_kernel, np, 256), 256, 0, s>>>(mesh, nx, ny, nz, pos, np, out,
+                                                              1);
   PMGB_LAUNCHED("read_kernel");
   return PMGB_OK;
 }
 
+// Three components in one pass when their meshes fit in L2 together (or
+// none does), else one pass per component: a particle order that is random
+// over the mesh then keeps one mesh resident in L2 at a time instead of
+// missing in all three (16.7M particles on 256^3, 64 MB per mesh: uniform
+// 3.75 ms in one pass, 1.23 ms in three; clustered 0.70 -> 0.48 ms), for
+// 12 B more of positions per particle and pass.
 int read3(const float *mesh3, int64_t cs, int nx, int ny, int nz, const float *pos,
           int64_t np, float *out, cudaStream_t s) {
   if (np == 0) return PMGB_OK;
+  const int64_t mesh_bytes = (int64_t)nx * ny * nz * (int64_t)sizeof(float);
+  const int64_t l2 = l2_bytes();
+  if (l2 > 0 && 3 * mesh_bytes > (l2 * 3) / 4 && 2 * mesh_bytes <= l2) {
+    for (int c = 0; c < 3; ++c) {
+      read_kernel<<<wave_grid(read_kernel, np, 256), 256, 0, s>>>(mesh3 + c * cs, nx, ny, nz,
+                                                                  pos, np, out + c, 3);
+      PMGB_LAUNCHED("read_kernel");
+    }
+    return PMGB_OK;
+  }
   read3_kernel<<<wave_grid(read3_kernel, np, 256), 256, 0, s>>>(
       mesh3, cs, nx, ny, nz, pos, np, out);
   PMGB_LAUNCHED("read3_kernel");

@@ -19,6 +19,8 @@ void clear_error();
 
 // Number of SMs of the current device (cached per device).
 int sm_count();
+// L2 cache bytes of the current device (cached per device).
+int64_t l2_bytes();
 
 #define PMGB_CUDA(call)                                                     \
   do {                                                                      \
