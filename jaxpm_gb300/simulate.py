@@ -224,16 +224,17 @@ class SortedFastPM:
         pieces on two copy streams.
 
         Where the potential pipeline serves the mesh the step is streamed
-        through the host link: each piece is painted
-        (``pmgb_cic_paint_f32``, ``paint_mode``, accumulating) as soon as it
-        has landed, the forces follow the last piece
+        through the host link: the position pieces go up first and each is
+        painted (``pmgb_cic_paint_f32``, ``paint_mode``, accumulating) as
+        soon as it has landed; the velocity pieces follow and are in flight
+        while the forces are evaluated after the last position piece
         (``pmgb_mesh_forces_f32``: the potential and its order-1 gradient
-        stencil), and each piece is gathered, kicked and drifted
-        (``pmgb_read3_kick_drift_f32``) and goes back down as soon as it is
-        done; piece c of the next step goes up as soon as piece c of this
-        one is down.  The link then carries both directions while the
-        pieces are painted and gathered, and only the force evaluation
-        leaves it idle.  Otherwise each step sorts the state by tile
+        stencil); each piece is then gathered, kicked and drifted
+        (``pmgb_read3_kick_drift_f32``) and goes back down, positions
+        before velocities, and piece c of the next step's positions
+        (velocities) goes up as soon as piece c of this step's positions
+        (velocities) is down.  The link then carries both directions
+        through the whole step.  Otherwise each step sorts the state by tile
         (``pmgb_tile_sort_f32``), runs the composite step
         (``pmgb_fpm_step_sorted_f32``) and returns it to the caller's order
         (``pmgb_unpermute3_f32``) before copying it back.
@@ -269,6 +270,11 @@ class SortedFastPM:
         came_down = [torch.cuda.Event() for _ in parts]
         ready = [torch.cuda.Event() for _ in parts]
         went_up = [torch.cuda.Event() for _ in parts]
+        # the streamed schedule's positions and velocities, piece by piece
+        pos_down = [torch.cuda.Event() for _ in parts]
+        vel_down = [torch.cuda.Event() for _ in parts]
+        pos_up = [torch.cuda.Event() for _ in parts]
+        vel_up = [torch.cuda.Event() for _ in parts]
         up.wait_stream(stream)
 
         def upload(i, c, sl):
@@ -304,22 +310,41 @@ class SortedFastPM:
             cs = nx * ny * nz
             for i in range(n):
                 kick, drift = float(self.kick[start + i]), float(self.drift[start + i])
-                # the density, piece by piece as the pieces land
+                # the density, piece by piece as the position pieces land
                 for c, sl in enumerate(parts):
-                    upload(i, c, sl)
-                    stream.wait_event(went_up[c])
+                    with torch.cuda.stream(up):
+                        if i > 0:
+                            up.wait_event(pos_down[c])
+                        dx[sl].copy_(hpos[sl], non_blocking=True)
+                        pos_up[c].record(up)
+                    stream.wait_event(pos_up[c])
                     _lib.call("pmgb_cic_paint_f32", _lib.ptr(mesh), nx, ny, nz, _lib.ptr(dx[sl]),
                               sl.stop - sl.start, None, 1.0, mode, 1 if c else 0, _lib.ptr(pws),
                               pb, s)
+                # the velocities go up while the forces are evaluated
+                with torch.cuda.stream(up):
+                    for c, sl in enumerate(parts):
+                        if i > 0:
+                            up.wait_event(vel_down[c])
+                        dv[sl].copy_(hvel[sl], non_blocking=True)
+                        vel_up[c].record(up)
                 _lib.call("pmgb_mesh_forces_f32", _lib.ptr(mesh), _lib.ptr(f3), nx, ny, nz,
                           self.r_split, _lib.ptr(mws), mb, s)
-                # gather + kick + drift piece by piece, each piece down when done
+                # gather + kick + drift piece by piece; positions down first
                 for c, sl in enumerate(parts):
+                    stream.wait_event(vel_up[c])
                     _lib.call("pmgb_read3_kick_drift_f32", _lib.ptr(f3), cs, nx, ny, nz,
                               _lib.ptr(dx[sl]), _lib.ptr(dv[sl]), sl.stop - sl.start, kick,
                               drift, None, s)
                     ready[c].record(stream)
-                    download(c, sl)
+                    with torch.cuda.stream(down):
+                        down.wait_event(ready[c])
+                        hpos[sl].copy_(dx[sl], non_blocking=True)
+                        pos_down[c].record(down)
+                with torch.cuda.stream(down):
+                    for c, sl in enumerate(parts):
+                        hvel[sl].copy_(dv[sl], non_blocking=True)
+                        vel_down[c].record(down)
         else:
             for i in range(n):
                 kick, drift = float(self.kick[start + i]), float(self.drift[start + i])
