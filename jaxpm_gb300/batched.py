@@ -34,6 +34,7 @@ class BatchedFastPM:
         self.shapes = [tuple(int(v) for v in s) for s in mesh_shapes]
         if len(cosmos) != len(self.shapes):
             raise ValueError("one cosmology per simulation is required")
+        self._setup = (list(cosmos), float(a0), float(a1))
         self.n_sims = len(self.shapes)
         self.counts = ([int(np.prod(s)) for s in self.shapes] if n_particles is None
                        else [int(n) for n in n_particles])
@@ -92,6 +93,73 @@ class BatchedFastPM:
         for i in range(start, start + (self.n_steps - start if steps is None else steps)):
             self.step(pos, vel, i)
         return pos, vel
+
+    def run_host(self, hpos, hvel, steps=None, start=0, groups=4):
+        """Steps a batch whose state lives in pinned host memory (``[sum np,
+        3]`` float32, table order, updated in place after each step): every
+        step copies the particles up, steps them and copies them back.  The
+        simulations are split into ``groups`` runs of about equal particle
+        counts, each stepped by its own table (``pmgb_fpm_step_batched_f32``
+        on the group's simulations): group g's upload, step and read-back
+        follow one another, and since the simulations are independent the
+        groups overlap, so the host link carries both directions while the
+        groups compute.  Group g of the next step goes up as soon as group g
+        of this one is down.  Returns when the last copy has been issued
+        (ordered before later work on the current stream)."""
+        if not (hpos.is_pinned() and hvel.is_pinned()):
+            raise ValueError("run_host needs pinned host tensors")
+        if hpos.numel() != 3 * self.n or hvel.numel() != 3 * self.n:
+            raise ValueError(f"expected [{self.n}, 3] particles")
+        start = int(start)
+        n = (self.n_steps - start) if steps is None else int(steps)
+        if start < 0 or n < 0 or start + n > self.n_steps:
+            raise ValueError(f"steps {start}..{start + n - 1} outside the engine's "
+                             f"{self.n_steps} steps")
+        groups = max(1, min(int(groups), self.n_sims))
+        if getattr(self, "_groups_key", None) != groups:
+            # cut the table where the running particle count passes g/groups
+            cum = self.offsets[1:]
+            cuts = [0]
+            for g in range(1, groups):
+                c = int(np.searchsorted(cum, self.n * g / groups)) + 1
+                if cuts[-1] < c < self.n_sims:
+                    cuts.append(c)
+            cuts.append(self.n_sims)
+            cosmos, a0, a1 = self._setup
+            self._subs = [(BatchedFastPM(self.shapes[a:b], cosmos[a:b], a0, a1, self.n_steps,
+                                         n_particles=self.counts[a:b], r_split=self.r_split,
+                                         device=self.device),
+                           slice(int(self.offsets[a]), int(self.offsets[b])))
+                          for a, b in zip(cuts[:-1], cuts[1:])]
+            f = dict(dtype=torch.float32, device=self.device)
+            self._host_bufs = (torch.empty((self.n, 3), **f), torch.empty((self.n, 3), **f),
+                               torch.cuda.Stream(self.device), torch.cuda.Stream(self.device))
+            self._groups_key = groups
+        dx, dv, up, down = self._host_bufs
+        stream = torch.cuda.current_stream(self.device)
+        s = _lib.stream(self.device)
+        hp, hv = hpos.reshape(-1, 3), hvel.reshape(-1, 3)
+        went_up = [torch.cuda.Event() for _ in self._subs]
+        ready = [torch.cuda.Event() for _ in self._subs]
+        came_down = [torch.cuda.Event() for _ in self._subs]
+        up.wait_stream(stream)
+        for i in range(n):
+            for g, (eng, sl) in enumerate(self._subs):
+                with torch.cuda.stream(up):
+                    if i > 0:
+                        up.wait_event(came_down[g])
+                    dx[sl].copy_(hp[sl], non_blocking=True)
+                    dv[sl].copy_(hv[sl], non_blocking=True)
+                    went_up[g].record(up)
+                stream.wait_event(went_up[g])
+                eng.step(dx[sl], dv[sl], start + i, stream=s)
+                ready[g].record(stream)
+                with torch.cuda.stream(down):
+                    down.wait_event(ready[g])
+                    hp[sl].copy_(dx[sl], non_blocking=True)
+                    hv[sl].copy_(dv[sl], non_blocking=True)
+                    came_down[g].record(down)
+        stream.wait_stream(down)
 
     def capture(self, pos, vel):
         """A CUDA graph of the whole run on the buffers ``pos`` / ``vel``

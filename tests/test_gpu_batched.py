@@ -284,3 +284,36 @@ def test_batched_groups_at_unaligned_offsets(cuda):
                                         drift[:, s], b.split(gx)[s].cpu().numpy(),
                                         b.split(gv)[s].cpu().numpy())
         assert rel_l2(b.split(gxb)[s].cpu(), gxr) < 1e-4, s
+
+
+@pytest.mark.parametrize("groups", [1, 3, 8])
+def test_batched_run_host_matches_device_run(cuda, groups):
+    """BatchedFastPM.run_host (state in pinned host memory, the simulations
+    streamed through the host link in groups that overlap) equals the device
+    run from the same state; two calls over the halves of the run equal one
+    call; a range past the engine's steps raises before any copy."""
+    from jaxpm_gb300 import batched
+    K = 4
+    b = batched.BatchedFastPM(SHAPES, cosmos(len(SHAPES), 3), 0.1, 1.0, K, device=cuda)
+    parts = [perturbed_lattice(s, 10 + i) for i, s in enumerate(SHAPES)]
+    x0 = np.concatenate(parts)
+    rng = np.random.default_rng(5)
+    v0 = rng.normal(0, 0.3, x0.shape).astype(np.float32)
+    x, v = T(x0, cuda), T(v0, cuda)
+    b.run(x, v)
+    hx = torch.from_numpy(x0.copy()).pin_memory()
+    hv = torch.from_numpy(v0.copy()).pin_memory()
+    b.run_host(hx, hv, groups=groups)
+    torch.cuda.synchronize(cuda)
+    assert rel_l2(hx.numpy() - x0, x.cpu().numpy() - x0) < TOL
+    assert rel_l2(hv.numpy() - v0, v.cpu().numpy() - v0) < 1e-4
+    hx2 = torch.from_numpy(x0.copy()).pin_memory()
+    hv2 = torch.from_numpy(v0.copy()).pin_memory()
+    b.run_host(hx2, hv2, steps=2, groups=groups)
+    b.run_host(hx2, hv2, steps=2, start=2, groups=groups)
+    torch.cuda.synchronize(cuda)
+    assert rel_l2(hx2.numpy() - x0, hx.numpy() - x0) < TOL
+    with pytest.raises(ValueError):
+        b.run_host(hx2, hv2, steps=3, start=2)
+    with pytest.raises(ValueError):
+        b.run_host(torch.from_numpy(x0.copy()), torch.from_numpy(v0.copy()))
