@@ -103,3 +103,27 @@ def test_forward_model_host_scalar_derivatives():
     k, d = ode.fpm_coefficients(fm.cosmology_of(t0), 0.1, 1.0, 8)
     assert np.allclose(out.detach().numpy()[4:12], k, rtol=1e-12)
     assert np.allclose(out.detach().numpy()[12:], d, rtol=1e-12)
+
+
+def test_reference_arm_line_on_a_small_mesh(capsys):
+    """bench.py --impl reference prints one JSON line with the contract's
+    keys, the GPU arm's metric and the workload it ran (the oracle on the
+    full workload at the given mesh; 16^3 here so it runs in seconds)."""
+    import json
+    import sys
+    import bench
+    argv = sys.argv
+    sys.argv = ["bench.py", "--impl", "reference", "--mesh", "16", "--steps", "2",
+                "--warmup", "1"]
+    try:
+        bench.main()
+    finally:
+        sys.argv = argv
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "impl", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["steps"] == 2 and line["value"] > 0
+    assert line["config"]["particles"] == 16 ** 3 and line["config"]["mesh"] == [16] * 3
+    assert line["cpu_baseline"]["kind"] == "port"
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
