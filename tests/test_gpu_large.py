@@ -1,6 +1,7 @@
 """Parity at full size: the 256^3 single-simulation configuration (2LPT to
-a = 0.1, 20 FastPM steps to a = 1, box 256 Mpc/h) against the oracle's own
-run of it (``tests/golden/large_256_20.npz``, made by
+a = 0.1, 20 FastPM steps to a = 1, box 256 Mpc/h) and the 512^3 large one
+(40 steps, box 512 Mpc/h) against the oracle's own runs of them
+(``tests/golden/large_256_20.npz``, ``large_512_40.npz``, made by
 ``tests/golden/make_large_golden.py`` in float32 and float64 from the same
 PCG64 white noise).
 
@@ -21,7 +22,7 @@ from conftest import GOLDEN, rel_l2
 
 pytestmark = pytest.mark.gpu
 
-PATH = os.path.join(GOLDEN, "large_256_20.npz")
+FIXTURES = ["large_256_20.npz", "large_512_40.npz"]
 
 
 def gpu_initial_state(n, box, seed, dev):
@@ -45,11 +46,12 @@ def lattice_sample(n, idx):
     return np.stack([i // (n * n), (i // n) % n, i % n], -1).astype(np.float64)
 
 
-@pytest.fixture(scope="module")
-def c2(cuda):
-    if not os.path.exists(PATH):
-        pytest.fail(f"fixture missing: {PATH}")
-    d = dict(np.load(PATH))
+@pytest.fixture(scope="module", params=FIXTURES)
+def c2(cuda, request):
+    path = os.path.join(GOLDEN, request.param)
+    if not os.path.exists(path):
+        pytest.fail(f"fixture missing: {path}")
+    d = dict(np.load(path))
     from jaxpm_gb300 import simulate
     n, box = int(d["n"]), float(d["box"])
     cosmo, x0, v0 = gpu_initial_state(n, box, int(d["seed"]), cuda)

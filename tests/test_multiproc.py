@@ -32,9 +32,9 @@ def worker(rank, world, port, out):
 def test_two_rank_replicas():
     world = 2
     port = free_port()
-    with mp.Manager() as m:
+    ctx = mp.get_context("spawn")  # nothing forks a process that runs threads
+    with ctx.Manager() as m:
         out = m.dict()
-        ctx = mp.get_context("spawn")
         procs = [ctx.Process(target=worker, args=(r, world, port, out)) for r in range(world)]
         for p in procs:
             p.start()
