@@ -87,7 +87,10 @@ def test_c2_initial_state_matches_oracle(c2):
     np.testing.assert_allclose(k, d["k"], rtol=1e-6)
     assert np.max(np.abs(pk0 / d["pk0_32"] - 1)) < 1e-4
     lat = lattice_sample(n, d["sample"])
-    assert rel_l2(x0 - lat, d["x0_32"] - lat) < 1e-5
+    # positions are absolute float32 cell coordinates up to n: their rounding,
+    # 2^-24 n, against displacements of about a cell grows with the mesh
+    tol = 1e-5 * max(1.0, n / 256)
+    assert rel_l2(x0 - lat, d["x0_32"] - lat) < tol
     assert rel_l2(v0, d["v0_32"]) < 1e-5
 
 
