@@ -218,7 +218,10 @@ int pmgb_fft_path(void);
  * launch): the quarters of the tiles the gather deals to its CTAs
  * statically before the rest go to whichever CTA asks first (0 to 4;
  * default 3), and the CTAs per SM of the gather and of the re-sort (0, the
- * default: as many as fit; otherwise at most that many).  Set by the
+ * default: as many as fit; otherwise at most that many), and the priority
+ * of the re-sort's stream (0, the default: the device's highest, so its
+ * blocks go ahead of the next force evaluation's; 1: the default priority,
+ * so they fill in beside it).  Set by the
  * autotuner (jaxpm_gb300/autotune.py), which times the candidates on the
  * caller's own workload.  No counterpart in the reference: XLA picks the
  * launch shapes of its scatter and gather (painting.py:43-44, :104-106). */
@@ -226,7 +229,8 @@ typedef struct {
   int gather_static_quarters;
   int gather_ctas_per_sm;
   int resort_ctas_per_sm;
-  int reserved[5];
+  int resort_priority;
+  int reserved[4];
 } pmgb_tuning;
 int pmgb_get_tuning(pmgb_tuning *out);
 int pmgb_set_tuning(const pmgb_tuning *in);

@@ -171,7 +171,8 @@ class Tuning(ctypes.Structure):
     _fields_ = [("gather_static_quarters", ctypes.c_int32),
                 ("gather_ctas_per_sm", ctypes.c_int32),
                 ("resort_ctas_per_sm", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 5)]
+                ("resort_priority", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 4)]
 
 
 def get_tuning():
@@ -179,14 +180,17 @@ def get_tuning():
     call("pmgb_get_tuning", ctypes.byref(t))
     return {"gather_static_quarters": t.gather_static_quarters,
             "gather_ctas_per_sm": t.gather_ctas_per_sm,
-            "resort_ctas_per_sm": t.resort_ctas_per_sm}
+            "resort_ctas_per_sm": t.resort_ctas_per_sm,
+            "resort_priority": t.resort_priority}
 
 
-def set_tuning(gather_static_quarters=3, gather_ctas_per_sm=0, resort_ctas_per_sm=0):
+def set_tuning(gather_static_quarters=3, gather_ctas_per_sm=0, resort_ctas_per_sm=0,
+               resort_priority=0):
     t = Tuning()
     t.gather_static_quarters = int(gather_static_quarters)
     t.gather_ctas_per_sm = int(gather_ctas_per_sm)
     t.resort_ctas_per_sm = int(resort_ctas_per_sm)
+    t.resort_priority = int(resort_priority)
     call("pmgb_set_tuning", ctypes.byref(t))
 
 

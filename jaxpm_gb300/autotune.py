@@ -24,10 +24,17 @@ import torch
 
 from . import _lib
 
-DEFAULT = {"gather_static_quarters": 3, "gather_ctas_per_sm": 0, "resort_ctas_per_sm": 0}
+DEFAULT = {"gather_static_quarters": 3, "gather_ctas_per_sm": 0, "resort_ctas_per_sm": 0,
+           "resort_priority": 0}
 
-CANDIDATES = {"gather_static_quarters": (2, 3, 4), "gather_ctas_per_sm": (0, 3),
-              "resort_ctas_per_sm": (0, 4)}
+# Measured at 512^3 (40 steps) before narrowing: a fourth static quarter and
+# 3 gather CTAs per SM were never faster (0.5 ms per step slower); 1-4
+# re-sort CTAs per SM leave it latency-bound (6.3-8.3 ms per step against
+# 6.27 with a full wave), 5-7 let the force evaluation run beside it (6.19
+# at 6); the default stream priority for the re-sort was no faster there
+# (6.27-6.32) but stays a candidate.
+CANDIDATES = {"gather_static_quarters": (2, 3), "gather_ctas_per_sm": (0,),
+              "resort_ctas_per_sm": (0, 5, 6, 7), "resort_priority": (0, 1)}
 
 _LOCK = threading.Lock()
 

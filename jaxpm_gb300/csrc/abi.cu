@@ -107,7 +107,7 @@ static int check_mode(int mode) {
 
 extern "C" {
 
-int pmgb_version(void) { return 100; }
+int pmgb_version(void) { return 101; }
 
 uint64_t pmgb_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
@@ -271,6 +271,7 @@ int pmgb_get_tuning(pmgb_tuning *out) {
   out->gather_static_quarters = t.gather_static_quarters;
   out->gather_ctas_per_sm = t.gather_ctas_per_sm;
   out->resort_ctas_per_sm = t.resort_ctas_per_sm;
+  out->resort_priority = t.resort_priority;
   return PMGB_OK;
 }
 
@@ -283,10 +284,13 @@ int pmgb_set_tuning(const pmgb_tuning *in) {
                "gather_ctas_per_sm must lie in [0, 32]");
   PMGB_REQUIRE(in->resort_ctas_per_sm >= 0 && in->resort_ctas_per_sm <= 32,
                "resort_ctas_per_sm must lie in [0, 32]");
+  PMGB_REQUIRE(in->resort_priority == 0 || in->resort_priority == 1,
+               "resort_priority must be 0 or 1");
   Tuning t;
   t.gather_static_quarters = in->gather_static_quarters;
   t.gather_ctas_per_sm = in->gather_ctas_per_sm;
   t.resort_ctas_per_sm = in->resort_ctas_per_sm;
+  t.resort_priority = in->resort_priority;
   set_tuning(t);
   return PMGB_OK;
 }

@@ -148,6 +148,7 @@ struct Tuning {
   int gather_static_quarters = 3;
   int gather_ctas_per_sm = 0;
   int resort_ctas_per_sm = 0;
+  int resort_priority = 0;  // 0: the highest stream priority, 1: the default
 };
 Tuning tuning();
 void set_tuning(const Tuning &t);

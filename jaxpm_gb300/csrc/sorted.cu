@@ -1611,7 +1611,8 @@ int fpm_step_sorted(const float *pos, float *vel, const unsigned *id, float *pos
 // thread and device, created on first use: make the first run call outside
 // any stream capture).
 struct Aux {
-  cudaStream_t s2 = nullptr;
+  cudaStream_t s2 = nullptr;   // the highest priority
+  cudaStream_t s2d = nullptr;  // the default priority
   cudaEvent_t gathered = nullptr, sorted = nullptr;
 };
 
@@ -1627,6 +1628,7 @@ static int aux_stream(Aux **out) {
     int least = 0, greatest = 0;
     PMGB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
     PMGB_CUDA(cudaStreamCreateWithPriority(&x.s2, cudaStreamNonBlocking, greatest));
+    PMGB_CUDA(cudaStreamCreateWithFlags(&x.s2d, cudaStreamNonBlocking));
     PMGB_CUDA(cudaEventCreateWithFlags(&x.gathered, cudaEventDisableTiming));
     PMGB_CUDA(cudaEventCreateWithFlags(&x.sorted, cudaEventDisableTiming));
   }
@@ -1654,6 +1656,8 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, flo
   unsigned *I[2] = {id_a, id_b};
   Aux *aux;
   PMGB_TRY(aux_stream(&aux));
+  // the re-sort's stream (Tuning::resort_priority)
+  cudaStream_t s2 = tuning().resort_priority ? aux->s2d : aux->s2;
   // Forces from the potential where the spectral pipeline serves the mesh:
   // one inverse transform instead of three, the order-1 gradient taken by
   // the gather as the equivalent real-space stencil (f3 then holds the
@@ -1698,21 +1702,21 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, flo
     // i+1 (from the density the gather just painted) are independent: they
     // touch disjoint buffers and overlap
     PMGB_CUDA(cudaEventRecord(aux->gathered, s));
-    PMGB_CUDA(cudaStreamWaitEvent(aux->s2, aux->gathered, 0));
+    PMGB_CUDA(cudaStreamWaitEvent(s2, aux->gathered, 0));
     if (!last) {
       // ids follow the gather (from the order it read), perm is rebuilt
       PMGB_TRY(index_resort(np, nx, ny, nz, i == 0 ? nullptr : perm[pc], perm[pc ^ 1],
-                            I[cur], I[out], sort_ws, sort_bytes, aux->s2));
+                            I[cur], I[out], sort_ws, sort_bytes, s2));
       pc ^= 1;
       cur = out;
     } else {
-      if (i > 0) PMGB_TRY(gather_u32(I[cur], perm[pc], np, I[out], aux->s2));
+      if (i > 0) PMGB_TRY(gather_u32(I[cur], perm[pc], np, I[out], s2));
       cur = out;
       PMGB_TRY(tile_scatter(P[cur], V[cur], I[cur], np, nx, ny, nz, P[cur ^ 1], V[cur ^ 1],
-                            I[cur ^ 1], nullptr, sort_ws, sort_bytes, aux->s2));
+                            I[cur ^ 1], nullptr, sort_ws, sort_bytes, s2));
       cur ^= 1;
     }
-    PMGB_CUDA(cudaEventRecord(aux->sorted, aux->s2));
+    PMGB_CUDA(cudaEventRecord(aux->sorted, s2));
     if (!last) PMGB_TRY(forces());
   }
   // the state ends in buffer n_steps & 1 (one buffer change per step: none

@@ -141,3 +141,24 @@ def test_failure_check_entry_points_validate_on_the_host(lib):
     with pytest.raises(_lib.PmgbError) as e:
         _lib.call("pmgb_test_wait_timeout", 100, None, None)
     assert "status is NULL" in str(e.value)
+
+
+def test_tuning_round_trip_and_ranges(lib):
+    """pmgb_set_tuning / pmgb_get_tuning round-trip every field and reject
+    values outside their ranges on the host, leaving the settings as they
+    were."""
+    from jaxpm_gb300 import _lib
+    before = _lib.get_tuning()
+    try:
+        _lib.set_tuning(gather_static_quarters=2, gather_ctas_per_sm=3, resort_ctas_per_sm=6,
+                        resort_priority=1)
+        assert _lib.get_tuning() == {"gather_static_quarters": 2, "gather_ctas_per_sm": 3,
+                                     "resort_ctas_per_sm": 6, "resort_priority": 1}
+        for bad in ({"gather_static_quarters": 5}, {"gather_ctas_per_sm": -1},
+                    {"resort_ctas_per_sm": 33}, {"resort_priority": 2}):
+            with pytest.raises(_lib.PmgbError) as e:
+                _lib.set_tuning(**bad)
+            assert e.value.status == 1
+            assert _lib.get_tuning()["resort_ctas_per_sm"] == 6
+    finally:
+        _lib.set_tuning(**before)
