@@ -181,6 +181,45 @@ def peaks():
         return 6800.0, "fallback"
 
 
+def link_rates(ha, hb, dev):
+    """GB/s of the host link for the pinned arrays ha, hb (the same size):
+    ha up alone, ha down alone, and ha up while hb goes down (two streams),
+    each the median of 3 copies timed with CUDA events."""
+    import torch
+    da, db = torch.empty_like(ha, device=dev), torch.empty_like(hb, device=dev)
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    cur = torch.cuda.current_stream(dev)
+    nb = ha.numel() * ha.element_size()
+
+    def timed(fn, nbytes):
+        out = []
+        for _ in range(3):
+            torch.cuda.synchronize(dev)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(cur)
+            fn()
+            b.record(cur)
+            torch.cuda.synchronize(dev)
+            out.append(a.elapsed_time(b))
+        return nbytes / (float(np.median(out)) / 1e3) / 1e9
+
+    def both():
+        s1.wait_stream(cur)
+        s2.wait_stream(cur)
+        with torch.cuda.stream(s1):
+            da.copy_(ha, non_blocking=True)
+        with torch.cuda.stream(s2):
+            hb.copy_(db, non_blocking=True)
+        cur.wait_stream(s1)
+        cur.wait_stream(s2)
+
+    rates = {"up": timed(lambda: da.copy_(ha, non_blocking=True), nb),
+             "down": timed(lambda: ha.copy_(da, non_blocking=True), nb),
+             "both": timed(both, 2 * nb)}
+    del da, db
+    return rates
+
+
 def profile_traffic():
     """Per-launch DRAM bytes of the dominant kernel from the committed ncu
     summary (``profiles/traffic.md``: lines ``kernel: bytes_per_particle``),
@@ -614,6 +653,16 @@ def run_gb300(args):
                                 "of this one is down",
                          "pk_vs_timed_run": {"max_rel_dev_per_bin": float(rel.max()),
                                              "bins": int(rel.size)}}
+        # the host link's own rates (copy engines, pinned memory, the same
+        # buffers): the e2e leg's roofline is its bytes per step over the
+        # two-direction rate
+        link = link_rates(hx, hv, dev)
+        moved = 2.0 * nbytes * K / (ems / 1e3) / 1e9
+        result["e2e"]["link"] = dict(link, unit="GB/s",
+                                     note="copy-engine rates of the pinned buffers: up alone, "
+                                          "down alone, both directions at once")
+        result["e2e"]["link_frac"] = {"achieved_gbs": moved, "peak_gbs": link["both"],
+                                      "frac": moved / link["both"]}
         del hx, hv
 
     # paint / read microbenchmarks (16.7M uniform and clustered particles on
