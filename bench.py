@@ -1016,10 +1016,38 @@ def paint_read_suite(dev, W, K, big=None, skip=()):
         del mesh3, out1, out3
         return res
 
-    results = {}
+    # the L2-resident mesh makes these kernels L2-bound, not HBM-bound: the
+    # library's rates of random atomics and random gathers on a buffer of the
+    # mesh's size (torch's index_add_ / index_select, uniform random indices,
+    # as many as the CIC paint's contributions), against which each paint and
+    # read reports its rate of CIC contributions as a ratio (not a ceiling:
+    # the paint pairs z-neighbours into one vector reduction)
+    cells = n**3
+    m = 8 * Np
+    gidx = torch.randint(0, cells, (m,), device=dev,
+                         generator=torch.Generator(device=dev).manual_seed(5))
+    ones = torch.ones(m, dtype=torch.float32, device=dev)
+    buf = torch.zeros(cells, dtype=torch.float32, device=dev)
+    t_add = timed(lambda: buf.index_add_(0, gidx, ones))
+    t_get = timed(lambda: torch.index_select(buf, 0, gidx))
+    del gidx, ones, buf
+    l2 = {"atomic_adds_per_s": m / (t_add / 1e3), "gathers_per_s": m / (t_get / 1e3),
+          "buffer_bytes": 4 * cells,
+          "how": "torch index_add_ / index_select of 8 x 16,777,216 uniform random "
+                 "indices into a float32 buffer of the 256^3 mesh's size"}
+
+    results = {"l2_reference": l2}
     for dname, pos in [("uniform", uni), ("clustered_a1", clustered)]:
         results[dname] = {"paint": paint_ops(pos, (n,) * 3, dname),
                           "read": read_ops(pos, (n,) * 3, dname)}
+        # each CIC contribution is one atomic (paint) or one load (read)
+        for name, r in results[dname]["paint"].items():
+            if isinstance(r, dict):
+                r["x_library_atomics"] = 8 * Np / (r["ms"] / 1e3) / l2["atomic_adds_per_s"]
+        rd = results[dname]["read"]
+        rd["read"]["x_library_gathers"] = 8 * Np / (rd["read"]["ms"] / 1e3) / l2["gathers_per_s"]
+        rd["read3"]["x_library_gathers"] = (24 * Np / (rd["read3"]["ms"] / 1e3)
+                                             / l2["gathers_per_s"])
     del uni, clustered
     if big is not None and "1024" not in skip:
         torch.cuda.empty_cache()
@@ -1027,8 +1055,9 @@ def paint_read_suite(dev, W, K, big=None, skip=()):
         torch.cuda.empty_cache()
     results["accounting"] = ("paint 12 B/particle read + 4 B/cell written; read 12 B/particle "
                              "positions + 4 B/particle out + the mesh once; read3 12 + 12 B/"
-                             "particle + three meshes once; fractions of the measured "
-                             "HBM copy bandwidth")
+                             "particle + three meshes once; frac: of the measured HBM copy "
+                             "bandwidth; x_library_*: 8 CIC contributions per particle (24 "
+                             "for read3) per second over l2_reference's random-index rates")
     return results, launches
 
 
