@@ -162,3 +162,31 @@ def test_tuning_round_trip_and_ranges(lib):
             assert _lib.get_tuning()["resort_ctas_per_sm"] == 6
     finally:
         _lib.set_tuning(**before)
+
+
+def test_sorted_path_limits_are_checked_on_the_host(lib):
+    """The sorted path's limits (32-bit particle slots, at most 256 tiles per
+    axis) and the piecewise return's arguments are rejected before any GPU
+    work, with the status and message of an invalid argument."""
+    from jaxpm_gb300 import _lib
+    P = ctypes.c_void_p(256)
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_tile_sort_f32", P, None, None, 1 << 32, 64, 64, 64, P, None, P, P,
+                  1 << 20, None)
+    assert e.value.status == 1 and "32 bits" in str(e.value)
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_tile_sort_dest_f32", P, None, None, 1000, 4096, 8, 8, P, None, P, P, P,
+                  1 << 20, None)
+    assert e.value.status == 1 and "tiles" in str(e.value)
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_tile_sort_dest_f32", P, None, None, 1000, 64, 64, 64, P, None, P, None,
+                  P, 1 << 20, None)
+    assert "dest is NULL" in str(e.value)
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_gather3_f32", P, -1, P, 4, ctypes.c_void_p(1 << 20), None)
+    assert e.value.status == 1 and "n_in" in str(e.value)
+    with pytest.raises(_lib.PmgbError) as e:  # out overlaps the source
+        _lib.call("pmgb_gather3_f32", ctypes.c_void_p(4096), 100, P, 10,
+                  ctypes.c_void_p(4096 + 40), None)
+    assert "overlap" in str(e.value)
+    assert _lib.call("pmgb_gather3_f32", None, 0, None, 0, None, None) == 0  # nothing to do
