@@ -1114,11 +1114,12 @@ def run_paint(args):
 # ---------------------------------------------------------------------------
 # gradient workload: d loss / d (noise, Omega_c, sigma8) through LPT + FastPM
 # ---------------------------------------------------------------------------
-def grad_case(n, steps, checkpoint_every, dev, fd_eps=1e-3):
+def grad_case(n, steps, checkpoint_every, dev, fd_eps=1e-3, engine="sorted"):
     """Forward model at n^3 (box 2n Mpc/h, 2LPT a=0.1, `steps` steps to a=1,
-    a checkpoint every `checkpoint_every` steps), MSE of the a=1 density
-    against the seed-2 target; times forward and forward+backward and checks
-    the gradients against central differences (eps = fd_eps)."""
+    a checkpoint every `checkpoint_every` steps, the steps on `engine`), MSE
+    of the a=1 density against the seed-2 target; times forward and
+    forward+backward and checks the gradients against central differences
+    (eps = fd_eps)."""
     import torch
     from jaxpm_gb300 import _lib, distributed, forward_model as fm, painting
 
@@ -1132,7 +1133,8 @@ def grad_case(n, steps, checkpoint_every, dev, fd_eps=1e-3):
         del xt
 
     def loss(nz, th):
-        x, _ = fm.lpt_nbody(nz, th, shape, box, n_steps=steps, checkpoint_every=checkpoint_every)
+        x, _ = fm.lpt_nbody(nz, th, shape, box, n_steps=steps, checkpoint_every=checkpoint_every,
+                            engine=engine)
         return fm.density_mse(x, target)
 
     from jaxpm_gb300 import growth
@@ -1150,7 +1152,7 @@ def grad_case(n, steps, checkpoint_every, dev, fd_eps=1e-3):
     a, b = ev(), ev()
     a.record(stream)
     with torch.no_grad():
-        l0 = loss(noise, theta0)
+        loss0 = loss(noise, theta0)
     b.record(stream)
     torch.cuda.synchronize(dev)
     fwd_ms = a.elapsed_time(b)
@@ -1183,8 +1185,8 @@ def grad_case(n, steps, checkpoint_every, dev, fd_eps=1e-3):
         an = float((nz.grad.double() * d.double()).sum())
         checks["noise_direction"] = {"adjoint": an, "finite_difference": fd,
                                      "rel_err": abs(an - fd) / max(abs(fd), 1e-30)}
-    return {"mesh": n, "steps": steps, "checkpoint_every": checkpoint_every,
-            "loss": float(l0), "forward_ms": fwd_ms, "forward_backward_ms": grad_ms,
+    return {"mesh": n, "steps": steps, "checkpoint_every": checkpoint_every, "engine": engine,
+            "loss": float(loss0), "forward_ms": fwd_ms, "forward_backward_ms": grad_ms,
             "backward_vs_forward": (grad_ms - fwd_ms) / fwd_ms, "gpu_launches": int(launches),
             "grad_check_eps": fd_eps, "grad_check": checks}
 
@@ -1202,7 +1204,7 @@ def run_grad(args):
     clocks = ClockSampler(local) if "clocks" not in skip else None
     if clocks:
         clocks.start()
-    main = grad_case(128, K, 4, dev)
+    main = grad_case(128, K, 4, dev, engine=args.engine)
     clk = clocks.stop() if clocks else None
     Np = 128**3
     value = Np * K / (main["forward_backward_ms"] / 1e3)
@@ -1217,11 +1219,15 @@ def run_grad(args):
                                      f"128^3 mesh (box 256 Mpc/h, 2LPT a=0.1, {K} steps, "
                                      f"checkpoints every 4) and a seed-2 target; gradient w.r.t. "
                                      f"the white noise and (Omega_c, sigma8)",
+                         "engine": args.engine,
                          "l2": "one timed pass; working set above L2 at 512^3"},
               "cases": [main],
               "gpu_launches": main["gpu_launches"]}
+    # the other engine on the same 128^3 case, for comparison
+    other = "lattice" if args.engine == "sorted" else "sorted"
+    result["cases"].append(grad_case(128, K, 4, dev, engine=other))
     if "512" not in skip:
-        result["cases"].append(grad_case(512, 64, 4, dev))
+        result["cases"].append(grad_case(512, 64, 4, dev, engine=args.engine))
     if clk is not None:
         result["clocks"] = clk
     print(json.dumps(result))

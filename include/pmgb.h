@@ -644,6 +644,22 @@ int pmgb_fpm_step_sorted_vjp_f32(const float *pos, const float *force3,
                                  void *workspace, size_t workspace_bytes,
                                  uint32_t *stats, pmgb_stream_t stream);
 
+/* The cotangents of a recorded sorted step's kick and drift coefficients
+ * (for gradients with respect to the cosmology, on which they depend),
+ * added to two device doubles: out[0] += <g_vel, F(pos)>, F the CIC read
+ * of the step's force meshes (comp_stride apart) at the positions it started
+ * from, g_vel the velocity cotangent pmgb_fpm_step_sorted_vjp_f32 returned
+ * (both order i); out[1] += <g_pos_next[dest], pos_next[dest] - pos>, with
+ * pos_next the positions the step ended with and g_pos_next their cotangents
+ * (order i+1; dest NULL = identity), i.e. drift * <g_x', v'>.  The kick's
+ * cotangent is out[0], the drift's out[1] / drift.  The reference gets them
+ * from JAX's autodiff through ode.py:20-80. */
+int pmgb_fpm_coef_cotangents_f32(const float *pos, const float *pos_next,
+                                 const uint32_t *dest, const float *force3,
+                                 int64_t comp_stride, int nx, int ny, int nz,
+                                 const float *g_pos_next, const float *g_vel,
+                                 int64_t np, double *out, pmgb_stream_t stream);
+
 /* pmgb_fpm_step_sorted_vjp_f32 for a step recorded by
  * pmgb_fpm_run_sorted_record_pot_f32: `potential` is the potential the step
  * took its forces from; the reverse gather derives each tile's forces from

@@ -106,6 +106,8 @@ SIGNATURES = {
     "pmgb_tile_sort_dest_f32": (c_int, [P, P, P, c_int64, c_int, c_int, c_int, P, P, P, P, P,
                                         c_size_t, P]),
     "pmgb_gather3_f32": (c_int, [P, c_int64, P, c_int64, P, P]),
+    "pmgb_fpm_coef_cotangents_f32": (c_int, [P, P, P, P, c_int64, c_int, c_int, c_int, P, P,
+                                             c_int64, P, P]),
     "pmgb_read3_kick_drift_binned_f32": (c_int, [P, c_int64, c_int, c_int, c_int, P, P, c_int64,
                                                  c_float, c_float, P, c_size_t, P, P]),
     "pmgb_cic_paint_sorted_f32": (c_int, [P, c_int, c_int, c_int, P, c_int64, P, c_size_t, P, P]),

@@ -911,6 +911,26 @@ int pmgb_fpm_step_sorted_vjp_f32(const float *pos, const float *force3, const ui
                          workspace_bytes, stats, stream, false);
 }
 
+int pmgb_fpm_coef_cotangents_f32(const float *pos, const float *pos_next, const uint32_t *dest,
+                                  const float *force3, int64_t comp_stride, int nx, int ny,
+                                  int nz, const float *g_pos_next, const float *g_vel,
+                                  int64_t np, double *out, pmgb_stream_t stream) {
+  BEGIN();
+  PMGB_TRY(check_mesh(nx, ny, nz));
+  NONNEG(np);
+  if (np == 0) return PMGB_OK;
+  NEED(pos);
+  NEED(pos_next);
+  NEED(force3);
+  NEED(g_pos_next);
+  NEED(g_vel);
+  NEED(out);
+  PMGB_REQUIRE(comp_stride >= (int64_t)nx * ny * nz,
+               "comp_stride must be at least nx*ny*nz");
+  return coef_cotangents(pos, pos_next, dest, force3, comp_stride, nx, ny, nz, g_pos_next,
+                         g_vel, np, out, stream);
+}
+
 int pmgb_fpm_step_sorted_vjp_pot_f32(const float *pos, const float *potential,
                                      const uint32_t *dest, const uint32_t *tile_offsets,
                                      const float *g_pos_in, const float *g_vel_in,

@@ -203,6 +203,13 @@ int fpm_step_sorted_vjp(const float *pos, const float *force3,
                         float kick, float drift, float r_split, void *mesh_ws,
                         size_t mesh_bytes, unsigned *stats, cudaStream_t s,
                         bool pot = false);
+// The cotangents of one sorted step's coefficients, added to out[0..1]:
+// out[0] += <g_vel, F(pos)> (F read from force3 at pos, order i), out[1] +=
+// <g_pos_next[dest], pos_next[dest] - pos> (order i+1 pulled to order i).
+int coef_cotangents(const float *pos, const float *pos_next, const unsigned *dest,
+                    const float *force3, int64_t cs, int nx, int ny, int nz,
+                    const float *g_pos_next, const float *g_vel, int64_t np, double *out,
+                    cudaStream_t s);
 // step.cu: paint of tile-sorted particles -> R2C -> k-space -> C2R inside the
 // composite workspace; *f3 receives the three force meshes (f3_out when it
 // is given, else the workspace's region).

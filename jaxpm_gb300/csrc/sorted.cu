@@ -2105,6 +2105,75 @@ adj_gather_tiles_kernel(const float *__restrict__ f3, int64_t cs, const float *_
   }
 }
 
+// The cotangents of step i's kick and drift coefficients, one pass over
+// the particles of order i (kick: <u, F(x)>, u the velocity cotangent the
+// reverse step returned and F the CIC read of the step's force meshes at
+// the positions it started from; drift: <g_x', x' - x> = drift <g_x', v'>,
+// x' and g_x' the positions the step ended with and their cotangents,
+// pulled from order i+1 by dest).  Float64 sums per block, then one double
+// atomic per block and quantity.
+__global__ void __launch_bounds__(256)
+coef_cotangent_kernel(const float *__restrict__ x, const float *__restrict__ xn,
+                      const unsigned *__restrict__ dest, const float *__restrict__ f3, int64_t cs,
+                      int nx, int ny, int nz, const float *__restrict__ gxn,
+                      const float *__restrict__ u, int64_t np, double *__restrict__ out) {
+  double gk = 0.0, gd = 0.0;
+  for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < np;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const float x0 = __ldg(x + 3 * p), x1 = __ldg(x + 3 * p + 1), x2 = __ldg(x + 3 * p + 2);
+    Axis ax = cic_axis(x0, nx), ay = cic_axis(x1, ny), az = cic_axis(x2, nz);
+    float F0 = 0.f, F1 = 0.f, F2 = 0.f;
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      const float w = __fmul_rn(__fmul_rn(conn_x(n) ? ax.k1 : ax.k0, conn_y(n) ? ay.k1 : ay.k0),
+                                conn_z(n) ? az.k1 : az.k0);
+      const int64_t c = cell_index(conn_x(n) ? ax.i1 : ax.i0, conn_y(n) ? ay.i1 : ay.i0,
+                                   conn_z(n) ? az.i1 : az.i0, ny, nz);
+      F0 += __ldg(f3 + c) * w;
+      F1 += __ldg(f3 + cs + c) * w;
+      F2 += __ldg(f3 + 2 * cs + c) * w;
+    }
+    gk += (double)__ldg(u + 3 * p) * F0 + (double)__ldg(u + 3 * p + 1) * F1 +
+          (double)__ldg(u + 3 * p + 2) * F2;
+    const int64_t d = dest ? (int64_t)__ldg(dest + p) : p;
+    if (d < np)
+      gd += (double)__ldg(gxn + 3 * d) * (__ldg(xn + 3 * d) - x0) +
+            (double)__ldg(gxn + 3 * d + 1) * (__ldg(xn + 3 * d + 1) - x1) +
+            (double)__ldg(gxn + 3 * d + 2) * (__ldg(xn + 3 * d + 2) - x2);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    gk += __shfl_xor_sync(0xffffffffu, gk, o);
+    gd += __shfl_xor_sync(0xffffffffu, gd, o);
+  }
+  __shared__ double part[2][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    part[0][warp] = gk;
+    part[1][warp] = gd;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      a += part[0][w];
+      b += part[1][w];
+    }
+    atomicAdd(out, a);
+    atomicAdd(out + 1, b);
+  }
+}
+
+int coef_cotangents(const float *pos, const float *pos_next, const unsigned *dest,
+                    const float *force3, int64_t cs, int nx, int ny, int nz,
+                    const float *g_pos_next, const float *g_vel, int64_t np, double *out,
+                    cudaStream_t s) {
+  if (np == 0) return PMGB_OK;
+  coef_cotangent_kernel<<<wave_grid(coef_cotangent_kernel, np, 256), 256, 0, s>>>(
+      pos, pos_next, dest, force3, cs, nx, ny, nz, g_pos_next, g_vel, np, out);
+  PMGB_LAUNCHED("coef_cotangent_kernel");
+  return PMGB_OK;
+}
+
 // One reverse step of the sorted loop (see the block comment above).
 // pos: the positions the step started from (order i); force3: the force
 // meshes the step used, or with `pot` the potential they were derived from

@@ -122,12 +122,14 @@ def _scalars(theta, base, a0, a1, n_steps, order):
 
 def lpt_nbody(noise, theta, mesh_shape, box_size, a0=0.1, a1=1.0, n_steps=32, order=2,
               checkpoint_every=4, base=None, paint_mode="atomic", r_split=0.0,
-              omega_step=1e-3, scalar_step=1e-5):
+              omega_step=1e-3, scalar_step=1e-5, engine="lattice"):
     """Final ``(pos, vel)`` of the forward model: ``linear_field`` of
     ``noise`` at ``cosmology_of(theta)``, LPT of order ``order`` at ``a0``
     on the mesh lattice, then ``n_steps`` FastPM steps to ``a1`` with a
     checkpoint every ``checkpoint_every`` steps.  Differentiable with
-    respect to ``noise`` and ``theta``."""
+    respect to ``noise`` and ``theta``.  ``engine`` picks the steps'
+    implementation (``simulate.nbody``): ``"lattice"`` (step by step) or
+    ``"sorted"`` (the tile-sorted engine, segment by segment)."""
     mesh_shape = tuple(int(s) for s in mesh_shape)
     box = tuple(float(b) for b in box_size)
     theta = torch.as_tensor(theta, dtype=torch.float64)
@@ -149,7 +151,7 @@ def lpt_nbody(noise, theta, mesh_shape, box_size, a0=0.1, a1=1.0, n_steps=32, or
     kick, drift = sc[4:4 + n_steps], sc[4 + n_steps:]
     return simulate.nbody(x, v, None, mesh_shape, a0, a1, n_steps, paint_mode=paint_mode,
                           r_split=r_split, checkpoint_every=checkpoint_every,
-                          coefficients=(kick, drift))
+                          coefficients=(kick, drift), engine=engine)
 
 
 def density_mse(pos, target, paint_mode="atomic"):

@@ -417,11 +417,19 @@ class SortedFastPM:
                 torch.empty((n, self.n), dtype=torch.int32, device=dev),
                 torch.empty((n, keys + 1), dtype=torch.int32, device=dev))
 
-    def vjp(self, pos, vel, g_pos, g_vel, store=None, check=True):
+    def vjp(self, pos, vel, g_pos, g_vel, store=None, check=True, coef_grads=False):
         """Forward run from ``(pos, vel)`` (caller's order) then the reverse
         sweep; returns the final state and the cotangents of the initial
         state, all in the caller's order.  With ``check`` (default) it waits
         for the sweep and raises if a kernel reported a failed wait.
+
+        With ``coef_grads`` it also returns the cotangents of every step's
+        coefficients (float64 arrays): ``<u_i, F_i(x_i)>`` for the kick
+        (``u_i`` the velocity cotangent the reverse step returns, ``F_i``
+        read from the recorded force meshes at the recorded positions) and
+        ``<g_x(i+1), v'_i>`` for the drift (``v'_i`` from the positions the
+        step started and ended with, ``(x_{i+1} - x_i) / drift``); it needs
+        the store of force meshes.
 
         Each forward step records the positions it starts from, its
         potential (or its force meshes, by the store's layout), where each
@@ -437,6 +445,8 @@ class SortedFastPM:
             store = self.alloc_store()
         xs, f3s, dests, offs = store
         pot = f3s.dim() == 4  # [n, nx, ny, nz]: the potentials
+        if coef_grads and pot:
+            raise ValueError("coef_grads needs the store of force meshes")
         record = "pmgb_fpm_run_sorted_record_pot_f32" if pot else "pmgb_fpm_run_sorted_record_f32"
         reverse = "pmgb_fpm_step_sorted_vjp_pot_f32" if pot else "pmgb_fpm_step_sorted_vjp_f32"
         self.load(pos, vel)
@@ -467,6 +477,10 @@ class SortedFastPM:
                   _lib.ptr(gxa), s)
         _lib.call("pmgb_permute3_f32", _lib.ptr(g_vel.contiguous()), _lib.ptr(idn), self.n,
                   _lib.ptr(gva), s)
+        # per step: <u_i, F_i(x_i)> and <g_x(i+1), x(i+1) - x_i>, summed on the
+        # device (pmgb_fpm_coef_cotangents_f32) and read back once
+        coef = torch.zeros((n, 2), dtype=torch.float64, device=gxa.device) if coef_grads \
+            else None
         for i in reversed(range(n)):
             _lib.call(reverse, _lib.ptr(xs[i]), _lib.ptr(f3s[i]),
                       _lib.ptr(dests[i]), _lib.ptr(offs[i]), _lib.ptr(gxa), _lib.ptr(gva),
@@ -474,11 +488,20 @@ class SortedFastPM:
                       float(self.drift[i]), self.r_split, _lib.ptr(self.ws), self.ws_bytes,
                       _lib.ptr(self.stats_buf), s)
             gxa, gxb, gva, gvb = gxb, gxa, gvb, gva
+            if coef_grads:
+                # u_i is now in gva; the step's output cotangents stay in gxb
+                x_next = xs[i + 1] if i + 1 < n else self.pos[self.cur]
+                _lib.call("pmgb_fpm_coef_cotangents_f32", _lib.ptr(xs[i]), _lib.ptr(x_next),
+                          _lib.ptr(dests[i]), _lib.ptr(f3s[i]), nx * ny * nz, nx, ny, nz,
+                          _lib.ptr(gxb), _lib.ptr(gva), self.n, _lib.ptr(coef[i]), s)
         gx, gv = torch.empty_like(gxa), torch.empty_like(gva)
         _lib.call("pmgb_unpermute3_f32", _lib.ptr(gxa), _lib.ptr(ids0), self.n, _lib.ptr(gx), s)
         _lib.call("pmgb_unpermute3_f32", _lib.ptr(gva), _lib.ptr(ids0), self.n, _lib.ptr(gv), s)
         if check:
             self.check(s)
+        if coef_grads:
+            c = coef.cpu().numpy()
+            return final, (gx, gv), (c[:, 0].copy(), c[:, 1] / np.asarray(self.drift[:n]))
         return final, (gx, gv)
 
 
@@ -548,19 +571,107 @@ def fpm_step(x, v, mesh_shape, kick, drift, paint_mode="atomic", r_split=0.0):
     return _Step.apply(x, v, tuple(mesh_shape), kick, drift, _mode(paint_mode), r_split)
 
 
+# segment engines of the sorted differentiable path, one per (device, mesh,
+# particle count, segment length): their workspaces outlive a call
+_SEGMENT_ENGINES = {}
+
+
+def _segment_engine(mesh_shape, n, steps, r_split, device):
+    key = (str(device), tuple(mesh_shape), int(n), int(steps), float(r_split))
+    eng = _SEGMENT_ENGINES.get(key)
+    if eng is None:
+        from .cosmology import Planck15
+        # the coefficients are replaced by the segment's before every use
+        eng = SortedFastPM(mesh_shape, Planck15(), 0.1, 1.0, steps, n_particles=n,
+                           r_split=r_split, device=device)
+        eng.store = eng.alloc_store(potential=False)
+        _SEGMENT_ENGINES[key] = eng
+    return eng
+
+
+class _SortedSegment(torch.autograd.Function):
+    """``len(kick)`` FastPM steps ``(x, v) -> (x', v')`` on the tile-sorted
+    engine.  Forward: the run loop (``pmgb_fpm_run_sorted_f32``), nothing
+    kept but the segment's first state.  Backward: the recording forward
+    run from that state and the reverse sweep
+    (``pmgb_fpm_step_sorted_vjp_f32`` per step), which also yields the
+    cotangents of the per-step coefficients ``kick`` and ``drift`` (1-D
+    tensors that may require grad)."""
+
+    @staticmethod
+    def forward(ctx, x, v, kick, drift, mesh_shape, r_split):
+        n = x.numel() // 3
+        eng = _segment_engine(mesh_shape, n, kick.numel(), r_split, x.device)
+        eng.kick = kick.detach().double().cpu().numpy().copy()
+        eng.drift = drift.detach().double().cpu().numpy().copy()
+        eng.load(x.contiguous(), v.contiguous())
+        eng.run()
+        xo, vo = eng.state()
+        ctx.save_for_backward(x, v, kick, drift)
+        ctx.args = (mesh_shape, r_split)
+        return xo, vo
+
+    @staticmethod
+    def backward(ctx, gx, gv):
+        x, v, kick, drift = ctx.saved_tensors
+        mesh_shape, r_split = ctx.args
+        eng = _segment_engine(mesh_shape, x.numel() // 3, kick.numel(), r_split, x.device)
+        eng.kick = kick.detach().double().cpu().numpy().copy()
+        eng.drift = drift.detach().double().cpu().numpy().copy()
+        gx = torch.zeros_like(x) if gx is None else gx.contiguous()
+        gv = torch.zeros_like(x) if gv is None else gv.contiguous()
+        need_coef = ctx.needs_input_grad[2] or ctx.needs_input_grad[3]
+        out = eng.vjp(x.contiguous(), v.contiguous(), gx, gv, store=eng.store,
+                      coef_grads=need_coef)
+        g_x, g_v = out[1]
+        g_kick = g_drift = None
+        if need_coef:
+            gk, gd = out[2]
+            g_kick = torch.as_tensor(gk, dtype=kick.dtype, device=kick.device)
+            g_drift = torch.as_tensor(gd, dtype=drift.dtype, device=drift.device)
+        return g_x.reshape(x.shape), g_v.reshape(v.shape), g_kick, g_drift, None, None
+
+
+def _sorted_supported(mesh_shape, n):
+    """The tile-sorted engine's limits: 32-bit particle slots, at most 256
+    tiles (2048 cells) per axis."""
+    return n < (1 << 32) - 1 and max(int(a) for a in mesh_shape) <= 2048
+
+
 def nbody(pos, vel, cosmo, mesh_shape, a0, a1, n_steps, paint_mode="atomic", r_split=0.0,
-          checkpoint_every=0, coefficients=None):
+          checkpoint_every=0, coefficients=None, engine="lattice"):
     """Differentiable FastPM integration from ``a0`` to ``a1`` in
     ``n_steps`` steps; returns the final ``(pos, vel)``.  With
     ``checkpoint_every = k > 0`` only every k-th state is kept for the
     backward pass and the steps in between are recomputed.
     ``coefficients`` (optional): the per-step ``(kick, drift)`` as 1-D
     tensors, which may require grad (see ``forward_model``); by default
-    they are computed from ``cosmo``."""
+    they are computed from ``cosmo``.
+
+    ``engine="sorted"`` runs each segment of ``checkpoint_every`` steps
+    (the whole run when it is 0) on the tile-sorted engine: the run loop
+    forward, the recording forward and the reverse sweep backward
+    (``_SortedSegment``); it keeps the recorded force meshes of one
+    segment at a time, and paints with the engine's own fixed-point tile
+    boxes whatever ``paint_mode`` says.  ``"lattice"`` differentiates step by step
+    (``fpm_step``), painting with ``paint_mode``."""
     if coefficients is None:
         kick, drift = fpm_coefficients(cosmo, a0, a1, n_steps)
     else:
         kick, drift = coefficients
+    if engine not in ("lattice", "sorted"):
+        raise ValueError(f"unknown engine {engine!r}")
+    if engine == "sorted" and _sorted_supported(mesh_shape, pos.numel() // 3):
+        k = checkpoint_every if checkpoint_every and checkpoint_every > 0 else n_steps
+        kt = kick if torch.is_tensor(kick) else torch.as_tensor(np.asarray(kick), dtype=torch.float64)
+        dt = drift if torch.is_tensor(drift) else torch.as_tensor(np.asarray(drift),
+                                                                   dtype=torch.float64)
+        x, v = pos, vel
+        for lo in range(0, n_steps, k):
+            hi = min(n_steps, lo + k)
+            x, v = _SortedSegment.apply(x, v, kt[lo:hi], dt[lo:hi], tuple(mesh_shape),
+                                        float(r_split))
+        return x, v
 
     def segment(x, v, lo, hi):
         for i in range(lo, hi):

@@ -53,7 +53,7 @@ def test_lpt2_source_adjoint_dot_product(cuda):
     assert abs(adj - fwd) < 1e-4 * abs(fwd), (adj, fwd)
 
 
-def _loss_setup(cuda, n=32, steps=6, order=2):
+def _loss_setup(cuda, n=32, steps=6, order=2, engine="lattice"):
     from jaxpm_gb300 import distributed, forward_model as fm
     shape, box = (n,) * 3, (2.0 * n,) * 3
     theta0 = torch.tensor([0.2589, 0.8159], dtype=torch.float64)
@@ -66,13 +66,15 @@ def _loss_setup(cuda, n=32, steps=6, order=2):
         target = painting.cic_paint(target, xt)
 
     def loss(nz, th):
-        x, _ = fm.lpt_nbody(nz, th, shape, box, n_steps=steps, order=order, checkpoint_every=2)
+        x, _ = fm.lpt_nbody(nz, th, shape, box, n_steps=steps, order=order, checkpoint_every=2,
+                            engine=engine)
         return fm.density_mse(x, target)
     return noise, theta0, loss
 
 
-def test_gradient_wrt_cosmology_matches_finite_differences(cuda):
-    noise, theta0, loss = _loss_setup(cuda)
+@pytest.mark.parametrize("engine", ["lattice", "sorted"])
+def test_gradient_wrt_cosmology_matches_finite_differences(cuda, engine):
+    noise, theta0, loss = _loss_setup(cuda, engine=engine)
     th = theta0.clone().requires_grad_(True)
     loss(noise, th).backward()
     eps = 1e-3
@@ -86,9 +88,9 @@ def test_gradient_wrt_cosmology_matches_finite_differences(cuda):
             assert abs(an - fd) < 5e-2 * abs(fd), (j, an, fd)
 
 
-@pytest.mark.parametrize("order", [1, 2])
-def test_gradient_wrt_noise_matches_finite_differences(cuda, order):
-    noise, theta0, loss = _loss_setup(cuda, order=order)
+@pytest.mark.parametrize("order,engine", [(1, "lattice"), (2, "lattice"), (2, "sorted")])
+def test_gradient_wrt_noise_matches_finite_differences(cuda, order, engine):
+    noise, theta0, loss = _loss_setup(cuda, order=order, engine=engine)
     nz = noise.clone().requires_grad_(True)
     loss(nz, theta0).backward()
     d = torch.randn(noise.shape, generator=torch.Generator(device=cuda).manual_seed(5),
@@ -119,3 +121,45 @@ def test_forward_model_matches_the_plain_pipeline(cuda):
                                 steps)
     assert torch.allclose(x, xr, rtol=1e-5, atol=1e-4)
     assert torch.allclose(v, vr, rtol=1e-5, atol=1e-5)
+
+
+@pytest.mark.parametrize("shape,k", [((32, 32, 32), 3), ((24, 40, 16), 0)])
+def test_sorted_engine_gradients_match_lattice_engine(cuda, shape, k):
+    """simulate.nbody's two engines: the same final state and the same
+    cotangents of the initial positions and velocities and of every step's
+    kick and drift coefficients (the sorted engine's from its reverse sweep,
+    the lattice engine's step by step), to float32 rounding of different
+    force and paint orders."""
+    from jaxpm_gb300 import cosmology, simulate
+    from jaxpm_gb300.ode import fpm_coefficients
+    steps = 6
+    n = int(np.prod(shape))
+    rng = np.random.default_rng(7)
+    lat = np.stack(np.meshgrid(*[np.arange(s, dtype=np.float32) for s in shape], indexing="ij"),
+                   -1).reshape(-1, 3)
+    x0 = torch.from_numpy(lat + rng.normal(0, 0.7, (n, 3)).astype(np.float32)).to(cuda)
+    v0 = torch.from_numpy(rng.normal(0, 0.3, (n, 3)).astype(np.float32)).to(cuda)
+    gxo = torch.from_numpy(rng.normal(0, 1, (n, 3)).astype(np.float32)).to(cuda)
+    gvo = torch.from_numpy(rng.normal(0, 1, (n, 3)).astype(np.float32)).to(cuda)
+    kc, dc = fpm_coefficients(cosmology.Planck15(), 0.1, 1.0, steps)
+    out = {}
+    for engine in ("lattice", "sorted"):
+        x = x0.clone().requires_grad_(True)
+        v = v0.clone().requires_grad_(True)
+        kick = torch.tensor(kc, dtype=torch.float64, requires_grad=True)
+        drift = torch.tensor(dc, dtype=torch.float64, requires_grad=True)
+        xf, vf = simulate.nbody(x, v, None, shape, 0.1, 1.0, steps, checkpoint_every=k,
+                                coefficients=(kick, drift), engine=engine)
+        ((xf * gxo).sum() + (vf * gvo).sum()).backward()
+        out[engine] = (xf.detach(), vf.detach(), x.grad, v.grad, kick.grad.numpy(),
+                       drift.grad.numpy())
+
+    def rel(a, b):
+        a, b = torch.as_tensor(a).double(), torch.as_tensor(b).double()
+        return float((a - b).norm() / b.norm())
+    L, S = out["lattice"], out["sorted"]
+    assert rel(S[0].cpu() - x0.cpu(), L[0].cpu() - x0.cpu()) < 1e-4
+    assert rel(S[1].cpu(), L[1].cpu()) < 1e-4
+    assert rel(S[2].cpu(), L[2].cpu()) < 1e-3
+    assert rel(S[3].cpu(), L[3].cpu()) < 1e-3
+    assert rel(S[4], L[4]) < 1e-3 and rel(S[5], L[5]) < 1e-3

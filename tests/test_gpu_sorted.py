@@ -566,3 +566,37 @@ def test_permuted_gather_abi_pieces_compose_to_the_run(cuda, lib):
     assert torch.equal(e.ids_current.sort().values, torch.arange(n, device=cuda,
                                                                   dtype=torch.int32))
     assert e.stats == {"paint": 0, "gather": 0, "tma_wait_timeout": 0}
+
+
+def test_coef_cotangents_match_a_torch_statement(cuda, lib):
+    """pmgb_fpm_coef_cotangents_f32 adds <g_vel, F(pos)> and
+    <g_pos_next[dest], pos_next[dest] - pos> to two device doubles: the
+    same sums computed with pmgb_cic_read3_f32 and torch gathers."""
+    from jaxpm_gb300 import _lib
+    shape = (32, 24, 16)
+    nx, ny, nz = shape
+    n = 20000
+    rng = np.random.default_rng(12)
+    pos = T(rng.uniform(-3, 40, (n, 3)).astype(np.float32), cuda)
+    pos_next = T(rng.uniform(-3, 40, (n, 3)).astype(np.float32), cuda)
+    dest = T(rng.permutation(n).astype(np.int32), cuda)
+    f3 = T(rng.standard_normal((3, nx, ny, nz)).astype(np.float32), cuda)
+    gpn = T(rng.standard_normal((n, 3)).astype(np.float32), cuda)
+    gv = T(rng.standard_normal((n, 3)).astype(np.float32), cuda)
+    out = torch.tensor([0.5, -0.25], dtype=torch.float64, device=cuda)  # added to
+    _lib.call("pmgb_fpm_coef_cotangents_f32", _lib.ptr(pos), _lib.ptr(pos_next), _lib.ptr(dest),
+              _lib.ptr(f3), nx * ny * nz, nx, ny, nz, _lib.ptr(gpn), _lib.ptr(gv), n,
+              _lib.ptr(out), _lib.stream())
+    F = torch.empty_like(pos)
+    _lib.call("pmgb_cic_read3_f32", _lib.ptr(f3), nx * ny * nz, nx, ny, nz, _lib.ptr(pos), n,
+              _lib.ptr(F), _lib.stream())
+    d = dest.long()
+    ref_k = float((gv.double() * F.double()).sum()) + 0.5
+    ref_d = float((gpn[d].double() * (pos_next[d].double() - pos.double())).sum()) - 0.25
+    got = out.cpu().numpy()
+    assert abs(got[0] - ref_k) < 1e-5 * (1 + abs(ref_k))
+    assert abs(got[1] - ref_d) < 1e-4 * (1 + abs(ref_d))
+    with pytest.raises(_lib.PmgbError):
+        _lib.call("pmgb_fpm_coef_cotangents_f32", _lib.ptr(pos), _lib.ptr(pos_next), None,
+                  _lib.ptr(f3), 10, nx, ny, nz, _lib.ptr(gpn), _lib.ptr(gv), n, _lib.ptr(out),
+                  _lib.stream())
