@@ -572,20 +572,31 @@ def fpm_step(x, v, mesh_shape, kick, drift, paint_mode="atomic", r_split=0.0):
 
 
 # segment engines of the sorted differentiable path, one per (device, mesh,
-# particle count, segment length): their workspaces outlive a call
+# particle count, segment length, r_split): their workspaces outlive a call.
+# The two most recently used are kept; release_segment_engines() drops all.
 _SEGMENT_ENGINES = {}
+_SEGMENT_KEEP = 2
+
+
+def release_segment_engines():
+    """Frees the device memory the sorted differentiable path keeps between
+    calls (its engines' buffers and recording stores)."""
+    _SEGMENT_ENGINES.clear()
 
 
 def _segment_engine(mesh_shape, n, steps, r_split, device):
     key = (str(device), tuple(mesh_shape), int(n), int(steps), float(r_split))
-    eng = _SEGMENT_ENGINES.get(key)
+    eng = _SEGMENT_ENGINES.pop(key, None)
     if eng is None:
         from .cosmology import Planck15
-        # the coefficients are replaced by the segment's before every use
+        while len(_SEGMENT_ENGINES) >= _SEGMENT_KEEP:
+            _SEGMENT_ENGINES.pop(next(iter(_SEGMENT_ENGINES)))
+        # the coefficients are replaced by the segment's before every use;
+        # the recording store is made by the first backward pass
         eng = SortedFastPM(mesh_shape, Planck15(), 0.1, 1.0, steps, n_particles=n,
                            r_split=r_split, device=device)
-        eng.store = eng.alloc_store(potential=False)
-        _SEGMENT_ENGINES[key] = eng
+        eng.store = None
+    _SEGMENT_ENGINES[key] = eng  # most recently used last
     return eng
 
 
@@ -621,6 +632,8 @@ class _SortedSegment(torch.autograd.Function):
         gx = torch.zeros_like(x) if gx is None else gx.contiguous()
         gv = torch.zeros_like(x) if gv is None else gv.contiguous()
         need_coef = ctx.needs_input_grad[2] or ctx.needs_input_grad[3]
+        if eng.store is None:
+            eng.store = eng.alloc_store(potential=False)
         out = eng.vjp(x.contiguous(), v.contiguous(), gx, gv, store=eng.store,
                       coef_grads=need_coef)
         g_x, g_v = out[1]
