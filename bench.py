@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--phases-only", action="store_true")
     ap.add_argument("--repeats", type=int, default=5,
                     help="timed repetitions of each K-step run (the median is reported)")
+    ap.add_argument("--tuning", default=None,
+                    help="JSON object of run-loop tuning fields to set instead of autotuning")
     ap.add_argument("--fft", default=None, choices=["cufft", "fused", "own"],
                     help="FFT path of the force evaluation (library default if omitted)")
     return ap.parse_args()
@@ -404,7 +406,12 @@ def run_gb300(args):
     # launch configuration of the run loop, tuned on this workload (untimed;
     # cached per mesh, particle count, step count and GPU)
     tuning = None
-    if engine == "sorted" and "tune" not in skip:
+    if args.tuning is not None:
+        fields = _lib.get_tuning()
+        fields.update(json.loads(args.tuning))
+        _lib.set_tuning(**fields)
+        tuning = {"choice": fields, "set_by": "--tuning"}
+    elif engine == "sorted" and "tune" not in skip:
         from jaxpm_gb300 import autotune
         choice, report = autotune.tune_run(eng, x0, v0, steps=K)
         tuning = {"choice": choice, "ms_per_step_by_candidate": report,
