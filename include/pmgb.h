@@ -182,8 +182,10 @@ int pmgb_fft_c2r_f32(void *in, float *out, int nx, int ny, int nz, int batch,
                      int normalize, pmgb_stream_t stream);
 
 /* The library's own 3-D FFT (power-of-two nx in [8,1024], ny in [64,512],
- * nz in [16,512]): a cluster-of-CTAs y-z plane transform and an x-column
- * transform, in-place radix-8 stages in shared memory.  Its half spectra
+ * nz in [16,512]): a y-z plane transform (cuFFT's batched 2-D transforms,
+ * or under PMGB_FFT_OWN the library's cluster-of-CTAs kernels) and the
+ * library's x-column transform, in-place radix-8 stages in shared memory.
+ * Its half spectra
  * use padded rows: [nx][ny][pmgb_fft3_pitch(nz)] complex, modes
  * kz < nz/2+1 meaningful (the forward transform zeroes the padding).  The
  * composite force calls (pmgb_pm_forces_f32, the FastPM steps and their

@@ -4,7 +4,7 @@
 //
 //   plane pass (forward): each x-plane [ny][nz] of a real mesh is transformed
 //     along z (real-to-complex, nz/2+1 modes) and y by one thread-block
-//     cluster of PLANE_CL CTAs.  CTA r holds the rows y = r + CL*l
+//     cluster of CL CTAs (16 for ny >= 256, else 8).  CTA r holds the rows y = r + CL*l
 //     (l < M = ny/CL) in shared memory, transforms them along z, then along
 //     l (an M-point DFT per column); the last radix-CL step of the y
 //     transform reads the CL partial results of every column from the
@@ -46,8 +46,12 @@ namespace cg = cooperative_groups;
 namespace pmgb {
 namespace {
 
-constexpr int PLANE_CL = 8;         // CTAs per cluster in the plane passes
-constexpr int PLANE_THREADS = 512;  // threads per plane-pass CTA
+// Plane passes: planes with ny >= 256 rows go to 16-CTA clusters of 256
+// threads (a 512^2 plane's rows in 66 KB of shared memory per CTA, three
+// CTAs per SM, so that the load, transform and store phases of different
+// clusters overlap); narrower planes to 8-CTA clusters of 512 threads.
+constexpr int PLANE_CL = 8;  // the smaller cluster; ny >= PLANE_CL^2
+constexpr int PLANE_CL_WIDE = 16;
 constexpr int XW = 8;               // kz columns per x-pass CTA (64-byte segments)
 constexpr int XPASS_THREADS = 256;
 
@@ -129,6 +133,36 @@ __device__ __forceinline__ void dft(float2 *v) {
   if (R == 8) dft8<INV>(v);
   else if (R == 4) dft4<INV>(v);
   else dft2<INV>(v);
+}
+
+// radix 2 x 8: the even and odd inputs' 8-point DFTs E, O, then
+// y[k] = E[k] + w16^k O[k], y[k+8] = E[k] - w16^k O[k] (w16 = exp(-+2 pi i / 16)).
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 *v) {
+  constexpr float c1 = 0.92387953251128674f, s1 = 0.38268343236508978f,
+                  r = 0.70710678118654752f;
+  constexpr float C[8] = {1.f, c1, r, s1, 0.f, -s1, -r, -c1};  // cos(pi k / 8)
+  constexpr float S[8] = {0.f, s1, r, c1, 1.f, c1, r, s1};     // sin(pi k / 8)
+  float2 e[8], o[8];
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    e[m] = v[2 * m];
+    o[m] = v[2 * m + 1];
+  }
+  dft8<INV>(e);
+  dft8<INV>(o);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const float2 t = cmul(o[k], make_float2(C[k], INV ? S[k] : -S[k]));
+    v[k] = cadd(e[k], t);
+    v[k + 8] = csub(e[k], t);
+  }
+}
+
+template <int CL, bool INV>
+__device__ __forceinline__ void dft_cl(float2 *v) {
+  if constexpr (CL == 16) dft16<INV>(v);
+  else dft8<INV>(v);
 }
 
 // ---- in-place radix-8 stages ------------------------------------------------
@@ -318,18 +352,20 @@ struct PlaneGeom {
 
 // Forward: real planes in[plane][ny][nz] -> out[plane][ky][kz] (pitch),
 // padding columns kz > nz/2 zeroed.
-__global__ void __cluster_dims__(PLANE_CL, 1, 1) __launch_bounds__(PLANE_THREADS, 1)
+// Launched in clusters of CL CTAs (a launch attribute), one cluster per plane.
+template <int CL, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
 plane_r2c_kernel(const float *__restrict__ in, float2 *__restrict__ out, PlaneGeom g,
                  const float2 *__restrict__ twy, const float2 *__restrict__ twz) {
   extern __shared__ __align__(16) float2 sm[];
   cg::cluster_group cluster = cg::this_cluster();
   const int r = (int)cluster.block_rank();
-  const int64_t plane = blockIdx.x / PLANE_CL;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = PLANE_THREADS / 32;
+  const int64_t plane = blockIdx.x / CL;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = NT / 32;
   const int lgh = g.lgz - 1, H = 1 << lgh;
   // 1. rows y = r + CL*l: load, H-point forward transform, real finish
   for (int l = warp; l < g.M; l += nwarp) {
-    const int y = r + PLANE_CL * l;
+    const int y = r + CL * l;
     const float4 *src =
         reinterpret_cast<const float4 *>(in + (plane * g.ny + y) * (int64_t)g.nz);
     float4 *dst = reinterpret_cast<float4 *>(sm + l * g.sp);
@@ -340,28 +376,28 @@ plane_r2c_kernel(const float *__restrict__ in, float2 *__restrict__ out, PlaneGe
   }
   __syncthreads();
   // 2. M-point forward transform along l of the H+1 columns (w_M = w_ny^CL)
-  fft_forward<true>(sm, g.lgm, g.sp, 1, H + 1, twy, g.lgy, tid, PLANE_THREADS);
+  fft_forward<true>(sm, g.lgm, g.sp, 1, H + 1, twy, g.lgy, tid, NT);
   cluster.sync();
   // 3. the last radix-CL step: X[k2 + M k1] = sum_s w_CL^(s k1) w_ny^(s k2) Y_s[k2]
-  const int kb = g.M / PLANE_CL;
-  for (int t = tid; t < kb * g.pitch; t += PLANE_THREADS) {
+  const int kb = g.M / CL;
+  for (int t = tid; t < kb * g.pitch; t += NT) {
     const int kk = t / g.pitch, kz = t - kk * g.pitch;
     const int k2 = r * kb + kk;
-    float2 v[PLANE_CL];
+    float2 v[CL];
     if (kz <= H) {
       const int row = dif_pos(k2, g.lgm);
 #pragma unroll
-      for (int s = 0; s < PLANE_CL; ++s) {
+      for (int s = 0; s < CL; ++s) {
         const float2 *rem = cluster.map_shared_rank(sm, s);
         v[s] = cmul(rem[row * g.sp + kz], __ldg(twy + s * k2));
       }
-      dft8<false>(v);
+      dft_cl<CL, false>(v);
     } else {
 #pragma unroll
-      for (int s = 0; s < PLANE_CL; ++s) v[s] = make_float2(0.f, 0.f);
+      for (int s = 0; s < CL; ++s) v[s] = make_float2(0.f, 0.f);
     }
 #pragma unroll
-    for (int k1 = 0; k1 < PLANE_CL; ++k1)
+    for (int k1 = 0; k1 < CL; ++k1)
       out[(plane * g.ny + k2 + g.M * k1) * (int64_t)g.pitch + kz] = v[k1];
   }
   cluster.sync();  // keep this CTA's shared memory alive while others read it
@@ -369,40 +405,41 @@ plane_r2c_kernel(const float *__restrict__ in, float2 *__restrict__ out, PlaneGe
 
 // Inverse: in[plane][ky][kz] (pitch) -> real planes out[plane][ny][nz]
 // (unnormalised).
-__global__ void __cluster_dims__(PLANE_CL, 1, 1) __launch_bounds__(PLANE_THREADS, 1)
+template <int CL, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
 plane_c2r_kernel(const float2 *__restrict__ in, float *__restrict__ out, PlaneGeom g,
                  const float2 *__restrict__ twy, const float2 *__restrict__ twz) {
   extern __shared__ __align__(16) float2 sm[];
   cg::cluster_group cluster = cg::this_cluster();
   const int r = (int)cluster.block_rank();
-  const int64_t plane = blockIdx.x / PLANE_CL;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = PLANE_THREADS / 32;
+  const int64_t plane = blockIdx.x / CL;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nwarp = NT / 32;
   const int lgh = g.lgz - 1, H = 1 << lgh;
   cluster.sync();  // every CTA of the cluster runs before any remote store
   // 1. first radix-CL step of the inverse y transform, scattered to the
   //    cluster: V_s[k2] = w_ny^(-s k2) sum_k1 w_CL^(-s k1) X[k2 + M k1]
-  const int kb = g.M / PLANE_CL;
-  for (int t = tid; t < kb * (H + 1); t += PLANE_THREADS) {
+  const int kb = g.M / CL;
+  for (int t = tid; t < kb * (H + 1); t += NT) {
     const int kk = t / (H + 1), kz = t - kk * (H + 1);
     const int k2 = r * kb + kk;
-    float2 v[PLANE_CL];
+    float2 v[CL];
 #pragma unroll
-    for (int k1 = 0; k1 < PLANE_CL; ++k1)
+    for (int k1 = 0; k1 < CL; ++k1)
       v[k1] = __ldg(in + (plane * g.ny + k2 + g.M * k1) * (int64_t)g.pitch + kz);
-    dft8<true>(v);
+    dft_cl<CL, true>(v);
     const int row = dif_pos(k2, g.lgm);
 #pragma unroll
-    for (int s = 0; s < PLANE_CL; ++s) {
+    for (int s = 0; s < CL; ++s) {
       float2 *rem = cluster.map_shared_rank(sm, s);
       rem[row * g.sp + kz] = cmulc(v[s], __ldg(twy + s * k2));
     }
   }
   cluster.sync();
   // 2. inverse M-point transform along the columns -> natural l
-  fft_inverse<true>(sm, g.lgm, g.sp, 1, H + 1, twy, g.lgy, tid, PLANE_THREADS);
+  fft_inverse<true>(sm, g.lgm, g.sp, 1, H + 1, twy, g.lgy, tid, NT);
   // 3. rows: half-complex -> packed, inverse H-point transform, store
   for (int l = warp; l < g.M; l += nwarp) {
-    const int y = r + PLANE_CL * l;
+    const int y = r + CL * l;
     float2 *row = sm + l * g.sp;
     row_c2r_start(row, lgh, twz, lane);
     fft_inverse<false>(row, lgh, 1, 0, 1, twz, g.lgz, lane, 32);
@@ -886,13 +923,13 @@ int ilog2(int n) {
 
 bool pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
-PlaneGeom plane_geom(int ny, int nz, int pitch) {
+PlaneGeom plane_geom(int ny, int nz, int pitch, int cl) {
   PlaneGeom g;
   g.ny = ny;
   g.nz = nz;
   g.lgy = ilog2(ny);
   g.lgz = ilog2(nz);
-  g.M = ny / PLANE_CL;
+  g.M = ny / cl;
   g.lgm = ilog2(g.M);
   g.sp = (nz / 2 + 2) & ~1;
   g.pitch = pitch;
@@ -906,28 +943,105 @@ int set_dyn_smem(const void *fn, size_t bytes) {
   return PMGB_OK;
 }
 
+// One cluster of CL CTAs per plane (cluster size as a launch attribute; 16
+// is above the portable 8 and needs the function's opt-in).
+template <typename Fn, typename... Args>
+int launch_planes(Fn fn, int cl, int nt, int nplanes, size_t smem, cudaStream_t s,
+                  Args... args) {
+  PMGB_TRY(set_dyn_smem((const void *)fn, smem));
+  if (cl > 8)
+    PMGB_CUDA(cudaFuncSetAttribute((const void *)fn,
+                                   cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)nplanes * cl);
+  cfg.blockDim = dim3(nt);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cl;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  PMGB_CUDA(cudaLaunchKernelEx(&cfg, fn, args...));
+  return PMGB_OK;
+}
+
+// Whether 16-CTA clusters of the wide plane kernels fit on this device
+// (queried once per device; otherwise the 8-CTA kernels run).
+bool wide_clusters_fit(int ny, int nz) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int64_t>, bool> known;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  const PlaneGeom g = plane_geom(ny, nz, nz / 2 + 1, PLANE_CL_WIDE);
+  const size_t smem = plane_smem(g);
+  std::lock_guard<std::mutex> lk(mu);
+  const auto key = std::make_pair(dev, (int64_t)smem);
+  auto it = known.find(key);
+  if (it != known.end()) return it->second;
+  bool ok = false;
+  const void *fns[2] = {(const void *)plane_r2c_kernel<PLANE_CL_WIDE, 256, 3>,
+                        (const void *)plane_c2r_kernel<PLANE_CL_WIDE, 256, 3>};
+  ok = true;
+  for (const void *fn : fns) {
+    int n = 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(PLANE_CL_WIDE);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = PLANE_CL_WIDE;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+            cudaSuccess ||
+        cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess || n < 1)
+      ok = false;
+  }
+  cudaGetLastError();  // a refused query leaves no sticky error behind
+  known[key] = ok;
+  return ok;
+}
+
 int plane_r2c(const float *in, float2 *out, int nplanes, int ny, int nz, int pitch,
               cudaStream_t s) {
-  const PlaneGeom g = plane_geom(ny, nz, pitch);
+  const bool wide = ny >= PLANE_CL_WIDE * PLANE_CL_WIDE && wide_clusters_fit(ny, nz);
+  const PlaneGeom g = plane_geom(ny, nz, pitch, wide ? PLANE_CL_WIDE : PLANE_CL);
   const float2 *twy, *twz;
   PMGB_TRY(twiddles(ny, &twy));
   PMGB_TRY(twiddles(nz, &twz));
   const size_t smem = plane_smem(g);
-  PMGB_TRY(set_dyn_smem((const void *)plane_r2c_kernel, smem));
-  plane_r2c_kernel<<<nplanes * PLANE_CL, PLANE_THREADS, smem, s>>>(in, out, g, twy, twz);
+  if (wide)
+    PMGB_TRY(launch_planes(plane_r2c_kernel<PLANE_CL_WIDE, 256, 3>, PLANE_CL_WIDE, 256, nplanes,
+                           smem, s, in, out, g, twy, twz));
+  else
+    PMGB_TRY(launch_planes(plane_r2c_kernel<PLANE_CL, 512, 1>, PLANE_CL, 512, nplanes, smem, s,
+                           in, out, g, twy, twz));
   PMGB_LAUNCHED("plane_r2c_kernel");
   return PMGB_OK;
 }
 
 int plane_c2r(const float2 *in, float *out, int nplanes, int ny, int nz, int pitch,
               cudaStream_t s) {
-  const PlaneGeom g = plane_geom(ny, nz, pitch);
+  const bool wide = ny >= PLANE_CL_WIDE * PLANE_CL_WIDE && wide_clusters_fit(ny, nz);
+  const PlaneGeom g = plane_geom(ny, nz, pitch, wide ? PLANE_CL_WIDE : PLANE_CL);
   const float2 *twy, *twz;
   PMGB_TRY(twiddles(ny, &twy));
   PMGB_TRY(twiddles(nz, &twz));
   const size_t smem = plane_smem(g);
-  PMGB_TRY(set_dyn_smem((const void *)plane_c2r_kernel, smem));
-  plane_c2r_kernel<<<nplanes * PLANE_CL, PLANE_THREADS, smem, s>>>(in, out, g, twy, twz);
+  if (wide)
+    PMGB_TRY(launch_planes(plane_c2r_kernel<PLANE_CL_WIDE, 256, 3>, PLANE_CL_WIDE, 256, nplanes,
+                           smem, s, in, out, g, twy, twz));
+  else
+    PMGB_TRY(launch_planes(plane_c2r_kernel<PLANE_CL, 512, 1>, PLANE_CL, 512, nplanes, smem, s,
+                           in, out, g, twy, twz));
   PMGB_LAUNCHED("plane_c2r_kernel");
   return PMGB_OK;
 }
@@ -1024,7 +1138,7 @@ int spectral_r2c(const float *in, void *out, int nx, int ny, int nz, int batch,
   PMGB_TRY(check_spectral(nx, ny, nz));
   const int pitch = spectral_pitch(nz);
   float2 *o = static_cast<float2 *>(out);
-  PMGB_TRY(plane_r2c(in, o, nx * batch, ny, nz, pitch, s));
+  PMGB_TRY(planes_r2c(in, o, nx * batch, ny, nz, pitch, s));
   const int64_t cs = (int64_t)nx * ny * pitch;
   for (int b = 0; b < batch; ++b)
     PMGB_TRY(xpass<X_FORWARD>(o + b * cs, o + b * cs, nx, ny, nz, pitch, cs, cs, 0.f, 1, 0,
@@ -1040,7 +1154,7 @@ int spectral_c2r(void *in, float *out, int nx, int ny, int nz, int batch, cudaSt
   for (int b = 0; b < batch; ++b)
     PMGB_TRY(xpass<X_INVERSE>(i2 + b * cs, i2 + b * cs, nx, ny, nz, pitch, cs, cs, 0.f, 1, 0,
                               1.f, s));
-  PMGB_TRY(plane_c2r(i2, out, nx * batch, ny, nz, pitch, s));
+  PMGB_TRY(planes_c2r(i2, out, nx * batch, ny, nz, pitch, s));
   return PMGB_OK;
 }
 

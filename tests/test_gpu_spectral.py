@@ -10,7 +10,7 @@ from conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(64, 64, 64), (8, 64, 16), (32, 128, 256), (128, 64, 32), (16, 512, 512)]
+SHAPES = [(64, 64, 64), (8, 64, 16), (32, 128, 256), (128, 64, 32), (8, 256, 64), (16, 512, 512)]
 
 
 @pytest.fixture(params=["fused", "own"])
@@ -52,7 +52,7 @@ def test_supported_shapes(lib):
 
 
 @pytest.mark.parametrize("shape", SHAPES)
-def test_r2c_matches_cufft(cuda, shape):
+def test_r2c_matches_cufft(cuda, fft_fused, shape):
     g = torch.Generator(device=cuda).manual_seed(1)
     x = torch.randn((2, *shape), device=cuda, generator=g)
     out = r2c(x, batch=2)
@@ -65,7 +65,7 @@ def test_r2c_matches_cufft(cuda, shape):
 
 
 @pytest.mark.parametrize("shape", SHAPES)
-def test_c2r_matches_cufft(cuda, shape):
+def test_c2r_matches_cufft(cuda, fft_fused, shape):
     g = torch.Generator(device=cuda).manual_seed(2)
     x = torch.randn(shape, device=cuda, generator=g)
     spec = r2c(x)
