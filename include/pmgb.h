@@ -237,6 +237,18 @@ typedef struct {
 int pmgb_get_tuning(pmgb_tuning *out);
 int pmgb_set_tuning(const pmgb_tuning *in);
 
+/* Launch timing of pmgb_fpm_run_sorted_f32 (process-wide, off by default):
+ * while enabled, each run records CUDA events on its streams around every
+ * gather, every force evaluation and every re-sort of the permutation.
+ * Once the run's stream has been synchronised, pmgb_run_timing returns the
+ * last timed run's mean milliseconds per launch of each phase (the re-sort
+ * over the steps but the last, whose full sort differs) and its step
+ * count; any pointer may be NULL.  An error before any timed run, or while
+ * the run is still in flight.  Runs hold a process-wide lock while timing
+ * is on.  No counterpart in the reference (XLA's profiler). */
+int pmgb_set_run_timing(int enable);
+int pmgb_run_timing(double *gather_ms, double *forces_ms, double *resort_ms, int *steps);
+
 /* ---- Fourier-space force kernel (jaxpm/pm.py:49-56) --------------------- */
 
 /* The spectral part of pm_forces on a real density mesh (pm.py:30-56 from

@@ -65,6 +65,8 @@ SIGNATURES = {
     "pmgb_set_fft_path": (c_int, [c_int]),
     "pmgb_get_tuning": (c_int, [P]),
     "pmgb_set_tuning": (c_int, [P]),
+    "pmgb_set_run_timing": (c_int, [c_int]),
+    "pmgb_run_timing": (c_int, [P, P, P, P]),
     "pmgb_fft_path": (c_int, []),
     "pmgb_mesh_forces_workspace_size": (c_size_t, [c_int, c_int, c_int]),
     "pmgb_mesh_forces_f32": (c_int, [P, P, c_int, c_int, c_int, c_float, P, c_size_t, P]),
@@ -194,6 +196,21 @@ def set_tuning(gather_static_quarters=3, gather_ctas_per_sm=0, resort_ctas_per_s
     t.resort_ctas_per_sm = int(resort_ctas_per_sm)
     t.resort_priority = int(resort_priority)
     call("pmgb_set_tuning", ctypes.byref(t))
+
+
+def set_run_timing(enable):
+    """Switches the run loop's launch timing on or off (``pmgb_set_run_timing``)."""
+    call("pmgb_set_run_timing", 1 if enable else 0)
+
+
+def run_timing():
+    """The last timed run's mean milliseconds per launch of its gathers, force
+    evaluations and re-sorts (``pmgb_run_timing``; its stream must have been
+    synchronised)."""
+    g, f, r = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    n = ctypes.c_int()
+    call("pmgb_run_timing", ctypes.byref(g), ctypes.byref(f), ctypes.byref(r), ctypes.byref(n))
+    return {"read_kick_drift": g.value, "forces": f.value, "sort": r.value, "steps": n.value}
 
 
 class PmgbError(RuntimeError):

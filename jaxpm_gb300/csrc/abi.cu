@@ -263,6 +263,17 @@ int pmgb_set_fft_path(int path) {
 
 int pmgb_fft_path(void) { return spectral_mode(); }
 
+int pmgb_set_run_timing(int enable) {
+  BEGIN();
+  PMGB_REQUIRE(enable == 0 || enable == 1, "enable must be 0 or 1");
+  return set_run_timing(enable != 0);
+}
+
+int pmgb_run_timing(double *gather_ms, double *forces_ms, double *resort_ms, int *steps) {
+  BEGIN();
+  return run_timing(gather_ms, forces_ms, resort_ms, steps);
+}
+
 int pmgb_get_tuning(pmgb_tuning *out) {
   BEGIN();
   NEED(out);

@@ -161,6 +161,11 @@ int rkd_sorted(const float *f3, int64_t cs, int nx, int ny, int nz,
 // n_steps sorted steps with the paint of each next density fused into the
 // gather; the state ping-pongs between the a and b buffers (in a after an
 // even number of steps).  kick/drift: host arrays of n_steps.
+// launch timing of fpm_run_sorted (off by default): per-launch mean
+// milliseconds of the last timed run's gathers, force evaluations and
+// re-sorts
+int set_run_timing(bool on);
+int run_timing(double *gather_ms, double *forces_ms, double *resort_ms, int *steps);
 int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b,
                    float *vel_b, unsigned *id_b, int64_t np, int nx, int ny,
                    int nz, int n_steps, const float *kick, const float *drift,

@@ -19,6 +19,8 @@
 #include <mutex>
 #include <algorithm>
 #include <cstring>
+#include <string>
+#include <vector>
 
 #include "common.cuh"
 #include "kernels.cuh"
@@ -1636,6 +1638,96 @@ static int aux_stream(Aux **out) {
   return PMGB_OK;
 }
 
+// Launch timing of the run loop (set_run_timing): while on, a run records
+// CUDA events around each of its gathers, force evaluations and re-sorts, on
+// the streams they run on; run_timing reads the last timed run's pairs back.
+// Event slots of step i: 6i + {0, 1} its gather, {2, 3} the force
+// evaluation issued after it (the next step's), {4, 5} its re-sort; the
+// force evaluation before step 0 takes 6n + {0, 1}.
+static std::mutex g_rt_mu;
+static bool g_rt_on = false;
+static int g_rt_dev = -1;
+static std::vector<cudaEvent_t> g_rt_ev;
+static int g_rt_steps = 0;  // steps of the last completed timed run (0: none)
+
+int set_run_timing(bool on) {
+  std::lock_guard<std::mutex> lk(g_rt_mu);
+  g_rt_on = on;
+  g_rt_steps = 0;
+  return PMGB_OK;
+}
+
+// Holds the timing lock for the whole run while timing is on, so that two
+// host threads' runs cannot interleave their event slots.
+class RunTimer {
+ public:
+  int begin(int n) {
+    std::unique_lock<std::mutex> lk(g_rt_mu);
+    if (!g_rt_on) return PMGB_OK;
+    int dev = 0;
+    PMGB_CUDA(cudaGetDevice(&dev));
+    if (dev != g_rt_dev) {
+      for (cudaEvent_t e : g_rt_ev) cudaEventDestroy(e);
+      g_rt_ev.clear();
+      g_rt_dev = dev;
+    }
+    while (g_rt_ev.size() < 6 * (size_t)n + 2) {
+      cudaEvent_t e = nullptr;
+      PMGB_CUDA(cudaEventCreate(&e));
+      g_rt_ev.push_back(e);
+    }
+    g_rt_steps = 0;
+    n_ = n;
+    lk_ = std::move(lk);
+    return PMGB_OK;
+  }
+  int mark(int slot, cudaStream_t s) {
+    if (lk_.owns_lock()) PMGB_CUDA(cudaEventRecord(g_rt_ev[slot], s));
+    return PMGB_OK;
+  }
+  void done() {
+    if (lk_.owns_lock()) g_rt_steps = n_;
+  }
+
+ private:
+  std::unique_lock<std::mutex> lk_;
+  int n_ = 0;
+};
+
+int run_timing(double *gather_ms, double *forces_ms, double *resort_ms, int *steps) {
+  std::lock_guard<std::mutex> lk(g_rt_mu);
+  if (g_rt_steps <= 0)
+    return fail(PMGB_ERR_INVALID_ARGUMENT,
+                "no timed run: switch timing on (pmgb_set_run_timing) before the run");
+  const int n = g_rt_steps;
+  auto span = [&](int a, double *acc) -> int {
+    float ms = 0.f;
+    const cudaError_t e = cudaEventElapsedTime(&ms, g_rt_ev[a], g_rt_ev[a + 1]);
+    if (e == cudaErrorNotReady) {
+      cudaGetLastError();
+      return fail(PMGB_ERR_CUDA, "the timed run has not finished: synchronise its stream first");
+    }
+    if (e != cudaSuccess) return fail(PMGB_ERR_CUDA, std::string("cudaEventElapsedTime: ") +
+                                                         cudaGetErrorString(e));
+    *acc += ms;
+    return PMGB_OK;
+  };
+  double g = 0.0, f = 0.0, r = 0.0;
+  PMGB_TRY(span(6 * n, &f));
+  for (int i = 0; i < n; ++i) {
+    PMGB_TRY(span(6 * i, &g));
+    if (i + 1 < n) {
+      PMGB_TRY(span(6 * i + 2, &f));
+      PMGB_TRY(span(6 * i + 4, &r));
+    }
+  }
+  if (gather_ms) *gather_ms = g / n;
+  if (forces_ms) *forces_ms = f / n;
+  if (resort_ms) *resort_ms = n > 1 ? r / (n - 1) : 0.0;
+  if (steps) *steps = n;
+  return PMGB_OK;
+}
+
 int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, float *vel_b,
                    unsigned *id_b, int64_t np, int nx, int ny, int nz, int n_steps,
                    const float *kick, const float *drift, float r_split, void *mesh_ws,
@@ -1682,8 +1774,12 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, flo
   unsigned *perm[2] = {reinterpret_cast<unsigned *>(drifted),
                        reinterpret_cast<unsigned *>(drifted) + np};
   SortScratch sc = sort_scratch(sort_ws, nx, ny, nz, np);
+  RunTimer rt;
+  PMGB_TRY(rt.begin(n_steps));
   PMGB_TRY(paint_sorted(mesh, nx, ny, nz, pos_a, np, sort_ws, sort_bytes, stats, s));
+  PMGB_TRY(rt.mark(6 * n_steps, s));
   PMGB_TRY(forces());
+  PMGB_TRY(rt.mark(6 * n_steps + 1, s));
   int cur = 0, pc = 0;  // buffer holding the state; perm[pc] its permutation
   for (int i = 0; i < n_steps; ++i) {
     const bool last = i + 1 == n_steps;
@@ -1695,14 +1791,17 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, flo
     io.perm = i == 0 ? nullptr : perm[pc];
     io.vel_out = V[out];
     perm_scratch(sort_ws, nx, ny, nz, np, &io);
+    PMGB_TRY(rt.mark(6 * i, s));
     PMGB_TRY(rkd_sorted(f3, (int64_t)nx * ny * nz, nx, ny, nz, P[cur], P[out], V[cur], np,
                         kick[i], drift[i], sort_ws, sort_bytes, stats, s,
                         last ? nullptr : mesh, pot, io));
+    PMGB_TRY(rt.mark(6 * i + 1, s));
     // the re-sort of step i (on the second stream) and the forces of step
     // i+1 (from the density the gather just painted) are independent: they
     // touch disjoint buffers and overlap
     PMGB_CUDA(cudaEventRecord(aux->gathered, s));
     PMGB_CUDA(cudaStreamWaitEvent(s2, aux->gathered, 0));
+    PMGB_TRY(rt.mark(6 * i + 4, s2));
     if (!last) {
       // ids follow the gather (from the order it read), perm is rebuilt
       PMGB_TRY(index_resort(np, nx, ny, nz, i == 0 ? nullptr : perm[pc], perm[pc ^ 1],
@@ -1716,14 +1815,20 @@ int fpm_run_sorted(float *pos_a, float *vel_a, unsigned *id_a, float *pos_b, flo
                             I[cur ^ 1], nullptr, sort_ws, sort_bytes, s2));
       cur ^= 1;
     }
+    PMGB_TRY(rt.mark(6 * i + 5, s2));
     PMGB_CUDA(cudaEventRecord(aux->sorted, s2));
-    if (!last) PMGB_TRY(forces());
+    if (!last) {
+      PMGB_TRY(rt.mark(6 * i + 2, s));
+      PMGB_TRY(forces());
+      PMGB_TRY(rt.mark(6 * i + 3, s));
+    }
   }
   // the state ends in buffer n_steps & 1 (one buffer change per step: none
   // in step 0, one in each later gather, one in the final scatter)
   (void)cur;
   // join: everything of the run is ordered before later work on s
   PMGB_CUDA(cudaStreamWaitEvent(s, aux->sorted, 0));
+  rt.done();
   return PMGB_OK;
 }
 

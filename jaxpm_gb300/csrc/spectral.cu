@@ -1139,6 +1139,12 @@ int spectral_r2c(const float *in, void *out, int nx, int ny, int nz, int batch,
   const int pitch = spectral_pitch(nz);
   float2 *o = static_cast<float2 *>(out);
   PMGB_TRY(planes_r2c(in, o, nx * batch, ny, nz, pitch, s));
+  if (g_spectral.load() != 2) {
+    // cuFFT writes the nz/2+1 modes of each row; the padding is zeroed here
+    const int nzh = nz / 2 + 1;
+    PMGB_CUDA(cudaMemset2DAsync(o + nzh, pitch * sizeof(float2), 0,
+                                (pitch - nzh) * sizeof(float2), (size_t)nx * ny * batch, s));
+  }
   const int64_t cs = (int64_t)nx * ny * pitch;
   for (int b = 0; b < batch; ++b)
     PMGB_TRY(xpass<X_FORWARD>(o + b * cs, o + b * cs, nx, ny, nz, pitch, cs, cs, 0.f, 1, 0,

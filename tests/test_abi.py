@@ -190,3 +190,19 @@ def test_sorted_path_limits_are_checked_on_the_host(lib):
                   ctypes.c_void_p(4096 + 40), None)
     assert "overlap" in str(e.value)
     assert _lib.call("pmgb_gather3_f32", None, 0, None, 0, None, None) == 0  # nothing to do
+
+
+def test_run_timing_switch_and_empty_read(lib):
+    """pmgb_set_run_timing takes 0 or 1; pmgb_run_timing reports an error
+    before any timed run (no GPU work)."""
+    from jaxpm_gb300 import _lib
+    with pytest.raises(_lib.PmgbError) as e:
+        _lib.call("pmgb_set_run_timing", 2)
+    assert e.value.status == 1
+    _lib.set_run_timing(True)
+    try:
+        with pytest.raises(_lib.PmgbError) as e:
+            _lib.run_timing()
+        assert e.value.status == 1 and "no timed run" in str(e.value)
+    finally:
+        _lib.set_run_timing(False)

@@ -600,3 +600,38 @@ def test_coef_cotangents_match_a_torch_statement(cuda, lib):
         _lib.call("pmgb_fpm_coef_cotangents_f32", _lib.ptr(pos), _lib.ptr(pos_next), None,
                   _lib.ptr(f3), 10, nx, ny, nz, _lib.ptr(gpn), _lib.ptr(gv), n, _lib.ptr(out),
                   _lib.stream())
+
+
+def test_run_timing_reads_the_runs_phases_and_changes_nothing(cuda):
+    """With launch timing on, a run records its gathers, force evaluations
+    and re-sorts: each phase's mean is positive and their sum fits in the
+    run's own time; the state equals that of an untimed run (up to the
+    order of the float atomics of the particles that leave their tiles)."""
+    from jaxpm_gb300 import _lib, cosmology, simulate
+    shape, K = (64, 64, 64), 5
+    rng = np.random.default_rng(23)
+    lat = cic.lattice(shape).reshape(-1, 3)
+    x0 = T((lat + rng.normal(0, 0.5, lat.shape)).astype(np.float32), cuda)
+    v0 = T(rng.normal(0, 0.3, lat.shape).astype(np.float32), cuda)
+    eng = simulate.SortedFastPM(shape, cosmology.Planck15(), 0.1, 1.0, K, device=cuda)
+    eng.load(x0, v0)
+    eng.run()
+    ref = [t.clone() for t in eng.state()]
+    _lib.set_run_timing(True)
+    try:
+        eng.load(x0, v0)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        eng.run()
+        b.record()
+        torch.cuda.synchronize()
+        t = _lib.run_timing()
+    finally:
+        _lib.set_run_timing(False)
+    total = a.elapsed_time(b)
+    assert t["steps"] == K
+    assert t["read_kick_drift"] > 0 and t["forces"] > 0 and t["sort"] > 0
+    assert K * t["read_kick_drift"] + K * t["forces"] < total
+    got = eng.state()
+    assert rel_l2(got[0].cpu(), ref[0].cpu()) < 1e-6
+    assert rel_l2(got[1].cpu(), ref[1].cpu()) < 1e-5
