@@ -107,7 +107,7 @@ static int check_mode(int mode) {
 
 extern "C" {
 
-int pmgb_version(void) { return 101; }
+int pmgb_version(void) { return 102; }
 
 uint64_t pmgb_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 

@@ -34,6 +34,7 @@
 #include <cmath>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <utility>
 #include <vector>
 
@@ -882,6 +883,262 @@ xpass_reg_kernel(const float2 *in, float2 *out, XGeom g, const float2 *__restric
   for (int m = 0; m < 8; ++m) out[gidx(b + T * m)] = v[m];
 }
 
+// ---- register-resident plane passes (16-CTA clusters; nz, ny in {256, 512}) ----
+//
+// The decomposition of plane_r2c_kernel / plane_c2r_kernel (CTA r of a
+// 16-CTA cluster holds the rows y = r + 16 l, l < M = ny/16), with the
+// transforms in registers: the CTA's rows are copied into shared memory at
+// once (cp.async, every copy in flight together), each group of 8 rows is
+// transformed along z by the x pass's register machinery (xforward /
+// xinverse: 8 elements per thread, radix-8 stages, padded exchanges), and
+// each column's M-point transform along l runs in one thread's registers.
+// Columns and rows stay in natural order, so the cluster step indexes row k2
+// directly.
+
+constexpr int PREG_THREADS = 256;
+
+// w32^e = exp(-2 pi i e / 32): cos and sin of pi e / 16, e < 22
+__device__ __constant__ float C32[22] = {
+    1.f, 0.98078528040323043f, 0.92387953251128674f, 0.83146961230254524f,
+    0.70710678118654752f, 0.55557023301960218f, 0.38268343236508978f, 0.19509032201612825f,
+    0.f, -0.19509032201612825f, -0.38268343236508978f, -0.55557023301960218f,
+    -0.70710678118654752f, -0.83146961230254524f, -0.92387953251128674f, -0.98078528040323043f,
+    -1.f, -0.98078528040323043f, -0.92387953251128674f, -0.83146961230254524f,
+    -0.70710678118654752f, -0.55557023301960218f};
+__device__ __constant__ float S32[22] = {
+    0.f, 0.19509032201612825f, 0.38268343236508978f, 0.55557023301960218f,
+    0.70710678118654752f, 0.83146961230254524f, 0.92387953251128674f, 0.98078528040323043f,
+    1.f, 0.98078528040323043f, 0.92387953251128674f, 0.83146961230254524f,
+    0.70710678118654752f, 0.55557023301960218f, 0.38268343236508978f, 0.19509032201612825f,
+    0.f, -0.19509032201612825f, -0.38268343236508978f, -0.55557023301960218f,
+    -0.70710678118654752f, -0.83146961230254524f};
+
+// 32-point DFT in place, radix 4 x 8: x[8a + b] -> DFT4 over a for each b,
+// times w32^(b c), then DFT8 over b for each c.  Slot 8c + d ends holding
+// X[c + 4d] (col_slot_freq).
+template <bool INV>
+__device__ __forceinline__ void dft32(float2 *v) {
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    float2 t[4] = {v[b], v[8 + b], v[16 + b], v[24 + b]};
+    dft4<INV>(t);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int e = b * c;
+      v[8 * c + b] =
+          e == 0 ? t[c] : cmul(t[c], make_float2(C32[e], INV ? S32[e] : -S32[e]));
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) dft8<INV>(v + 8 * c);
+}
+
+// the M-point column transform (natural order in) and the frequency its
+// slot s holds afterwards
+template <int M, bool INV>
+__device__ __forceinline__ void dft_col(float2 *v) {
+  if constexpr (M == 32) dft32<INV>(v);
+  else dft16<INV>(v);
+}
+template <int M>
+__device__ __forceinline__ constexpr int col_slot_freq(int s) {
+  return M == 32 ? (s >> 3) + 4 * (s & 7) : s;
+}
+
+template <int LGH, int M>
+struct PregPlan {
+  using PL = XPlan<LGH>;
+  static constexpr int H = 1 << LGH;
+  static constexpr int GPR = PREG_THREADS / (PL::T * XW);  // row groups per pass
+  static constexpr int PASSES = M / (8 * GPR);
+  static constexpr int TW = xtw_offset<LGH>(PL::NS);  // packed row twiddles
+  static constexpr int XBUF = 2 * GPR * PL::BUF;
+};
+
+template <int LGH, int M>
+size_t preg_smem(int sp) {
+  using P = PregPlan<LGH, M>;
+  return ((size_t)M * sp + P::XBUF + P::TW) * sizeof(float2);
+}
+
+// cp.async of the CTA's M rows (nz floats each) into rows[l * sp]
+template <int LGH, int M>
+__device__ __forceinline__ void preg_load_rows(const float *in, float2 *rows, int64_t row0,
+                                               int ny_stride, int sp, int tid) {
+  constexpr int PER_ROW = (2 << LGH) / 4;  // 16-byte pieces per row
+  const uint32_t base = static_cast<uint32_t>(__cvta_generic_to_shared(rows));
+  for (int i = tid; i < M * PER_ROW; i += PREG_THREADS) {
+    const int l = i / PER_ROW, c = i - l * PER_ROW;
+    const float *src = in + (row0 + (int64_t)ny_stride * l) * (2 << LGH) + 4 * c;
+    const uint32_t dst = base + (uint32_t)(l * sp * (int)sizeof(float2) + 16 * c);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+  }
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <int LGH, int M>
+__global__ void __launch_bounds__(PREG_THREADS, 2)
+plane_r2c_reg_kernel(const float *__restrict__ in, float2 *__restrict__ out, PlaneGeom g,
+                     const float2 *__restrict__ twh, const float2 *__restrict__ twy,
+                     const float2 *__restrict__ twz) {
+  using P = PregPlan<LGH, M>;
+  using PL = typename P::PL;
+  constexpr int H = P::H, T = PL::T, NS = PL::NS, CL = PLANE_CL_WIDE, KB = M / CL;
+  extern __shared__ __align__(16) float2 sm[];
+  float2 *rows = sm;
+  float2 *xbuf = rows + M * g.sp;
+  float2 *tw = xbuf + P::XBUF;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int64_t plane = blockIdx.x / CL;
+  const int tid = threadIdx.x;
+  preg_load_rows<LGH, M>(in, rows, plane * g.ny + r, CL, g.sp, tid);
+  xload_twiddles<LGH>(tw, twh, tid, PREG_THREADS);
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+  __syncthreads();
+  // 1. rows, 8 per group: the H-point forward transform of the packed row
+  //    z[p] = x[2p] + i x[2p+1], written back in natural frequency order
+  const int grp = tid / (T * XW), gt = tid - grp * (T * XW), w = gt % XW, b = gt / XW;
+  float2 *buf0 = xbuf + 2 * grp * PL::BUF, *buf1 = buf0 + PL::BUF;
+  int flip = 0;
+  for (int q = 0; q < P::PASSES; ++q) {
+    float2 *row = rows + ((q * P::GPR + grp) * 8 + w) * g.sp;
+    float2 v[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) v[m] = row[b + T * m];
+    xforward<LGH>(v, b, w, tw, buf0, buf1, flip);  // every read of row precedes its barriers
+#pragma unroll
+    for (int m = 0; m < 8; ++m) row[xfreq<LGH>(xpos<LGH, NS - 1>(b, m))] = v[m];
+  }
+  __syncthreads();
+  // real finish in place, one thread per mode pair (j, H - j): X[j] = E + w^j O,
+  // X[H-j] = conj(E - w^j O) (as row_r2c_finish)
+  for (int i = tid; i < M * (H / 2 + 1); i += PREG_THREADS) {
+    const int l = i / (H / 2 + 1), j = i - l * (H / 2 + 1);
+    float2 *row = rows + l * g.sp;
+    const float2 a = row[j];
+    const float2 c = conjf2(row[(H - j) & (H - 1)]);
+    const float2 e = cscale(cadd(a, c), 0.5f);
+    const float2 o = cscale(mul_ni<false>(csub(a, c)), 0.5f);
+    const float2 t = cmul(__ldg(twz + j), o);
+    row[j] = cadd(e, t);
+    row[H - j] = conjf2(csub(e, t));
+  }
+  __syncthreads();
+  // 2. columns: the M-point forward transform along l of each of the H + 1
+  //    columns in one thread's registers
+  for (int kz = tid; kz <= H; kz += PREG_THREADS) {
+    float2 v[M];
+#pragma unroll
+    for (int l = 0; l < M; ++l) v[l] = rows[l * g.sp + kz];
+    dft_col<M, false>(v);
+#pragma unroll
+    for (int s = 0; s < M; ++s) rows[col_slot_freq<M>(s) * g.sp + kz] = v[s];
+  }
+  cluster.sync();
+  // 3. the last radix-16 step: X[k2 + M k1] = sum_s w16^(s k1) w_ny^(s k2) Y_s[k2]
+  for (int t = tid; t < KB * g.pitch; t += PREG_THREADS) {
+    const int kk = t / g.pitch, kz = t - kk * g.pitch;
+    const int k2 = r * KB + kk;
+    float2 v[CL];
+    if (kz <= H) {
+#pragma unroll
+      for (int s = 0; s < CL; ++s) {
+        const float2 *rem = cluster.map_shared_rank(rows, s);
+        v[s] = cmul(rem[k2 * g.sp + kz], __ldg(twy + s * k2));
+      }
+      dft16<false>(v);
+    } else {
+#pragma unroll
+      for (int s = 0; s < CL; ++s) v[s] = make_float2(0.f, 0.f);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < CL; ++k1)
+      out[(plane * g.ny + k2 + M * k1) * (int64_t)g.pitch + kz] = v[k1];
+  }
+  cluster.sync();  // keep this CTA's shared memory alive while others read it
+}
+
+template <int LGH, int M>
+__global__ void __launch_bounds__(PREG_THREADS, 2)
+plane_c2r_reg_kernel(const float2 *__restrict__ in, float *__restrict__ out, PlaneGeom g,
+                     const float2 *__restrict__ twh, const float2 *__restrict__ twy,
+                     const float2 *__restrict__ twz) {
+  using P = PregPlan<LGH, M>;
+  using PL = typename P::PL;
+  constexpr int H = P::H, T = PL::T, NS = PL::NS, CL = PLANE_CL_WIDE, KB = M / CL;
+  extern __shared__ __align__(16) float2 sm[];
+  float2 *rows = sm;
+  float2 *xbuf = rows + M * g.sp;
+  float2 *tw = xbuf + P::XBUF;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int r = (int)cluster.block_rank();
+  const int64_t plane = blockIdx.x / CL;
+  const int tid = threadIdx.x;
+  xload_twiddles<LGH>(tw, twh, tid, PREG_THREADS);
+  cluster.sync();  // every CTA of the cluster runs before any remote store
+  // 1. first radix-16 step of the inverse y transform, scattered to the
+  //    cluster: V_s[k2] = w_ny^(-s k2) sum_k1 w16^(-s k1) X[k2 + M k1]
+  for (int t = tid; t < KB * (H + 1); t += PREG_THREADS) {
+    const int kk = t / (H + 1), kz = t - kk * (H + 1);
+    const int k2 = r * KB + kk;
+    float2 v[CL];
+#pragma unroll
+    for (int k1 = 0; k1 < CL; ++k1)
+      v[k1] = __ldg(in + (plane * g.ny + k2 + M * k1) * (int64_t)g.pitch + kz);
+    dft16<true>(v);
+#pragma unroll
+    for (int s = 0; s < CL; ++s) {
+      float2 *rem = cluster.map_shared_rank(rows, s);
+      rem[k2 * g.sp + kz] = cmulc(v[s], __ldg(twy + s * k2));
+    }
+  }
+  cluster.sync();
+  // 2. columns: the inverse M-point transform, natural k in, natural l out
+  for (int kz = tid; kz <= H; kz += PREG_THREADS) {
+    float2 v[M];
+#pragma unroll
+    for (int k = 0; k < M; ++k) v[k] = rows[k * g.sp + kz];
+    dft_col<M, true>(v);
+#pragma unroll
+    for (int s = 0; s < M; ++s) rows[col_slot_freq<M>(s) * g.sp + kz] = v[s];
+  }
+  __syncthreads();
+  // 3. rows: half-complex -> packed in place, one thread per mode pair (as
+  //    row_c2r_start, natural order), then the H-point inverse transform of
+  //    8 rows per group and the real rows to HBM
+  for (int i = tid; i < M * (H / 2 + 1); i += PREG_THREADS) {
+    const int l = i / (H / 2 + 1), j = i - l * (H / 2 + 1);
+    float2 *row = rows + l * g.sp;
+    float2 a = row[j], c = row[H - j];
+    if (j == 0) {
+      a.y = 0.f;
+      c.y = 0.f;
+    }
+    const float2 p = cadd(a, conjf2(c));
+    const float2 d = csub(a, conjf2(c));
+    const float2 t = mul_ni<true>(cmulc(d, __ldg(twz + j)));
+    row[j] = cadd(p, t);
+    if (j > 0 && j < H / 2) row[H - j] = conjf2(csub(p, t));
+  }
+  __syncthreads();
+  const int grp = tid / (T * XW), gt = tid - grp * (T * XW), w = gt % XW, b = gt / XW;
+  float2 *buf0 = xbuf + 2 * grp * PL::BUF, *buf1 = buf0 + PL::BUF;
+  int flip = 0;
+  for (int q = 0; q < P::PASSES; ++q) {
+    const int l = (q * P::GPR + grp) * 8 + w;
+    const float2 *row = rows + l * g.sp;
+    float2 v[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) v[m] = row[xfreq<LGH>(xpos<LGH, NS - 1>(b, m))];
+    xinverse<LGH>(v, b, w, tw, buf0, buf1, flip);
+    float2 *dst =
+        reinterpret_cast<float2 *>(out + (plane * g.ny + r + CL * l) * (int64_t)(2 * H));
+#pragma unroll
+    for (int m = 0; m < 8; ++m) dst[b + T * m] = v[m];
+  }
+}
+
 // ---- host side ----------------------------------------------------------------
 
 std::mutex g_tw_mu;
@@ -968,80 +1225,130 @@ int launch_planes(Fn fn, int cl, int nt, int nplanes, size_t smem, cudaStream_t 
   return PMGB_OK;
 }
 
-// Whether 16-CTA clusters of the wide plane kernels fit on this device
-// (queried once per device; otherwise the 8-CTA kernels run).
-bool wide_clusters_fit(int ny, int nz) {
+// Whether 16-CTA clusters of `fn` (nt threads, smem bytes of dynamic shared
+// memory) can be resident on this device; queried once per (device, kernel,
+// smem).  Where they cannot, the 8-CTA kernels run.
+bool clusters_fit(const void *fn, int nt, size_t smem) {
   static std::mutex mu;
-  static std::map<std::pair<int, int64_t>, bool> known;
+  static std::map<std::tuple<int, const void *, size_t>, bool> known;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
-  const PlaneGeom g = plane_geom(ny, nz, nz / 2 + 1, PLANE_CL_WIDE);
-  const size_t smem = plane_smem(g);
   std::lock_guard<std::mutex> lk(mu);
-  const auto key = std::make_pair(dev, (int64_t)smem);
+  const auto key = std::make_tuple(dev, fn, smem);
   auto it = known.find(key);
   if (it != known.end()) return it->second;
-  bool ok = false;
-  const void *fns[2] = {(const void *)plane_r2c_kernel<PLANE_CL_WIDE, 256, 3>,
-                        (const void *)plane_c2r_kernel<PLANE_CL_WIDE, 256, 3>};
-  ok = true;
-  for (const void *fn : fns) {
-    int n = 0;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(PLANE_CL_WIDE);
-    cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = smem;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = PLANE_CL_WIDE;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-            cudaSuccess ||
-        cudaOccupancyMaxActiveClusters(&n, fn, &cfg) != cudaSuccess || n < 1)
-      ok = false;
-  }
+  int n = 0;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(PLANE_CL_WIDE);
+  cfg.blockDim = dim3(nt);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = PLANE_CL_WIDE;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  const bool ok =
+      cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+          cudaSuccess &&
+      cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+          cudaSuccess &&
+      cudaOccupancyMaxActiveClusters(&n, fn, &cfg) == cudaSuccess && n >= 1;
   cudaGetLastError();  // a refused query leaves no sticky error behind
   known[key] = ok;
   return ok;
 }
 
+// The register-resident kernels' shapes: nz and ny each 256 or 512.
+template <bool FWD, int LGH, int M>
+const void *preg_fn() {
+  return FWD ? (const void *)plane_r2c_reg_kernel<LGH, M>
+             : (const void *)plane_c2r_reg_kernel<LGH, M>;
+}
+
+template <bool FWD, int LGH, int M>
+int preg_try(const void *in, void *out, int nplanes, int ny, int nz, int pitch, cudaStream_t s,
+             bool *done) {
+  const PlaneGeom g = plane_geom(ny, nz, pitch, PLANE_CL_WIDE);
+  const size_t smem = preg_smem<LGH, M>(g.sp);
+  *done = false;
+  if (!clusters_fit(preg_fn<FWD, LGH, M>(), PREG_THREADS, smem)) return PMGB_OK;
+  const float2 *twh, *twy, *twz;
+  PMGB_TRY(twiddles(1 << LGH, &twh));
+  PMGB_TRY(twiddles(ny, &twy));
+  PMGB_TRY(twiddles(nz, &twz));
+  if (FWD)
+    PMGB_TRY(launch_planes(plane_r2c_reg_kernel<LGH, M>, PLANE_CL_WIDE, PREG_THREADS, nplanes,
+                           smem, s, static_cast<const float *>(in), static_cast<float2 *>(out),
+                           g, twh, twy, twz));
+  else
+    PMGB_TRY(launch_planes(plane_c2r_reg_kernel<LGH, M>, PLANE_CL_WIDE, PREG_THREADS, nplanes,
+                           smem, s, static_cast<const float2 *>(in), static_cast<float *>(out),
+                           g, twh, twy, twz));
+  *done = true;
+  return PMGB_OK;
+}
+
+template <bool FWD>
+int preg_dispatch(const void *in, void *out, int nplanes, int ny, int nz, int pitch,
+                  cudaStream_t s, bool *done) {
+  *done = false;
+  if (nz == 512 && ny == 512) return preg_try<FWD, 8, 32>(in, out, nplanes, ny, nz, pitch, s, done);
+  if (nz == 512 && ny == 256) return preg_try<FWD, 8, 16>(in, out, nplanes, ny, nz, pitch, s, done);
+  if (nz == 256 && ny == 512) return preg_try<FWD, 7, 32>(in, out, nplanes, ny, nz, pitch, s, done);
+  if (nz == 256 && ny == 256) return preg_try<FWD, 7, 16>(in, out, nplanes, ny, nz, pitch, s, done);
+  return PMGB_OK;
+}
+
 int plane_r2c(const float *in, float2 *out, int nplanes, int ny, int nz, int pitch,
               cudaStream_t s) {
-  const bool wide = ny >= PLANE_CL_WIDE * PLANE_CL_WIDE && wide_clusters_fit(ny, nz);
+  bool done = false;
+  PMGB_TRY(preg_dispatch<true>(in, out, nplanes, ny, nz, pitch, s, &done));
+  if (done) {
+    PMGB_LAUNCHED("plane_r2c_reg_kernel");
+    return PMGB_OK;
+  }
+  bool wide = ny >= PLANE_CL_WIDE * PLANE_CL_WIDE;
   const PlaneGeom g = plane_geom(ny, nz, pitch, wide ? PLANE_CL_WIDE : PLANE_CL);
+  const size_t smem = plane_smem(g);
+  wide = wide && clusters_fit((const void *)plane_r2c_kernel<PLANE_CL_WIDE, 256, 3>, 256, smem);
+  const PlaneGeom g8 = wide ? g : plane_geom(ny, nz, pitch, PLANE_CL);
   const float2 *twy, *twz;
   PMGB_TRY(twiddles(ny, &twy));
   PMGB_TRY(twiddles(nz, &twz));
-  const size_t smem = plane_smem(g);
   if (wide)
     PMGB_TRY(launch_planes(plane_r2c_kernel<PLANE_CL_WIDE, 256, 3>, PLANE_CL_WIDE, 256, nplanes,
                            smem, s, in, out, g, twy, twz));
   else
-    PMGB_TRY(launch_planes(plane_r2c_kernel<PLANE_CL, 512, 1>, PLANE_CL, 512, nplanes, smem, s,
-                           in, out, g, twy, twz));
+    PMGB_TRY(launch_planes(plane_r2c_kernel<PLANE_CL, 512, 1>, PLANE_CL, 512, nplanes,
+                           plane_smem(g8), s, in, out, g8, twy, twz));
   PMGB_LAUNCHED("plane_r2c_kernel");
   return PMGB_OK;
 }
 
 int plane_c2r(const float2 *in, float *out, int nplanes, int ny, int nz, int pitch,
               cudaStream_t s) {
-  const bool wide = ny >= PLANE_CL_WIDE * PLANE_CL_WIDE && wide_clusters_fit(ny, nz);
+  bool done = false;
+  PMGB_TRY(preg_dispatch<false>(in, out, nplanes, ny, nz, pitch, s, &done));
+  if (done) {
+    PMGB_LAUNCHED("plane_c2r_reg_kernel");
+    return PMGB_OK;
+  }
+  bool wide = ny >= PLANE_CL_WIDE * PLANE_CL_WIDE;
   const PlaneGeom g = plane_geom(ny, nz, pitch, wide ? PLANE_CL_WIDE : PLANE_CL);
+  const size_t smem = plane_smem(g);
+  wide = wide && clusters_fit((const void *)plane_c2r_kernel<PLANE_CL_WIDE, 256, 3>, 256, smem);
+  const PlaneGeom g8 = wide ? g : plane_geom(ny, nz, pitch, PLANE_CL);
   const float2 *twy, *twz;
   PMGB_TRY(twiddles(ny, &twy));
   PMGB_TRY(twiddles(nz, &twz));
-  const size_t smem = plane_smem(g);
   if (wide)
     PMGB_TRY(launch_planes(plane_c2r_kernel<PLANE_CL_WIDE, 256, 3>, PLANE_CL_WIDE, 256, nplanes,
                            smem, s, in, out, g, twy, twz));
   else
-    PMGB_TRY(launch_planes(plane_c2r_kernel<PLANE_CL, 512, 1>, PLANE_CL, 512, nplanes, smem, s,
-                           in, out, g, twy, twz));
+    PMGB_TRY(launch_planes(plane_c2r_kernel<PLANE_CL, 512, 1>, PLANE_CL, 512, nplanes,
+                           plane_smem(g8), s, in, out, g8, twy, twz));
   PMGB_LAUNCHED("plane_c2r_kernel");
   return PMGB_OK;
 }

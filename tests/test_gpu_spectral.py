@@ -10,7 +10,8 @@ from conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-SHAPES = [(64, 64, 64), (8, 64, 16), (32, 128, 256), (128, 64, 32), (8, 256, 64), (16, 512, 512)]
+SHAPES = [(64, 64, 64), (8, 64, 16), (32, 128, 256), (128, 64, 32), (8, 256, 64), (8, 256, 256),
+          (8, 512, 256), (8, 256, 512), (16, 512, 512)]
 
 
 @pytest.fixture(params=["fused", "own"])
