@@ -3,13 +3,16 @@
 // hand-written FFTs in three passes over HBM for power-of-two meshes:
 //
 //   plane pass (forward): each x-plane [ny][nz] of a real mesh is transformed
-//     along z (real-to-complex, nz/2+1 modes) and y by one thread-block
-//     cluster of CL CTAs (16 for ny >= 256, else 8).  CTA r holds the rows y = r + CL*l
+//     along z (real-to-complex, nz/2+1 modes) and y.  By default cuFFT's
+//     batched 2-D transforms do this (fft.cu); the library's own plane
+//     kernels (path 2) use one thread-block cluster of CL CTAs per plane (16
+//     for ny >= 256, else 8).  CTA r holds the rows y = r + CL*l
 //     (l < M = ny/CL) in shared memory, transforms them along z, then along
 //     l (an M-point DFT per column); the last radix-CL step of the y
 //     transform reads the CL partial results of every column from the
 //     cluster's shared memories (DSMEM) and writes the plane's spectrum
-//     [ky][kz] (row pitch `pitch` complex) to HBM.
+//     [ky][kz] (row pitch `pitch` complex) to HBM.  For nz, ny in {256, 512}
+//     the row and column transforms run in registers (plane_*_reg_kernel).
 //   x pass: one CTA per (ky, XW consecutive kz) transforms the nx values of
 //     each column along x; in the force pipeline it also multiplies by the
 //     three force kernels and transforms each product back along x, so the
