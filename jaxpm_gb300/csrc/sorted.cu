@@ -1904,9 +1904,11 @@ int fpm_run_sorted_record(float *xs, float *vel_a, unsigned *id_a, float *vel_b,
 // rho_bar = sum_c A_c^T paint(w_c) (A_c the k-space operator of force
 // component c, A_c^T its conjugate multiplier between an R2C and a C2R).
 // ---------------------------------------------------------------------------
-constexpr int ADJ_WARPS = 4;
+// The adjoint paint: a CTA of two warps paints one tile at a time into one
+// shared box (11.8 KB), so that 16 CTAs (32 warps) fit on an SM.
+constexpr int ADJ_THREADS = 64;
 constexpr int ADJ_BOX_WORDS = (3 * TBOX + 31) / 32 * 32;  // three components, 128-byte multiple
-constexpr int ADJ_PAINT_SMEM = ADJ_WARPS * ADJ_BOX_WORDS * 4;
+constexpr int ADJ_PAINT_SMEM = ADJ_BOX_WORDS * 4;
 constexpr unsigned ADJ_BOX_COUNT = 8192;  // larger tiles paint with global atomics
 
 __device__ __forceinline__ void adj_cotangent(const float *__restrict__ gx,
@@ -1923,12 +1925,13 @@ __device__ __forceinline__ void adj_cotangent(const float *__restrict__ gx,
   }
 }
 
-// Paint of the three components of w = kick * u, one warp per tile.  The
-// cotangents have no fixed range, so each tile uses block floating point:
-// a first pass finds max |w| over the tile, the box then accumulates
-// round(W * w * S) in int32 with native shared atomics, S a power of two
-// chosen so that no cell can overflow (|sum| <= count * max * S <= 2^30).
-__global__ void __launch_bounds__(ADJ_WARPS * 32)
+// Paint of the three components of w = kick * u, one tile per CTA of two
+// warps at a time (tiles from a counter).  The cotangents have no fixed
+// range, so each tile uses block floating point: a first pass finds max |w|
+// over the tile, the box then accumulates round(W * w * S) in int32 with
+// native shared atomics, S a power of two chosen so that no cell can
+// overflow (|sum| <= count * max * S <= 2^30).
+__global__ void __launch_bounds__(ADJ_THREADS)
 adj_paint3_tiles_kernel(float *__restrict__ g3, int64_t cs, int nx, int ny, int nz,
                         const float *__restrict__ pos, const unsigned *__restrict__ dest,
                         const float *__restrict__ gx, const float *__restrict__ gv, float kick,
@@ -1936,13 +1939,16 @@ adj_paint3_tiles_kernel(float *__restrict__ g3, int64_t cs, int nx, int ny, int 
                         unsigned *__restrict__ next_tile, unsigned *__restrict__ stats, int vec,
                         const __grid_constant__ CUtensorMap tmap, int use_tma) {
   extern __shared__ __align__(128) int abox[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int *acc = abox + warp * ADJ_BOX_WORDS;
+  __shared__ uint32_t s_key[2];  // the grabbed tile, alternating between iterations
+  __shared__ float s_max[ADJ_THREADS / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int *acc = abox;
   float *fb = reinterpret_cast<float *>(acc);
-  for (;;) {
-    uint32_t key = 0;
-    if (lane == 0) key = atomicAdd(next_tile, 1u);
-    key = __shfl_sync(0xffffffffu, key, 0);
+  for (uint32_t it = 0;; ++it) {
+    // every branch below is uniform across the CTA (it depends on the tile only)
+    if (tid == 0) s_key[it & 1] = atomicAdd(next_tile, 1u);
+    __syncthreads();
+    const uint32_t key = s_key[it & 1];
     if (key >= nkeys) break;
     const unsigned beg = __ldg(offsets + key), end = __ldg(offsets + key + 1);
     if (beg == end) continue;
@@ -1951,14 +1957,19 @@ adj_paint3_tiles_kernel(float *__restrict__ g3, int64_t cs, int nx, int ny, int 
     const unsigned count = end - beg;
     // pass 1: the tile's largest cotangent component
     float m = 0.f;
-    for (unsigned p = beg + lane; p < end; p += 32) {
+    for (unsigned p = beg + tid; p < end; p += ADJ_THREADS) {
       float g[3], u[3], w[3];
       adj_cotangent(gx, gv, dest, p, kick, drift, g, u, w);
       m = fmaxf(m, fmaxf(fabsf(w[0]), fmaxf(fabsf(w[1]), fabsf(w[2]))));
       if (isnan(w[0] + w[1] + w[2])) m = INFINITY;  // fmaxf drops NaN: keep it visible
     }
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (m == 0.f) continue;  // nothing to paint (uniform across the warp)
+    if (lane == 0) s_max[warp] = m;
+    __syncthreads();
+    m = s_max[0];
+#pragma unroll
+    for (int k = 1; k < ADJ_THREADS / 32; ++k) m = fmaxf(m, s_max[k]);
+    if (m == 0.f) continue;  // nothing to paint
     // non-finite cotangents skip the box and propagate through global atomics
     const bool boxed = count < ADJ_BOX_COUNT && isfinite(m);
     int e = 0;
@@ -1966,11 +1977,11 @@ adj_paint3_tiles_kernel(float *__restrict__ g3, int64_t cs, int nx, int ny, int 
       // S = 2^e with m * S * count <= 2^30
       e = (int)floorf(30.0f - log2f((float)count) - log2f(m));
       e = max(-120, min(120, e));
-      for (int q = lane; q < 3 * TBOX; q += 32) acc[q] = 0;
+      for (int q = tid; q < 3 * TBOX; q += ADJ_THREADS) acc[q] = 0;
     }
     const float S = ldexpf(1.0f, e);
-    __syncwarp();
-    for (unsigned p = beg + lane; p < end; p += 32) {
+    __syncthreads();
+    for (unsigned p = beg + tid; p < end; p += ADJ_THREADS) {
       float g[3], u[3], w[3];
       adj_cotangent(gx, gv, dest, p, kick, drift, g, u, w);
       const float x = __ldg(pos + 3 * (int64_t)p), y = __ldg(pos + 3 * (int64_t)p + 1),
@@ -2005,20 +2016,20 @@ adj_paint3_tiles_kernel(float *__restrict__ g3, int64_t cs, int nx, int ny, int 
       }
     }
     if (!boxed) continue;
-    __syncwarp();
+    __syncthreads();
     const float inv = ldexpf(1.0f, -e);
-    for (int q = lane; q < 3 * TBOX; q += 32) fb[q] = (float)acc[q] * inv;
+    for (int q = tid; q < 3 * TBOX; q += ADJ_THREADS) fb[q] = (float)acc[q] * inv;
     const bool tma = use_tma && box_interior(ox, oy, oz, nx, ny, nz);
     if (tma) fence_async_shared();
-    __syncwarp();
+    __syncthreads();
     if (tma) {
-      if (lane == 0) {
+      if (tid == 0) {
         tma_reduce_add_4d(&tmap, oz, oy, ox, 0, fb);
         bulk_commit();
         bulk_wait_read();
       }
     } else if (vec) {
-      for (int q = lane; q < 3 * TB * TB * 3; q += 32) {
+      for (int q = tid; q < 3 * TB * TB * 3; q += ADJ_THREADS) {
         const int gq = q % 3, r = q / 3, b = r % TB, r2 = r / TB, a = r2 % TB, c = r2 / TB;
         const float4 v =
             *reinterpret_cast<const float4 *>(fb + c * TBOX + (a * TB + b) * TBZ + 4 * gq);
@@ -2029,7 +2040,7 @@ adj_paint3_tiles_kernel(float *__restrict__ g3, int64_t cs, int nx, int ny, int 
         }
       }
     } else {
-      for (int q = lane; q < 3 * TB * TB * TB; q += 32) {
+      for (int q = tid; q < 3 * TB * TB * TB; q += ADJ_THREADS) {
         const int cz = q % TB, r = q / TB, b = r % TB, r2 = r / TB, a = r2 % TB, c = r2 / TB;
         const float v = fb[c * TBOX + (a * TB + b) * TBZ + cz];
         if (v != 0.f)
@@ -2037,9 +2048,9 @@ adj_paint3_tiles_kernel(float *__restrict__ g3, int64_t cs, int nx, int ny, int 
                                              wrap_index(oz + cz, nz), ny, nz), v);
       }
     }
-    __syncwarp();
+    __syncthreads();  // the box is free for the next tile once the reduce has read it
   }
-  if (use_tma && lane == 0) bulk_wait_all();
+  if (use_tma && tid == 0) bulk_wait_all();
 }
 
 // Both position terms of the adjoint in one tile-staged gather (one CTA per
@@ -2336,9 +2347,10 @@ int fpm_step_sorted_vjp(const float *pos, const float *force3, const unsigned *d
   }
   // 1. paint of the cotangent-weighted forces
   PMGB_CUDA(cudaMemsetAsync(work, 0, sizeof(unsigned), s));
-  const unsigned pgrid = (unsigned)std::min<int64_t>((keys + ADJ_WARPS - 1) / ADJ_WARPS,
-                                                     (int64_t)sm_count() * 4);
-  adj_paint3_tiles_kernel<<<pgrid, ADJ_WARPS * 32, ADJ_PAINT_SMEM, s>>>(
+  const unsigned pgrid = (unsigned)std::min<int64_t>(
+      keys, (int64_t)resident_ctas((const void *)adj_paint3_tiles_kernel, ADJ_THREADS,
+                                   ADJ_PAINT_SMEM));
+  adj_paint3_tiles_kernel<<<pgrid, ADJ_THREADS, ADJ_PAINT_SMEM, s>>>(
       g3, ncell, nx, ny, nz, pos, dest, gx_in, gv_in, kick, drift, offsets, (uint32_t)keys, work,
       stats, aligned ? 1 : 0, gmap, use_tma);
   PMGB_LAUNCHED("adj_paint3_tiles_kernel");
