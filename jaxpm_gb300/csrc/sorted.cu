@@ -1904,9 +1904,11 @@ int fpm_run_sorted_record(float *xs, float *vel_a, unsigned *id_a, float *vel_b,
 // rho_bar = sum_c A_c^T paint(w_c) (A_c the k-space operator of force
 // component c, A_c^T its conjugate multiplier between an R2C and a C2R).
 // ---------------------------------------------------------------------------
-// The adjoint paint: a CTA of two warps paints one tile at a time into one
-// shared box (11.8 KB), so that 16 CTAs (32 warps) fit on an SM.
-constexpr int ADJ_THREADS = 64;
+// The adjoint paint: a CTA of four warps paints one tile at a time into one
+// shared box (11.8 KB), ten CTAs (40 warps) to an SM.  Measured on the
+// 512^3 forward+adjoint step: one tile per warp with four boxes per CTA
+// (16 warps per SM) 16.64 ms, two warps per box 16.28, three or four 15.97.
+constexpr int ADJ_THREADS = 128;
 constexpr int ADJ_BOX_WORDS = (3 * TBOX + 31) / 32 * 32;  // three components, 128-byte multiple
 constexpr int ADJ_PAINT_SMEM = ADJ_BOX_WORDS * 4;
 constexpr unsigned ADJ_BOX_COUNT = 8192;  // larger tiles paint with global atomics
@@ -1925,8 +1927,8 @@ __device__ __forceinline__ void adj_cotangent(const float *__restrict__ gx,
   }
 }
 
-// Paint of the three components of w = kick * u, one tile per CTA of two
-// warps at a time (tiles from a counter).  The cotangents have no fixed
+// Paint of the three components of w = kick * u, one tile per CTA at a
+// time (tiles from a counter).  The cotangents have no fixed
 // range, so each tile uses block floating point: a first pass finds max |w|
 // over the tile, the box then accumulates round(W * w * S) in int32 with
 // native shared atomics, S a power of two chosen so that no cell can
