@@ -571,6 +571,9 @@ def run_gb300(args):
                           "traffic": (tr * Np if tr is not None else None)}
     result["kernels_frac_of_peak"] = {k: alg[k] * Np / (launch_ms[k] / 1e3) / 1e9 / peak
                                       for k in alg}
+    # the same from the phase pass, each phase alone on the GPU
+    result["kernels_frac_of_peak_alone"] = {
+        k: alg[k] * Np / (phase_ms[k] / 1e3) / 1e9 / peak for k in alg}
     if args.phases_only:
         print(json.dumps(result))
         return
