@@ -1543,14 +1543,19 @@ stencil_adjoint_kernel(const float *__restrict__ g3, float *__restrict__ out, in
 // marches along ST_XCH planes of x, keeping each thread's column along x in a
 // register window (the x stencil) and staging the current plane (with the
 // halo its y and z stencils need) in shared memory, so each input value
-// comes from DRAM about once.  Needs nz % 32 == 0, ny % 8 == 0, nx % ST_XCH == 0.
+// comes from DRAM about once.  The next plane's values are loaded into
+// registers while the current plane is computed, so one plane's loads are
+// always in flight.  Needs nz % 32 == 0, ny % 8 == 0, nx % ST_XCH == 0.
 constexpr int ST_TZ = 32, ST_TY = 8, ST_XCH = 32;
+constexpr int ST_THREADS = ST_TZ * ST_TY;
 
 __device__ __forceinline__ int wrap_lo_hi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(ST_THREADS)
 stencil_forces_tiled_kernel(const float *__restrict__ pot, float *__restrict__ f3, int nx, int ny,
                             int nz) {
+  constexpr int HALO = (ST_TY + 4) * (ST_TZ + 4);  // the plane tile with its y and z halo
+  constexpr int PER = (HALO + ST_THREADS - 1) / ST_THREADS;
   __shared__ float pl[ST_TY + 4][ST_TZ + 4];
   const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * ST_TZ + tz;
   const int xch = nx / ST_XCH, b = blockIdx.z / xch;
@@ -1559,35 +1564,56 @@ stencil_forces_tiled_kernel(const float *__restrict__ pot, float *__restrict__ f
   pot += b * n;  // batch entry b: [b][nx][ny][nz] in, [b][3][nx][ny][nz] out
   f3 += 3 * b * n;
   const int64_t col = (int64_t)(yb + ty) * nz + zb + tz;
+  auto load_tile = [&](int x, float (&v)[PER]) {
+    const float *P = pot + (int64_t)x * plane;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int q = tid + ST_THREADS * i;
+      if (q < HALO) {
+        const int r = q / (ST_TZ + 4), c = q - r * (ST_TZ + 4);
+        v[i] = __ldg(P + (int64_t)wrap_lo_hi(yb + r - 2, ny) * nz + wrap_lo_hi(zb + c - 2, nz));
+      }
+    }
+  };
   float w0 = __ldg(pot + wrap_lo_hi(x0 - 2, nx) * plane + col);
   float w1 = __ldg(pot + wrap_lo_hi(x0 - 1, nx) * plane + col);
-  float w2 = __ldg(pot + (int64_t)x0 * plane + col);
   float w3 = __ldg(pot + wrap_lo_hi(x0 + 1, nx) * plane + col);
+  float w4 = __ldg(pot + wrap_lo_hi(x0 + 2, nx) * plane + col);
+  float tile[PER];
+  load_tile(x0, tile);
   for (int x = x0; x < x0 + ST_XCH; ++x) {
-    const float w4 = __ldg(pot + wrap_lo_hi(x + 2, nx) * plane + col);
-    const float *P = pot + (int64_t)x * plane;
-    for (int q = tid; q < (ST_TY + 4) * (ST_TZ + 4); q += ST_TZ * ST_TY) {
-      const int r = q / (ST_TZ + 4), c = q - r * (ST_TZ + 4);
-      pl[r][c] = __ldg(P + (int64_t)wrap_lo_hi(yb + r - 2, ny) * nz + wrap_lo_hi(zb + c - 2, nz));
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int q = tid + ST_THREADS * i;
+      if (q < HALO) (&pl[0][0])[q] = tile[i];
     }
     __syncthreads();
+    // the next plane's loads, in flight while this plane is computed
+    float w5 = 0.f;
+    if (x + 1 < x0 + ST_XCH) {
+      load_tile(x + 1, tile);
+      w5 = __ldg(pot + wrap_lo_hi(x + 3, nx) * plane + col);
+    }
     const int64_t e = (int64_t)x * plane + col;
     f3[e] = -d_stencil(w0, w1, w3, w4);
     f3[n + e] = -d_stencil(pl[ty][tz + 2], pl[ty + 1][tz + 2], pl[ty + 3][tz + 2],
                            pl[ty + 4][tz + 2]);
     f3[2 * n + e] = -d_stencil(pl[ty + 2][tz], pl[ty + 2][tz + 1], pl[ty + 2][tz + 3],
                                pl[ty + 2][tz + 4]);
+    const float w2 = pl[ty + 2][tz + 2];  // pot at plane x: the next window's x-1 value
     __syncthreads();
     w0 = w1;
     w1 = w2;
-    w2 = w3;
     w3 = w4;
+    w4 = w5;
   }
 }
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(ST_THREADS)
 stencil_adjoint_tiled_kernel(const float *__restrict__ g3, float *__restrict__ out, int nx,
                              int ny, int nz) {
+  constexpr int HY = (ST_TY + 4) * ST_TZ, HZ = ST_TY * (ST_TZ + 4);  // y and z halo tiles
+  constexpr int PER = (HY + HZ + ST_THREADS - 1) / ST_THREADS;
   __shared__ float gy[ST_TY + 4][ST_TZ];
   __shared__ float gz[ST_TY][ST_TZ + 4];
   const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * ST_TZ + tz;
@@ -1597,29 +1623,51 @@ stencil_adjoint_tiled_kernel(const float *__restrict__ g3, float *__restrict__ o
   g3 += 3 * b * n;  // batch entry b: [b][3][nx][ny][nz] in, [b][nx][ny][nz] out
   out += b * n;
   const int64_t col = (int64_t)(yb + ty) * nz + zb + tz;
+  // item q < HY: gy[r][c] of the y component; else gz of the z component
+  auto load_tiles = [&](int x, float (&v)[PER]) {
+    const float *Py = g3 + n + (int64_t)x * plane, *Pz = g3 + 2 * n + (int64_t)x * plane;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int q = tid + ST_THREADS * i;
+      if (q < HY) {
+        const int r = q / ST_TZ, c = q - r * ST_TZ;
+        v[i] = __ldg(Py + (int64_t)wrap_lo_hi(yb + r - 2, ny) * nz + zb + c);
+      } else if (q < HY + HZ) {
+        const int qz = q - HY, r = qz / (ST_TZ + 4), c = qz - r * (ST_TZ + 4);
+        v[i] = __ldg(Pz + (int64_t)(yb + r) * nz + wrap_lo_hi(zb + c - 2, nz));
+      }
+    }
+  };
   float w0 = __ldg(g3 + wrap_lo_hi(x0 - 2, nx) * plane + col);
   float w1 = __ldg(g3 + wrap_lo_hi(x0 - 1, nx) * plane + col);
+  float w2 = __ldg(g3 + (int64_t)x0 * plane + col);
   float w3 = __ldg(g3 + wrap_lo_hi(x0 + 1, nx) * plane + col);
+  float w4 = __ldg(g3 + wrap_lo_hi(x0 + 2, nx) * plane + col);
+  float tiles[PER];
+  load_tiles(x0, tiles);
   for (int x = x0; x < x0 + ST_XCH; ++x) {
-    const float w4 = __ldg(g3 + wrap_lo_hi(x + 2, nx) * plane + col);
-    const float *Py = g3 + n + (int64_t)x * plane, *Pz = g3 + 2 * n + (int64_t)x * plane;
-    for (int q = tid; q < (ST_TY + 4) * ST_TZ; q += ST_TZ * ST_TY) {
-      const int r = q / ST_TZ, c = q - r * ST_TZ;
-      gy[r][c] = __ldg(Py + (int64_t)wrap_lo_hi(yb + r - 2, ny) * nz + zb + c);
-    }
-    for (int q = tid; q < ST_TY * (ST_TZ + 4); q += ST_TZ * ST_TY) {
-      const int r = q / (ST_TZ + 4), c = q - r * (ST_TZ + 4);
-      gz[r][c] = __ldg(Pz + (int64_t)(yb + r) * nz + wrap_lo_hi(zb + c - 2, nz));
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int q = tid + ST_THREADS * i;
+      if (q < HY) (&gy[0][0])[q] = tiles[i];
+      else if (q < HY + HZ) (&gz[0][0])[q - HY] = tiles[i];
     }
     __syncthreads();
+    float w5 = 0.f;
+    if (x + 1 < x0 + ST_XCH) {
+      load_tiles(x + 1, tiles);
+      w5 = __ldg(g3 + wrap_lo_hi(x + 3, nx) * plane + col);
+    }
     out[(int64_t)x * plane + col] =
         d_stencil(w0, w1, w3, w4) +
         d_stencil(gy[ty][tz], gy[ty + 1][tz], gy[ty + 3][tz], gy[ty + 4][tz]) +
         d_stencil(gz[ty][tz], gz[ty][tz + 1], gz[ty][tz + 3], gz[ty][tz + 4]);
     __syncthreads();
     w0 = w1;
-    w1 = __ldg(g3 + (int64_t)x * plane + col);
+    w1 = w2;
+    w2 = w3;
     w3 = w4;
+    w4 = w5;
   }
 }
 
