@@ -370,13 +370,14 @@ def test_permuted_run_leaves_tile_order_and_chains(cuda, lib, split):
                                                                   dtype=torch.int32))
 
 
+@pytest.mark.parametrize("shape", [(64, 64, 64), (32, 128, 64)])
 @pytest.mark.parametrize("r_split", [0.0, 1.5])
-def test_run_loop_potential_path_matches_oracle(cuda, r_split):
-    """At 64^3 the run loop takes the forces from the potential (one inverse
-    transform; the order-1 gradient as its real-space stencil in the
-    gather).  Three steps against the oracle's FastPM steps (float64)."""
+def test_run_loop_potential_path_matches_oracle(cuda, shape, r_split):
+    """On the potential pipeline's shapes (cubic and not) the run loop takes
+    the forces from the potential (one inverse transform; the order-1
+    gradient as its real-space stencil in the gather).  Three steps against
+    the oracle's FastPM steps (float64)."""
     from jaxpm_gb300 import cosmology, simulate
-    shape = (64, 64, 64)
     rng = np.random.default_rng(31)
     lat = cic.lattice(shape).reshape(-1, 3)
     x0 = (lat + rng.normal(0, 1.0, lat.shape)).astype(np.float32)
