@@ -1543,11 +1543,12 @@ stencil_adjoint_kernel(const float *__restrict__ g3, float *__restrict__ out, in
 // marches along ST_XCH planes of x, keeping each thread's column along x in a
 // register window (the x stencil) and staging the current plane (with the
 // halo its y and z stencils need) in shared memory, so each input value
-// comes from DRAM about once.  The next plane's values are loaded into
-// registers while the current plane is computed, so one plane's loads are
-// always in flight.  Needs nz % 32 == 0, ny % 8 == 0, nx % ST_XCH == 0.
+// comes from DRAM about once.  The values of the plane two ahead are loaded
+// into registers while the current plane is computed, so two planes' loads
+// are in flight.  Needs nz % 32 == 0, ny % 8 == 0, nx % ST_XCH == 0.
 constexpr int ST_TZ = 32, ST_TY = 8, ST_XCH = 32;
 constexpr int ST_THREADS = ST_TZ * ST_TY;
+static_assert(ST_XCH % 2 == 0, "the tiled stencils march two planes per loop trip");
 
 __device__ __forceinline__ int wrap_lo_hi(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
@@ -1560,6 +1561,7 @@ stencil_forces_tiled_kernel(const float *__restrict__ pot, float *__restrict__ f
   const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * ST_TZ + tz;
   const int xch = nx / ST_XCH, b = blockIdx.z / xch;
   const int zb = blockIdx.x * ST_TZ, yb = blockIdx.y * ST_TY, x0 = (blockIdx.z - b * xch) * ST_XCH;
+  const int x1 = x0 + ST_XCH;
   const int64_t plane = (int64_t)ny * nz, n = plane * nx;
   pot += b * n;  // batch entry b: [b][nx][ny][nz] in, [b][3][nx][ny][nz] out
   f3 += 3 * b * n;
@@ -1575,24 +1577,27 @@ stencil_forces_tiled_kernel(const float *__restrict__ pot, float *__restrict__ f
       }
     }
   };
-  float w0 = __ldg(pot + wrap_lo_hi(x0 - 2, nx) * plane + col);
-  float w1 = __ldg(pot + wrap_lo_hi(x0 - 1, nx) * plane + col);
-  float w3 = __ldg(pot + wrap_lo_hi(x0 + 1, nx) * plane + col);
-  float w4 = __ldg(pot + wrap_lo_hi(x0 + 2, nx) * plane + col);
-  float tile[PER];
-  load_tile(x0, tile);
-  for (int x = x0; x < x0 + ST_XCH; ++x) {
+  auto at_col = [&](int x) { return __ldg(pot + wrap_lo_hi(x, nx) * plane + col); };
+  // the x window: pot at x-2, x-1, x+1, x+2 for plane x, and x+3 already
+  // loaded (two planes ahead, like the tiles)
+  float w0 = at_col(x0 - 2), w1 = at_col(x0 - 1), w3 = at_col(x0 + 1), w4 = at_col(x0 + 2);
+  float w5 = at_col(x0 + 3);
+  float ta[PER], tb[PER];  // tiles of planes x and x + 1 (x even within the run)
+  load_tile(x0, ta);
+  load_tile(x0 + 1, tb);
+  // one plane: its tile into shared memory, the loads of two planes ahead
+  // issued into the registers it frees, then the stencils
+  auto step = [&](int x, float (&tile)[PER]) {
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
       const int q = tid + ST_THREADS * i;
       if (q < HALO) (&pl[0][0])[q] = tile[i];
     }
     __syncthreads();
-    // the next plane's loads, in flight while this plane is computed
-    float w5 = 0.f;
-    if (x + 1 < x0 + ST_XCH) {
-      load_tile(x + 1, tile);
-      w5 = __ldg(pot + wrap_lo_hi(x + 3, nx) * plane + col);
+    float w6 = 0.f;
+    if (x + 2 < x1) {
+      load_tile(x + 2, tile);
+      w6 = at_col(x + 4);
     }
     const int64_t e = (int64_t)x * plane + col;
     f3[e] = -d_stencil(w0, w1, w3, w4);
@@ -1606,6 +1611,11 @@ stencil_forces_tiled_kernel(const float *__restrict__ pot, float *__restrict__ f
     w1 = w2;
     w3 = w4;
     w4 = w5;
+    w5 = w6;
+  };
+  for (int x = x0; x < x1; x += 2) {  // ST_XCH is even
+    step(x, ta);
+    step(x + 1, tb);
   }
 }
 
@@ -1619,6 +1629,7 @@ stencil_adjoint_tiled_kernel(const float *__restrict__ g3, float *__restrict__ o
   const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * ST_TZ + tz;
   const int xch = nx / ST_XCH, b = blockIdx.z / xch;
   const int zb = blockIdx.x * ST_TZ, yb = blockIdx.y * ST_TY, x0 = (blockIdx.z - b * xch) * ST_XCH;
+  const int x1 = x0 + ST_XCH;
   const int64_t plane = (int64_t)ny * nz, n = plane * nx;
   g3 += 3 * b * n;  // batch entry b: [b][3][nx][ny][nz] in, [b][nx][ny][nz] out
   out += b * n;
@@ -1638,14 +1649,13 @@ stencil_adjoint_tiled_kernel(const float *__restrict__ g3, float *__restrict__ o
       }
     }
   };
-  float w0 = __ldg(g3 + wrap_lo_hi(x0 - 2, nx) * plane + col);
-  float w1 = __ldg(g3 + wrap_lo_hi(x0 - 1, nx) * plane + col);
-  float w2 = __ldg(g3 + (int64_t)x0 * plane + col);
-  float w3 = __ldg(g3 + wrap_lo_hi(x0 + 1, nx) * plane + col);
-  float w4 = __ldg(g3 + wrap_lo_hi(x0 + 2, nx) * plane + col);
-  float tiles[PER];
-  load_tiles(x0, tiles);
-  for (int x = x0; x < x0 + ST_XCH; ++x) {
+  auto at_col = [&](int x) { return __ldg(g3 + wrap_lo_hi(x, nx) * plane + col); };
+  float w0 = at_col(x0 - 2), w1 = at_col(x0 - 1), w2 = at_col(x0), w3 = at_col(x0 + 1),
+        w4 = at_col(x0 + 2), w5 = at_col(x0 + 3);
+  float ta[PER], tb[PER];  // tiles of planes x and x + 1 (x even within the run)
+  load_tiles(x0, ta);
+  load_tiles(x0 + 1, tb);
+  auto step = [&](int x, float (&tiles)[PER]) {
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
       const int q = tid + ST_THREADS * i;
@@ -1653,10 +1663,10 @@ stencil_adjoint_tiled_kernel(const float *__restrict__ g3, float *__restrict__ o
       else if (q < HY + HZ) (&gz[0][0])[q - HY] = tiles[i];
     }
     __syncthreads();
-    float w5 = 0.f;
-    if (x + 1 < x0 + ST_XCH) {
-      load_tiles(x + 1, tiles);
-      w5 = __ldg(g3 + wrap_lo_hi(x + 3, nx) * plane + col);
+    float w6 = 0.f;
+    if (x + 2 < x1) {
+      load_tiles(x + 2, tiles);
+      w6 = at_col(x + 4);
     }
     out[(int64_t)x * plane + col] =
         d_stencil(w0, w1, w3, w4) +
@@ -1668,6 +1678,11 @@ stencil_adjoint_tiled_kernel(const float *__restrict__ g3, float *__restrict__ o
     w2 = w3;
     w3 = w4;
     w4 = w5;
+    w5 = w6;
+  };
+  for (int x = x0; x < x1; x += 2) {  // ST_XCH is even
+    step(x, ta);
+    step(x + 1, tb);
   }
 }
 
